@@ -1,0 +1,119 @@
+/*
+ * Batched tridiagonal solvers for one NVIDIA GB300 (sm_103a): C ABI of
+ * libtridiag.so.
+ *
+ * Part 1 keeps the solver entry points of the reference's
+ * Tridiagonal_CUDA/tridiagonal.h (NIC0NIC0NI/TridiagonalSolver) with the same
+ * names, signatures and contract, so the reference's driver links against
+ * this library unchanged:
+ *   - all pointers are DEVICE pointers allocated by the caller;
+ *   - layout 0: a, b, c, d hold n_batch systems of n_eqt rows, system j in
+ *     [j*n_eqt, (j+1)*n_eqt); a[j*n_eqt] and c[j*n_eqt+n_eqt-1] are unused;
+ *   - in place: a and b are preserved, c may be overwritten, d receives x;
+ *   - synchronous: each call returns after the solve completed
+ *     (cudaDeviceSynchronize, as the reference's wrappers do).
+ * The reference's entry points return void; the status of the last call on
+ * the calling thread is available from tridiag_last_status().
+ *
+ * Part 2 adds int-returning entry points (0 = success, TRIDIAG_ERR_* else)
+ * that take a layout, an algorithm and a CUDA stream (cudaStream_t passed as
+ * void*; NULL = legacy default stream).  They are asynchronous: they return
+ * after enqueueing work on the stream.
+ */
+#ifndef TRIDIAGONAL_H_INCLUDED
+#define TRIDIAGONAL_H_INCLUDED 1
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Part 1: the reference's entry points (Tridiagonal_CUDA/tridiagonal.h).    */
+
+/* naive Thomas -- replaces Tridiagonal_CUDA/tridiagonal.h:20-21 (kernel
+ * Tridiagonal_CUDA/tridiagonal_basic.cu:4-30, wrappers :171-190). */
+void Thomas_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+
+/* ------------------------------------------------------------------------ */
+/* Part 2: extensions (no counterpart in the reference unless stated).       */
+
+/* status codes */
+#define TRIDIAG_SUCCESS 0
+#define TRIDIAG_ERR_INVALID_VALUE 1 /* bad size, null pointer, unknown layout/algorithm */
+#define TRIDIAG_ERR_NOT_SUPPORTED 2 /* valid but unsupported combination */
+#define TRIDIAG_ERR_CUDA 3          /* a CUDA runtime call or launch failed */
+#define TRIDIAG_ERR_WORKSPACE 4     /* workspace missing or too small */
+#define TRIDIAG_ERR_SINGULAR 5      /* a zero pivot was met (see info arrays) */
+#define TRIDIAG_ERR_TIMEOUT 6       /* a bounded device-side wait gave up */
+
+/* layouts: 0 and 1 are the reference's (Tridiagonal_CUDA/helpers.h:17);
+ * 2 is new: row i of system j at [i*n_batch + j] in each of a, b, c, d. */
+#define TRIDIAG_LAYOUT_CONTIGUOUS 0
+#define TRIDIAG_LAYOUT_PACKED 1
+#define TRIDIAG_LAYOUT_INTERLEAVED 2
+
+/* algorithms */
+#define TRIDIAG_ALGO_AUTO 0
+#define TRIDIAG_ALGO_THOMAS 1 /* unpivoted, one thread per system */
+#define TRIDIAG_ALGO_GTSV 5   /* partial pivoting, one thread per system */
+
+/* Status of the last library call made by the calling host thread. */
+int tridiag_last_status(void);
+/* Static description of a status code. */
+const char *tridiag_status_string(int status);
+/* Library version as major*10000 + minor*100 + patch. */
+int tridiag_version(void);
+/* First error a kernel recorded on the device since the last reset (0 if
+ * none; TRIDIAG_ERR_TIMEOUT when a bounded wait gave up).  Synchronous. */
+int tridiag_device_error(int reset);
+
+/* In-place solve with the reference's contract (c may be overwritten, d <- x)
+ * in any layout.  For TRIDIAG_LAYOUT_PACKED pass the packed base pointer as
+ * a and NULL for b, c, d.  TRIDIAG_ALGO_GTSV allocates its workspace with
+ * cudaMallocAsync on `stream`. */
+int tridiag_solve_single(int algo, int layout, float *a, float *b, float *c, float *d, int n_eqt, int n_batch,
+                         void *stream);
+int tridiag_solve_double(int algo, int layout, double *a, double *b, double *c, double *d, int n_eqt,
+                         int n_batch, void *stream);
+
+/* Bytes of workspace tridiag_gtsv_* needs (precision: 0 = single, 1 = double). */
+size_t tridiag_gtsv_workspace_size(int precision, int layout, int n_eqt, int n_batch);
+/* Bytes of the pivot record written by tridiag_gtsv_* (one bit per row). */
+size_t tridiag_pivot_record_size(int n_eqt, int n_batch);
+
+/* Gaussian elimination with partial pivoting (the algorithm of LAPACK ?gtsv,
+ * the reference's MKL row: Tridiagonal_AVX512/tridiagonal_basic.cpp:131-143),
+ * one thread per system.  a, b, c are read only; d holds the right-hand side
+ * on entry and x on exit.  pivots (may be NULL) receives the pivot record for
+ * tridiag_gtsv_adjoint_*; info (may be NULL) receives per system 0 or k+1 for
+ * the first zero pivot U(k,k).  work: tridiag_gtsv_workspace_size() bytes. */
+int tridiag_gtsv_single(int layout, const float *a, const float *b, const float *c, float *d,
+                        unsigned int *pivots, int *info, void *work, size_t work_bytes, int n_eqt, int n_batch,
+                        void *stream);
+int tridiag_gtsv_double(int layout, const double *a, const double *b, const double *c, double *d,
+                        unsigned int *pivots, int *info, void *work, size_t work_bytes, int n_eqt, int n_batch,
+                        void *stream);
+
+/* Adjoint of x = A^{-1} d for a scalar loss with dL/dx = xbar: solves
+ * A^T lambda = xbar reusing the pivots of the forward tridiag_gtsv_* call
+ * (the factors are recomputed from a, b, c with those pivots, bit-identical
+ * to the forward factorisation), then writes
+ *   gd = lambda, ga_i = -lambda_i x_{i-1}, gb_i = -lambda_i x_i,
+ *   gc_i = -lambda_i x_{i+1}   (ga_0 = gc_{n-1} = 0).
+ * x is the forward solution.  work: tridiag_gtsv_workspace_size() bytes. */
+int tridiag_gtsv_adjoint_single(int layout, const float *a, const float *b, const float *c, const float *x,
+                                const unsigned int *pivots, const float *xbar, float *ga, float *gb, float *gc,
+                                float *gd, void *work, size_t work_bytes, int n_eqt, int n_batch, void *stream);
+int tridiag_gtsv_adjoint_double(int layout, const double *a, const double *b, const double *c, const double *x,
+                                const unsigned int *pivots, const double *xbar, double *ga, double *gb,
+                                double *gc, double *gd, void *work, size_t work_bytes, int n_eqt, int n_batch,
+                                void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

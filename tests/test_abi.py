@@ -1,0 +1,79 @@
+"""The C ABI of libtridiag.so without a GPU: the library builds, loads, and
+exports every function include/tridiagonal.h declares; argument checks and
+status strings work before any device call."""
+import ctypes
+import re
+import subprocess
+
+import pytest
+
+from tests.conftest import ROOT
+
+HEADER = ROOT / "include" / "tridiagonal.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\([^;]*\)\s*;", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from tridiagonalsolver_gb300 import build
+
+    build.build()
+    from tridiagonalsolver_gb300 import _lib
+
+    return _lib.lib()
+
+
+def test_header_declares_reference_names():
+    names = declared_functions()
+    for n in ("Thomas_single", "Thomas_double", "tridiag_last_status"):
+        assert n in names
+    assert len(names) >= 10
+
+
+def test_every_declared_symbol_is_exported(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(ROOT / "tridiagonalsolver_gb300" / "lib" / "libtridiag.so")],
+                         capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    for n in declared_functions():
+        assert hasattr(lib, n)
+
+
+def test_python_signatures_cover_header(lib):
+    from tridiagonalsolver_gb300 import _lib
+
+    missing = [n for n in declared_functions() if n not in _lib.SIGNATURES]
+    assert not missing, f"no ctypes signature for: {missing}"
+
+
+def test_status_strings(lib):
+    from tridiagonalsolver_gb300 import _lib
+
+    assert lib.tridiag_status_string(_lib.SUCCESS) == b"success"
+    assert lib.tridiag_status_string(_lib.ERR_SINGULAR) == b"zero pivot"
+    assert lib.tridiag_status_string(12345) == b"unknown status"
+    assert lib.tridiag_version() >= 100
+
+
+def test_argument_checks_need_no_device(lib):
+    from tridiagonalsolver_gb300 import _lib
+
+    # invalid sizes and null pointers are rejected before any CUDA call
+    assert lib.tridiag_solve_double(1, 0, None, None, None, None, 16, 4, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_solve_single(1, 0, ctypes.c_void_p(16), None, None, None, 0, 4, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_solve_single(1, 7, ctypes.c_void_p(16), None, None, None, 8, 4, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_last_status() == _lib.ERR_INVALID_VALUE
+    # gtsv without workspace
+    p = ctypes.c_void_p(256)
+    st = lib.tridiag_gtsv_double(0, p, p, p, p, None, None, None, 0, 8, 2, None)
+    assert st == _lib.ERR_WORKSPACE
+    assert lib.tridiag_gtsv_workspace_size(1, 0, 0, 4) == 0
+    assert lib.tridiag_gtsv_workspace_size(1, 0, 100, 7) >= 2 * 100 * 7 * 8
+    assert lib.tridiag_pivot_record_size(64, 3) == 2 * 3 * 4

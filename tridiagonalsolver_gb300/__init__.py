@@ -1,0 +1,14 @@
+"""GB300-native batched tridiagonal solvers.
+
+The compute path is libtridiag.so (hand-written sm_103a CUDA behind the C ABI
+in include/tridiagonal.h, the reference's Tridiagonal_CUDA/tridiagonal.h
+entry points plus extensions).  This package loads it with ctypes and offers
+PyTorch-tensor wrappers; it has no CPU fallback.
+"""
+from ._lib import ALGOS, LAYOUTS, LIB_PATH, TridiagError, check, last_status, lib
+from .ops import gtsv, gtsv_adjoint, gtsv_workspace, pivot_record, reference_call, solve
+
+__all__ = [
+    "ALGOS", "LAYOUTS", "LIB_PATH", "TridiagError", "check", "last_status", "lib",
+    "gtsv", "gtsv_adjoint", "gtsv_workspace", "pivot_record", "reference_call", "solve",
+]

@@ -1,0 +1,87 @@
+"""ctypes binding of libtridiag.so (the C ABI in include/tridiagonal.h).
+
+The library is built in-tree (``python -m tridiagonalsolver_gb300.build``)
+into ``tridiagonalsolver_gb300/lib/libtridiag.so``.  There is no fallback:
+if the library is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libtridiag.so"
+
+# status codes (include/tridiagonal.h)
+SUCCESS = 0
+ERR_INVALID_VALUE = 1
+ERR_NOT_SUPPORTED = 2
+ERR_CUDA = 3
+ERR_WORKSPACE = 4
+ERR_SINGULAR = 5
+ERR_TIMEOUT = 6
+
+LAYOUTS = {"contiguous": 0, "packed": 1, "interleaved": 2}
+ALGOS = {"auto": 0, "thomas": 1, "cr": 2, "pcr": 3, "wm": 4, "gtsv": 5, "wm_pivot": 6}
+
+_lock = threading.Lock()
+_lib = None
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_SZ = ctypes.c_size_t
+
+# name -> (restype, argtypes); only symbols declared in include/tridiagonal.h
+_REF_SIG = [_P, _P, _P, _P, _I, _I]
+SIGNATURES: dict[str, tuple] = {
+    "tridiag_last_status": (_I, []),
+    "tridiag_status_string": (ctypes.c_char_p, [_I]),
+    "tridiag_version": (_I, []),
+    "tridiag_device_error": (_I, [_I]),
+    "tridiag_solve_single": (_I, [_I, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_solve_double": (_I, [_I, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_gtsv_workspace_size": (_SZ, [_I, _I, _I, _I]),
+    "tridiag_pivot_record_size": (_SZ, [_I, _I]),
+    "tridiag_gtsv_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_gtsv_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_gtsv_adjoint_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_gtsv_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+}
+# the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
+REFERENCE_SOLVERS = ["Thomas_single", "Thomas_double"]
+for _name in REFERENCE_SOLVERS:
+    SIGNATURES[_name] = (None, _REF_SIG)
+
+
+class TridiagError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = lib().tridiag_status_string(status).decode() if _lib is not None else str(status)
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+
+
+def lib() -> ctypes.CDLL:
+    """Load libtridiag.so once; raise if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m tridiagonalsolver_gb300.build`")
+            L = ctypes.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != SUCCESS:
+        raise TridiagError(status, what)
+
+
+def last_status() -> int:
+    return int(lib().tridiag_last_status())

@@ -1,0 +1,229 @@
+// C ABI of libtridiag.so: argument checking, workspace carving, dispatch to
+// the kernel launchers, and the per-thread status of the last call.
+// Declarations and contracts: include/tridiagonal.h.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/tridiagonal.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+thread_local int g_status = TRIDIAG_SUCCESS;
+
+int set_status(int s) {
+  g_status = s;
+  return s;
+}
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? TRIDIAG_SUCCESS : TRIDIAG_ERR_CUDA; }
+
+bool valid_dims(int n, int batch) { return n > 0 && batch > 0; }
+
+bool valid_layout(int layout) {
+  return layout == TRIDIAG_LAYOUT_CONTIGUOUS || layout == TRIDIAG_LAYOUT_PACKED ||
+         layout == TRIDIAG_LAYOUT_INTERLEAVED;
+}
+
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+// Expand the four array pointers of a packed (layout 1) base pointer.
+template <typename T>
+void packed_ptrs(int layout, T*& a, T*& b, T*& c, T*& d, int n) {
+  if (layout == TRIDIAG_LAYOUT_PACKED) {
+    b = a + n;
+    c = a + 2 * (size_t)n;
+    d = a + 3 * (size_t)n;
+  }
+}
+
+template <typename T>
+size_t gtsv_ws_bytes(int n, int batch) {
+  size_t elems = (size_t)n * (size_t)batch;
+  return 2 * align_up(elems * sizeof(T)) + align_up(tdg::pivot_words(n, batch) * sizeof(unsigned));
+}
+
+template <typename T>
+struct GtsvWs {
+  T* w1;
+  T* w2;
+  unsigned* piv;
+};
+
+template <typename T>
+GtsvWs<T> carve_gtsv(void* work, int n, int batch) {
+  size_t elems = (size_t)n * (size_t)batch;
+  char* p = static_cast<char*>(work);
+  GtsvWs<T> w;
+  w.w1 = reinterpret_cast<T*>(p);
+  p += align_up(elems * sizeof(T));
+  w.w2 = reinterpret_cast<T*>(p);
+  p += align_up(elems * sizeof(T));
+  w.piv = reinterpret_cast<unsigned*>(p);
+  return w;
+}
+
+template <typename T>
+int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pivots, int* info, void* work,
+              size_t work_bytes, int n, int batch, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !d) return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout == TRIDIAG_LAYOUT_PACKED) {
+    b = a + n;
+    c = a + 2 * (size_t)n;
+  } else if (!b || !c) {
+    return TRIDIAG_ERR_INVALID_VALUE;
+  }
+  if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
+  GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
+  unsigned* piv = pivots ? pivots : w.piv;
+  if (tdg::tw_eligible(layout, n, batch, sizeof(T))) {
+    bool used = false;
+    cudaError_t e = tdg::launch_gtsv_tw<T>(layout, a, b, c, d, w.w1, w.w2, piv, info, n, batch, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_INVALID_VALUE;  // misaligned base pointer
+  }
+  return cuda_status(tdg::launch_gtsv_seq<T>(layout, a, b, c, d, w.w1, w.w2, piv, info, n, batch, s));
+}
+
+template <typename T>
+int adjoint_impl(int layout, const T* a, const T* b, const T* c, const T* x, const unsigned* piv, const T* g,
+                 T* ga, T* gb, T* gc, T* gd, void* work, size_t work_bytes, int n, int batch, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout)) return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout == TRIDIAG_LAYOUT_PACKED) return TRIDIAG_ERR_NOT_SUPPORTED;
+  if (!a || !b || !c || !x || !piv || !g || !ga || !gb || !gc || !gd) return TRIDIAG_ERR_INVALID_VALUE;
+  if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
+  GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
+  if (tdg::tw_eligible(layout, n, batch, sizeof(T))) {
+    bool used = false;
+    cudaError_t e =
+        tdg::launch_gtsv_adjoint_tw<T>(layout, a, b, c, x, piv, g, ga, gb, gc, gd, w.w1, w.w2, n, batch, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_INVALID_VALUE;
+  }
+  return cuda_status(
+      tdg::launch_gtsv_adjoint<T>(layout, a, b, c, x, piv, g, ga, gb, gc, gd, w.w1, w.w2, n, batch, s));
+}
+
+template <typename T>
+int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout) || !a) return TRIDIAG_ERR_INVALID_VALUE;
+  packed_ptrs(layout, a, b, c, d, n);
+  if (!b || !c || !d) return TRIDIAG_ERR_INVALID_VALUE;
+  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_THOMAS;
+  switch (algo) {
+    case TRIDIAG_ALGO_THOMAS: {
+      bool used = false;
+      cudaError_t e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
+      if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
+      return cuda_status(e);
+    }
+    case TRIDIAG_ALGO_GTSV: {
+      size_t bytes = gtsv_ws_bytes<T>(n, batch);
+      void* work = nullptr;
+      cudaError_t e = cudaMallocAsync(&work, bytes, s);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      int st = gtsv_impl<T>(layout == TRIDIAG_LAYOUT_PACKED ? TRIDIAG_LAYOUT_PACKED : layout, a, b, c, d, nullptr,
+                            nullptr, work, bytes, n, batch, s);
+      e = cudaFreeAsync(work, s);
+      if (st == TRIDIAG_SUCCESS && e != cudaSuccess) st = TRIDIAG_ERR_CUDA;
+      return st;
+    }
+    default:
+      return TRIDIAG_ERR_INVALID_VALUE;
+  }
+}
+
+// Reference-style synchronous wrapper: launch, then wait for the device.
+template <typename F>
+void sync_call(F&& f) {
+  int st = f();
+  if (st == TRIDIAG_SUCCESS) st = cuda_status(cudaDeviceSynchronize());
+  set_status(st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tridiag_last_status(void) { return g_status; }
+
+const char* tridiag_status_string(int status) {
+  switch (status) {
+    case TRIDIAG_SUCCESS: return "success";
+    case TRIDIAG_ERR_INVALID_VALUE: return "invalid value";
+    case TRIDIAG_ERR_NOT_SUPPORTED: return "not supported";
+    case TRIDIAG_ERR_CUDA: return "CUDA error";
+    case TRIDIAG_ERR_WORKSPACE: return "workspace missing or too small";
+    case TRIDIAG_ERR_SINGULAR: return "zero pivot";
+    case TRIDIAG_ERR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+int tridiag_version(void) { return 100; }
+
+int tridiag_device_error(int reset) {
+  int code = 0;
+  cudaError_t e = tdg::read_device_error(&code, reset != 0);
+  if (e != cudaSuccess) return set_status(TRIDIAG_ERR_CUDA);
+  return code;
+}
+
+// ---- reference entry points ------------------------------------------------
+
+void Thomas_single(float* a, float* b, float* c, float* d, int n, int batch) {
+  sync_call([&] { return solve_impl<float>(TRIDIAG_ALGO_THOMAS, TRIDIAG_LAYOUT_CONTIGUOUS, a, b, c, d, n, batch, 0); });
+}
+void Thomas_double(double* a, double* b, double* c, double* d, int n, int batch) {
+  sync_call([&] { return solve_impl<double>(TRIDIAG_ALGO_THOMAS, TRIDIAG_LAYOUT_CONTIGUOUS, a, b, c, d, n, batch, 0); });
+}
+
+// ---- extensions ---------------------------------------------------------------
+
+int tridiag_solve_single(int algo, int layout, float* a, float* b, float* c, float* d, int n, int batch,
+                         void* stream) {
+  return set_status(solve_impl<float>(algo, layout, a, b, c, d, n, batch, (cudaStream_t)stream));
+}
+int tridiag_solve_double(int algo, int layout, double* a, double* b, double* c, double* d, int n, int batch,
+                         void* stream) {
+  return set_status(solve_impl<double>(algo, layout, a, b, c, d, n, batch, (cudaStream_t)stream));
+}
+
+size_t tridiag_gtsv_workspace_size(int precision, int layout, int n, int batch) {
+  (void)layout;
+  if (!valid_dims(n, batch)) return 0;
+  return precision ? gtsv_ws_bytes<double>(n, batch) : gtsv_ws_bytes<float>(n, batch);
+}
+
+size_t tridiag_pivot_record_size(int n, int batch) {
+  if (!valid_dims(n, batch)) return 0;
+  return tdg::pivot_words(n, batch) * sizeof(unsigned);
+}
+
+int tridiag_gtsv_single(int layout, const float* a, const float* b, const float* c, float* d, unsigned* pivots,
+                        int* info, void* work, size_t work_bytes, int n, int batch, void* stream) {
+  return set_status(gtsv_impl<float>(layout, a, b, c, d, pivots, info, work, work_bytes, n, batch,
+                                     (cudaStream_t)stream));
+}
+int tridiag_gtsv_double(int layout, const double* a, const double* b, const double* c, double* d,
+                        unsigned* pivots, int* info, void* work, size_t work_bytes, int n, int batch,
+                        void* stream) {
+  return set_status(gtsv_impl<double>(layout, a, b, c, d, pivots, info, work, work_bytes, n, batch,
+                                      (cudaStream_t)stream));
+}
+
+int tridiag_gtsv_adjoint_single(int layout, const float* a, const float* b, const float* c, const float* x,
+                                const unsigned* piv, const float* g, float* ga, float* gb, float* gc, float* gd,
+                                void* work, size_t work_bytes, int n, int batch, void* stream) {
+  return set_status(adjoint_impl<float>(layout, a, b, c, x, piv, g, ga, gb, gc, gd, work, work_bytes, n, batch,
+                                        (cudaStream_t)stream));
+}
+int tridiag_gtsv_adjoint_double(int layout, const double* a, const double* b, const double* c, const double* x,
+                                const unsigned* piv, const double* g, double* ga, double* gb, double* gc,
+                                double* gd, void* work, size_t work_bytes, int n, int batch, void* stream) {
+  return set_status(adjoint_impl<double>(layout, a, b, c, x, piv, g, ga, gb, gc, gd, work, work_bytes, n, batch,
+                                         (cudaStream_t)stream));
+}
+
+}  // extern "C"

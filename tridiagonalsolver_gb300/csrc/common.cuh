@@ -1,0 +1,103 @@
+// Shared device helpers for the batched tridiagonal kernels (sm_103a).
+//
+// Conventions used by every kernel in this directory:
+//   * a system is   a_i x_{i-1} + b_i x_i + c_i x_{i+1} = d_i,  i = 0..n-1;
+//     a_0 and c_{n-1} are never read (treated as 0).
+//   * layouts (the reference's numbering, Tridiagonal_CUDA/helpers.h:17,
+//     plus one new):
+//       CONTIG      (0)  a[j*n + i]           system-major, the reference's layout 0
+//       PACKED      (1)  base[j*4n + k*n + i] with k = 0..3 for a,b,c,d
+//                        (BPLG layout, Tridiagonal_CUDA/utils.cu:255-260)
+//       INTERLEAVED (2)  a[i*batch + j]       batch-fastest, coalesced for a
+//                        thread-per-system sweep
+//   * FP64 arithmetic on GB300 runs at ~1/50 of the FP32 rate, while the
+//     MUFU reciprocal approximation and integer ops run at full rate.  The
+//     FP64 paths therefore take reciprocals from rcp.approx.ftz.f64 refined
+//     by one third-order Newton step (3 FP64 FMAs) and compare magnitudes on
+//     the integer bit patterns.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tdg {
+
+enum Layout : int { CONTIG = 0, PACKED = 1, INTERLEAVED = 2 };
+
+// Element offset of row i of system j for array k (0..3 = a,b,c,d) relative
+// to that array's base pointer.  For PACKED all four arrays share one base
+// pointer (the caller passes the same pointer four times, offset by k*n).
+template <int L>
+__host__ __device__ __forceinline__ size_t idx(int i, int j, int n, int batch) {
+  if (L == INTERLEAVED) return (size_t)i * (size_t)batch + (size_t)j;
+  if (L == PACKED) return (size_t)j * 4u * (size_t)n + (size_t)i;
+  return (size_t)j * (size_t)n + (size_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// Reciprocals.
+
+// 1/x in FP64: MUFU seed (rcp.approx.ftz.f64), then one third-order
+// Newton-Raphson step r <- r (1 + e + e^2) with e = 1 - x r, which cubes the
+// seed's relative error (the classical iterative reciprocal refinement, e.g.
+// Markstein, "IA-64 and Elementary Functions", 2000).  x = 0 gives NaN/Inf.
+__device__ __forceinline__ double rcp(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  e = fma(e, e, e);
+  return fma(r, e, r);
+}
+
+// 1/x in FP32: the MUFU approximation (at most 1 ulp from the rounded
+// reciprocal), the same class of division the reference's GPU kernels use
+// by default (div.approx.ftz.f32, Tridiagonal_CUDA/intrin.h:56-61).
+__device__ __forceinline__ float rcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// |x| >= |y| on the IEEE bit patterns (integer pipe; NaN compares as large).
+__device__ __forceinline__ bool abs_ge(double x, double y) {
+  unsigned long long ux = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  unsigned long long uy = (unsigned long long)__double_as_longlong(y) & 0x7fffffffffffffffull;
+  return ux >= uy;
+}
+__device__ __forceinline__ bool abs_ge(float x, float y) {
+  unsigned ux = (unsigned)__float_as_int(x) & 0x7fffffffu;
+  unsigned uy = (unsigned)__float_as_int(y) & 0x7fffffffu;
+  return ux >= uy;
+}
+
+__device__ __forceinline__ bool is_zero(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
+}
+__device__ __forceinline__ bool is_zero(float x) { return ((unsigned)__float_as_int(x) << 1) == 0u; }
+
+// ---------------------------------------------------------------------------
+// Streaming memory access with cache hints.  Inputs that are read once go
+// through the read-only path and are marked evict-first; values re-read soon
+// (forward-sweep intermediates) use the default policy.
+
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
+template <typename T>
+__device__ __forceinline__ T ld_keep(const T* p) { return __ldcg(p); }
+template <typename T>
+__device__ __forceinline__ void st_stream(T* p, T v) { __stcs(p, v); }
+template <typename T>
+__device__ __forceinline__ void st_keep(T* p, T v) { __stcg(p, v); }
+
+// ---------------------------------------------------------------------------
+// Warp helpers.
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T>
+__device__ __forceinline__ T shfl(T v, int lane) { return __shfl_sync(FULL, v, lane); }
+template <typename T>
+__device__ __forceinline__ T shfl_up(T v, int d) { return __shfl_up_sync(FULL, v, d); }
+template <typename T>
+__device__ __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(FULL, v, d); }
+
+}  // namespace tdg

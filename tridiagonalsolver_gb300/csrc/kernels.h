@@ -1,0 +1,51 @@
+// Launchers of the device kernels (host side), one family per .cu file.
+// All are asynchronous on the given stream and return the launch status.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace tdg {
+
+// seq.cu: one thread per system
+template <typename T>
+cudaError_t launch_thomas_seq(int layout, T* a, T* b, T* c, T* d, int n, int batch, cudaStream_t s);
+template <typename T>
+cudaError_t launch_gtsv_seq(int layout, const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv,
+                            int* info, int n, int batch, cudaStream_t s);
+template <typename T>
+cudaError_t launch_gtsv_adjoint(int layout, const T* a, const T* b, const T* c, const T* x, const unsigned* piv,
+                                const T* g, T* ga, T* gb, T* gc, T* gd, T* wz, T* wm, int n, int batch,
+                                cudaStream_t s);
+
+// tw.cu: two-ended sweeps over TMA-staged tiles (CONTIG / INTERLEAVED).
+// *used is false when the arrays cannot be described by tensor maps (the
+// caller then falls back to the seq.cu kernels, or reports an error where
+// the choice must match an earlier call -- see tw_eligible).
+template <typename T>
+cudaError_t launch_thomas_tw(int layout, T* a, T* b, T* c, T* d, int n, int batch, cudaStream_t s, bool* used);
+template <typename T>
+cudaError_t launch_gtsv_tw(int layout, const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv,
+                           int* info, int n, int batch, cudaStream_t s, bool* used);
+template <typename T>
+cudaError_t launch_gtsv_adjoint_tw(int layout, const T* a, const T* b, const T* c, const T* x, const unsigned* piv,
+                                   const T* g, T* ga, T* gb, T* gc, T* gd, T* wz, T* wm, int n, int batch,
+                                   cudaStream_t s, bool* used);
+
+// Whether the two-ended kernels apply, decided on the shape alone (the row
+// stride of a tensor map must be a multiple of 16 bytes).  The pivot record
+// format of the pivoted solve depends on this choice, so the forward solve
+// and its adjoint always agree.
+inline bool tw_eligible(int layout, int n, int batch, int elem) {
+  if (layout == 2) return ((size_t)batch * elem) % 16 == 0;
+  if (layout == 0) return ((size_t)n * elem) % 16 == 0;
+  return false;
+}
+
+// The library's device error word on the current device (allocated on first
+// use, 4 bytes per device), and a synchronous read (optionally clearing it).
+int* error_word();
+cudaError_t read_device_error(int* code, bool reset);
+
+// pivot record: one 32-bit word per 32 rows per system
+inline size_t pivot_words(int n, int batch) { return (size_t)((n + 31) / 32) * (size_t)batch; }
+
+}  // namespace tdg

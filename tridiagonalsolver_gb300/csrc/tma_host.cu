@@ -1,0 +1,66 @@
+// Host-side tensor-map encoding through the driver entry point obtained from
+// the runtime (no link-time dependency on libcuda).
+#include <cudaTypedefs.h>
+#include <mutex>
+
+#include "kernels.h"
+#include "tma.cuh"
+
+namespace tdg {
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+bool encode_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype, int elem_bytes, uint64_t inner,
+                    uint64_t outer, uint64_t outer_stride_bytes, uint32_t box_inner, uint32_t box_outer,
+                    CUtensorMapSwizzle swizzle) {
+  auto fn = encode_fn();
+  if (!fn || !base) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (outer_stride_bytes & 15u) != 0) return false;
+  if (outer_stride_bytes < inner * (uint64_t)elem_bytes || inner == 0 || outer == 0) return false;
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {outer_stride_bytes};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+static std::mutex g_err_mu;
+static int* g_err_words[64] = {};
+
+int* error_word() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  if (!g_err_words[dev]) {
+    int* p = nullptr;
+    if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return nullptr;
+    g_err_words[dev] = p;
+  }
+  return g_err_words[dev];
+}
+
+cudaError_t read_device_error(int* code, bool reset) {
+  *code = 0;
+  int* w = error_word();
+  if (!w) return cudaErrorMemoryAllocation;
+  cudaError_t e = cudaMemcpy(code, w, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && reset && *code != 0) e = cudaMemset(w, 0, sizeof(int));
+  return e;
+}
+
+}  // namespace tdg

@@ -1,0 +1,119 @@
+"""PyTorch front end of libtridiag.so: device memory and streams come from
+torch, all arithmetic from the CUDA kernels of the library.
+
+Arrays are CUDA tensors holding ``batch`` systems of ``n`` rows in one of the
+layouts of include/tridiagonal.h:
+
+* ``"contiguous"`` (reference layout 0): shape ``(batch, n)`` or flat;
+* ``"interleaved"``: shape ``(n, batch)`` or flat (row i of system j at
+  ``i*batch + j``);
+* ``"packed"`` (reference layout 1): one tensor of ``batch*4*n`` elements.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from ._lib import ALGOS, LAYOUTS, check, lib
+
+_DT = {torch.float32: "single", torch.float64: "double"}
+
+
+def _stream_ptr(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def _ptr(t: torch.Tensor | None, dtype=None) -> int | None:
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("tensor must be on a CUDA device")
+    if not t.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"expected {dtype}, got {t.dtype}")
+    return int(t.data_ptr())
+
+
+def _prec(t: torch.Tensor) -> str:
+    if t.dtype not in _DT:
+        raise TypeError(f"unsupported dtype {t.dtype} (float32 or float64)")
+    return _DT[t.dtype]
+
+
+def _dims(t: torch.Tensor, n: int, layout: str) -> int:
+    per = 4 * n if layout == "packed" else n
+    if n <= 0 or t.numel() % per:
+        raise ValueError(f"tensor of {t.numel()} elements does not hold whole systems of n={n}")
+    return t.numel() // per
+
+
+def solve(a, b, c, d, n: int, algo: str = "auto", layout: str = "contiguous", stream=None):
+    """In-place solve with the reference's contract: c may be overwritten,
+    d receives x.  Returns d.  For layout "packed" pass the packed tensor as
+    ``a`` and None for b, c, d (the solution is in rows 3n..4n of each
+    system)."""
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    fn = getattr(lib(), f"tridiag_solve_{p}")
+    st = fn(ALGOS[algo], LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype),
+            _ptr(d, a.dtype), n, batch, _stream_ptr(stream))
+    check(st, f"tridiag_solve_{p}({algo}, {layout})")
+    return d if d is not None else a
+
+
+def gtsv_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
+    batch = _dims(a, n, layout)
+    nbytes = lib().tridiag_gtsv_workspace_size(1 if a.dtype == torch.float64 else 0, LAYOUTS[layout], n, batch)
+    return torch.empty(nbytes, dtype=torch.uint8, device=a.device)
+
+
+def pivot_record(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
+    batch = _dims(a, n, layout)
+    nbytes = lib().tridiag_pivot_record_size(n, batch)
+    return torch.empty(nbytes // 4, dtype=torch.int32, device=a.device)
+
+
+def gtsv(a, b, c, d, n: int, layout: str = "contiguous", pivots=None, info=None, work=None, out=None,
+         stream=None):
+    """Partial-pivoting solve; a, b, c, d are not modified.  Returns x (a new
+    tensor, or ``out``).  ``pivots`` (from :func:`pivot_record`) receives the
+    pivot record for :func:`gtsv_adjoint`; ``info`` (int32, batch) receives
+    0 or k+1 for the first zero pivot of each system."""
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    x = out if out is not None else torch.empty_like(d)
+    if x.data_ptr() != d.data_ptr():
+        x.copy_(d)
+    work = work if work is not None else gtsv_workspace(a, n, layout)
+    st = getattr(lib(), f"tridiag_gtsv_{p}")(
+        LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), _ptr(x, a.dtype),
+        _ptr(pivots), _ptr(info), _ptr(work), work.numel(), n, batch, _stream_ptr(stream))
+    check(st, f"tridiag_gtsv_{p}")
+    return x
+
+
+def gtsv_adjoint(a, b, c, x, pivots, xbar, n: int, layout: str = "contiguous", work=None, stream=None):
+    """Gradients (ga, gb, gc, gd) of L with dL/dx = xbar through x = A^-1 d,
+    reusing the forward call's pivot record."""
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    ga, gb, gc, gd = (torch.empty_like(a) for _ in range(4))
+    work = work if work is not None else gtsv_workspace(a, n, layout)
+    st = getattr(lib(), f"tridiag_gtsv_adjoint_{p}")(
+        LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), _ptr(x, a.dtype), _ptr(pivots),
+        _ptr(xbar, a.dtype), _ptr(ga), _ptr(gb), _ptr(gc), _ptr(gd), _ptr(work), work.numel(), n, batch,
+        _stream_ptr(stream))
+    check(st, f"tridiag_gtsv_adjoint_{p}")
+    return ga, gb, gc, gd
+
+
+def reference_call(name: str, a, b, c, d, n: int):
+    """Call one of the reference's entry points (e.g. "WM5_reg_double") on
+    layout-0 tensors; synchronous like the reference.  Returns d."""
+    batch = _dims(a, n, "contiguous")
+    f = getattr(lib(), name)
+    f(_ptr(a), _ptr(b), _ptr(c), _ptr(d), n, batch)
+    check(_lib.last_status(), name)
+    return d

@@ -32,6 +32,20 @@ extern "C" {
 /* ------------------------------------------------------------------------ */
 /* Part 1: the reference's entry points (Tridiagonal_CUDA/tridiagonal.h).    */
 
+/* WM-pGE (partitioned Gaussian elimination, reduced interface system by
+ * PCR; no pivoting, like the reference) -- replaces
+ * Tridiagonal_CUDA/tridiagonal.h:32,37,42,47 (WM{5,4}_{shmem,reg}; kernels
+ * Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884).  One on-chip kernel serves
+ * all four variants of each precision. */
+void WM5_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void WM4_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void WM5_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void WM4_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void WM5_shmem_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void WM4_shmem_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void WM5_reg_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void WM4_reg_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+
 /* naive Thomas -- replaces Tridiagonal_CUDA/tridiagonal.h:20-21 (kernel
  * Tridiagonal_CUDA/tridiagonal_basic.cu:4-30, wrappers :171-190). */
 void Thomas_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
@@ -58,6 +72,7 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 /* algorithms */
 #define TRIDIAG_ALGO_AUTO 0
 #define TRIDIAG_ALGO_THOMAS 1 /* unpivoted, one thread per system */
+#define TRIDIAG_ALGO_WM 4     /* WM-pGE, one warp per system, unpivoted */
 #define TRIDIAG_ALGO_GTSV 5   /* partial pivoting, one thread per system */
 
 /* Status of the last library call made by the calling host thread. */
@@ -78,6 +93,19 @@ int tridiag_solve_single(int algo, int layout, float *a, float *b, float *c, flo
                          void *stream);
 int tridiag_solve_double(int algo, int layout, double *a, double *b, double *c, double *d, int n_eqt,
                          int n_batch, void *stream);
+
+/* Out-of-place solve: a, b, c, d are read only, x receives the solution.
+ * TRIDIAG_ALGO_WM / AUTO run the on-chip WM-pGE where the shape allows
+ * (contiguous layout) and need no workspace there; shapes it does not cover,
+ * and TRIDIAG_ALGO_THOMAS / GTSV, use `work` of
+ * tridiag_solve_out_workspace_size() bytes.  The packed layout is not
+ * supported here. */
+size_t tridiag_solve_out_workspace_size(int precision, int algo, int layout, int n_eqt, int n_batch);
+int tridiag_solve_out_single(int algo, int layout, const float *a, const float *b, const float *c, const float *d,
+                             float *x, void *work, size_t work_bytes, int n_eqt, int n_batch, void *stream);
+int tridiag_solve_out_double(int algo, int layout, const double *a, const double *b, const double *c,
+                             const double *d, double *x, void *work, size_t work_bytes, int n_eqt, int n_batch,
+                             void *stream);
 
 /* Bytes of workspace tridiag_gtsv_* needs (precision: 0 = single, 1 = double). */
 size_t tridiag_gtsv_workspace_size(int precision, int layout, int n_eqt, int n_batch);

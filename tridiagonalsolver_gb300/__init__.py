@@ -6,9 +6,11 @@ entry points plus extensions).  This package loads it with ctypes and offers
 PyTorch-tensor wrappers; it has no CPU fallback.
 """
 from ._lib import ALGOS, LAYOUTS, LIB_PATH, TridiagError, check, last_status, lib
-from .ops import gtsv, gtsv_adjoint, gtsv_workspace, pivot_record, reference_call, solve
+from .ops import (gtsv, gtsv_adjoint, gtsv_workspace, pivot_record, reference_call, solve, solve_out,
+                  solve_out_workspace)
 
 __all__ = [
     "ALGOS", "LAYOUTS", "LIB_PATH", "TridiagError", "check", "last_status", "lib",
-    "gtsv", "gtsv_adjoint", "gtsv_workspace", "pivot_record", "reference_call", "solve",
+    "gtsv", "gtsv_adjoint", "gtsv_workspace", "pivot_record", "reference_call", "solve", "solve_out",
+    "solve_out_workspace",
 ]

@@ -41,6 +41,9 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_solve_single": (_I, [_I, _I, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_solve_double": (_I, [_I, _I, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_gtsv_workspace_size": (_SZ, [_I, _I, _I, _I]),
+    "tridiag_solve_out_workspace_size": (_SZ, [_I, _I, _I, _I, _I]),
+    "tridiag_solve_out_single": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_solve_out_double": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_pivot_record_size": (_SZ, [_I, _I]),
     "tridiag_gtsv_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_gtsv_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
@@ -48,7 +51,11 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_gtsv_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
-REFERENCE_SOLVERS = ["Thomas_single", "Thomas_double"]
+REFERENCE_SOLVERS = [
+    "Thomas_single", "Thomas_double",
+    "WM5_shmem_single", "WM4_shmem_single", "WM5_reg_single", "WM4_reg_single",
+    "WM5_shmem_double", "WM4_shmem_double", "WM5_reg_double", "WM4_reg_double",
+]
 for _name in REFERENCE_SOLVERS:
     SIGNATURES[_name] = (None, _REF_SIG)
 

@@ -118,6 +118,15 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
       if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
       return cuda_status(e);
     }
+    case TRIDIAG_ALGO_WM: {
+      bool used = false;
+      cudaError_t e = tdg::launch_wm_warp<T>(layout, a, b, c, d, d, n, batch, s, &used);
+      if (e == cudaSuccess && !used) {
+        e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
+        if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
+      }
+      return cuda_status(e);
+    }
     case TRIDIAG_ALGO_GTSV: {
       size_t bytes = gtsv_ws_bytes<T>(n, batch);
       void* work = nullptr;
@@ -128,6 +137,55 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
       e = cudaFreeAsync(work, s);
       if (st == TRIDIAG_SUCCESS && e != cudaSuccess) st = TRIDIAG_ERR_CUDA;
       return st;
+    }
+    default:
+      return TRIDIAG_ERR_INVALID_VALUE;
+  }
+}
+
+// Out-of-place solve: a, b, c, d untouched, x receives the solution.  The
+// on-chip algorithms need no workspace; the sweeps that spill (Thomas) copy
+// d into x and use `work` for the c' spill.
+template <typename T>
+size_t solve_out_ws(int algo, int n, int batch) {
+  if (algo == TRIDIAG_ALGO_THOMAS) return align_up((size_t)n * (size_t)batch * sizeof(T));
+  if (algo == TRIDIAG_ALGO_GTSV) return gtsv_ws_bytes<T>(n, batch);
+  return 0;
+}
+
+template <typename T>
+int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, const T* d, T* x, void* work,
+                   size_t work_bytes, int n, int batch, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !b || !c || !d || !x) return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout == TRIDIAG_LAYOUT_PACKED) return TRIDIAG_ERR_NOT_SUPPORTED;
+  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_WM;
+  if (work_bytes < solve_out_ws<T>(algo, n, batch) || (solve_out_ws<T>(algo, n, batch) && !work))
+    return TRIDIAG_ERR_WORKSPACE;
+  switch (algo) {
+    case TRIDIAG_ALGO_WM: {
+      bool used = false;
+      cudaError_t e = tdg::launch_wm_warp<T>(layout, a, b, c, d, x, n, batch, s, &used);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      if (used) return TRIDIAG_SUCCESS;
+      if (!work || work_bytes < solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, n, batch)) return TRIDIAG_ERR_WORKSPACE;
+      algo = TRIDIAG_ALGO_THOMAS;
+    }
+      // fall through: shapes beyond the on-chip kernel use the Thomas sweep
+    case TRIDIAG_ALGO_THOMAS: {
+      T* cs = static_cast<T*>(work);
+      size_t bytes = (size_t)n * (size_t)batch * sizeof(T);
+      if (cudaMemcpyAsync(cs, c, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      if (x != d && cudaMemcpyAsync(x, d, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      bool used = false;
+      cudaError_t e = tdg::launch_thomas_tw<T>(layout, const_cast<T*>(a), const_cast<T*>(b), cs, x, n, batch, s, &used);
+      if (e == cudaSuccess && !used)
+        e = tdg::launch_thomas_seq<T>(layout, const_cast<T*>(a), const_cast<T*>(b), cs, x, n, batch, s);
+      return cuda_status(e);
+    }
+    case TRIDIAG_ALGO_GTSV: {
+      size_t bytes = (size_t)n * (size_t)batch * sizeof(T);
+      if (x != d && cudaMemcpyAsync(x, d, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      return gtsv_impl<T>(layout, a, b, c, x, nullptr, nullptr, work, work_bytes, n, batch, s);
     }
     default:
       return TRIDIAG_ERR_INVALID_VALUE;
@@ -179,6 +237,22 @@ void Thomas_double(double* a, double* b, double* c, double* d, int n, int batch)
   sync_call([&] { return solve_impl<double>(TRIDIAG_ALGO_THOMAS, TRIDIAG_LAYOUT_CONTIGUOUS, a, b, c, d, n, batch, 0); });
 }
 
+#define TDG_REF_ENTRY(NAME, T, ALGO)                                                                        \
+  void NAME(T* a, T* b, T* c, T* d, int n, int batch) {                                                    \
+    sync_call([&] { return solve_impl<T>(ALGO, TRIDIAG_LAYOUT_CONTIGUOUS, a, b, c, d, n, batch, 0); });    \
+  }
+// WM-pGE -- replace Tridiagonal_CUDA/tridiagonal.h:32,37,42,47 (shmem/reg, 5/4 rounds; kernels
+// Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884, wrappers :1437-1569).  All four names run the
+// on-chip WM-pGE of wm.cu; the round count of the reference is a tile-shape choice there.
+TDG_REF_ENTRY(WM5_shmem_single, float, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM4_shmem_single, float, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM5_reg_single, float, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM4_reg_single, float, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM5_shmem_double, double, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM4_shmem_double, double, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM5_reg_double, double, TRIDIAG_ALGO_WM)
+TDG_REF_ENTRY(WM4_reg_double, double, TRIDIAG_ALGO_WM)
+
 // ---- extensions ---------------------------------------------------------------
 
 int tridiag_solve_single(int algo, int layout, float* a, float* b, float* c, float* d, int n, int batch,
@@ -188,6 +262,23 @@ int tridiag_solve_single(int algo, int layout, float* a, float* b, float* c, flo
 int tridiag_solve_double(int algo, int layout, double* a, double* b, double* c, double* d, int n, int batch,
                          void* stream) {
   return set_status(solve_impl<double>(algo, layout, a, b, c, d, n, batch, (cudaStream_t)stream));
+}
+
+size_t tridiag_solve_out_workspace_size(int precision, int algo, int layout, int n, int batch) {
+  (void)layout;
+  if (!valid_dims(n, batch)) return 0;
+  if (algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM) algo = TRIDIAG_ALGO_THOMAS;  // possible fallback
+  return precision ? solve_out_ws<double>(algo, n, batch) : solve_out_ws<float>(algo, n, batch);
+}
+
+int tridiag_solve_out_single(int algo, int layout, const float* a, const float* b, const float* c, const float* d,
+                             float* x, void* work, size_t work_bytes, int n, int batch, void* stream) {
+  return set_status(solve_out_impl<float>(algo, layout, a, b, c, d, x, work, work_bytes, n, batch, (cudaStream_t)stream));
+}
+int tridiag_solve_out_double(int algo, int layout, const double* a, const double* b, const double* c,
+                             const double* d, double* x, void* work, size_t work_bytes, int n, int batch,
+                             void* stream) {
+  return set_status(solve_out_impl<double>(algo, layout, a, b, c, d, x, work, work_bytes, n, batch, (cudaStream_t)stream));
 }
 
 size_t tridiag_gtsv_workspace_size(int precision, int layout, int n, int batch) {

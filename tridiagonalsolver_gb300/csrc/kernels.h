@@ -45,6 +45,12 @@ inline bool tw_eligible(int layout, int n, int batch, int elem) {
 int* error_word();
 cudaError_t read_device_error(int* code, bool reset);
 
+// wm.cu: WM-pGE, one warp per system (CONTIG / PACKED, n <= 1024 FP32,
+// 512 FP64).  x may alias d.  *used is false when the shape is not covered.
+template <typename T>
+cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                           cudaStream_t st, bool* used);
+
 // pivot record: one 32-bit word per 32 rows per system
 inline size_t pivot_words(int n, int batch) { return (size_t)((n + 31) / 32) * (size_t)batch; }
 

@@ -1,0 +1,441 @@
+// WM-pGE: partitioned Gaussian elimination with the reduced interface
+// system solved by PCR, one warp per system, everything on chip.
+//
+// Lane t owns a contiguous chunk of m rows [s, e] in registers (HBM traffic
+// is the algorithmic 5n: read a, b, c, d once, write x once).  The last row
+// e of every chunk is a separator; the rows [s, e-1] are the chunk's
+// interior.  With x_L = x_{s-1} (previous separator) and x_R = x_e:
+//   * a bottom-up elimination of the interior gives the first interior row
+//     as x_s = y''_s - a''_s x_L + v''_s x_R (needed by lane t-1);
+//   * a top-down elimination gives x_i = y'_i + w'_i x_L - c'_i x_{i+1}
+//     (kept in registers for the back substitution);
+//   * substituting both into separator row e gives one tridiagonal equation
+//     per lane in the separators, solved by 5 PCR steps over warp shuffles;
+//   * each lane back-substitutes its interior from (x_L, x_R).
+// The reduced system inherits diagonal dominance from A, so PCR needs no
+// pivoting for the dominant systems this kernel serves.
+//
+// Reference: the WM-pGE ("Wang-Mou partition + parallel GE") kernels,
+// Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884, and their CPU versions
+// Tridiagonal_AVX512/tridiagonal_d_avx512.cpp:74-416 (block elimination over
+// a partition, cross-block elimination, per-block back sweep).  The reference
+// streams 64-row tiles through a warp and spills c', d' to global memory;
+// this version keeps the whole system in registers.
+#include "common.cuh"
+#include "kernels.h"
+#include "tw.cuh"
+
+namespace tdg {
+
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using V = float4;
+  static constexpr int N = 4;
+  __device__ static __forceinline__ float get(const V& v, int q) {
+    return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
+  }
+  template <int M>
+  __device__ static __forceinline__ V make(const float (&r)[M], int k) {
+    return make_float4(r[k], r[k + 1], r[k + 2], r[k + 3]);
+  }
+};
+template <>
+struct Vec16<double> {
+  using V = double2;
+  static constexpr int N = 2;
+  __device__ static __forceinline__ double get(const V& v, int q) { return q == 0 ? v.x : v.y; }
+  template <int M>
+  __device__ static __forceinline__ V make(const double (&r)[M], int k) {
+    return make_double2(r[k], r[k + 1]);
+  }
+};
+
+// Load rows [s, s+M) of one array into registers (rows outside [s, s+m) get
+// `fill`).  With vec, n and m are multiples of the vector width, so a
+// chunk's valid length is too and no vector load crosses the end of a
+// system.
+template <typename T, int M, bool RO>
+__device__ __forceinline__ void load_chunk(T (&r)[M], const T* p, int s, int m, bool vec, T fill) {
+  using W = Vec16<T>;
+  constexpr int NV = W::N;
+  if (vec) {
+#pragma unroll
+    for (int k = 0; k < M; k += NV) {
+      if (k < m) {
+        const typename W::V* pp = reinterpret_cast<const typename W::V*>(p + s + k);
+        const typename W::V v = RO ? __ldg(pp) : *pp;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) r[k + q] = W::get(v, q);
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) r[k + q] = fill;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; ++k) r[k] = k < m ? (RO ? __ldg(p + s + k) : p[s + k]) : fill;
+  }
+}
+
+template <typename T, int M>
+__device__ __forceinline__ void store_chunk(const T (&r)[M], T* p, int s, int m, bool vec) {
+  using W = Vec16<T>;
+  constexpr int NV = W::N;
+  if (vec) {
+#pragma unroll
+    for (int k = 0; k < M; k += NV)
+      if (k < m) *reinterpret_cast<typename W::V*>(p + s + k) = W::make(r, k);
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; ++k)
+      if (k < m) p[s + k] = r[k];
+  }
+}
+
+// PCR over segments of G lanes of a warp (G = 4..32, one system per
+// segment): equation alpha x_{t-1} + beta x_t + gamma x_{t+1} = delta per
+// lane, t = lane % G; returns x_t.
+template <typename T, int G>
+__device__ __forceinline__ T warp_pcr(T al, T be, T ga, T de, int tl) {
+#pragma unroll
+  for (int s = 1; s < G; s <<= 1) {
+    T aL = __shfl_up_sync(FULL, al, s, G), bL = __shfl_up_sync(FULL, be, s, G);
+    T gL = __shfl_up_sync(FULL, ga, s, G), dL = __shfl_up_sync(FULL, de, s, G);
+    T aR = __shfl_down_sync(FULL, al, s, G), bR = __shfl_down_sync(FULL, be, s, G);
+    T gR = __shfl_down_sync(FULL, ga, s, G), dR = __shfl_down_sync(FULL, de, s, G);
+    if (tl < s) { aL = T(0); bL = T(1); gL = T(0); dL = T(0); }
+    if (tl + s >= G) { aR = T(0); bR = T(1); gR = T(0); dR = T(0); }
+    const T k1 = al * Div<T>(bL).inv();
+    const T k2 = ga * Div<T>(bR).inv();
+    const T nb = fma(-k2, aR, fma(-k1, gL, be));
+    const T nd = fma(-k2, dR, fma(-k1, dL, de));
+    al = -k1 * aL;
+    ga = -k2 * gR;
+    be = nb;
+    de = nd;
+  }
+  return Div<T>(be).div(de);
+}
+
+// The per-lane WM-pGE solve of one system whose chunk (m rows starting at
+// row s) is already in registers A, B, C, D; returns x of the chunk in X.
+template <typename T, int M, int G>
+__device__ __forceinline__ void wm_lane_solve(T (&A)[M], T (&B)[M], T (&C)[M], T (&D)[M], T (&X)[M], int n, int s,
+                                              int m, int mt, int lane) {
+  if (s == 0) A[0] = T(0);             // a_0 is not part of the system
+  const int last = n - 1 - s;          // local index of row n-1 (if in this chunk)
+#pragma unroll
+  for (int k = 0; k < M; ++k)
+    if (k == last) C[k] = T(0);        // c_{n-1} is not part of the system
+  const int ni = mt - 1;               // interior rows [0, ni)
+
+  // bottom-up over the interior: first-row coefficients
+  T ap = T(0), yp = T(0), vp = T(0);
+#pragma unroll
+  for (int kk = 0; kk < M - 1; ++kk) {
+    const int k = M - 2 - kk;
+    if (k < ni) {
+      const bool lastrow = (k == ni - 1);
+      const T ck = lastrow ? T(0) : C[k];  // coupling to x_R handled by v''
+      const Div<T> q(fma(-ck, ap, B[k]));
+      const T nap = q.div(A[k]);
+      const T nyp = q.div(fma(-ck, yp, D[k]));
+      const T nvp = lastrow ? -q.div(C[k]) : -q.div(ck * vp);
+      ap = nap;
+      yp = nyp;
+      vp = nvp;
+    }
+  }
+  // first interior row of this chunk: x_s = yp - ap x_L + vp x_R;
+  // an empty interior means the "first interior row" is the separator itself
+  const T f_y = ni > 0 ? yp : T(0);
+  const T f_a = ni > 0 ? ap : T(0);
+  const T f_v = ni > 0 ? vp : T(1);
+
+  // top-down over the interior: c' -> C, y' -> D, w' -> A
+  T cp = T(0), yq = T(0), wq = T(0);
+#pragma unroll
+  for (int k = 0; k < M - 1; ++k) {
+    if (k < ni) {
+      const T ak = A[k];
+      const Div<T> q(fma(-ak, cp, B[k]));
+      cp = q.div(C[k]);
+      yq = q.div(fma(-ak, yq, D[k]));
+      wq = k == 0 ? -q.div(ak) : -q.div(ak * wq);
+      C[k] = cp;
+      D[k] = yq;
+      A[k] = wq;
+    }
+  }
+  // last interior row: x_{e-1} = yq + wq x_L - cp x_R (empty interior: x_{e-1} = x_L)
+  const T l_y = ni > 0 ? yq : T(0);
+  const T l_w = ni > 0 ? wq : T(1);
+  const T l_c = ni > 0 ? cp : T(0);
+
+  // separator row e = s + ni
+  T ae = T(0), be = T(1), ce = T(0), de = T(0);
+#pragma unroll
+  for (int k = 0; k < M; ++k)
+    if (k == ni) { ae = A[k]; be = B[k]; ce = C[k]; de = D[k]; }
+  const T n_y = __shfl_down_sync(FULL, f_y, 1, G), n_a = __shfl_down_sync(FULL, f_a, 1, G);
+  const T n_v = __shfl_down_sync(FULL, f_v, 1, G);
+  const bool has_next = (lane < G - 1) && (s + m < n);
+  T al, bt, gm, dl;
+  if (mt > 0) {
+    al = ae * l_w;
+    bt = fma(-ae, l_c, be);
+    dl = fma(-ae, l_y, de);
+    gm = T(0);
+    if (has_next) {
+      bt = fma(-ce, n_a, bt);
+      dl = fma(-ce, n_y, dl);
+      gm = ce * n_v;
+    }
+  } else {
+    al = T(0); bt = T(1); gm = T(0); dl = T(0);
+  }
+  const T xe = warp_pcr<T, G>(al, bt, gm, dl, lane);
+  T xL = __shfl_up_sync(FULL, xe, 1, G);
+  if (lane == 0) xL = T(0);
+
+  // back substitution: x_e, then interior from the top-down coefficients
+  T xn = xe;
+#pragma unroll
+  for (int kk = 0; kk < M; ++kk) {
+    const int k = M - 1 - kk;
+    if (k == ni) X[k] = xe;
+    if (k < ni) {
+      xn = fma(A[k], xL, fma(-C[k], xn, D[k]));
+      X[k] = xn;
+    }
+  }
+}
+
+// One warp per system, direct (L1-cached) loads; any n with m <= M.
+// Layout CONTIG (stride n between systems) or PACKED (stride 4n; the
+// caller passes the four array pointers of system 0).
+template <typename T, int M>
+__global__ void __launch_bounds__(128) wm_warp_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                      const T* __restrict__ c, const T* d, T* x, int n, int batch,
+                                                      size_t sys_stride, int m, bool vec) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= batch) return;
+  const size_t base = (size_t)j * sys_stride;
+  const int s = lane * m;
+  const int mt = max(0, min(m, n - s));  // rows of this lane's chunk
+  T A[M], B[M], C[M], D[M], X[M];
+  load_chunk<T, M, true>(A, a + base, s, mt, vec, T(0));
+  load_chunk<T, M, true>(B, b + base, s, mt, vec, T(1));
+  load_chunk<T, M, true>(C, c + base, s, mt, vec, T(0));
+  load_chunk<T, M, false>(D, d + base, s, mt, vec, T(0));
+  wm_lane_solve<T, M, 32>(A, B, C, D, X, n, s, m, mt, lane);
+  store_chunk<T, M>(X, x + base, s, mt, vec);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent TMA-fed variant for n = G*m (G = 4..32 lanes per system, m rows
+// per lane, m*sizeof(T) in {16, 32, 64, 128} bytes).  Each array is viewed
+// as a 2-D tensor of G*batch chunk rows of m elements; one box {m, 32} holds
+// the 32/G systems of one warp.  The chunk width picks the shared-memory
+// swizzle (none / 32B / 64B / 128B) that makes each lane's 16-byte reads of
+// its own chunk conflict free.  Every warp runs a ring of WM_SLOTS input
+// buffers; a buffer is refilled as soon as its lanes have read it, so
+// WM_SLOTS-1 loads stay in flight while the warp solves, and x leaves
+// through a separate buffer by TMA store.
+constexpr int WM_SLOTS = 3;
+
+template <typename T, int M>
+struct WmSlot {
+  alignas(1024) T buf[4][32 * M];
+};
+template <typename T, int M>
+struct WmOut {
+  alignas(1024) T buf[32 * M];
+};
+
+// warps per CTA: as many as fit their buffers in 210 KB, at most 8
+template <typename T, int M>
+constexpr int wm_warps() {
+  return (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 8 <= 215040 ? 8
+         : (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 4 <= 215040 ? 4 : 2;
+}
+
+// byte offset of (chunk row t, 16-byte unit q) under the TMA swizzle whose
+// span equals the row width
+template <int ROWB>
+__device__ __forceinline__ int wm_swz(int t, int q) {
+  const int logical = t * ROWB + q * 16;
+  constexpr int mask = ROWB >= 128 ? 7 : ROWB == 64 ? 3 : ROWB == 32 ? 1 : 0;
+  return logical ^ (((logical >> 7) & mask) << 4);
+}
+
+template <typename T, int M, int G>
+__global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
+    wm_tma_kernel(const __grid_constant__ TwMaps maps, int n, int nboxes, int* err) {
+  constexpr int WARPS = wm_warps<T, M>();
+  using W = Vec16<T>;
+  constexpr int NV = W::N;
+  constexpr int ROWB = M * (int)sizeof(T);
+  constexpr int BYTES = 32 * M * (int)sizeof(T);
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WmSlot<T, M>* slots = reinterpret_cast<WmSlot<T, M>*>(base) + warp * WM_SLOTS;
+  WmOut<T, M>* out = reinterpret_cast<WmOut<T, M>*>(base + sizeof(WmSlot<T, M>) * WM_SLOTS * WARPS) + warp;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * WARPS) +
+                   warp * WM_SLOTS;
+  const int gw = blockIdx.x * WARPS + warp, nw = gridDim.x * WARPS;
+  if (lane == 0) {
+    for (int q = 0; q < WM_SLOTS; ++q) mbar_init(&bars[q], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  auto load = [&](int i, int q) {  // box i of this warp -> slot q
+    const int bx = gw + i * nw;
+    mbar_arrive_expect_tx(&bars[q], 4 * BYTES);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tma_load_2d(slots[q].buf[k], &maps.m[k], 0, bx * 32, &bars[q]);
+  };
+  const int count = gw < nboxes ? (nboxes - gw + nw - 1) / nw : 0;
+  if (lane == 0)
+    for (int i = 0; i < count && i < WM_SLOTS; ++i) load(i, i);
+  const int tl = lane % G;
+  unsigned parity = 0;
+  for (int i = 0; i < count; ++i) {
+    const int q = i % WM_SLOTS;
+    const bool ok = __all_sync(FULL, mbar_wait(&bars[q], (parity >> q) & 1u, err));
+    parity ^= 1u << q;
+    if (!ok) break;
+    T A[M], B[M], C[M], D[M], X[M];
+#pragma unroll
+    for (int u = 0; u < M / NV; ++u) {
+      const int off = wm_swz<ROWB>(lane, u);
+      const typename W::V va = *reinterpret_cast<const typename W::V*>(reinterpret_cast<unsigned char*>(slots[q].buf[0]) + off);
+      const typename W::V vb = *reinterpret_cast<const typename W::V*>(reinterpret_cast<unsigned char*>(slots[q].buf[1]) + off);
+      const typename W::V vc = *reinterpret_cast<const typename W::V*>(reinterpret_cast<unsigned char*>(slots[q].buf[2]) + off);
+      const typename W::V vd = *reinterpret_cast<const typename W::V*>(reinterpret_cast<unsigned char*>(slots[q].buf[3]) + off);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        A[u * NV + v] = W::get(va, v);
+        B[u * NV + v] = W::get(vb, v);
+        C[u * NV + v] = W::get(vc, v);
+        D[u * NV + v] = W::get(vd, v);
+      }
+    }
+    __syncwarp();
+    // the slot is free again: refill it with the box WM_SLOTS ahead
+    if (lane == 0 && i + WM_SLOTS < count) load(i + WM_SLOTS, q);
+    wm_lane_solve<T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
+    if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < M / NV; ++u) {
+      const int off = wm_swz<ROWB>(lane, u);
+      *reinterpret_cast<typename W::V*>(reinterpret_cast<unsigned char*>(out->buf) + off) = W::make(X, u * NV);
+    }
+    fence_async_smem();
+    __syncwarp();
+    if (lane == 0) {
+      tma_store_2d(&maps.m[4], 0, (gw + i * nw) * 32, out->buf);
+      bulk_commit();
+    }
+  }
+  if (lane == 0) bulk_wait_all();
+}
+
+template <typename T, int M, int G>
+static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch, cudaStream_t st,
+                            cudaError_t* e) {
+  constexpr int ROWB = M * (int)sizeof(T);
+  constexpr int WARPS = wm_warps<T, M>();
+  const CUtensorMapSwizzle sw = ROWB == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                : ROWB == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                                             : CU_TENSOR_MAP_SWIZZLE_NONE;
+  const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const uint64_t rows = (uint64_t)G * batch;  // chunk rows
+  TwMaps maps;
+  const T* ptrs[5] = {a, b, c, d, x};
+  for (int k = 0; k < 5; ++k)
+    if (!encode_tmap_2d(&maps.m[k], ptrs[k], dt, sizeof(T), (uint64_t)M, rows, (uint64_t)M * sizeof(T), M, 32, sw))
+      return false;
+  const int nboxes = (int)((rows + 31) / 32);
+  const size_t smem =
+      (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * WARPS + 8 * WM_SLOTS * WARPS + 1024;
+  *e = cudaFuncSetAttribute(wm_tma_kernel<T, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (*e != cudaSuccess) return true;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int need = (nboxes + WARPS - 1) / WARPS;
+  const int grid = need < sms ? need : sms;
+  wm_tma_kernel<T, M, G><<<grid, 32 * WARPS, smem, st>>>(maps, n, nboxes, error_word());
+  *e = cudaGetLastError();
+  return true;
+}
+
+template <typename T, int M>
+static cudaError_t launch_wm_m(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                               size_t stride, int m, cudaStream_t st) {
+  constexpr int NV = Vec16<T>::N;
+  const bool vec = (m % NV == 0) && (n % NV == 0) && (stride % NV == 0) &&
+                   ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(c) |
+                     reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(x)) %
+                        16 ==
+                    0);
+  const int warps_per_block = 4;
+  dim3 grid((batch + warps_per_block - 1) / warps_per_block);
+  wm_warp_kernel<T, M><<<grid, 32 * warps_per_block, 0, st>>>(a, b, c, d, x, n, batch, stride, m, vec);
+  return cudaGetLastError();
+}
+
+// Chunk length m = ceil(n/32) (at least 2 rows), rounded up to the vector
+// width when that keeps all 32 chunks within n; the template M is the
+// smallest supported bound >= m.
+template <typename T>
+cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                           cudaStream_t st, bool* used) {
+  *used = false;
+  if (layout != CONTIG && layout != PACKED) return cudaSuccess;
+  constexpr int NV = Vec16<T>::N;
+  // whole-system TMA boxes: CONTIG, n = G*m with 16 rows per lane preferred
+  // (FP64: 8), G in {4, 8, 16, 32}; x may alias d (each warp reads a box
+  // completely before its x leaves)
+  if (layout == CONTIG) {
+    cudaError_t e = cudaSuccess;
+    bool done = false;
+    constexpr int MP = sizeof(T) == 4 ? 16 : 8;  // preferred rows per lane
+    if (n == 4 * MP) done = launch_wm_tma_m<T, MP, 4>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 8 * MP) done = launch_wm_tma_m<T, MP, 8>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 16 * MP) done = launch_wm_tma_m<T, MP, 16>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 32 * MP) done = launch_wm_tma_m<T, MP, 32>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 64 * MP) done = launch_wm_tma_m<T, 2 * MP, 32>(a, b, c, d, x, n, batch, st, &e);
+    if (done) {
+      *used = true;
+      return e;
+    }
+  }
+  int m = (n + 31) / 32;
+  if (m < 2) m = 2;
+  const size_t stride = layout == PACKED ? 4 * (size_t)n : (size_t)n;
+  const int maxm = sizeof(T) == 4 ? 32 : 16;
+  if (n % NV == 0 && ((m + NV - 1) / NV) * NV <= maxm) m = ((m + NV - 1) / NV) * NV;
+  if (m > maxm) return cudaSuccess;
+  *used = true;
+  if (m <= 4) return launch_wm_m<T, 4>(a, b, c, d, x, n, batch, stride, m, st);
+  if (m <= 8) return launch_wm_m<T, 8>(a, b, c, d, x, n, batch, stride, m, st);
+  if (m <= 16) return launch_wm_m<T, 16>(a, b, c, d, x, n, batch, stride, m, st);
+  if constexpr (sizeof(T) == 4) return launch_wm_m<T, 32>(a, b, c, d, x, n, batch, stride, m, st);
+  *used = false;
+  return cudaSuccess;
+}
+
+template cudaError_t launch_wm_warp<float>(int, const float*, const float*, const float*, const float*, float*, int,
+                                           int, cudaStream_t, bool*);
+template cudaError_t launch_wm_warp<double>(int, const double*, const double*, const double*, const double*, double*,
+                                            int, int, cudaStream_t, bool*);
+
+}  // namespace tdg

@@ -63,6 +63,27 @@ def solve(a, b, c, d, n: int, algo: str = "auto", layout: str = "contiguous", st
     return d if d is not None else a
 
 
+def solve_out_workspace(a: torch.Tensor, n: int, algo: str = "auto", layout: str = "contiguous") -> torch.Tensor:
+    batch = _dims(a, n, layout)
+    nbytes = lib().tridiag_solve_out_workspace_size(1 if a.dtype == torch.float64 else 0, ALGOS[algo],
+                                                     LAYOUTS[layout], n, batch)
+    return torch.empty(max(nbytes, 1), dtype=torch.uint8, device=a.device)
+
+
+def solve_out(a, b, c, d, n: int, algo: str = "auto", layout: str = "contiguous", out=None, work=None,
+              stream=None):
+    """Out-of-place solve: a, b, c, d untouched; returns x (new or ``out``)."""
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    x = out if out is not None else torch.empty_like(d)
+    work = work if work is not None else solve_out_workspace(a, n, algo, layout)
+    st = getattr(lib(), f"tridiag_solve_out_{p}")(
+        ALGOS[algo], LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), _ptr(d, a.dtype),
+        _ptr(x, a.dtype), _ptr(work), work.numel(), n, batch, _stream_ptr(stream))
+    check(st, f"tridiag_solve_out_{p}({algo}, {layout})")
+    return x
+
+
 def gtsv_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
     batch = _dims(a, n, layout)
     nbytes = lib().tridiag_gtsv_workspace_size(1 if a.dtype == torch.float64 else 0, LAYOUTS[layout], n, batch)

@@ -140,6 +140,28 @@ int tridiag_gtsv_adjoint_double(int layout, const double *a, const double *b, co
                                 double *gc, double *gd, void *work, size_t work_bytes, int n_eqt, int n_batch,
                                 void *stream);
 
+/* Size of the static scratch array of tridiag_gtsv_noalloc_* (32 MiB). */
+#define TRIDIAG_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* Partial-pivoting solve that allocates no device memory (no counterpart in
+ * the reference).  For callers that cannot allocate where they solve -- a
+ * loop with a hard latency budget, in which cudaMalloc may synchronise the
+ * device, or a process whose GPU memory belongs to another allocator or a
+ * fixed quota.  Arguments and results as tridiag_gtsv_* (d: right-hand side
+ * in, x out; info may be NULL), without pivot record or workspace: the
+ * scratch is one static device array of TRIDIAG_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library holds until exit.  The first call on a
+ * device looks up that array's device address; make it before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU
+ * race and must be serialised by the caller.  Returns TRIDIAG_ERR_WORKSPACE,
+ * launching nothing, when 2*n*batch*sizeof(T) plus the pivot bits (each
+ * rounded up to 256 bytes) exceed the array.  Returns its status directly
+ * (tridiag_last_status() is not updated). */
+int tridiag_gtsv_noalloc_single(int layout, const float *a, const float *b, const float *c, float *d, int *info,
+                                int n_eqt, int n_batch, void *stream);
+int tridiag_gtsv_noalloc_double(int layout, const double *a, const double *b, const double *c, double *d,
+                                int *info, int n_eqt, int n_batch, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

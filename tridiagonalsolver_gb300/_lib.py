@@ -49,6 +49,8 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_gtsv_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_gtsv_adjoint_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_gtsv_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_gtsv_noalloc_single": (_I, [_I, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_gtsv_noalloc_double": (_I, [_I, _P, _P, _P, _P, _P, _I, _I, _P]),
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
 REFERENCE_SOLVERS = [

@@ -32,6 +32,27 @@ extern "C" {
 /* ------------------------------------------------------------------------ */
 /* Part 1: the reference's entry points (Tridiagonal_CUDA/tridiagonal.h).    */
 
+/* cuSPARSE gtsv2StridedBatch, the reference's vendor row -- replaces
+ * Tridiagonal_CUDA/tridiagonal.h:8-12 (Tridiagonal_CUDA/tridiagonal_basic.cu:
+ * 207-246): NVIDIA's library solve with the same init (handle + library
+ * workspace, returns 0 or an error) / synchronous solve / final protocol.
+ * Status of the last cuSparse_* call: tridiag_vendor_last_status(). */
+int cuSparse_init_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+int cuSparse_init_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void cuSparse_final(void);
+void cuSparse_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void cuSparse_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+int tridiag_vendor_last_status(void);
+
+/* BPLG -- replaces Tridiagonal_CUDA/tridiagonal.h:14-17 (FP32, packed
+ * layout 1: [batch][a|b|c|d][n] at a_gbl; b_gbl, c_gbl, d_gbl are ignored,
+ * x lands in the d rows).  Served by this library's kernels: BPLG_WM ->
+ * WM-pGE, BPLG_CR and BPLG_LF -> CR-PCR, BPLG_PCR -> PCR-pThomas. */
+void BPLG_WM(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void BPLG_LF(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void BPLG_CR(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void BPLG_PCR(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+
 /* WM-pGE (partitioned Gaussian elimination, reduced interface system by
  * PCR; no pivoting, like the reference) -- replaces
  * Tridiagonal_CUDA/tridiagonal.h:32,37,42,47 (WM{5,4}_{shmem,reg}; kernels
@@ -45,6 +66,39 @@ void WM5_shmem_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl
 void WM4_shmem_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
 void WM5_reg_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
 void WM4_reg_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+
+/* PCR-pThomas (5 PCR steps split the system into 32 interleaved chains,
+ * each solved by Thomas) -- replaces Tridiagonal_CUDA/tridiagonal.h:33-34,
+ * 38-39,43-44,48-49 (PCR{5,4}_{shmem,reg}; kernels
+ * Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:886-1431).  One on-chip kernel
+ * serves all four variants of each precision. */
+void PCR5_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void PCR4_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void PCR5_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void PCR4_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void PCR5_shmem_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void PCR4_shmem_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void PCR5_reg_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void PCR4_reg_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+
+/* CR -- replaces Tridiagonal_CUDA/tridiagonal.h:24-28 (global-memory cyclic
+ * reduction, Tridiagonal_CUDA/tridiagonal_basic.cu:32-204) and the
+ * register-packed CR_reg{4,8,16} of tridiagonal.h:50-55
+ * (Tridiagonal_CUDA/tridiagonal_onchip.cu:218-820).  All run the on-chip
+ * CR-PCR hybrid (cyclic reduction in registers, warp PCR on the reduced
+ * rows).  It needs no scratch: CR_init_* validates the sizes and returns 0
+ * without allocating, CR_final does nothing. */
+int CR_init_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+int CR_init_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void CR_final(void);
+void CR_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void CR_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void CR_reg4_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void CR_reg8_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void CR_reg16_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, int n_eqt, int n_batch);
+void CR_reg4_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void CR_reg8_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
+void CR_reg16_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 
 /* naive Thomas -- replaces Tridiagonal_CUDA/tridiagonal.h:20-21 (kernel
  * Tridiagonal_CUDA/tridiagonal_basic.cu:4-30, wrappers :171-190). */
@@ -72,6 +126,8 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 /* algorithms */
 #define TRIDIAG_ALGO_AUTO 0
 #define TRIDIAG_ALGO_THOMAS 1 /* unpivoted, one thread per system */
+#define TRIDIAG_ALGO_CR 2     /* CR-PCR hybrid, one warp per system */
+#define TRIDIAG_ALGO_PCR 3    /* PCR-pThomas, one warp per system */
 #define TRIDIAG_ALGO_WM 4     /* WM-pGE, one warp per system, unpivoted */
 #define TRIDIAG_ALGO_GTSV 5   /* partial pivoting, one thread per system */
 

@@ -54,12 +54,25 @@ SIGNATURES: dict[str, tuple] = {
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
 REFERENCE_SOLVERS = [
+    "cuSparse_single", "cuSparse_double", "BPLG_WM", "BPLG_LF", "BPLG_CR", "BPLG_PCR",
     "Thomas_single", "Thomas_double",
     "WM5_shmem_single", "WM4_shmem_single", "WM5_reg_single", "WM4_reg_single",
     "WM5_shmem_double", "WM4_shmem_double", "WM5_reg_double", "WM4_reg_double",
+    "PCR5_shmem_single", "PCR4_shmem_single", "PCR5_reg_single", "PCR4_reg_single",
+    "PCR5_shmem_double", "PCR4_shmem_double", "PCR5_reg_double", "PCR4_reg_double",
+    "CR_single", "CR_double", "CR_reg4_single", "CR_reg8_single", "CR_reg16_single",
+    "CR_reg4_double", "CR_reg8_double", "CR_reg16_double",
 ]
 for _name in REFERENCE_SOLVERS:
     SIGNATURES[_name] = (None, _REF_SIG)
+# init / final hooks of the reference registry (Tridiagonal_CUDA/helpers.h:12-19)
+SIGNATURES["CR_init_single"] = (_I, _REF_SIG)
+SIGNATURES["CR_init_double"] = (_I, _REF_SIG)
+SIGNATURES["CR_final"] = (None, [])
+SIGNATURES["cuSparse_init_single"] = (_I, _REF_SIG)
+SIGNATURES["cuSparse_init_double"] = (_I, _REF_SIG)
+SIGNATURES["cuSparse_final"] = (None, [])
+SIGNATURES["tridiag_vendor_last_status"] = (_I, [])
 
 
 class TridiagError(RuntimeError):

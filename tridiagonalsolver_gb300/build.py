@@ -29,7 +29,7 @@ DRIVER = LIB_DIR / "test"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills", "-I", str(INCLUDE)]
-LINK_LIBS = ["-lcusparse", "-lcuda"]
+LINK_LIBS = ["-lcusparse"]
 
 
 def nvcc() -> str:

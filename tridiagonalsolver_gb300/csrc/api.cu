@@ -118,9 +118,13 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
       if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
       return cuda_status(e);
     }
+    case TRIDIAG_ALGO_CR:
+    case TRIDIAG_ALGO_PCR:
     case TRIDIAG_ALGO_WM: {
       bool used = false;
-      cudaError_t e = tdg::launch_wm_warp<T>(layout, a, b, c, d, d, n, batch, s, &used);
+      cudaError_t e = algo == TRIDIAG_ALGO_CR    ? tdg::launch_crpcr_warp<T>(layout, a, b, c, d, d, n, batch, s, &used)
+                      : algo == TRIDIAG_ALGO_PCR ? tdg::launch_pcr_warp<T>(layout, a, b, c, d, d, n, batch, s, &used)
+                                                 : tdg::launch_wm_warp<T>(layout, a, b, c, d, d, n, batch, s, &used);
       if (e == cudaSuccess && !used) {
         e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
         if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
@@ -162,9 +166,13 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
   if (work_bytes < solve_out_ws<T>(algo, n, batch) || (solve_out_ws<T>(algo, n, batch) && !work))
     return TRIDIAG_ERR_WORKSPACE;
   switch (algo) {
+    case TRIDIAG_ALGO_CR:
+    case TRIDIAG_ALGO_PCR:
     case TRIDIAG_ALGO_WM: {
       bool used = false;
-      cudaError_t e = tdg::launch_wm_warp<T>(layout, a, b, c, d, x, n, batch, s, &used);
+      cudaError_t e = algo == TRIDIAG_ALGO_CR    ? tdg::launch_crpcr_warp<T>(layout, a, b, c, d, x, n, batch, s, &used)
+                      : algo == TRIDIAG_ALGO_PCR ? tdg::launch_pcr_warp<T>(layout, a, b, c, d, x, n, batch, s, &used)
+                                                 : tdg::launch_wm_warp<T>(layout, a, b, c, d, x, n, batch, s, &used);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       if (!work || work_bytes < solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, n, batch)) return TRIDIAG_ERR_WORKSPACE;
@@ -253,6 +261,52 @@ TDG_REF_ENTRY(WM4_shmem_double, double, TRIDIAG_ALGO_WM)
 TDG_REF_ENTRY(WM5_reg_double, double, TRIDIAG_ALGO_WM)
 TDG_REF_ENTRY(WM4_reg_double, double, TRIDIAG_ALGO_WM)
 
+// PCR-pThomas -- replace Tridiagonal_CUDA/tridiagonal.h:33-34,38-39,43-44,48-49 (PCR{5,4}_{shmem,reg};
+// kernels Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:886-1431).  All run pcr.cu's 5-step PCR-pThomas.
+TDG_REF_ENTRY(PCR5_shmem_single, float, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR4_shmem_single, float, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR5_reg_single, float, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR4_reg_single, float, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR5_shmem_double, double, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR4_shmem_double, double, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR5_reg_double, double, TRIDIAG_ALGO_PCR)
+TDG_REF_ENTRY(PCR4_reg_double, double, TRIDIAG_ALGO_PCR)
+
+// CR -- replaces Tridiagonal_CUDA/tridiagonal.h:24-28 (kernel Tridiagonal_CUDA/tridiagonal_basic.cu:32-164,
+// wrappers :177-204) and the register-packed CR_reg{4,8,16} of tridiagonal.h:50-55 (kernels
+// Tridiagonal_CUDA/tridiagonal_onchip.cu:218-820).  All run the on-chip CR-PCR hybrid of wm.cu, which
+// needs no scratch: CR_init returns 0 without allocating and CR_final does nothing.
+TDG_REF_ENTRY(CR_single, float, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_double, double, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_reg4_single, float, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_reg8_single, float, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_reg16_single, float, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_reg4_double, double, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_reg8_double, double, TRIDIAG_ALGO_CR)
+TDG_REF_ENTRY(CR_reg16_double, double, TRIDIAG_ALGO_CR)
+int CR_init_single(float*, float*, float*, float*, int n, int batch) {
+  return set_status(valid_dims(n, batch) ? TRIDIAG_SUCCESS : TRIDIAG_ERR_INVALID_VALUE);
+}
+int CR_init_double(double*, double*, double*, double*, int n, int batch) {
+  return set_status(valid_dims(n, batch) ? TRIDIAG_SUCCESS : TRIDIAG_ERR_INVALID_VALUE);
+}
+void CR_final(void) { set_status(TRIDIAG_SUCCESS); }
+
+// BPLG -- replaces Tridiagonal_CUDA/tridiagonal.h:14-17 (the BPLG library's WM / LF / CR / PCR solvers,
+// Tridiagonal_CUDA/tridiagonal_third_party.cu:1-41), which take the packed layout 1
+// ([batch][a|b|c|d][n], base pointer a; the reference's driver passes a_gbl).  They run this
+// library's on-chip kernels on that layout: WM -> WM-pGE, CR and LF -> CR-PCR, PCR -> PCR-pThomas.
+#define TDG_BPLG_ENTRY(NAME, ALGO)                                                                          \
+  void NAME(float* a, float*, float*, float*, int n, int batch) {                                          \
+    sync_call([&] {                                                                                         \
+      return solve_impl<float>(ALGO, TRIDIAG_LAYOUT_PACKED, a, nullptr, nullptr, nullptr, n, batch, 0);    \
+    });                                                                                                     \
+  }
+TDG_BPLG_ENTRY(BPLG_WM, TRIDIAG_ALGO_WM)
+TDG_BPLG_ENTRY(BPLG_LF, TRIDIAG_ALGO_CR)
+TDG_BPLG_ENTRY(BPLG_CR, TRIDIAG_ALGO_CR)
+TDG_BPLG_ENTRY(BPLG_PCR, TRIDIAG_ALGO_PCR)
+
 // ---- extensions ---------------------------------------------------------------
 
 int tridiag_solve_single(int algo, int layout, float* a, float* b, float* c, float* d, int n, int batch,
@@ -267,7 +321,8 @@ int tridiag_solve_double(int algo, int layout, double* a, double* b, double* c, 
 size_t tridiag_solve_out_workspace_size(int precision, int algo, int layout, int n, int batch) {
   (void)layout;
   if (!valid_dims(n, batch)) return 0;
-  if (algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM) algo = TRIDIAG_ALGO_THOMAS;  // possible fallback
+  if (algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM || algo == TRIDIAG_ALGO_CR || algo == TRIDIAG_ALGO_PCR)
+    algo = TRIDIAG_ALGO_THOMAS;  // possible fallback
   return precision ? solve_out_ws<double>(algo, n, batch) : solve_out_ws<float>(algo, n, batch);
 }
 

@@ -51,6 +51,18 @@ template <typename T>
 cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                            cudaStream_t st, bool* used);
 
+// wm.cu: CR-PCR hybrid on the same chunk layout (cyclic reduction in
+// registers down to one row per lane, warp PCR on those rows).
+template <typename T>
+cudaError_t launch_crpcr_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                              cudaStream_t st, bool* used);
+
+// pcr.cu: PCR-pThomas, one warp per system (CONTIG / PACKED, n <= 1024
+// FP32, 512 FP64).  x may alias d.
+template <typename T>
+cudaError_t launch_pcr_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                            cudaStream_t st, bool* used);
+
 // pivot record: one 32-bit word per 32 rows per system
 inline size_t pivot_words(int n, int batch) { return (size_t)((n + 31) / 32) * (size_t)batch; }
 

@@ -213,10 +213,88 @@ __device__ __forceinline__ void wm_lane_solve(T (&A)[M], T (&B)[M], T (&C)[M], T
   }
 }
 
+// CR-PCR hybrid on the same chunk layout: the lane's M = 2^k rows are
+// reduced by k levels of odd/even cyclic reduction in registers (only the
+// first row of a lane needs the previous lane's row, one shuffle per level),
+// leaving one row per lane; the G reduced rows are solved by segmented warp
+// PCR; the eliminated rows are recovered level by level, each from the
+// coefficients it had when it was eliminated (kept in place in A..D).
+// Rows past n are identity rows (they decouple: c_{n-1} = 0).
+//
+// Reference: the cyclic-reduction solvers, CR_kernel
+// (Tridiagonal_CUDA/tridiagonal_basic.cu:32-164) and the register-packed
+// CR_reg{4,8,16} kernels (Tridiagonal_CUDA/tridiagonal_onchip.cu:218-820):
+// registers hold R rows per thread, then a shared CR / PCR tail.
+template <typename T, int M, int G>
+__device__ __forceinline__ void crpcr_lane_solve(T (&A)[M], T (&B)[M], T (&C)[M], T (&D)[M], T (&X)[M], int n,
+                                                 int s, int m, int mt, int tl) {
+  static_assert((M & (M - 1)) == 0, "rows per lane must be a power of two");
+  // rows of this chunk beyond n (or an empty chunk) become identity rows
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    if (k >= mt) { A[k] = T(0); B[k] = T(1); C[k] = T(0); D[k] = T(0); }
+  }
+  if (s == 0) A[0] = T(0);
+  const int last = n - 1 - s;
+#pragma unroll
+  for (int k = 0; k < M; ++k)
+    if (k == last) C[k] = T(0);
+  (void)m;
+  // forward reduction
+#pragma unroll
+  for (int st = 1; st < M; st <<= 1) {
+    // previous lane's row M - st (its last row surviving to this level)
+    T pa = __shfl_up_sync(FULL, A[M - st], 1, G), pb = __shfl_up_sync(FULL, B[M - st], 1, G);
+    T pc = __shfl_up_sync(FULL, C[M - st], 1, G), pd = __shfl_up_sync(FULL, D[M - st], 1, G);
+    if (tl == 0) { pa = T(0); pb = T(1); pc = T(0); pd = T(0); }
+#pragma unroll
+    for (int i = 0; i < M; i += 2 * st) {
+      const T la = i == 0 ? pa : A[i - st], lb = i == 0 ? pb : B[i - st];
+      const T lc = i == 0 ? pc : C[i - st], ld = i == 0 ? pd : D[i - st];
+      const T ra = A[i + st], rb = B[i + st], rc = C[i + st], rd = D[i + st];
+      const T k1 = A[i] * Div<T>(lb).inv();
+      const T k2 = C[i] * Div<T>(rb).inv();
+      const T nb = fma(-k2, ra, fma(-k1, lc, B[i]));
+      const T nd = fma(-k2, rd, fma(-k1, ld, D[i]));
+      A[i] = -k1 * la;
+      C[i] = -k2 * rc;
+      B[i] = nb;
+      D[i] = nd;
+    }
+  }
+  // reduced system: row 0 of every lane, coupled to row 0 of the neighbours
+  const T x0 = warp_pcr<T, G>(A[0], B[0], C[0], D[0], tl);
+  T xr = __shfl_down_sync(FULL, x0, 1, G);  // x of the next lane's row 0
+  if (tl == G - 1) xr = T(0);
+  X[0] = x0;
+  // back substitution
+#pragma unroll
+  for (int st = M >> 1; st >= 1; st >>= 1) {
+#pragma unroll
+    for (int i = st; i < M; i += 2 * st) {
+      const T xl = X[i - st];
+      const T xrr = (i + st < M) ? X[i + st] : xr;
+      X[i] = Div<T>(B[i]).div(fma(-C[i], xrr, fma(-A[i], xl, D[i])));
+    }
+  }
+}
+
+// Per-lane solve selector for the chunk-layout kernels.
+enum ChunkAlgo { CHUNK_WM = 0, CHUNK_CRPCR = 1 };
+
+template <int ALG, typename T, int M, int G>
+__device__ __forceinline__ void chunk_solve(T (&A)[M], T (&B)[M], T (&C)[M], T (&D)[M], T (&X)[M], int n, int s,
+                                            int m, int mt, int tl) {
+  if constexpr (ALG == CHUNK_CRPCR)
+    crpcr_lane_solve<T, M, G>(A, B, C, D, X, n, s, m, mt, tl);
+  else
+    wm_lane_solve<T, M, G>(A, B, C, D, X, n, s, m, mt, tl);
+}
+
 // One warp per system, direct (L1-cached) loads; any n with m <= M.
 // Layout CONTIG (stride n between systems) or PACKED (stride 4n; the
 // caller passes the four array pointers of system 0).
-template <typename T, int M>
+template <int ALG, typename T, int M>
 __global__ void __launch_bounds__(128) wm_warp_kernel(const T* __restrict__ a, const T* __restrict__ b,
                                                       const T* __restrict__ c, const T* d, T* x, int n, int batch,
                                                       size_t sys_stride, int m, bool vec) {
@@ -231,7 +309,7 @@ __global__ void __launch_bounds__(128) wm_warp_kernel(const T* __restrict__ a, c
   load_chunk<T, M, true>(B, b + base, s, mt, vec, T(1));
   load_chunk<T, M, true>(C, c + base, s, mt, vec, T(0));
   load_chunk<T, M, false>(D, d + base, s, mt, vec, T(0));
-  wm_lane_solve<T, M, 32>(A, B, C, D, X, n, s, m, mt, lane);
+  chunk_solve<ALG, T, M, 32>(A, B, C, D, X, n, s, m, mt, lane);
   store_chunk<T, M>(X, x + base, s, mt, vec);
 }
 
@@ -272,7 +350,7 @@ __device__ __forceinline__ int wm_swz(int t, int q) {
   return logical ^ (((logical >> 7) & mask) << 4);
 }
 
-template <typename T, int M, int G>
+template <int ALG, typename T, int M, int G>
 __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
     wm_tma_kernel(const __grid_constant__ TwMaps maps, int n, int nboxes, int* err) {
   constexpr int WARPS = wm_warps<T, M>();
@@ -328,7 +406,7 @@ __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
     __syncwarp();
     // the slot is free again: refill it with the box WM_SLOTS ahead
     if (lane == 0 && i + WM_SLOTS < count) load(i + WM_SLOTS, q);
-    wm_lane_solve<T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
+    chunk_solve<ALG, T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
     if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer
     __syncwarp();
 #pragma unroll
@@ -346,7 +424,7 @@ __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
   if (lane == 0) bulk_wait_all();
 }
 
-template <typename T, int M, int G>
+template <int ALG, typename T, int M, int G>
 static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch, cudaStream_t st,
                             cudaError_t* e) {
   constexpr int ROWB = M * (int)sizeof(T);
@@ -365,19 +443,19 @@ static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x
   const int nboxes = (int)((rows + 31) / 32);
   const size_t smem =
       (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * WARPS + 8 * WM_SLOTS * WARPS + 1024;
-  *e = cudaFuncSetAttribute(wm_tma_kernel<T, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  *e = cudaFuncSetAttribute(wm_tma_kernel<ALG, T, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (*e != cudaSuccess) return true;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int need = (nboxes + WARPS - 1) / WARPS;
   const int grid = need < sms ? need : sms;
-  wm_tma_kernel<T, M, G><<<grid, 32 * WARPS, smem, st>>>(maps, n, nboxes, error_word());
+  wm_tma_kernel<ALG, T, M, G><<<grid, 32 * WARPS, smem, st>>>(maps, n, nboxes, error_word());
   *e = cudaGetLastError();
   return true;
 }
 
-template <typename T, int M>
+template <int ALG, typename T, int M>
 static cudaError_t launch_wm_m(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                                size_t stride, int m, cudaStream_t st) {
   constexpr int NV = Vec16<T>::N;
@@ -388,16 +466,16 @@ static cudaError_t launch_wm_m(const T* a, const T* b, const T* c, const T* d, T
                     0);
   const int warps_per_block = 4;
   dim3 grid((batch + warps_per_block - 1) / warps_per_block);
-  wm_warp_kernel<T, M><<<grid, 32 * warps_per_block, 0, st>>>(a, b, c, d, x, n, batch, stride, m, vec);
+  wm_warp_kernel<ALG, T, M><<<grid, 32 * warps_per_block, 0, st>>>(a, b, c, d, x, n, batch, stride, m, vec);
   return cudaGetLastError();
 }
 
 // Chunk length m = ceil(n/32) (at least 2 rows), rounded up to the vector
 // width when that keeps all 32 chunks within n; the template M is the
 // smallest supported bound >= m.
-template <typename T>
-cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
-                           cudaStream_t st, bool* used) {
+template <int ALG, typename T>
+static cudaError_t launch_chunk(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                                cudaStream_t st, bool* used) {
   *used = false;
   if (layout != CONTIG && layout != PACKED) return cudaSuccess;
   constexpr int NV = Vec16<T>::N;
@@ -408,11 +486,11 @@ cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const
     cudaError_t e = cudaSuccess;
     bool done = false;
     constexpr int MP = sizeof(T) == 4 ? 16 : 8;  // preferred rows per lane
-    if (n == 4 * MP) done = launch_wm_tma_m<T, MP, 4>(a, b, c, d, x, n, batch, st, &e);
-    else if (n == 8 * MP) done = launch_wm_tma_m<T, MP, 8>(a, b, c, d, x, n, batch, st, &e);
-    else if (n == 16 * MP) done = launch_wm_tma_m<T, MP, 16>(a, b, c, d, x, n, batch, st, &e);
-    else if (n == 32 * MP) done = launch_wm_tma_m<T, MP, 32>(a, b, c, d, x, n, batch, st, &e);
-    else if (n == 64 * MP) done = launch_wm_tma_m<T, 2 * MP, 32>(a, b, c, d, x, n, batch, st, &e);
+    if (n == 4 * MP) done = launch_wm_tma_m<ALG, T, MP, 4>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 8 * MP) done = launch_wm_tma_m<ALG, T, MP, 8>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 16 * MP) done = launch_wm_tma_m<ALG, T, MP, 16>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 32 * MP) done = launch_wm_tma_m<ALG, T, MP, 32>(a, b, c, d, x, n, batch, st, &e);
+    else if (n == 64 * MP) done = launch_wm_tma_m<ALG, T, 2 * MP, 32>(a, b, c, d, x, n, batch, st, &e);
     if (done) {
       *used = true;
       return e;
@@ -425,17 +503,33 @@ cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const
   if (n % NV == 0 && ((m + NV - 1) / NV) * NV <= maxm) m = ((m + NV - 1) / NV) * NV;
   if (m > maxm) return cudaSuccess;
   *used = true;
-  if (m <= 4) return launch_wm_m<T, 4>(a, b, c, d, x, n, batch, stride, m, st);
-  if (m <= 8) return launch_wm_m<T, 8>(a, b, c, d, x, n, batch, stride, m, st);
-  if (m <= 16) return launch_wm_m<T, 16>(a, b, c, d, x, n, batch, stride, m, st);
-  if constexpr (sizeof(T) == 4) return launch_wm_m<T, 32>(a, b, c, d, x, n, batch, stride, m, st);
+  if (m <= 4) return launch_wm_m<ALG, T, 4>(a, b, c, d, x, n, batch, stride, 4 > m && ALG == CHUNK_CRPCR ? 4 : m, st);
+  if (m <= 8) return launch_wm_m<ALG, T, 8>(a, b, c, d, x, n, batch, stride, ALG == CHUNK_CRPCR ? 8 : m, st);
+  if (m <= 16) return launch_wm_m<ALG, T, 16>(a, b, c, d, x, n, batch, stride, ALG == CHUNK_CRPCR ? 16 : m, st);
+  if constexpr (sizeof(T) == 4)
+    return launch_wm_m<ALG, T, 32>(a, b, c, d, x, n, batch, stride, ALG == CHUNK_CRPCR ? 32 : m, st);
   *used = false;
   return cudaSuccess;
 }
 
-template cudaError_t launch_wm_warp<float>(int, const float*, const float*, const float*, const float*, float*, int,
-                                           int, cudaStream_t, bool*);
-template cudaError_t launch_wm_warp<double>(int, const double*, const double*, const double*, const double*, double*,
-                                            int, int, cudaStream_t, bool*);
+template <typename T>
+cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                           cudaStream_t st, bool* used) {
+  return launch_chunk<CHUNK_WM, T>(layout, a, b, c, d, x, n, batch, st, used);
+}
+template <typename T>
+cudaError_t launch_crpcr_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                              cudaStream_t st, bool* used) {
+  return launch_chunk<CHUNK_CRPCR, T>(layout, a, b, c, d, x, n, batch, st, used);
+}
+
+#define INST(T)                                                                                                   \
+  template cudaError_t launch_wm_warp<T>(int, const T*, const T*, const T*, const T*, T*, int, int, cudaStream_t, \
+                                         bool*);                                                                  \
+  template cudaError_t launch_crpcr_warp<T>(int, const T*, const T*, const T*, const T*, T*, int, int,            \
+                                            cudaStream_t, bool*);
+INST(float)
+INST(double)
+#undef INST
 
 }  // namespace tdg

@@ -179,7 +179,7 @@ def run_ours(args):
     for pi, part in enumerate(PARTS):
         a, b, c, d = make_inputs(torch, part, seed=1000 * rank + pi, device=dev)
         x = torch.empty_like(d)
-        work = T.solve_out_workspace(a, part["n"], part["algo"] if part["algo"] in T.ALGOS else "auto")
+        work = T.solve_out_workspace(a, part["n"], part["algo"])
         data.append(dict(part=part, a=a, b=b, c=c, d=d, x=x, work=work))
 
     stream = torch.cuda.Stream(device=dev)
@@ -188,9 +188,6 @@ def run_ours(args):
     def solve_part(item, s):
         part = item["part"]
         algo = part["algo"]
-        # algorithms not yet built fall back to the on-chip WM-pGE (recorded)
-        if algo not in ("wm", "gtsv", "thomas") and not _has_algo(T, algo):
-            algo = "wm"
         algo_used[part["name"]] = algo
         T.solve_out(item["a"], item["b"], item["c"], item["d"], part["n"], algo=algo, out=item["x"],
                     work=item["work"], stream=s)
@@ -312,10 +309,6 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
-
-
-def _has_algo(T, algo):
-    return algo in ("wm", "gtsv", "thomas") or getattr(T, "_algo_available", lambda a: False)(algo)
 
 
 def _accuracy(torch, data, sample=16):

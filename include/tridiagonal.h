@@ -54,10 +54,13 @@ void BPLG_CR(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, 
 void BPLG_PCR(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 
 /* WM-pGE (partitioned Gaussian elimination, reduced interface system by
- * PCR; no pivoting, like the reference) -- replaces
- * Tridiagonal_CUDA/tridiagonal.h:32,37,42,47 (WM{5,4}_{shmem,reg}; kernels
- * Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884).  One on-chip kernel serves
- * all four variants of each precision. */
+ * PCR) -- replaces Tridiagonal_CUDA/tridiagonal.h:32,37,42,47
+ * (WM{5,4}_{shmem,reg}; kernels Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:
+ * 17-884).  One kernel family serves all four variants of each precision:
+ * systems that fit one warp (n <= 1024 FP32, 512 FP64) run the on-chip
+ * version without pivoting, as the reference does; longer systems run the
+ * partitioned solve with partial pivoting inside each partition (one CTA per
+ * system, up to ~8K rows FP32 / ~5K FP64), beyond that the Thomas sweep. */
 void WM5_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 void WM4_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 void WM5_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
@@ -195,6 +198,34 @@ int tridiag_gtsv_adjoint_double(int layout, const double *a, const double *b, co
                                 const unsigned int *pivots, const double *xbar, double *ga, double *gb,
                                 double *gc, double *gd, void *work, size_t work_bytes, int n_eqt, int n_batch,
                                 void *stream);
+
+/* Mixed-precision refined solve (no counterpart in the reference): FP64
+ * arrays in and out, the eliminations in FP32.  a, b, c, d are converted to
+ * FP32 once, x0 is the FP32 partial-pivoting solve, and each of `iters`
+ * refinement steps forms r = d - A x in FP64 and adds the FP32 solve of
+ * A dx = r.  Two steps bring the normwise backward error to the FP64 level
+ * for condition numbers up to ~1e7.  Layouts: contiguous or interleaved.
+ * a, b, c, d are read only; x receives the solution; info (may be NULL) as
+ * tridiag_gtsv_*, from the FP32 factorisation.  iters in [0, 8].
+ * work: tridiag_refine_workspace_size() bytes. */
+size_t tridiag_refine_workspace_size(int layout, int n_eqt, int n_batch);
+int tridiag_refine_double(int layout, const double *a, const double *b, const double *c, const double *d,
+                          double *x, int iters, int *info, void *work, size_t work_bytes, int n_eqt, int n_batch,
+                          void *stream);
+
+/* FP64 -> FP32 narrowing (round to nearest even) and FP32 -> FP64 widening
+ * as the refined solve performs them on the integer pipe: out[k] = (float)
+ * in[k], back[k] = (double)out[k].  For tests of that conversion. */
+int tridiag_convert_check(const double *in, float *out, double *back, size_t count, void *stream);
+
+/* Diagnostics: how many systems the partitioned partial-pivoting solve (used
+ * by tridiag_gtsv_* without a pivot record, tridiag_solve_out_* with
+ * TRIDIAG_ALGO_GTSV and the WM entry points on long systems) handed to its
+ * sequential fallback on the current device since the last reset -- systems
+ * whose partition-local pivoting broke down or failed the solve's
+ * growth/residual check.  Synchronous; reset != 0 clears the count; -1 on a
+ * CUDA error. */
+long long tridiag_partition_fallbacks(int reset);
 
 /* Size of the static scratch array of tridiag_gtsv_noalloc_* (32 MiB). */
 #define TRIDIAG_NOALLOC_SCRATCH_BYTES (32u << 20)

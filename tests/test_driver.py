@@ -30,6 +30,9 @@ def test_usage_and_algorithm_table(driver):
     names = re.findall(r"^\s*(\d+): (.+)$", single, flags=re.M)
     for i, nm in enumerate(REF_FLOAT):
         assert (str(i), nm) in names
+    # names go into one CSV field
+    for _, nm in re.findall(r"^\s*(\d+): (.+)$", p.stdout, flags=re.M):
+        assert "," not in nm
 
 
 @pytest.mark.parametrize("args", [["2", "1", "64", "4", "1"], ["0", "-1", "64", "4", "1"], ["0", "1", "0", "4", "1"],

@@ -1,0 +1,153 @@
+"""Partitioned partial-pivoting solve (WM-pGE, one CTA per system) against
+the oracle: every partition-count variant, sizes around the partition
+boundaries, the breakdown fallback (singular interior blocks) and LAPACK's
+info for singular matrices.
+
+Tolerances: normwise backward error <= 1e-12 (FP64) and <= 1e-6 (FP32),
+computed in FP64 by the oracle; forward differences to the oracle's
+LAPACK-style solve <= 1e-11 (FP64) / 1e-3 (FP32) relative to max|x| in the
+median over systems (random U[-1,1] systems reach condition numbers ~1e6).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tridiagonalsolver_gb300 import inputs
+
+pytestmark = pytest.mark.gpu
+
+ETA = {np.float64: 1e-12, np.float32: 1e-6}
+
+
+def _rel(x, xr):
+    return np.max(np.abs(x - xr), axis=1) / np.maximum(np.max(np.abs(xr), axis=1), 1e-300)
+
+
+def _solve(cuda, arrs, dt, n):
+    import tridiagonalsolver_gb300 as T
+
+    batch = arrs[0].shape[0]
+    ts = [cuda.from_numpy(np.ascontiguousarray(v.astype(dt))).cuda() for v in arrs]
+    info = cuda.full((batch,), -7, dtype=cuda.int32, device="cuda")
+    x = T.gtsv(*ts, n, info=info)  # no pivot record requested: the partitioned solve
+    cuda.cuda.synchronize()
+    return x.double().cpu().numpy().reshape(batch, n), info.cpu().numpy()
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,batch", [(65, 9), (100, 33), (128, 5), (129, 40), (255, 7), (256, 16), (257, 16),
+                                     (1000, 37), (2048, 8), (4095, 8), (4096, 24), (5000, 6), (5248, 4)])
+def test_pge_matches_oracle(cuda, dt, n, batch):
+    a, b, c, d = inputs.nondominant(n, batch, seed=3 * n + batch)
+    x, info = _solve(cuda, (a, b, c, d), dt, n)
+    assert (info == 0).all()
+    a_, b_, c_, d_ = (v.astype(dt).astype(np.float64) for v in (a, b, c, d))
+    _, worst = O.backward_error(a_, b_, c_, d_, x, n)
+    assert worst <= ETA[dt]
+    xo = O.gtsv(a_, b_, c_, d_, n).reshape(batch, n)
+    assert np.median(_rel(x, xo)) <= (1e-11 if dt == np.float64 else 1e-3)
+
+
+@pytest.mark.parametrize("n,batch", [(6000, 4), (8192, 6), (10000, 2)])
+def test_pge_fp32_long(cuda, n, batch):
+    a, b, c, d = inputs.nondominant(n, batch, seed=n)
+    x, info = _solve(cuda, (a, b, c, d), np.float32, n)
+    assert (info == 0).all()
+    _, worst = O.backward_error(*(v.astype(np.float32).astype(np.float64) for v in (a, b, c, d)), x, n)
+    assert worst <= 1e-6
+
+
+def test_pge_dominant_forward_error(cuda):
+    n, batch = 4096, 16
+    a, b, c, d = inputs.dominant(n, batch, seed=5)
+    x, info = _solve(cuda, (a, b, c, d), np.float64, n)
+    xo = O.gtsv(a, b, c, d, n).reshape(batch, n)
+    assert np.max(_rel(x, xo)) <= 1e-14
+
+
+def test_pge_singular_interior_block_falls_back(cuda):
+    """Row 32 (first interior row of partition 1 for n = 4096, 128
+    partitions) has a zero diagonal and superdiagonal: that interior block is
+    singular, the matrix is not."""
+    n, batch = 4096, 4
+    a, b, c, d = inputs.nondominant(n, batch, seed=11)
+    for j in (1, 3):
+        b[j, 32] = 0.0
+        c[j, 32] = 0.0
+        a[j, 32] = 1.0
+    import tridiagonalsolver_gb300 as T
+
+    T.lib().tridiag_partition_fallbacks(1)
+    x, info = _solve(cuda, (a, b, c, d), np.float64, n)
+    assert T.lib().tridiag_partition_fallbacks(1) >= 2
+    assert (info == 0).all()
+    _, worst = O.backward_error(a, b, c, d, x, n)
+    assert worst <= 1e-12
+
+
+def test_pge_singular_matrix_info(cuda):
+    """A zero row makes the matrix singular: info is LAPACK's k+1."""
+    from scipy.linalg import lapack
+
+    n, batch = 1000, 3
+    a, b, c, d = inputs.nondominant(n, batch, seed=12)
+    a[1, 500] = b[1, 500] = c[1, 500] = 0.0
+    _, info = _solve(cuda, (a, b, c, d), np.float64, n)
+    want = lapack.dgtsv(a[1, 1:].copy(), b[1].copy(), c[1, :-1].copy(), d[1].copy())[4]
+    assert info[0] == 0 and info[2] == 0
+    assert info[1] == want and want > 0
+
+
+def test_pge_bench_shape_fp64(cuda):
+    """FP64, n = 4096, 4096 non-dominant systems (the pivoted benchmark
+    part): all info 0 and 64 sampled systems within the FP64 bar."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    n, batch = 4096, 4096
+    g = torch.Generator(device="cuda")
+    g.manual_seed(77)
+    a, b, c, d = (torch.rand((batch, n), dtype=torch.float64, device="cuda", generator=g) * 2 - 1 for _ in range(4))
+    info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
+    T.lib().tridiag_partition_fallbacks(1)
+    x = T.gtsv(a, b, c, d, n, info=info)
+    assert int((info != 0).sum()) == 0
+    fb = T.lib().tridiag_partition_fallbacks(1)
+    print(f"partitioned solve: {fb} of {batch} systems took the sequential fallback")
+    assert fb <= batch // 256  # the fast path serves (nearly) every system
+    idx = torch.arange(0, batch, batch // 64, device="cuda")
+    host = [t.index_select(0, idx).cpu().numpy() for t in (a, b, c, d, x)]
+    host[0][:, 0] = 0.0
+    host[2][:, -1] = 0.0
+    _, worst = O.backward_error(*host, n)
+    assert worst <= 1e-12
+
+
+@pytest.mark.parametrize("name,dt,n", [("WM5_reg_double", np.float64, 4096), ("WM4_shmem_single", np.float32, 3000)])
+def test_reference_wm_names_long_systems(cuda, name, dt, n):
+    """The reference's WM entry points on systems beyond one warp use the
+    partitioned solve (in place, d <- x)."""
+    import tridiagonalsolver_gb300 as T
+
+    batch = 8
+    a, b, c, d = inputs.dominant(n, batch, seed=n)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    T.reference_call(name, *ts, n)
+    x = ts[3].double().cpu().numpy().reshape(batch, n)
+    _, worst = O.backward_error(*(v.astype(dt).astype(np.float64) for v in (a, b, c, d)), x, n)
+    assert worst <= ETA[dt]
+
+
+def test_bplg_packed_long(cuda):
+    """Packed layout (BPLG entry point) through the partitioned solve."""
+    import tridiagonalsolver_gb300 as T
+
+    n, batch = 2048, 6
+    a, b, c, d = inputs.dominant(n, batch, seed=4)
+    packed = cuda.from_numpy(inputs.to_packed(a, b, c, d).astype(np.float32)).cuda()
+    T.lib().BPLG_WM(packed.data_ptr(), packed.data_ptr() + 4 * n, packed.data_ptr() + 8 * n,
+                    packed.data_ptr() + 12 * n, n, batch)
+    assert T.last_status() == 0
+    x = packed.double().cpu().numpy().reshape(batch, 4, n)[:, 3, :]
+    _, worst = O.backward_error(*(v.astype(np.float32).astype(np.float64) for v in (a, b, c, d)), x, n)
+    assert worst <= 1e-6

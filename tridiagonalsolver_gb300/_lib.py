@@ -51,6 +51,10 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_gtsv_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_gtsv_noalloc_single": (_I, [_I, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_gtsv_noalloc_double": (_I, [_I, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_refine_workspace_size": (_SZ, [_I, _I, _I]),
+    "tridiag_refine_double": (_I, [_I, _P, _P, _P, _P, _P, _I, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_convert_check": (_I, [_P, _P, _P, _SZ, _P]),
+    "tridiag_partition_fallbacks": (ctypes.c_longlong, [_I]),
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
 REFERENCE_SOLVERS = [

@@ -1,0 +1,56 @@
+"""torch.autograd wrapper of the pivoted solve and its adjoint kernel.
+
+``x = solve_ad(a, b, c, d)`` solves the batch of tridiagonal systems
+A x = d with partial pivoting (``tridiag_gtsv_*``), keeping the pivot record;
+``x.backward(xbar)`` then runs ``tridiag_gtsv_adjoint_*``, which solves
+A^T lambda = xbar with the same factorisation and pivots and returns
+
+    grad_d = lambda,  grad_a[i] = -lambda[i] x[i-1],  grad_b[i] = -lambda[i] x[i],
+    grad_c[i] = -lambda[i] x[i+1]
+
+(grad_a[0] = grad_c[n-1] = 0: those entries are outside the matrix).  Both
+directions are the library's CUDA kernels; this module only owns the
+bookkeeping between them.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import ops
+
+
+class TridiagonalSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, a, b, c, d, n, layout):
+        a, b, c, d = (t.contiguous() for t in (a, b, c, d))
+        piv = ops.pivot_record(a, n, layout)
+        work = ops.gtsv_workspace(a, n, layout)
+        x = ops.gtsv(a, b, c, d, n, layout=layout, pivots=piv, work=work)
+        ctx.save_for_backward(a, b, c, x, piv, work)
+        ctx.n, ctx.layout = n, layout
+        return x
+
+    @staticmethod
+    def backward(ctx, xbar):
+        a, b, c, x, piv, work = ctx.saved_tensors
+        ga, gb, gc, gd = ops.gtsv_adjoint(a, b, c, x, piv, xbar.contiguous(), ctx.n, layout=ctx.layout,
+                                          work=work)
+        need = ctx.needs_input_grad
+        return (ga if need[0] else None, gb if need[1] else None, gc if need[2] else None,
+                gd if need[3] else None, None, None)
+
+
+def solve_ad(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor, d: torch.Tensor, n: int | None = None,
+             layout: str = "contiguous") -> torch.Tensor:
+    """Differentiable batched solve.  ``a, b, c, d`` share one shape: (batch, n)
+    for layout "contiguous" or (n, batch) for "interleaved"; ``n`` defaults to
+    the matching dimension."""
+    if layout not in ("contiguous", "interleaved"):
+        raise ValueError("solve_ad supports the contiguous and interleaved layouts")
+    if not (a.shape == b.shape == c.shape == d.shape):
+        raise ValueError("a, b, c, d must have the same shape")
+    if n is None:
+        if a.dim() != 2:
+            raise ValueError("pass n for flat tensors")
+        n = a.shape[1] if layout == "contiguous" else a.shape[0]
+    return TridiagonalSolve.apply(a, b, c, d, n, layout)

@@ -75,6 +75,13 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
     return TRIDIAG_ERR_INVALID_VALUE;
   }
   if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
+  if (!pivots && tdg::pge_eligible<T>(layout, n)) {
+    // no pivot record wanted: the partitioned solve (many chains per system)
+    bool used = false;
+    cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, d, info, n, batch, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    if (used) return TRIDIAG_SUCCESS;
+  }
   GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
   unsigned* piv = pivots ? pivots : w.piv;
   if (tdg::tw_eligible(layout, n, batch, sizeof(T))) {
@@ -125,6 +132,8 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
       cudaError_t e = algo == TRIDIAG_ALGO_CR    ? tdg::launch_crpcr_warp<T>(layout, a, b, c, d, d, n, batch, s, &used)
                       : algo == TRIDIAG_ALGO_PCR ? tdg::launch_pcr_warp<T>(layout, a, b, c, d, d, n, batch, s, &used)
                                                  : tdg::launch_wm_warp<T>(layout, a, b, c, d, d, n, batch, s, &used);
+      if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM)
+        e = tdg::launch_pge<T>(layout, a, b, c, d, d, nullptr, n, batch, s, &used);
       if (e == cudaSuccess && !used) {
         e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
         if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
@@ -173,6 +182,8 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
       cudaError_t e = algo == TRIDIAG_ALGO_CR    ? tdg::launch_crpcr_warp<T>(layout, a, b, c, d, x, n, batch, s, &used)
                       : algo == TRIDIAG_ALGO_PCR ? tdg::launch_pcr_warp<T>(layout, a, b, c, d, x, n, batch, s, &used)
                                                  : tdg::launch_wm_warp<T>(layout, a, b, c, d, x, n, batch, s, &used);
+      if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM)
+        e = tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       if (!work || work_bytes < solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, n, batch)) return TRIDIAG_ERR_WORKSPACE;
@@ -191,6 +202,10 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
       return cuda_status(e);
     }
     case TRIDIAG_ALGO_GTSV: {
+      bool used = false;
+      cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      if (used) return TRIDIAG_SUCCESS;
       size_t bytes = (size_t)n * (size_t)batch * sizeof(T);
       if (x != d && cudaMemcpyAsync(x, d, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
       return gtsv_impl<T>(layout, a, b, c, x, nullptr, nullptr, work, work_bytes, n, batch, s);
@@ -198,6 +213,70 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
     default:
       return TRIDIAG_ERR_INVALID_VALUE;
   }
+}
+
+// Refined solve workspace: FP32 a, b, c; two FP32 vectors (right-hand side /
+// correction, ping-ponged); one FP64 iterate; the FP32 pivoted solve's own
+// workspace.
+struct RefineWs {
+  float *a32, *b32, *c32, *v0, *v1;
+  double* w64;
+  void* gws;
+  size_t gws_bytes;
+};
+
+size_t refine_ws_bytes(int n, int batch) {
+  const size_t elems = (size_t)n * (size_t)batch;
+  return 5 * align_up(elems * sizeof(float)) + align_up(elems * sizeof(double)) + gtsv_ws_bytes<float>(n, batch);
+}
+
+RefineWs carve_refine(void* work, int n, int batch) {
+  const size_t elems = (size_t)n * (size_t)batch;
+  char* p = static_cast<char*>(work);
+  RefineWs w;
+  float** f[5] = {&w.a32, &w.b32, &w.c32, &w.v0, &w.v1};
+  for (float** q : f) {
+    *q = reinterpret_cast<float*>(p);
+    p += align_up(elems * sizeof(float));
+  }
+  w.w64 = reinterpret_cast<double*>(p);
+  p += align_up(elems * sizeof(double));
+  w.gws = p;
+  w.gws_bytes = gtsv_ws_bytes<float>(n, batch);
+  return w;
+}
+
+int refine_impl(int layout, const double* a, const double* b, const double* c, const double* d, double* x,
+                int iters, int* info, void* work, size_t work_bytes, int n, int batch, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !a || !b || !c || !d || !x || iters < 0 || iters > 8)
+    return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout != TRIDIAG_LAYOUT_CONTIGUOUS && layout != TRIDIAG_LAYOUT_INTERLEAVED) return TRIDIAG_ERR_NOT_SUPPORTED;
+  if (!work || work_bytes < refine_ws_bytes(n, batch)) return TRIDIAG_ERR_WORKSPACE;
+  const size_t elems = (size_t)n * (size_t)batch;
+  RefineWs w = carve_refine(work, n, batch);
+  // FP32 copies; v0 <- d
+  if (tdg::launch_narrow4(a, b, c, d, w.a32, w.b32, w.c32, w.v0, elems, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  // x0: FP32 pivoted solve in place in v0
+  int st = gtsv_impl<float>(layout, w.a32, w.b32, w.c32, w.v0, nullptr, info, w.gws, w.gws_bytes, n, batch, s);
+  if (st != TRIDIAG_SUCCESS) return st;
+  // The iterate lives in FP64 (x or w64, alternating so that the last step
+  // lands in x); dx holds the latest FP32 solution or correction.
+  const double* xcur = nullptr;
+  float* dx = w.v0;
+  float* spare = w.v1;
+  double* xs[2] = {(iters % 2) ? x : w.w64, (iters % 2) ? w.w64 : x};
+  for (int it = 0; it < iters; ++it) {
+    double* xnew = xs[it % 2];
+    if (tdg::launch_residual(layout, a, b, c, d, xcur, dx, xnew, spare, n, batch, s) != cudaSuccess)
+      return TRIDIAG_ERR_CUDA;
+    st = gtsv_impl<float>(layout, w.a32, w.b32, w.c32, spare, nullptr, nullptr, w.gws, w.gws_bytes, n, batch, s);
+    if (st != TRIDIAG_SUCCESS) return st;
+    xcur = xnew;
+    float* t = dx;
+    dx = spare;
+    spare = t;
+  }
+  return cuda_status(tdg::launch_update(xcur, dx, x, elems, s));
 }
 
 // Reference-style synchronous wrapper: launch, then wait for the device.
@@ -373,3 +452,32 @@ int tridiag_gtsv_adjoint_double(int layout, const double* a, const double* b, co
 }
 
 }  // extern "C"
+
+extern "C" {
+
+size_t tridiag_refine_workspace_size(int layout, int n, int batch) {
+  (void)layout;
+  if (!valid_dims(n, batch)) return 0;
+  return refine_ws_bytes(n, batch);
+}
+
+int tridiag_refine_double(int layout, const double* a, const double* b, const double* c, const double* d,
+                          double* x, int iters, int* info, void* work, size_t work_bytes, int n, int batch,
+                          void* stream) {
+  return set_status(refine_impl(layout, a, b, c, d, x, iters, info, work, work_bytes, n, batch,
+                                (cudaStream_t)stream));
+}
+
+int tridiag_convert_check(const double* in, float* out, double* back, size_t count, void* stream) {
+  if (!in || !out || !back) return set_status(TRIDIAG_ERR_INVALID_VALUE);
+  if (count == 0) return set_status(TRIDIAG_SUCCESS);
+  return set_status(cuda_status(tdg::launch_convert_probe(in, out, back, count, (cudaStream_t)stream)));
+}
+
+}  // extern "C"
+
+extern "C" long long tridiag_partition_fallbacks(int reset) {
+  unsigned long long v = 0;
+  if (tdg::pge_fallback_count(&v, reset != 0) != cudaSuccess) return -1;
+  return (long long)v;
+}

@@ -88,11 +88,11 @@ const Solver<double> kDouble[] = {
 constexpr int kExtBase = 32;
 const Solver<float> kFloatExt[] = {
     {ext_gtsv<float>, "GB300 pivoted WM-pGE (gtsv)", nullptr, nullptr, 0},
-    {ext_thomas_interleaved<float>, "GB300 Thomas, interleaved", nullptr, nullptr, 2},
+    {ext_thomas_interleaved<float>, "GB300 Thomas (interleaved layout)", nullptr, nullptr, 2},
 };
 const Solver<double> kDoubleExt[] = {
     {ext_gtsv<double>, "GB300 pivoted WM-pGE (gtsv)", nullptr, nullptr, 0},
-    {ext_thomas_interleaved<double>, "GB300 Thomas, interleaved", nullptr, nullptr, 2},
+    {ext_thomas_interleaved<double>, "GB300 Thomas (interleaved layout)", nullptr, nullptr, 2},
 };
 
 template <typename T>

@@ -63,6 +63,29 @@ template <typename T>
 cudaError_t launch_pcr_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                             cudaStream_t st, bool* used);
 
+// pge.cu: partitioned partial-pivoting solve (WM-pGE), one CTA per system
+// staged in shared memory (CONTIG / PACKED; n up to ~5K FP64, ~8K FP32).
+// Writes no pivot record.  x may alias d; info (may be null) per system.
+template <typename T>
+bool pge_eligible(int layout, int n);
+template <typename T>
+cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                       cudaStream_t s, bool* used);
+
+// Number of systems the partitioned solve handed to its sequential fallback
+// (synchronous read; optionally reset).
+cudaError_t pge_fallback_count(unsigned long long* out, bool reset);
+
+// refine.cu: pieces of the mixed-precision refined solve (FP64 in/out).
+cudaError_t launch_narrow4(const double* a, const double* b, const double* c, const double* d, float* a32,
+                           float* b32, float* c32, float* d32, size_t count, cudaStream_t s);
+// x_new = x_old + dx, r = d - A x_new (FP64, stored as FP32); x_old may be null (zero).
+cudaError_t launch_residual(int layout, const double* a, const double* b, const double* c, const double* d,
+                            const double* xold, const float* dx, double* xnew, float* r32, int n, int batch,
+                            cudaStream_t s);
+cudaError_t launch_update(const double* xold, const float* dx, double* xout, size_t count, cudaStream_t s);
+cudaError_t launch_convert_probe(const double* in, float* out, double* back, size_t count, cudaStream_t s);
+
 // pivot record: one 32-bit word per 32 rows per system
 inline size_t pivot_words(int n, int batch) { return (size_t)((n + 31) / 32) * (size_t)batch; }
 

@@ -1,0 +1,522 @@
+// Partitioned Gaussian elimination with partial pivoting (WM-pGE), one CTA
+// per system, the whole system staged in shared memory.
+//
+// The NT threads of a CTA split the system into NT partitions of m rows;
+// in each partition the first m-1 rows are "interior" and the last row is a
+// separator.  Thread t eliminates its interior block with partial pivoting
+// (the row interchanges of LAPACK ?gtsv) for three right-hand sides at once:
+// d, the left spike a_first e_1 (coupling to the previous separator) and the
+// right spike c_last e_{m-1} (coupling to its own separator), so that every
+// interior unknown becomes
+//     x_i = Y_i - V_i s_{t-1} - W_i s_t.
+// Substituting the neighbouring interior rows into each separator row gives
+// a tridiagonal system in the NT separators, solved by parallel cyclic
+// reduction in shared memory (log2 NT steps), or, when PCR's result fails a
+// backward-error check, with partial pivoting by one warp.  The interior unknowns then
+// follow from the formula above and x is written back with coalesced stores.
+// Zero pivots or non-finite results in a system (possible when an interior
+// block is singular although the whole matrix is not) send that system to a
+// sequential partial-pivoting solve by one thread of the CTA, which also
+// produces LAPACK's info value for singular matrices.
+//
+// Parallelism per system is NT chains instead of the one or two chains of a
+// Thomas-type sweep, which on GB300 matters most for FP64: the FP64 pipe
+// issues one warp instruction per ~70 cycles per SM sub-partition, so the
+// sweep needs every sub-partition busy.  Per row the interior work is ~8
+// FP64 operations forward, 9 backward and 2 for the final combination.
+//
+// Reference: the partition idea is the reference's WM-pGE
+// (Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884, without pivoting there);
+// the pivoting is that of its MKL row (Tridiagonal_AVX512/
+// tridiagonal_basic.cpp:131-143).
+#include <cstdint>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "tw.cuh"
+
+namespace tdg {
+
+__device__ __forceinline__ bool finite_val(double v) {
+  return (((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffull) != 0x7ffull;
+}
+__device__ __forceinline__ bool finite_val(float v) { return (((unsigned)__float_as_int(v) >> 23) & 0xffu) != 0xffu; }
+
+// Magnitude bits (|v| as an unsigned pattern, ordered like |v|) and the
+// biased exponent, on the integer pipe.
+__device__ __forceinline__ unsigned long long mag(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned mag(float v) { return (unsigned)__float_as_int(v) & 0x7fffffffu; }
+__device__ __forceinline__ int expo(double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff; }
+__device__ __forceinline__ int expo(float v) { return (int)((unsigned)__float_as_int(v) >> 23) & 0xff; }
+template <typename T>
+struct Fmt;
+template <>
+struct Fmt<double> {
+  static constexpr int BIAS = 1023;
+  static constexpr int GROWTH_LOG2 = 10;       // interior cancellation allowed: 2^10
+  static constexpr double SEP_TOL = 2.5e-13;   // separator-row backward error allowed
+  __device__ static double from_mag(unsigned long long m) { return __longlong_as_double((long long)m); }
+};
+template <>
+struct Fmt<float> {
+  static constexpr int BIAS = 127;
+  static constexpr int GROWTH_LOG2 = 2;
+  static constexpr double SEP_TOL = 5e-7;
+  __device__ static float from_mag(unsigned m) { return __int_as_float((int)m); }
+};
+
+// Sequential partial-pivoting solve of system `base` by one thread (the
+// fallback), U rows kept in shared memory (4 arrays of n).  Returns LAPACK's
+// info (0, or k+1 for the first zero pivot).  x may alias d.
+template <typename T>
+__device__ int pge_fallback(const T* a, const T* b, const T* c, const T* d, T* x, size_t base, int n, T* U0, T* U1,
+                            T* U2, T* Y) {
+  int info = 0;
+  T cb = b[base], cc = n > 1 ? c[base] : T(0), cy = d[base];
+  for (int i = 0; i + 1 < n; ++i) {
+    const T na = a[base + i + 1], nb = b[base + i + 1];
+    const T nc = i + 2 < n ? c[base + i + 1] : T(0);
+    const T ny = d[base + i + 1];
+    const bool sw = !abs_ge(cb, na);
+    const T piv = sw ? na : cb;
+    if (is_zero(piv) && !info) info = i + 1;
+    const T inv = T(1) / piv;
+    const T l = (sw ? cb : na) * inv;
+    U0[i] = inv;
+    U1[i] = sw ? nb : cc;
+    U2[i] = sw ? nc : T(0);
+    Y[i] = sw ? ny : cy;
+    const T ncb = fma(-l, sw ? nb : cc, sw ? cc : nb);
+    const T ncc = sw ? -l * nc : nc;
+    const T ncy = fma(-l, sw ? ny : cy, sw ? cy : ny);
+    cb = ncb;
+    cc = ncc;
+    cy = ncy;
+  }
+  if (is_zero(cb) && !info) info = n;
+  if (info) return info;
+  T x1 = cy / cb, x2 = T(0);
+  x[base + n - 1] = x1;
+  for (int i = n - 2; i >= 0; --i) {
+    const T xi = (Y[i] - U1[i] * x1 - U2[i] * x2) * U0[i];
+    x[base + i] = xi;
+    x2 = x1;
+    x1 = xi;
+  }
+  return 0;
+}
+
+constexpr int PGE_TMP = 9 * 32;
+
+// Systems that took the sequential fallback since the last reset (per device).
+__device__ unsigned long long g_pge_fallbacks = 0ull;
+
+// Pivoted solve of the NT-row separator system (rows sa/sb/sc/sd at SEP[0],
+// SEP[NT], SEP[2NT], SEP[3NT]) by one warp, solution to sx[0..NT).  Lane l
+// takes the K = NT/32 consecutive rows lK .. lK+K-1: its first K-1 rows are
+// eliminated with partial pivoting (three right-hand sides, as in the main
+// sweep) so that each becomes Y - V s_{l-1} - W s_l in the lanes' last rows
+// s; those 32 rows form a tridiagonal system that lane 0 solves
+// sequentially with partial pivoting.  Returns true on breakdown.
+template <typename T, int NT>
+__device__ bool sep_solve_pivoted(const T* SEP, T* sx, T* tmp, int lane) {
+  constexpr int K = NT / 32;
+  constexpr int MI = K - 1;
+  static_assert(K >= 2, "at least two separators per lane");
+  const int r0 = lane * K;
+  T a_[K], b_[K], c_[K], d_[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    a_[k] = SEP[r0 + k];
+    b_[k] = SEP[NT + r0 + k];
+    c_[k] = SEP[2 * NT + r0 + k];
+    d_[k] = SEP[3 * NT + r0 + k];
+  }
+  bool bad = false;
+  T inv[MI], u1[MI], u2[MI], ry[MI], rv[MI];
+  T cb = b_[0], cc = MI > 1 ? c_[0] : T(0), cy = d_[0], cv = a_[0], cw = MI == 1 ? c_[0] : T(0);
+  T w_prev = T(0);
+#pragma unroll
+  for (int i = 0; i + 1 < MI; ++i) {
+    const T na = a_[i + 1], nb = b_[i + 1], cn = c_[i + 1], ny = d_[i + 1];
+    const bool last = i + 2 == MI;
+    const T nc = last ? T(0) : cn;
+    const bool sw = !abs_ge(cb, na);
+    const T piv = sw ? na : cb;
+    bad |= is_zero(piv);
+    inv[i] = Div<T>(piv).inv();
+    const T l = (sw ? cb : na) * inv[i];
+    u1[i] = sw ? nb : cc;
+    u2[i] = sw ? nc : T(0);
+    ry[i] = sw ? ny : cy;
+    rv[i] = sw ? T(0) : cv;
+    cb = fma(-l, u1[i], sw ? cc : nb);
+    cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
+    cy = fma(-l, ry[i], sw ? cy : ny);
+    cv = sw ? cv : -l * cv;
+    if (last) {
+      w_prev = sw ? cn : cw;
+      cw = fma(-l, w_prev, sw ? cw : cn);
+    }
+  }
+  bad |= is_zero(cb);
+  inv[MI - 1] = Div<T>(cb).inv();
+  u1[MI - 1] = T(0);
+  u2[MI - 1] = T(0);
+  ry[MI - 1] = cy;
+  rv[MI - 1] = cv;
+  T Y[MI], V[MI], W[MI];
+#pragma unroll
+  for (int i = MI - 1; i >= 0; --i) {
+    const T y1 = i + 1 < MI ? Y[i + 1] : T(0), v1 = i + 1 < MI ? V[i + 1] : T(0), w1 = i + 1 < MI ? W[i + 1] : T(0);
+    const T y2 = i + 2 < MI ? Y[i + 2] : T(0), v2 = i + 2 < MI ? V[i + 2] : T(0), w2 = i + 2 < MI ? W[i + 2] : T(0);
+    const T wi = i == MI - 1 ? cw : (i == MI - 2 ? w_prev : T(0));
+    Y[i] = fma(-u2[i], y2, fma(-u1[i], y1, ry[i])) * inv[i];
+    V[i] = fma(-u2[i], v2, fma(-u1[i], v1, rv[i])) * inv[i];
+    W[i] = fma(-u2[i], w2, fma(-u1[i], w1, wi)) * inv[i];
+  }
+  // top-level row of this lane (its last row) and lane 0's sequential solve
+  const T Yf = shfl_down(Y[0], 1), Vf = shfl_down(V[0], 1), Wf = shfl_down(W[0], 1);
+  const bool has_next = lane < 31;
+  const T as = a_[K - 1], bs = b_[K - 1], cs = has_next ? c_[K - 1] : T(0), ds = d_[K - 1];
+  tmp[lane] = -as * V[MI - 1];
+  tmp[32 + lane] = fma(-cs, has_next ? Vf : T(0), fma(-as, W[MI - 1], bs));
+  tmp[64 + lane] = -cs * (has_next ? Wf : T(0));
+  tmp[96 + lane] = fma(-cs, has_next ? Yf : T(0), fma(-as, Y[MI - 1], ds));
+  __syncwarp();
+  int top_bad = 0;
+  if (lane == 0)
+    top_bad = pge_fallback<T>(tmp, tmp + 32, tmp + 64, tmp + 96, tmp + 128, 0, 32, tmp + 160, tmp + 192, tmp + 224,
+                              tmp + 256);
+  bad |= __shfl_sync(FULL, top_bad, 0) != 0;
+  __syncwarp();
+  const T sp = lane > 0 ? tmp[128 + lane - 1] : T(0);
+  const T st = tmp[128 + lane];
+#pragma unroll
+  for (int i = 0; i < MI; ++i) sx[r0 + i] = fma(-W[i], st, fma(-V[i], sp, Y[i]));
+  sx[r0 + K - 1] = st;
+  return bad;
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, const T* __restrict__ gb,
+                                                    const T* __restrict__ gc, const T* gd, T* gx, int* info, int n,
+                                                    int m, int ms, size_t sys_stride) {
+  constexpr int NW = NT / 32;
+  extern __shared__ __align__(16) unsigned char pge_smem[];
+  T* SA = reinterpret_cast<T*>(pge_smem);
+  T* SB = SA + NT * ms;
+  T* SC = SB + NT * ms;
+  T* SD = SC + NT * ms;
+  T* SV = SD + NT * ms;
+  T* SEP = SV + NT * ms;  // [3][4][NT] separator rows: original + ping-pong
+  T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
+  T* TMP = FST + 3 * NT;  // [PGE_TMP]: the FP32 separator solve's top level
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const size_t base = (size_t)blockIdx.x * sys_stride;
+  using MagT = decltype(mag(T(0)));
+  __shared__ MagT s_amax, s_dmax, s_xmax;
+  MagT amax = 0, dmax = 0;
+  if (t == 0) {
+    s_amax = 0;
+    s_dmax = 0;
+    s_xmax = 0;
+  }
+
+  // ---- stage the system: warp w loads partitions w, w+NW, ... (rows of a
+  // partition are contiguous in global memory); rows past n are identity rows
+#pragma unroll 4
+  for (int p = warp; p < NT; p += NW) {
+    for (int i = lane; i < m; i += 32) {
+      const int r = p * m + i;
+      T va = T(0), vb = T(1), vc = T(0), vd = T(0);
+      if (r < n) {
+        va = r > 0 ? ga[base + r] : T(0);
+        vb = gb[base + r];
+        vc = r < n - 1 ? gc[base + r] : T(0);
+        vd = gd[base + r];
+      }
+      const int s = p * ms + i;
+      SA[s] = va;
+      SB[s] = vb;
+      SC[s] = vc;
+      SD[s] = vd;
+      amax = max(amax, max(mag(va), max(mag(vb), mag(vc))));
+      dmax = max(dmax, mag(vd));
+    }
+  }
+  __syncthreads();
+  atomicMax(&s_amax, amax);
+  atomicMax(&s_dmax, dmax);
+
+  // ---- interior elimination of partition t (rows 0 .. mi-1), three RHS
+  const int mi = m - 1;
+  T* A = SA + t * ms;
+  T* B = SB + t * ms;
+  T* C = SC + t * ms;
+  T* D = SD + t * ms;
+  T* V = SV + t * ms;
+  bool bad = false;
+  unsigned long long swaps = 0ull;
+  T cb = B[0], cc = mi > 1 ? C[0] : T(0), cy = D[0], cv = A[0], cw = mi == 1 ? C[0] : T(0);
+  T w_prev = T(0);  // w of U row mi-2 (the only other row with a nonzero w)
+  for (int i = 0; i + 1 < mi; ++i) {
+    const T na = A[i + 1], nb = B[i + 1], cn = C[i + 1], ny = D[i + 1];
+    const bool last = i + 2 == mi;  // row i+1 is the last interior row
+    const T nc = last ? T(0) : cn;
+    const bool sw = !abs_ge(cb, na);
+    const T piv = sw ? na : cb;
+    bad |= is_zero(piv);
+    const Div<T> q(piv);
+    const T inv = q.inv();
+    const T l = (sw ? cb : na) * inv;
+    const T u1 = sw ? nb : cc;
+    const T uy = sw ? ny : cy;
+    A[i] = inv;
+    B[i] = u1;
+    D[i] = uy;
+    V[i] = sw ? T(0) : cv;
+    swaps |= (unsigned long long)sw << i;
+    cb = fma(-l, u1, sw ? cc : nb);
+    cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
+    cy = fma(-l, uy, sw ? cy : ny);
+    cv = sw ? cv : -l * cv;
+    if (last) {  // the right spike enters with row mi-1
+      const T nw = cn;
+      w_prev = sw ? nw : cw;
+      cw = fma(-l, w_prev, sw ? cw : nw);
+    }
+  }
+  // U row mi-1 is the remaining candidate row
+  bad |= is_zero(cb);
+  const T inv_last = Div<T>(cb).inv();
+  // back substitution for Y, V, W; results overwrite D (Y), V (V), A (W)
+  T Y1 = cy * inv_last, V1 = cv * inv_last, W1 = cw * inv_last;
+  T Y2 = T(0), V2 = T(0), W2 = T(0);
+  const T Ylast = Y1, Vlast = V1, Wlast = W1;
+  D[mi - 1] = Y1;
+  V[mi - 1] = V1;
+  A[mi - 1] = W1;
+  for (int i = mi - 2; i >= 0; --i) {
+    const T inv = A[i], u1 = B[i];
+    const T u2 = ((swaps >> i) & 1ull) && i + 2 < mi ? C[i + 1] : T(0);
+    const T wi = i == mi - 2 ? w_prev : T(0);
+    const T Yi = fma(-u2, Y2, fma(-u1, Y1, D[i])) * inv;
+    const T Vi = fma(-u2, V2, fma(-u1, V1, V[i])) * inv;
+    const T Wi = fma(-u2, W2, fma(-u1, W1, wi)) * inv;
+    D[i] = Yi;
+    V[i] = Vi;
+    A[i] = Wi;
+    Y2 = Y1;
+    V2 = V1;
+    W2 = W1;
+    Y1 = Yi;
+    V1 = Vi;
+    W1 = Wi;
+  }
+  // first-row values for the neighbouring separator
+  FST[t] = Y1;
+  FST[NT + t] = V1;
+  FST[2 * NT + t] = W1;
+  __syncthreads();
+
+  // ---- separator system: row m-1 of partition t couples to the last
+  // interior row of t and the first row of t+1
+  const T as = A[mi], bs = B[mi], cs = C[mi], ds = D[mi];
+  {
+    const bool has_next = t + 1 < NT;
+    const T Yf = has_next ? FST[t + 1] : T(0);
+    const T Vf = has_next ? FST[NT + t + 1] : T(0);
+    const T Wf = has_next ? FST[2 * NT + t + 1] : T(0);
+    SEP[t] = -as * Vlast;
+    SEP[NT + t] = fma(-cs, Vf, fma(-as, Wlast, bs));
+    SEP[2 * NT + t] = -cs * Wf;
+    SEP[3 * NT + t] = fma(-cs, Yf, fma(-as, Ylast, ds));
+  }
+  __syncthreads();
+  // Parallel cyclic reduction of the separator system (SEP[0..4NT) keeps the
+  // original rows, SEP[4NT..12NT) is the ping-pong pair) ...
+  {
+    const T* cur = SEP;
+    int ph = 1;
+#pragma unroll 1
+    for (int s = 1; s < NT; s <<= 1) {
+      T* nxt = SEP + ph * 4 * NT;
+      const T a0 = cur[t], b0 = cur[NT + t], c0 = cur[2 * NT + t], d0 = cur[3 * NT + t];
+      T nb = b0, nd = d0, na = T(0), nc = T(0);
+      if (t >= s) {
+        const T al = Div<T>(cur[NT + t - s]).div(a0);
+        nb = fma(-al, cur[2 * NT + t - s], nb);
+        nd = fma(-al, cur[3 * NT + t - s], nd);
+        na = -al * cur[t - s];
+      }
+      if (t + s < NT) {
+        const T gm = Div<T>(cur[NT + t + s]).div(c0);
+        nb = fma(-gm, cur[t + s], nb);
+        nd = fma(-gm, cur[3 * NT + t + s], nd);
+        nc = -gm * cur[2 * NT + t + s];
+      }
+      nxt[t] = na;
+      nxt[NT + t] = nb;
+      nxt[2 * NT + t] = nc;
+      nxt[3 * NT + t] = nd;
+      cur = nxt;
+      ph = 3 - ph;
+      __syncthreads();
+    }
+    FST[t] = Div<T>(cur[NT + t]).div(cur[3 * NT + t]);  // FST is free again: separator values
+  }
+  __syncthreads();
+  // ... accepted when its normwise backward error on the separator system is
+  // within a few units of roundoff; otherwise (PCR does not pivot, and on
+  // non-dominant separator systems its growth can be large) warp 0 solves
+  // the separator system again with partial pivoting.
+  {
+    const T st = FST[t];
+    const T sp = t > 0 ? FST[t - 1] : T(0), sn = t + 1 < NT ? FST[t + 1] : T(0);
+    const T sa = SEP[t], sb = SEP[NT + t], sc = SEP[2 * NT + t], sd = SEP[3 * NT + t];
+    const T r = fma(-sc, sn, fma(-sb, st, fma(-sa, sp, sd)));
+    const T scale = fabs(sa * sp) + fabs(sb * st) + fabs(sc * sn) + fabs(sd);
+    const T tol = sizeof(T) == 8 ? T(16 * 1.1102230246251565e-16) : T(4 * 5.9604645e-8);
+    const bool reject = !(fabs(r) <= tol * scale);  // also catches NaN/Inf
+    if (__syncthreads_or(reject)) {
+      if (warp == 0) bad |= sep_solve_pivoted<T, NT>(SEP, FST, TMP, lane);
+    }
+  }
+  __syncthreads();
+  // ---- combination x = Y - V s_{t-1} - W s_t, and the acceptance test:
+  // the result is kept when (1) no interior row cancels more than
+  // 2^GROWTH_LOG2 against max(|x|, |d|/|A|) -- estimated from exponents on
+  // the integer pipe -- so the interior rows' residuals stay within a few
+  // ulps of |A||x|, and (2) the separator rows' residuals, computed exactly,
+  // meet SEP_TOL relative to max|A| max|x| + max|d|.  Rejected systems (and
+  // breakdowns) take the sequential partial-pivoting solve.
+  const T sp = t > 0 ? FST[t - 1] : T(0);
+  const T st = FST[t];
+  int gexp = 0;
+  MagT xmax = mag(st);
+  {
+    const int esp = expo(sp), est = expo(st);
+    T x_last = T(0);
+    for (int i = 0; i < mi; ++i) {
+      const T Yi = D[i], Vi = V[i], Wi = A[i];
+      const T xi = fma(-Wi, st, fma(-Vi, sp, Yi));
+      gexp = max(gexp, max(expo(Yi), max(expo(Vi) + esp, expo(Wi) + est) - Fmt<T>::BIAS));
+      xmax = max(xmax, mag(xi));
+      bad |= !finite_val(xi);
+      D[i] = xi;
+      x_last = xi;
+    }
+    bad |= !finite_val(st);
+    D[mi] = st;
+    FST[NT + t] = D[0];  // first x of the partition, for the separator residual of t-1
+    atomicMax(&s_xmax, xmax);
+    __syncthreads();
+    const T x_next = t + 1 < NT ? FST[NT + t + 1] : T(0);
+    // (one row per partition: formed in FP64 for both precisions)
+    const double r = fma(-(double)cs, (double)x_next,
+                         fma(-(double)bs, (double)st, fma(-(double)as, (double)x_last, (double)ds)));
+    const T amx = Fmt<T>::from_mag(s_amax), xmx = Fmt<T>::from_mag(s_xmax), dmx = Fmt<T>::from_mag(s_dmax);
+    bad |= !(fabs(r) <= Fmt<T>::SEP_TOL * fma((double)amx, (double)xmx, (double)dmx));
+    // interior: 2^gexp against max(|x|, |d|/|A|) (exponent arithmetic)
+    const int xref = max(expo(xmx), expo(dmx) - expo(amx) + Fmt<T>::BIAS);
+    bad |= gexp > xref + Fmt<T>::GROWTH_LOG2;
+  }
+  if (__syncthreads_or(bad)) {
+    // an interior block or the separator system broke down or lost accuracy
+    if (t == 0) {
+      atomicAdd(&g_pge_fallbacks, 1ull);
+      const int inf = pge_fallback<T>(ga, gb, gc, gd, gx, base, n, SA, SB, SC, SD);
+      if (info) info[blockIdx.x] = inf;
+    }
+    return;
+  }
+  if (info && t == 0) info[blockIdx.x] = 0;
+#pragma unroll 4
+  for (int p = warp; p < NT; p += NW) {
+    for (int i = lane; i < m; i += 32) {
+      const int r = p * m + i;
+      if (r < n) gx[base + r] = SD[p * ms + i];
+    }
+  }
+}
+
+template <typename T, int NT>
+static size_t pge_smem_bytes(int ms) {
+  return ((size_t)5 * NT * ms + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
+}
+
+constexpr size_t PGE_SMEM_MAX = 227 * 1024 - 64;  // dynamic + the kernel's few static bytes
+
+template <typename T, int NT>
+static bool pge_fits(int n, int* m_out, int* ms_out) {
+  const int m = (n + NT - 1) / NT;
+  if (m < 2 || m > 64) return false;
+  const int ms = m | 1;  // odd stride: a warp's rows fall into distinct banks
+  if (pge_smem_bytes<T, NT>(ms) > PGE_SMEM_MAX) return false;
+  *m_out = m;
+  *ms_out = ms;
+  return true;
+}
+
+template <typename T, int NT>
+static cudaError_t pge_launch(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                              int m, int ms, size_t stride, cudaStream_t s) {
+  const size_t smem = pge_smem_bytes<T, NT>(ms);
+  cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  pge_kernel<T, NT><<<batch, NT, smem, s>>>(a, b, c, d, x, info, n, m, ms, stride);
+  return cudaGetLastError();
+}
+
+template <typename T>
+bool pge_eligible(int layout, int n) {
+  int m, ms;
+  if (layout != CONTIG && layout != PACKED) return false;
+  return pge_fits<T, 128>(n, &m, &ms) || pge_fits<T, 64>(n, &m, &ms) || pge_fits<T, 256>(n, &m, &ms);
+}
+
+template <typename T>
+cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                       cudaStream_t s, bool* used) {
+  *used = false;
+  if (layout != CONTIG && layout != PACKED) return cudaSuccess;
+  const size_t stride = layout == PACKED ? 4 * (size_t)n : (size_t)n;
+  int m, ms;
+  // 128 partitions where the system fits (four warps: one per SM
+  // sub-partition), else fewer for short systems or more for long ones
+  if (pge_fits<T, 128>(n, &m, &ms)) {
+    *used = true;
+    return pge_launch<T, 128>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+  }
+  if (n < 256 && pge_fits<T, 64>(n, &m, &ms)) {
+    *used = true;
+    return pge_launch<T, 64>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+  }
+  if (pge_fits<T, 256>(n, &m, &ms)) {
+    *used = true;
+    return pge_launch<T, 256>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+  }
+  return cudaSuccess;
+}
+
+cudaError_t pge_fallback_count(unsigned long long* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_pge_fallbacks, sizeof(*out));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long zero = 0ull;
+    e = cudaMemcpyToSymbol(g_pge_fallbacks, &zero, sizeof(zero));
+  }
+  return e;
+}
+
+#define INST(T)                                                                                                   \
+  template bool pge_eligible<T>(int, int);                                                                        \
+  template cudaError_t launch_pge<T>(int, const T*, const T*, const T*, const T*, T*, int*, int, int, cudaStream_t, \
+                                     bool*);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace tdg

@@ -1,0 +1,186 @@
+// Kernels of the mixed-precision refined solve: FP64 inputs, FP32 pivoted
+// solves, FP64 residuals.
+//
+//   narrow:   a, b, c, d (FP64) -> FP32 copies
+//   residual: x_new = x_old + dx (FP64), r = d - A x_new (FP64) -> FP32
+//   update:   x_out = x_old + dx
+//
+// On GB300 the FP64 pipe (and with it cvt.f32.f64 / cvt.f64.f32) runs at
+// ~1/50 of the FP32 rate, so the conversions here use the integer pipe: an
+// FP64 -> FP32 narrowing is the IEEE 754 round-to-nearest-even of the 52-bit
+// significand to 23 bits done on the bit pattern, and FP32 -> FP64 widening
+// is exact (re-biased exponent, significand shifted by 29).  Only zeros,
+// infinities, NaNs and values outside the FP32 normal range take the
+// hardware conversion.  The FP64 pipe then carries only the residual's three
+// FMAs and the update's add per row.
+#include <cstdint>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace tdg {
+
+__device__ __forceinline__ float narrow_rn(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  const int e32 = e - 1023 + 127;
+  if (e == 0) return __uint_as_float(sign);  // zero, or an FP64 subnormal (rounds to zero in FP32)
+  if (e32 >= 1 && e32 <= 254) {
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of the 52 significand bits
+    const unsigned half = (lo >> 28) & 1u;                    // first dropped bit
+    const unsigned rest = lo & 0x0fffffffu;                   // the other 28 dropped bits
+    unsigned r = sign | ((unsigned)e32 << 23) | m;
+    r += half & ((rest != 0u) | (m & 1u));  // ties to even; a carry rolls into the exponent (up to inf)
+    return __uint_as_float(r);
+  }
+  return __double2float_rn(v);  // inf, NaN, overflow, FP32 subnormal range
+}
+
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  if (e == 0u || e == 255u) return (double)f;  // FP32 subnormal, inf, NaN
+  const unsigned hi = (u & 0x80000000u) | ((e + 1023u - 127u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// a, b, c, d -> FP32, two elements per thread and array when the arrays are
+// 16-byte aligned (checked on the host), else one.
+template <bool VEC>
+__global__ void __launch_bounds__(256) narrow4_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                      const double* __restrict__ c, const double* __restrict__ d,
+                                                      float* __restrict__ a32, float* __restrict__ b32,
+                                                      float* __restrict__ c32, float* __restrict__ d32,
+                                                      size_t count) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (VEC) {
+    const size_t pairs = count / 2;
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += stride) {
+      const double2 va = __ldg(reinterpret_cast<const double2*>(a) + p);
+      const double2 vb = __ldg(reinterpret_cast<const double2*>(b) + p);
+      const double2 vc = __ldg(reinterpret_cast<const double2*>(c) + p);
+      const double2 vd = __ldg(reinterpret_cast<const double2*>(d) + p);
+      reinterpret_cast<float2*>(a32)[p] = make_float2(narrow_rn(va.x), narrow_rn(va.y));
+      reinterpret_cast<float2*>(b32)[p] = make_float2(narrow_rn(vb.x), narrow_rn(vb.y));
+      reinterpret_cast<float2*>(c32)[p] = make_float2(narrow_rn(vc.x), narrow_rn(vc.y));
+      reinterpret_cast<float2*>(d32)[p] = make_float2(narrow_rn(vd.x), narrow_rn(vd.y));
+    }
+    if ((count & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+      const size_t k = count - 1;
+      a32[k] = narrow_rn(a[k]);
+      b32[k] = narrow_rn(b[k]);
+      c32[k] = narrow_rn(c[k]);
+      d32[k] = narrow_rn(d[k]);
+    }
+  } else {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+      a32[k] = narrow_rn(a[k]);
+      b32[k] = narrow_rn(b[k]);
+      c32[k] = narrow_rn(c[k]);
+      d32[k] = narrow_rn(d[k]);
+    }
+  }
+}
+
+// Row i of system j lives at j*n + i (CONTIG) or i*batch + j (INTERLEAVED);
+// the neighbours of a row are one element (CONTIG) or one row of the batch
+// (INTERLEAVED) away.  The grid walks (outer, inner) tiles: outer = system
+// for CONTIG, row for INTERLEAVED; inner is the unit-stride index.
+template <int L>
+__global__ void __launch_bounds__(256) residual_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                       const double* __restrict__ c, const double* __restrict__ d,
+                                                       const double* __restrict__ xold, const float* __restrict__ dx,
+                                                       double* __restrict__ xnew, float* __restrict__ r32, int n,
+                                                       int batch) {
+  const int inner_len = L == INTERLEAVED ? batch : n;
+  const int outer_len = L == INTERLEAVED ? n : batch;
+  const size_t nb = (size_t)(L == INTERLEAVED ? batch : 1);  // distance to the neighbouring row
+  for (int o = blockIdx.y; o < outer_len; o += gridDim.y) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < inner_len; t += gridDim.x * blockDim.x) {
+      const size_t k = (size_t)o * inner_len + t;
+      const int i = L == INTERLEAVED ? o : t;  // row index within the system
+      auto xat = [&](size_t q) { return (xold ? xold[q] : 0.0) + widen(dx[q]); };
+      const double xi = xat(k);
+      double r = fma(-__ldg(b + k), xi, __ldg(d + k));
+      if (i > 0) r = fma(-__ldg(a + k), xat(k - nb), r);
+      if (i < n - 1) r = fma(-__ldg(c + k), xat(k + nb), r);
+      xnew[k] = xi;
+      r32[k] = narrow_rn(r);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) update_kernel(const double* __restrict__ xold, const float* __restrict__ dx,
+                                                     double* xout, size_t count) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride)
+    xout[k] = (xold ? xold[k] : 0.0) + widen(dx[k]);
+}
+
+static int grid_for(size_t work, int threads) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t want = (work + threads - 1) / threads;
+  const size_t cap = (size_t)sms * 8;
+  return (int)(want < cap ? (want ? want : 1) : cap);
+}
+
+cudaError_t launch_narrow4(const double* a, const double* b, const double* c, const double* d, float* a32,
+                           float* b32, float* c32, float* d32, size_t count, cudaStream_t s) {
+  const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+                     reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(d) |
+                     reinterpret_cast<uintptr_t>(a32) | reinterpret_cast<uintptr_t>(b32) |
+                     reinterpret_cast<uintptr_t>(c32) | reinterpret_cast<uintptr_t>(d32)) &
+                    15u) == 0;
+  if (vec)
+    narrow4_kernel<true><<<grid_for(count / 2, 256), 256, 0, s>>>(a, b, c, d, a32, b32, c32, d32, count);
+  else
+    narrow4_kernel<false><<<grid_for(count, 256), 256, 0, s>>>(a, b, c, d, a32, b32, c32, d32, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_residual(int layout, const double* a, const double* b, const double* c, const double* d,
+                            const double* xold, const float* dx, double* xnew, float* r32, int n, int batch,
+                            cudaStream_t s) {
+  const int inner = layout == INTERLEAVED ? batch : n;
+  const int outer = layout == INTERLEAVED ? n : batch;
+  const int threads = 256;
+  const int gx = (inner + threads - 1) / threads;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int gy_cap = (sms * 8 + gx - 1) / gx;
+  const int gy = outer < gy_cap ? outer : (gy_cap < 65535 ? gy_cap : 65535);
+  dim3 grid(gx, gy > 0 ? gy : 1);
+  if (layout == INTERLEAVED)
+    residual_kernel<INTERLEAVED><<<grid, threads, 0, s>>>(a, b, c, d, xold, dx, xnew, r32, n, batch);
+  else
+    residual_kernel<CONTIG><<<grid, threads, 0, s>>>(a, b, c, d, xold, dx, xnew, r32, n, batch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update(const double* xold, const float* dx, double* xout, size_t count, cudaStream_t s) {
+  update_kernel<<<grid_for(count, 256), 256, 0, s>>>(xold, dx, xout, count);
+  return cudaGetLastError();
+}
+
+// Conversion check used by the tests: out[k] = narrow_rn(in[k]) and
+// back[k] = widen(out[k]).
+__global__ void convert_probe_kernel(const double* in, float* out, double* back, size_t count) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (size_t)gridDim.x * blockDim.x) {
+    const float f = narrow_rn(in[k]);
+    out[k] = f;
+    back[k] = widen(f);
+  }
+}
+
+cudaError_t launch_convert_probe(const double* in, float* out, double* back, size_t count, cudaStream_t s) {
+  convert_probe_kernel<<<grid_for(count, 256), 256, 0, s>>>(in, out, back, count);
+  return cudaGetLastError();
+}
+
+}  // namespace tdg

@@ -36,6 +36,14 @@ def _ptr(t: torch.Tensor | None, dtype=None) -> int | None:
     return int(t.data_ptr())
 
 
+def _al(t: torch.Tensor | None) -> torch.Tensor | None:
+    """A read-only input with a 16-byte aligned start (the TMA kernels need
+    one): views at odd offsets are copied, everything else passes through."""
+    if t is None or (t.is_contiguous() and t.data_ptr() % 16 == 0):
+        return t
+    return t.contiguous().clone()
+
+
 def _prec(t: torch.Tensor) -> str:
     if t.dtype not in _DT:
         raise TypeError(f"unsupported dtype {t.dtype} (float32 or float64)")
@@ -75,6 +83,7 @@ def solve_out(a, b, c, d, n: int, algo: str = "auto", layout: str = "contiguous"
     """Out-of-place solve: a, b, c, d untouched; returns x (new or ``out``)."""
     p = _prec(a)
     batch = _dims(a, n, layout)
+    a, b, c, d = _al(a), _al(b), _al(c), _al(d)
     x = out if out is not None else torch.empty_like(d)
     work = work if work is not None else solve_out_workspace(a, n, algo, layout)
     st = getattr(lib(), f"tridiag_solve_out_{p}")(
@@ -104,7 +113,8 @@ def gtsv(a, b, c, d, n: int, layout: str = "contiguous", pivots=None, info=None,
     0 or k+1 for the first zero pivot of each system."""
     p = _prec(a)
     batch = _dims(a, n, layout)
-    x = out if out is not None else torch.empty_like(d)
+    a, b, c = _al(a), _al(b), _al(c)
+    x = out if out is not None else torch.empty_like(d, memory_format=torch.contiguous_format)
     if x.data_ptr() != d.data_ptr():
         x.copy_(d)
     work = work if work is not None else gtsv_workspace(a, n, layout)
@@ -120,6 +130,7 @@ def gtsv_adjoint(a, b, c, x, pivots, xbar, n: int, layout: str = "contiguous", w
     reusing the forward call's pivot record."""
     p = _prec(a)
     batch = _dims(a, n, layout)
+    a, b, c, x, xbar = _al(a), _al(b), _al(c), _al(x), _al(xbar)
     ga, gb, gc, gd = (torch.empty_like(a) for _ in range(4))
     work = work if work is not None else gtsv_workspace(a, n, layout)
     st = getattr(lib(), f"tridiag_gtsv_adjoint_{p}")(
@@ -128,6 +139,39 @@ def gtsv_adjoint(a, b, c, x, pivots, xbar, n: int, layout: str = "contiguous", w
         _stream_ptr(stream))
     check(st, f"tridiag_gtsv_adjoint_{p}")
     return ga, gb, gc, gd
+
+
+def refine_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
+    batch = _dims(a, n, layout)
+    return torch.empty(lib().tridiag_refine_workspace_size(LAYOUTS[layout], n, batch), dtype=torch.uint8,
+                       device=a.device)
+
+
+def refine(a, b, c, d, n: int, iters: int = 2, layout: str = "contiguous", info=None, work=None, out=None,
+           stream=None):
+    """Mixed-precision solve of FP64 systems: FP32 partial-pivoting solves,
+    ``iters`` refinement steps with the residual d - A x formed in FP64.
+    a, b, c, d (float64) are not modified; returns x (float64)."""
+    if a.dtype != torch.float64:
+        raise TypeError("refine takes float64 arrays")
+    batch = _dims(a, n, layout)
+    a, b, c, d = _al(a), _al(b), _al(c), _al(d)
+    x = out if out is not None else torch.empty_like(d)
+    work = work if work is not None else refine_workspace(a, n, layout)
+    st = lib().tridiag_refine_double(LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype),
+                                     _ptr(d, a.dtype), _ptr(x, a.dtype), iters, _ptr(info), _ptr(work),
+                                     work.numel(), n, batch, _stream_ptr(stream))
+    check(st, "tridiag_refine_double")
+    return x
+
+
+def convert_check(v: torch.Tensor):
+    """(float32 narrowing, float64 widening of it) as the refined solve computes them."""
+    out = torch.empty(v.numel(), dtype=torch.float32, device=v.device)
+    back = torch.empty(v.numel(), dtype=torch.float64, device=v.device)
+    check(lib().tridiag_convert_check(_ptr(v, torch.float64), _ptr(out), _ptr(back), v.numel(), _stream_ptr()),
+          "tridiag_convert_check")
+    return out, back
 
 
 def reference_call(name: str, a, b, c, d, n: int):

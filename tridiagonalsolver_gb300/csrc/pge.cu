@@ -110,6 +110,16 @@ __device__ int pge_fallback(const T* a, const T* b, const T* c, const T* d, T* x
 
 constexpr int PGE_TMP = 9 * 32;
 
+// One element global -> shared, asynchronously (cp.async, 4 or 8 bytes).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
 // Systems that took the sequential fallback since the last reset (per device).
 __device__ unsigned long long g_pge_fallbacks = 0ull;
 
@@ -225,29 +235,43 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
     s_xmax = 0;
   }
 
-  // ---- stage the system: warp w loads partitions w, w+NW, ... (rows of a
-  // partition are contiguous in global memory); rows past n are identity rows
+  // ---- stage the system with asynchronous element copies (cp.async): warp
+  // w copies partitions w, w+NW, ... (a partition's rows are contiguous in
+  // global memory, so each copy instruction moves 32 consecutive elements)
+  // into the odd-stride layout; every copy is in flight before the first
+  // wait.  a_0, c_{n-1} and the identity rows past n are stored directly.
 #pragma unroll 4
   for (int p = warp; p < NT; p += NW) {
     for (int i = lane; i < m; i += 32) {
       const int r = p * m + i;
-      T va = T(0), vb = T(1), vc = T(0), vd = T(0);
-      if (r < n) {
-        va = r > 0 ? ga[base + r] : T(0);
-        vb = gb[base + r];
-        vc = r < n - 1 ? gc[base + r] : T(0);
-        vd = gd[base + r];
-      }
       const int s = p * ms + i;
-      SA[s] = va;
-      SB[s] = vb;
-      SC[s] = vc;
-      SD[s] = vd;
-      amax = max(amax, max(mag(va), max(mag(vb), mag(vc))));
-      dmax = max(dmax, mag(vd));
+      if (r < n) {
+        if (r > 0) cp_async_elem(SA + s, ga + base + r); else SA[s] = T(0);
+        cp_async_elem(SB + s, gb + base + r);
+        if (r < n - 1) cp_async_elem(SC + s, gc + base + r); else SC[s] = T(0);
+        cp_async_elem(SD + s, gd + base + r);
+      } else {
+        SA[s] = T(0);
+        SB[s] = T(1);
+        SC[s] = T(0);
+        SD[s] = T(0);
+      }
     }
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
+  // magnitudes for the acceptance test: max |a|, |b|, |c| and max |d| over
+  // the partition's rows (integer pipe)
+  {
+    const T* A0 = SA + t * ms;
+    const T* B0 = SB + t * ms;
+    const T* C0 = SC + t * ms;
+    const T* D0 = SD + t * ms;
+    for (int i = 0; i < m; ++i) {
+      amax = max(amax, max(mag(A0[i]), max(mag(B0[i]), mag(C0[i]))));
+      dmax = max(dmax, mag(D0[i]));
+    }
+  }
   atomicMax(&s_amax, amax);
   atomicMax(&s_dmax, dmax);
 
@@ -423,6 +447,38 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
     // interior: 2^gexp against max(|x|, |d|/|A|) (exponent arithmetic)
     const int xref = max(expo(xmx), expo(dmx) - expo(amx) + Fmt<T>::BIAS);
     bad |= gexp > xref + Fmt<T>::GROWTH_LOG2;
+  }
+  if (__syncthreads_or(bad)) {
+    // The bound above is conservative: measure the normwise backward error
+    // max|d - A x| / (|A|_inf |x|_inf + |d|_inf) exactly (FP64, inputs
+    // re-read from global memory) before giving up on this result.
+    __shared__ unsigned long long s_rmax, s_anorm;
+    if (t == 0) {
+      s_rmax = 0ull;
+      s_anorm = 0ull;
+    }
+    __syncthreads();
+    unsigned long long rmax = 0ull, anorm = 0ull;
+    bool nonfinite = false;
+    auto xs = [&](int r) { return (double)SD[(r / m) * ms + (r % m)]; };
+    for (int r = t; r < n; r += NT) {
+      const double ar = r > 0 ? (double)ga[base + r] : 0.0, br = (double)gb[base + r];
+      const double cr = r < n - 1 ? (double)gc[base + r] : 0.0, dr = (double)gd[base + r];
+      const double xr = xs(r);
+      double res = fma(-br, xr, dr);
+      if (r > 0) res = fma(-ar, xs(r - 1), res);
+      if (r < n - 1) res = fma(-cr, xs(r + 1), res);
+      nonfinite |= !finite_val(res);
+      rmax = max(rmax, mag(res));
+      anorm = max(anorm, mag(fabs(ar) + fabs(br) + fabs(cr)));
+    }
+    atomicMax(&s_rmax, rmax);
+    atomicMax(&s_anorm, anorm);
+    __syncthreads();
+    const double eta = __longlong_as_double((long long)s_rmax) /
+                       fma(__longlong_as_double((long long)s_anorm), (double)Fmt<T>::from_mag(s_xmax),
+                           (double)Fmt<T>::from_mag(s_dmax));
+    bad = nonfinite || !(eta <= Fmt<T>::SEP_TOL);
   }
   if (__syncthreads_or(bad)) {
     // an interior block or the separator system broke down or lost accuracy

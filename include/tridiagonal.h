@@ -60,7 +60,7 @@ void BPLG_PCR(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt,
  * systems that fit one warp (n <= 1024 FP32, 512 FP64) run the on-chip
  * version without pivoting, as the reference does; longer systems run the
  * partitioned solve with partial pivoting inside each partition (one CTA per
- * system, up to ~8K rows FP32 / ~5K FP64), beyond that the Thomas sweep. */
+ * system, up to 8960 rows FP32 / 4480 FP64), beyond that the Thomas sweep. */
 void WM5_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 void WM4_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 void WM5_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
@@ -132,7 +132,8 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 #define TRIDIAG_ALGO_CR 2     /* CR-PCR hybrid, one warp per system */
 #define TRIDIAG_ALGO_PCR 3    /* PCR-pThomas, one warp per system */
 #define TRIDIAG_ALGO_WM 4     /* WM-pGE, one warp per system, unpivoted */
-#define TRIDIAG_ALGO_GTSV 5   /* partial pivoting, one thread per system */
+#define TRIDIAG_ALGO_GTSV 5   /* partial pivoting: PGE for n >= 1024 where it fits, else one thread per system */
+#define TRIDIAG_ALGO_PGE 6    /* WM-pGE with partial pivoting inside partitions, one CTA per system */
 
 /* Status of the last library call made by the calling host thread. */
 int tridiag_last_status(void);
@@ -217,6 +218,22 @@ int tridiag_refine_double(int layout, const double *a, const double *b, const do
  * as the refined solve performs them on the integer pipe: out[k] = (float)
  * in[k], back[k] = (double)out[k].  For tests of that conversion. */
 int tridiag_convert_check(const double *in, float *out, double *back, size_t count, void *stream);
+
+/* WM-pGE with partial pivoting inside each partition, one CTA per system
+ * staged in shared memory (contiguous or packed layout; n from 65 up to
+ * 8960 rows FP32, 4480 FP64, else TRIDIAG_ERR_NOT_SUPPORTED).  The NT
+ * threads of a CTA each eliminate one partition (three right-hand sides);
+ * the separator system is solved by PCR, or with partial pivoting when
+ * PCR's result fails a backward-error check; results whose separator rows
+ * miss the residual bound and then an exact backward-error check are
+ * refined in the kernel (FP64 residual, up to two correction passes) and,
+ * if that does not reach the bound, recomputed by a sequential
+ * partial-pivoting solve.  a, b, c, d are read
+ * only (x may alias d); info (may be NULL) as tridiag_gtsv_*. */
+int tridiag_pge_single(int layout, const float *a, const float *b, const float *c, const float *d, float *x,
+                       int *info, int n_eqt, int n_batch, void *stream);
+int tridiag_pge_double(int layout, const double *a, const double *b, const double *c, const double *d, double *x,
+                       int *info, int n_eqt, int n_batch, void *stream);
 
 /* Diagnostics: how many systems the partitioned partial-pivoting solve (used
  * by tridiag_gtsv_* without a pivot record, tridiag_solve_out_* with

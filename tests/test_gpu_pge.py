@@ -29,14 +29,14 @@ def _solve(cuda, arrs, dt, n):
     batch = arrs[0].shape[0]
     ts = [cuda.from_numpy(np.ascontiguousarray(v.astype(dt))).cuda() for v in arrs]
     info = cuda.full((batch,), -7, dtype=cuda.int32, device="cuda")
-    x = T.gtsv(*ts, n, info=info)  # no pivot record requested: the partitioned solve
+    x = T.pge(*ts, n, info=info)
     cuda.cuda.synchronize()
     return x.double().cpu().numpy().reshape(batch, n), info.cpu().numpy()
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32])
 @pytest.mark.parametrize("n,batch", [(65, 9), (100, 33), (128, 5), (129, 40), (255, 7), (256, 16), (257, 16),
-                                     (1000, 37), (2048, 8), (4095, 8), (4096, 24), (5000, 6), (5248, 4)])
+                                     (1000, 37), (2048, 8), (4095, 8), (4096, 24), (4480, 6)])
 def test_pge_matches_oracle(cuda, dt, n, batch):
     a, b, c, d = inputs.nondominant(n, batch, seed=3 * n + batch)
     x, info = _solve(cuda, (a, b, c, d), dt, n)
@@ -48,7 +48,7 @@ def test_pge_matches_oracle(cuda, dt, n, batch):
     assert np.median(_rel(x, xo)) <= (1e-11 if dt == np.float64 else 1e-3)
 
 
-@pytest.mark.parametrize("n,batch", [(6000, 4), (8192, 6), (10000, 2)])
+@pytest.mark.parametrize("n,batch", [(6000, 4), (8192, 6), (8960, 2)])
 def test_pge_fp32_long(cuda, n, batch):
     a, b, c, d = inputs.nondominant(n, batch, seed=n)
     x, info = _solve(cuda, (a, b, c, d), np.float32, n)
@@ -110,7 +110,7 @@ def test_pge_bench_shape_fp64(cuda):
     a, b, c, d = (torch.rand((batch, n), dtype=torch.float64, device="cuda", generator=g) * 2 - 1 for _ in range(4))
     info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
     T.lib().tridiag_partition_fallbacks(1)
-    x = T.gtsv(a, b, c, d, n, info=info)
+    x = T.gtsv(a, b, c, d, n, info=info)  # no pivot record requested: the partitioned solve
     assert int((info != 0).sum()) == 0
     fb = T.lib().tridiag_partition_fallbacks(1)
     print(f"partitioned solve: {fb} of {batch} systems took the sequential fallback")
@@ -136,6 +136,16 @@ def test_reference_wm_names_long_systems(cuda, name, dt, n):
     x = ts[3].double().cpu().numpy().reshape(batch, n)
     _, worst = O.backward_error(*(v.astype(dt).astype(np.float64) for v in (a, b, c, d)), x, n)
     assert worst <= ETA[dt]
+
+
+def test_pge_unsupported_sizes(cuda):
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import TridiagError
+
+    for n in (1, 64, 20000):
+        t = cuda.ones(n * 2, dtype=cuda.float64, device="cuda")
+        with pytest.raises(TridiagError):
+            T.pge(t, t, t, t, n)
 
 
 def test_bplg_packed_long(cuda):

@@ -22,7 +22,7 @@ ERR_SINGULAR = 5
 ERR_TIMEOUT = 6
 
 LAYOUTS = {"contiguous": 0, "packed": 1, "interleaved": 2}
-ALGOS = {"auto": 0, "thomas": 1, "cr": 2, "pcr": 3, "wm": 4, "gtsv": 5, "wm_pivot": 6}
+ALGOS = {"auto": 0, "thomas": 1, "cr": 2, "pcr": 3, "wm": 4, "gtsv": 5, "pge": 6}
 
 _lock = threading.Lock()
 _lib = None
@@ -55,6 +55,8 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_refine_double": (_I, [_I, _P, _P, _P, _P, _P, _I, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_convert_check": (_I, [_P, _P, _P, _SZ, _P]),
     "tridiag_partition_fallbacks": (ctypes.c_longlong, [_I]),
+    "tridiag_pge_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_pge_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
 REFERENCE_SOLVERS = [

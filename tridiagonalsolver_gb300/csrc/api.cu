@@ -28,6 +28,10 @@ bool valid_layout(int layout) {
 
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
+// Below this size the thread-per-system sweeps beat the partitioned solve
+// (measured on GB300 at batch 2^25 / n, FP32 and FP64).
+constexpr int PGE_MIN_N = 1024;
+
 // Expand the four array pointers of a packed (layout 1) base pointer.
 template <typename T>
 void packed_ptrs(int layout, T*& a, T*& b, T*& c, T*& d, int n) {
@@ -75,7 +79,7 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
     return TRIDIAG_ERR_INVALID_VALUE;
   }
   if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
-  if (!pivots && tdg::pge_eligible<T>(layout, n)) {
+  if (!pivots && n >= PGE_MIN_N && tdg::pge_eligible<T>(layout, n)) {
     // no pivot record wanted: the partitioned solve (many chains per system)
     bool used = false;
     cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, d, info, n, batch, s, &used);
@@ -132,13 +136,19 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
       cudaError_t e = algo == TRIDIAG_ALGO_CR    ? tdg::launch_crpcr_warp<T>(layout, a, b, c, d, d, n, batch, s, &used)
                       : algo == TRIDIAG_ALGO_PCR ? tdg::launch_pcr_warp<T>(layout, a, b, c, d, d, n, batch, s, &used)
                                                  : tdg::launch_wm_warp<T>(layout, a, b, c, d, d, n, batch, s, &used);
-      if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM)
+      if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM && n >= PGE_MIN_N)
         e = tdg::launch_pge<T>(layout, a, b, c, d, d, nullptr, n, batch, s, &used);
       if (e == cudaSuccess && !used) {
         e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
         if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
       }
       return cuda_status(e);
+    }
+    case TRIDIAG_ALGO_PGE: {
+      bool used = false;
+      cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, d, nullptr, n, batch, s, &used);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_NOT_SUPPORTED;
     }
     case TRIDIAG_ALGO_GTSV: {
       size_t bytes = gtsv_ws_bytes<T>(n, batch);
@@ -182,7 +192,7 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
       cudaError_t e = algo == TRIDIAG_ALGO_CR    ? tdg::launch_crpcr_warp<T>(layout, a, b, c, d, x, n, batch, s, &used)
                       : algo == TRIDIAG_ALGO_PCR ? tdg::launch_pcr_warp<T>(layout, a, b, c, d, x, n, batch, s, &used)
                                                  : tdg::launch_wm_warp<T>(layout, a, b, c, d, x, n, batch, s, &used);
-      if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM)
+      if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM && n >= PGE_MIN_N)
         e = tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
@@ -201,9 +211,16 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
         e = tdg::launch_thomas_seq<T>(layout, const_cast<T*>(a), const_cast<T*>(b), cs, x, n, batch, s);
       return cuda_status(e);
     }
-    case TRIDIAG_ALGO_GTSV: {
+    case TRIDIAG_ALGO_PGE: {
       bool used = false;
       cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_NOT_SUPPORTED;
+    }
+    case TRIDIAG_ALGO_GTSV: {
+      bool used = false;
+      cudaError_t e = n >= PGE_MIN_N ? tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used)
+                                     : cudaSuccess;
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       size_t bytes = (size_t)n * (size_t)batch * sizeof(T);
@@ -480,4 +497,32 @@ extern "C" long long tridiag_partition_fallbacks(int reset) {
   unsigned long long v = 0;
   if (tdg::pge_fallback_count(&v, reset != 0) != cudaSuccess) return -1;
   return (long long)v;
+}
+
+namespace {
+template <typename T>
+int pge_entry(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+              cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !x) return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout == TRIDIAG_LAYOUT_PACKED) {
+    b = a + n;
+    c = a + 2 * (size_t)n;
+    d = a + 3 * (size_t)n;
+  } else if (!b || !c || !d) {
+    return TRIDIAG_ERR_INVALID_VALUE;
+  }
+  bool used = false;
+  cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, x, info, n, batch, s, &used);
+  if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_NOT_SUPPORTED;
+}
+}  // namespace
+
+extern "C" int tridiag_pge_single(int layout, const float* a, const float* b, const float* c, const float* d,
+                                  float* x, int* info, int n, int batch, void* stream) {
+  return set_status(pge_entry<float>(layout, a, b, c, d, x, info, n, batch, (cudaStream_t)stream));
+}
+extern "C" int tridiag_pge_double(int layout, const double* a, const double* b, const double* c, const double* d,
+                                  double* x, int* info, int n, int batch, void* stream) {
+  return set_status(pge_entry<double>(layout, a, b, c, d, x, info, n, batch, (cudaStream_t)stream));
 }

@@ -141,6 +141,21 @@ def gtsv_adjoint(a, b, c, x, pivots, xbar, n: int, layout: str = "contiguous", w
     return ga, gb, gc, gd
 
 
+def pge(a, b, c, d, n: int, layout: str = "contiguous", info=None, out=None, stream=None):
+    """WM-pGE with partial pivoting inside partitions (one CTA per system);
+    a, b, c, d are not modified; returns x.  Raises for sizes it does not
+    cover (TRIDIAG_ERR_NOT_SUPPORTED)."""
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    a, b, c, d = _al(a), _al(b), _al(c), _al(d)
+    x = out if out is not None else torch.empty_like(d if d is not None else a)
+    st = getattr(lib(), f"tridiag_pge_{p}")(LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype),
+                                          _ptr(d, a.dtype), _ptr(x, a.dtype), _ptr(info), n, batch,
+                                          _stream_ptr(stream))
+    check(st, f"tridiag_pge_{p}")
+    return x
+
+
 def refine_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
     batch = _dims(a, n, layout)
     return torch.empty(lib().tridiag_refine_workspace_size(LAYOUTS[layout], n, batch), dtype=torch.uint8,

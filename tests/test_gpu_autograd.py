@@ -109,3 +109,33 @@ def test_requires_grad_subset(cuda):
     xo = O.gtsv(a, b, c, d, n).reshape(batch, n)
     lam = O.adjoint_f64(a, b, c, xo, w, n)[3].reshape(batch, n)
     assert np.max(np.abs(td.grad.cpu().numpy() - lam)) <= 1e-9 * np.max(np.abs(lam))
+
+
+def test_solve_from_a_fresh_host_thread(cuda):
+    """A thread that has made no CUDA call yet (like autograd's worker) can
+    launch the TMA-fed kernels: the library binds the device context."""
+    import threading
+
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    n, batch = 64, 32
+    a, b, c, d = inputs.nondominant(n, batch, seed=31)
+    ts = [torch.from_numpy(v.copy()).cuda() for v in (a, b, c, d)]
+    piv = T.pivot_record(ts[0], n)
+    torch.cuda.synchronize()
+    out = {}
+
+    def work():
+        try:
+            out["x"] = T.gtsv(*ts, n, pivots=piv)
+            torch.cuda.synchronize()
+        except Exception as e:  # reported below
+            out["err"] = e
+
+    th = threading.Thread(target=work)
+    th.start()
+    th.join()
+    assert "err" not in out, out.get("err")
+    _, eta = O.backward_error(a, b, c, d, out["x"].cpu().numpy(), n)
+    assert eta <= 1e-12

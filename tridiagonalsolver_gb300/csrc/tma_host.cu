@@ -1,6 +1,8 @@
 // Host-side tensor-map encoding through the driver entry point obtained from
 // the runtime (no link-time dependency on libcuda).
 #include <cudaTypedefs.h>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "kernels.h"
@@ -25,8 +27,19 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 bool encode_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype, int elem_bytes, uint64_t inner,
                     uint64_t outer, uint64_t outer_stride_bytes, uint32_t box_inner, uint32_t box_outer,
                     CUtensorMapSwizzle swizzle) {
+  // cuTensorMapEncodeTiled needs a current context on the calling thread; a
+  // thread that has made no runtime call yet (e.g. an autograd worker) has
+  // none, so bind the current device's primary context first.
+  thread_local bool bound = false;
+  if (!bound) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) bound = true;
+  }
   auto fn = encode_fn();
-  if (!fn || !base) return false;
+  if (!fn || !base) {
+    if (std::getenv("TRIDIAG_DEBUG")) std::fprintf(stderr, "tridiag: no tensor-map encoder (%p) or null base\n", (void*)fn);
+    return false;
+  }
   if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (outer_stride_bytes & 15u) != 0) return false;
   if (outer_stride_bytes < inner * (uint64_t)elem_bytes || inner == 0 || outer == 0) return false;
   cuuint64_t dims[2] = {inner, outer};
@@ -35,6 +48,10 @@ bool encode_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtyp
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS && std::getenv("TRIDIAG_DEBUG"))
+    std::fprintf(stderr, "tridiag: tensor map refused (CUresult %d): base %p dims %llu x %llu stride %llu box %u x %u\n",
+                 (int)r, base, (unsigned long long)inner, (unsigned long long)outer,
+                 (unsigned long long)outer_stride_bytes, box_inner, box_outer);
   return r == CUDA_SUCCESS;
 }
 

@@ -142,8 +142,8 @@ def test_pge_unsupported_sizes(cuda):
     import tridiagonalsolver_gb300 as T
     from tridiagonalsolver_gb300 import TridiagError
 
-    for n in (1, 64, 20000):
-        t = cuda.ones(n * 2, dtype=cuda.float64, device="cuda")
+    for dt, n in ((cuda.float64, 1), (cuda.float64, 64), (cuda.float64, 30000), (cuda.float32, 70000)):
+        t = cuda.ones(n * 2, dtype=dt, device="cuda")
         with pytest.raises(TridiagError):
             T.pge(t, t, t, t, n)
 

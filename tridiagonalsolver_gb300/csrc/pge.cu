@@ -30,6 +30,7 @@
 // (Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884, without pivoting there);
 // the pivoting is that of its MKL row (Tridiagonal_AVX512/
 // tridiagonal_basic.cpp:131-143).
+#include <cooperative_groups.h>
 #include <cstdint>
 
 #include "common.cuh"
@@ -125,17 +126,88 @@ __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
 // Systems that took the sequential fallback since the last reset (per device).
 __device__ unsigned long long g_pge_fallbacks = 0ull;
 
+// A chunk of K consecutive rows of a tridiagonal system held in registers:
+// rows 0..K-2 are interior, row K-1 is the chunk's top-level row.  The
+// interior is eliminated with partial pivoting for three right-hand sides
+// (d, the left coupling a_0 e_0, the right coupling c_{K-2} e_{K-2}) and
+// fully back-substituted, so that interior row i is
+//     x_i = Y_i - V_i s_prev - W_i s_own,
+// s_prev being the previous chunk's top row and s_own this chunk's.
+template <typename T, int K>
+struct ChunkSpikes {
+  static constexpr int MI = K - 1;
+  T Y[MI], V[MI], W[MI];
+  T as, bs, cs, ds;  // the top row
+
+  __device__ bool eliminate(const T (&a_)[K], const T (&b_)[K], const T (&c_)[K], const T (&d_)[K]) {
+    bool bad = false;
+    T inv[MI], u1[MI], u2[MI], ry[MI], rv[MI];
+    T cb = b_[0], cc = MI > 1 ? c_[0] : T(0), cy = d_[0], cv = a_[0], cw = MI == 1 ? c_[0] : T(0);
+    T w_prev = T(0);
+#pragma unroll
+    for (int i = 0; i + 1 < MI; ++i) {
+      const T na = a_[i + 1], nb = b_[i + 1], cn = c_[i + 1], ny = d_[i + 1];
+      const bool last = i + 2 == MI;
+      const T nc = last ? T(0) : cn;
+      const bool sw = !abs_ge(cb, na);
+      const T piv = sw ? na : cb;
+      bad |= is_zero(piv);
+      inv[i] = Div<T>(piv).inv();
+      const T l = (sw ? cb : na) * inv[i];
+      u1[i] = sw ? nb : cc;
+      u2[i] = sw ? nc : T(0);
+      ry[i] = sw ? ny : cy;
+      rv[i] = sw ? T(0) : cv;
+      cb = fma(-l, u1[i], sw ? cc : nb);
+      cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
+      cy = fma(-l, ry[i], sw ? cy : ny);
+      cv = sw ? cv : -l * cv;
+      if (last) {
+        w_prev = sw ? cn : cw;
+        cw = fma(-l, w_prev, sw ? cw : cn);
+      }
+    }
+    bad |= is_zero(cb);
+    inv[MI - 1] = Div<T>(cb).inv();
+    u1[MI - 1] = T(0);
+    u2[MI - 1] = T(0);
+    ry[MI - 1] = cy;
+    rv[MI - 1] = cv;
+#pragma unroll
+    for (int i = MI - 1; i >= 0; --i) {
+      const T y1 = i + 1 < MI ? Y[i + 1] : T(0), v1 = i + 1 < MI ? V[i + 1] : T(0), w1 = i + 1 < MI ? W[i + 1] : T(0);
+      const T y2 = i + 2 < MI ? Y[i + 2] : T(0), v2 = i + 2 < MI ? V[i + 2] : T(0), w2 = i + 2 < MI ? W[i + 2] : T(0);
+      const T wi = i == MI - 1 ? cw : (i == MI - 2 ? w_prev : T(0));
+      Y[i] = fma(-u2[i], y2, fma(-u1[i], y1, ry[i])) * inv[i];
+      V[i] = fma(-u2[i], v2, fma(-u1[i], v1, rv[i])) * inv[i];
+      W[i] = fma(-u2[i], w2, fma(-u1[i], w1, wi)) * inv[i];
+    }
+    as = a_[K - 1];
+    bs = b_[K - 1];
+    cs = c_[K - 1];
+    ds = d_[K - 1];
+    return bad;
+  }
+  // The top row in terms of the neighbouring top rows, given the next
+  // chunk's first-row values (zero and has_next = false for the last chunk).
+  __device__ void top_row(T Yf, T Vf, T Wf, bool has_next, T& ta, T& tb, T& tc, T& td) const {
+    const T c = has_next ? cs : T(0);
+    ta = -as * V[MI - 1];
+    tb = fma(-c, has_next ? Vf : T(0), fma(-as, W[MI - 1], bs));
+    tc = -c * (has_next ? Wf : T(0));
+    td = fma(-c, has_next ? Yf : T(0), fma(-as, Y[MI - 1], ds));
+  }
+  __device__ T value(int i, T sp, T st) const { return fma(-W[i], st, fma(-V[i], sp, Y[i])); }
+};
+
 // Pivoted solve of the NT-row separator system (rows sa/sb/sc/sd at SEP[0],
 // SEP[NT], SEP[2NT], SEP[3NT]) by one warp, solution to sx[0..NT).  Lane l
-// takes the K = NT/32 consecutive rows lK .. lK+K-1: its first K-1 rows are
-// eliminated with partial pivoting (three right-hand sides, as in the main
-// sweep) so that each becomes Y - V s_{l-1} - W s_l in the lanes' last rows
-// s; those 32 rows form a tridiagonal system that lane 0 solves
-// sequentially with partial pivoting.  Returns true on breakdown.
+// takes the K = NT/32 consecutive rows lK .. lK+K-1 as a chunk; the 32
+// chunk top rows form a tridiagonal system that lane 0 solves sequentially
+// with partial pivoting.  Returns true on breakdown.
 template <typename T, int NT>
 __device__ bool sep_solve_pivoted(const T* SEP, T* sx, T* tmp, int lane) {
   constexpr int K = NT / 32;
-  constexpr int MI = K - 1;
   static_assert(K >= 2, "at least two separators per lane");
   const int r0 = lane * K;
   T a_[K], b_[K], c_[K], d_[K];
@@ -146,57 +218,10 @@ __device__ bool sep_solve_pivoted(const T* SEP, T* sx, T* tmp, int lane) {
     c_[k] = SEP[2 * NT + r0 + k];
     d_[k] = SEP[3 * NT + r0 + k];
   }
-  bool bad = false;
-  T inv[MI], u1[MI], u2[MI], ry[MI], rv[MI];
-  T cb = b_[0], cc = MI > 1 ? c_[0] : T(0), cy = d_[0], cv = a_[0], cw = MI == 1 ? c_[0] : T(0);
-  T w_prev = T(0);
-#pragma unroll
-  for (int i = 0; i + 1 < MI; ++i) {
-    const T na = a_[i + 1], nb = b_[i + 1], cn = c_[i + 1], ny = d_[i + 1];
-    const bool last = i + 2 == MI;
-    const T nc = last ? T(0) : cn;
-    const bool sw = !abs_ge(cb, na);
-    const T piv = sw ? na : cb;
-    bad |= is_zero(piv);
-    inv[i] = Div<T>(piv).inv();
-    const T l = (sw ? cb : na) * inv[i];
-    u1[i] = sw ? nb : cc;
-    u2[i] = sw ? nc : T(0);
-    ry[i] = sw ? ny : cy;
-    rv[i] = sw ? T(0) : cv;
-    cb = fma(-l, u1[i], sw ? cc : nb);
-    cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
-    cy = fma(-l, ry[i], sw ? cy : ny);
-    cv = sw ? cv : -l * cv;
-    if (last) {
-      w_prev = sw ? cn : cw;
-      cw = fma(-l, w_prev, sw ? cw : cn);
-    }
-  }
-  bad |= is_zero(cb);
-  inv[MI - 1] = Div<T>(cb).inv();
-  u1[MI - 1] = T(0);
-  u2[MI - 1] = T(0);
-  ry[MI - 1] = cy;
-  rv[MI - 1] = cv;
-  T Y[MI], V[MI], W[MI];
-#pragma unroll
-  for (int i = MI - 1; i >= 0; --i) {
-    const T y1 = i + 1 < MI ? Y[i + 1] : T(0), v1 = i + 1 < MI ? V[i + 1] : T(0), w1 = i + 1 < MI ? W[i + 1] : T(0);
-    const T y2 = i + 2 < MI ? Y[i + 2] : T(0), v2 = i + 2 < MI ? V[i + 2] : T(0), w2 = i + 2 < MI ? W[i + 2] : T(0);
-    const T wi = i == MI - 1 ? cw : (i == MI - 2 ? w_prev : T(0));
-    Y[i] = fma(-u2[i], y2, fma(-u1[i], y1, ry[i])) * inv[i];
-    V[i] = fma(-u2[i], v2, fma(-u1[i], v1, rv[i])) * inv[i];
-    W[i] = fma(-u2[i], w2, fma(-u1[i], w1, wi)) * inv[i];
-  }
-  // top-level row of this lane (its last row) and lane 0's sequential solve
-  const T Yf = shfl_down(Y[0], 1), Vf = shfl_down(V[0], 1), Wf = shfl_down(W[0], 1);
-  const bool has_next = lane < 31;
-  const T as = a_[K - 1], bs = b_[K - 1], cs = has_next ? c_[K - 1] : T(0), ds = d_[K - 1];
-  tmp[lane] = -as * V[MI - 1];
-  tmp[32 + lane] = fma(-cs, has_next ? Vf : T(0), fma(-as, W[MI - 1], bs));
-  tmp[64 + lane] = -cs * (has_next ? Wf : T(0));
-  tmp[96 + lane] = fma(-cs, has_next ? Yf : T(0), fma(-as, Y[MI - 1], ds));
+  ChunkSpikes<T, K> ch;
+  bool bad = ch.eliminate(a_, b_, c_, d_);
+  const T Yf = shfl_down(ch.Y[0], 1), Vf = shfl_down(ch.V[0], 1), Wf = shfl_down(ch.W[0], 1);
+  ch.top_row(Yf, Vf, Wf, lane < 31, tmp[lane], tmp[32 + lane], tmp[64 + lane], tmp[96 + lane]);
   __syncwarp();
   int top_bad = 0;
   if (lane == 0) top_bad = seq_pivoted_inplace<T>(tmp, tmp + 32, tmp + 64, tmp + 96, 32);
@@ -205,7 +230,7 @@ __device__ bool sep_solve_pivoted(const T* SEP, T* sx, T* tmp, int lane) {
   const T sp = lane > 0 ? tmp[96 + lane - 1] : T(0);
   const T st = tmp[96 + lane];
 #pragma unroll
-  for (int i = 0; i < MI; ++i) sx[r0 + i] = fma(-W[i], st, fma(-V[i], sp, Y[i]));
+  for (int i = 0; i < K - 1; ++i) sx[r0 + i] = ch.value(i, sp, st);
   sx[r0 + K - 1] = st;
   return bad;
 }
@@ -302,8 +327,15 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
   T om1 = T(0), om2 = T(0);                    // omega_{i-1}, omega_{i-2}
   T pu1 = T(0), pu2a = T(0), pu2b = T(0);      // u1_{i-1}, u2_{i-1}, u2_{i-2}
   T Y0 = T(0), V0 = T(0);                      // omega . y', omega . v'
+  // software-pipelined: row i+2 (at most the separator row, which always
+  // exists) is loaded while row i+1 is eliminated
+  T pa = A[1], pb = B[1], pc = C[1], py = D[1];
   for (int i = 0; i + 1 < mi; ++i) {
-    const T na = A[i + 1], nb = B[i + 1], cn = C[i + 1], ny = D[i + 1];
+    const T na = pa, nb = pb, cn = pc, ny = py;
+    pa = A[i + 2];
+    pb = B[i + 2];
+    pc = C[i + 2];
+    py = D[i + 2];
     const bool last = i + 2 == mi;  // row i+1 is the last interior row
     const T nc = last ? T(0) : cn;
     const bool sw = !abs_ge(cb, na);
@@ -439,11 +471,21 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
     xmax = max(xmax, mag(x1));
     bad |= !finite_val(x1);
     x_last = x1;
+    // software-pipelined: row i-1's factors are loaded while row i is solved
+    int j = mi - 2 >= 0 ? mi - 2 : 0;
+    T qv = V[j], qd = D[j], qb = B[j], qa = A[j], qc = C[j + 1];
     for (int i = mi - 2; i >= 0; --i) {
-      const T u2 = ((swaps >> i) & 1ull) && i + 2 < mi ? C[i + 1] : T(0);
-      T r = fma(-V[i], sp, D[i]);
+      const T vi = qv, di = qd, bi = qb, ai = qa, ci1 = qc;
+      j = i > 0 ? i - 1 : 0;
+      qv = V[j];
+      qd = D[j];
+      qb = B[j];
+      qa = A[j];
+      qc = C[j + 1];
+      const T u2 = ((swaps >> i) & 1ull) && i + 2 < mi ? ci1 : T(0);
+      T r = fma(-vi, sp, di);
       if (i == mi - 2) r = fma(-w_prev, st, r);
-      const T xi = fma(-u2, x2, fma(-B[i], x1, r)) * A[i];
+      const T xi = fma(-u2, x2, fma(-bi, x1, r)) * ai;
       D[i] = xi;
       xmax = max(xmax, mag(xi));
       bad |= !finite_val(xi);
@@ -582,6 +624,397 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
   }
 }
 
+// ---------------------------------------------------------------------------
+// Cluster version for systems longer than one CTA's shared memory: a cluster
+// of CL CTAs holds one system, CTA r the rows [r NT m, (r+1) NT m), so the
+// system is read from HBM once and kept in the cluster's distributed shared
+// memory.  Partitions, forward elimination, back substitution and the
+// acceptance test are those of pge_kernel with the partition index
+// P = r NT + t; the separator system of the R = CL NT partitions is gathered
+// into CTA 0 and solved there with partial pivoting in two levels (each
+// thread eliminates a chunk of CL separators, warp 0 solves the NT chunk
+// tops).  Neighbouring values across CTA boundaries travel through DSMEM.
+// A result that fails the exact backward-error check after PGE_REFINE_CL
+// correction passes is still written, with info = n + 1.
+
+constexpr int PGE_REFINE_CL = 3;
+
+template <typename T, int NT, int CL>
+struct PgcLayout {
+  static constexpr int R = CL * NT;
+  // element offsets after the 6 NT ms staging arrays
+  static constexpr int FST = 0, XF = 3 * NT, RED = 4 * NT, SOL = RED + 4 * R, XCH = SOL + R, TOP = XCH + 3 * NT,
+                       TSOL = TOP + 4 * NT, TMP = TSOL + NT, END = TMP + PGE_TMP;
+};
+
+template <typename T, int NT, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1)
+    pgc_kernel(const T* __restrict__ ga, const T* __restrict__ gb, const T* __restrict__ gc, const T* gd, T* gx,
+               int* info, int n, int m, int ms, size_t sys_stride) {
+  namespace cg = cooperative_groups;
+  using Lay = PgcLayout<T, NT, CL>;
+  constexpr int R = Lay::R;
+  constexpr int NW = NT / 32;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char pge_smem[];
+  T* SA = reinterpret_cast<T*>(pge_smem);
+  T* SB = SA + NT * ms;
+  T* SC = SB + NT * ms;
+  T* SD = SC + NT * ms;
+  T* SV = SD + NT * ms;
+  T* SX = SV + NT * ms;
+  T* EXT = SX + NT * ms;
+  T* FST = EXT + Lay::FST;
+  T* XF = EXT + Lay::XF;
+  T* RED = EXT + Lay::RED;
+  T* SOL = EXT + Lay::SOL;
+  T* XCH = EXT + Lay::XCH;
+  T* TOP = EXT + Lay::TOP;
+  T* TSOL = EXT + Lay::TSOL;
+  T* TMP = EXT + Lay::TMP;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int P = rank * NT + t;
+  const size_t base = (size_t)(blockIdx.x / CL) * sys_stride;
+  const int rows = NT * m;  // rows per CTA
+  const int row0 = rank * rows;
+  using MagT = decltype(mag(T(0)));
+  __shared__ MagT s_amax, s_dmax, s_xmax;
+  __shared__ unsigned long long s_rmax, s_anorm, s_xn, s_dn;
+  __shared__ int s_bad, s_nf;
+  // cluster-wide accumulators live in CTA 0
+  MagT* c_amax = cluster.map_shared_rank(&s_amax, 0);
+  MagT* c_dmax = cluster.map_shared_rank(&s_dmax, 0);
+  MagT* c_xmax = cluster.map_shared_rank(&s_xmax, 0);
+  unsigned long long* c_rmax = cluster.map_shared_rank(&s_rmax, 0);
+  unsigned long long* c_anorm = cluster.map_shared_rank(&s_anorm, 0);
+  unsigned long long* c_xn = cluster.map_shared_rank(&s_xn, 0);
+  unsigned long long* c_dn = cluster.map_shared_rank(&s_dn, 0);
+  int* c_bad = cluster.map_shared_rank(&s_bad, 0);
+  int* c_nf = cluster.map_shared_rank(&s_nf, 0);
+  T* RED0 = cluster.map_shared_rank(RED, 0);
+  T* SOL0 = cluster.map_shared_rank(SOL, 0);
+  if (t == 0) {
+    s_amax = 0;
+    s_dmax = 0;
+    s_xmax = 0;
+    s_rmax = s_anorm = s_xn = s_dn = 0ull;
+    s_bad = 0;
+    s_nf = 0;
+  }
+  auto sidx = [&](int lr) { return (lr / m) * ms + (lr % m); };  // local row -> staging index
+
+  // ---- stage this CTA's rows
+#pragma unroll 4
+  for (int p = warp; p < NT; p += NW) {
+    for (int i = lane; i < m; i += 32) {
+      const int r = row0 + p * m + i;
+      const int q = p * ms + i;
+      if (r < n) {
+        if (r > 0) cp_async_elem(SA + q, ga + base + r); else SA[q] = T(0);
+        cp_async_elem(SB + q, gb + base + r);
+        if (r < n - 1) cp_async_elem(SC + q, gc + base + r); else SC[q] = T(0);
+        cp_async_elem(SD + q, gd + base + r);
+      } else {
+        SA[q] = T(0);
+        SB[q] = T(1);
+        SC[q] = T(0);
+        SD[q] = T(0);
+      }
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  cluster.sync();  // staging done everywhere, CTA 0's accumulators initialised
+  {
+    MagT amax = 0, dmax = 0;
+    const T* A0 = SA + t * ms;
+    const T* B0 = SB + t * ms;
+    const T* C0 = SC + t * ms;
+    const T* D0 = SD + t * ms;
+    for (int i = 0; i < m; ++i) {
+      amax = max(amax, max(mag(A0[i]), max(mag(B0[i]), mag(C0[i]))));
+      dmax = max(dmax, mag(D0[i]));
+    }
+    atomicMax(c_amax, amax);
+    atomicMax(c_dmax, dmax);
+  }
+
+  const int mi = m - 1;
+  T* A = SA + t * ms;
+  T* B = SB + t * ms;
+  T* C = SC + t * ms;
+  T* D = SD + t * ms;
+  T* V = SV + t * ms;
+  bool accepted = false;
+#pragma unroll 1
+  for (int pass = 0; pass <= PGE_REFINE_CL; ++pass) {
+    // ---- forward elimination of the partition (as pge_kernel)
+    bool bad = false;
+    unsigned long long swaps = 0ull;
+    T cb = B[0], cc = mi > 1 ? C[0] : T(0), cy = D[0], cv = A[0], cw = mi == 1 ? C[0] : T(0);
+    T w_prev = T(0);
+    T om1 = T(0), om2 = T(0);
+    T pu1 = T(0), pu2a = T(0), pu2b = T(0);
+    T Y0 = T(0), V0 = T(0);
+    // software-pipelined: row i+2 (at most the separator row, which always
+    // exists) is loaded while row i+1 is eliminated
+    T pa = A[1], pb = B[1], pc = C[1], py = D[1];
+    for (int i = 0; i + 1 < mi; ++i) {
+      const T na = pa, nb = pb, cn = pc, ny = py;
+      pa = A[i + 2];
+      pb = B[i + 2];
+      pc = C[i + 2];
+      py = D[i + 2];
+      const bool last = i + 2 == mi;
+      const T nc = last ? T(0) : cn;
+      const bool sw = !abs_ge(cb, na);
+      const T piv = sw ? na : cb;
+      bad |= is_zero(piv);
+      const T inv = Div<T>(piv).inv();
+      const T l = (sw ? cb : na) * inv;
+      const T u1 = sw ? nb : cc;
+      const T u2 = sw ? nc : T(0);
+      const T uy = sw ? ny : cy;
+      const T uv = sw ? T(0) : cv;
+      const T om = fma(-om2, pu2b, fma(-om1, pu1, i == 0 ? T(1) : T(0))) * inv;
+      Y0 = fma(om, uy, Y0);
+      V0 = fma(om, uv, V0);
+      om2 = om1;
+      om1 = om;
+      pu2b = pu2a;
+      pu2a = u2;
+      pu1 = u1;
+      A[i] = inv;
+      B[i] = u1;
+      D[i] = uy;
+      V[i] = uv;
+      swaps |= (unsigned long long)sw << i;
+      cb = fma(-l, u1, sw ? cc : nb);
+      cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
+      cy = fma(-l, uy, sw ? cy : ny);
+      cv = sw ? cv : -l * cv;
+      if (last) {
+        w_prev = sw ? cn : cw;
+        cw = fma(-l, w_prev, sw ? cw : cn);
+      }
+    }
+    bad |= is_zero(cb);
+    const T inv_last = Div<T>(cb).inv();
+    {
+      const T om = fma(-om2, pu2b, fma(-om1, pu1, mi == 1 ? T(1) : T(0))) * inv_last;
+      Y0 = fma(om, cy, Y0);
+      V0 = fma(om, cv, V0);
+      FST[t] = Y0;
+      FST[NT + t] = V0;
+      FST[2 * NT + t] = fma(om1, w_prev, om * cw);
+    }
+    const T Ylast = cy * inv_last, Vlast = cv * inv_last, Wlast = cw * inv_last;
+    A[mi - 1] = inv_last;
+    B[mi - 1] = T(0);
+    D[mi - 1] = cy;
+    V[mi - 1] = cv;
+    cluster.sync();
+
+    // ---- separator row of partition P, into CTA 0's gather buffer
+    const T as = A[mi], bs = B[mi], cs = C[mi], ds = D[mi];
+    {
+      T Yf = T(0), Vf = T(0), Wf = T(0);
+      if (t + 1 < NT) {
+        Yf = FST[t + 1];
+        Vf = FST[NT + t + 1];
+        Wf = FST[2 * NT + t + 1];
+      } else if (rank + 1 < CL) {
+        const T* nf = cluster.map_shared_rank(FST, rank + 1);
+        Yf = nf[0];
+        Vf = nf[NT];
+        Wf = nf[2 * NT];
+      }
+      RED0[P] = -as * Vlast;
+      RED0[R + P] = fma(-cs, Vf, fma(-as, Wlast, bs));
+      RED0[2 * R + P] = -cs * Wf;
+      RED0[3 * R + P] = fma(-cs, Yf, fma(-as, Ylast, ds));
+    }
+    cluster.sync();
+
+    // ---- CTA 0: the R-row separator system with partial pivoting, in two
+    // levels (chunks of CL rows per thread, then warp 0 on the NT tops)
+    if (rank == 0) {
+      T a_[CL], b_[CL], c_[CL], d_[CL];
+#pragma unroll
+      for (int k = 0; k < CL; ++k) {
+        a_[k] = RED[t * CL + k];
+        b_[k] = RED[R + t * CL + k];
+        c_[k] = RED[2 * R + t * CL + k];
+        d_[k] = RED[3 * R + t * CL + k];
+      }
+      ChunkSpikes<T, CL> ch;
+      bool rbad = ch.eliminate(a_, b_, c_, d_);
+      XCH[t] = ch.Y[0];
+      XCH[NT + t] = ch.V[0];
+      XCH[2 * NT + t] = ch.W[0];
+      __syncthreads();
+      const bool has_next = t + 1 < NT;
+      ch.top_row(has_next ? XCH[t + 1] : T(0), has_next ? XCH[NT + t + 1] : T(0),
+                 has_next ? XCH[2 * NT + t + 1] : T(0), has_next, TOP[t], TOP[NT + t], TOP[2 * NT + t],
+                 TOP[3 * NT + t]);
+      __syncthreads();
+      if (warp == 0) rbad |= sep_solve_pivoted<T, NT>(TOP, TSOL, TMP, lane);
+      __syncthreads();
+      const T sp = t > 0 ? TSOL[t - 1] : T(0), st = TSOL[t];
+#pragma unroll
+      for (int k = 0; k < CL - 1; ++k) SOL[t * CL + k] = ch.value(k, sp, st);
+      SOL[t * CL + CL - 1] = st;
+      if (rbad) atomicOr(&s_bad, 1);
+    }
+    cluster.sync();
+
+    // ---- back substitution with the separators in place (as pge_kernel)
+    const T sp = P > 0 ? SOL0[P - 1] : T(0);
+    const T st = SOL0[P];
+    MagT xmax = mag(st);
+    T x_last;
+    {
+      T x1 = (fma(-cw, st, fma(-V[mi - 1], sp, D[mi - 1]))) * inv_last;
+      T x2 = T(0);
+      D[mi - 1] = x1;
+      xmax = max(xmax, mag(x1));
+      bad |= !finite_val(x1);
+      x_last = x1;
+      // software-pipelined: row i-1's factors are loaded while row i is solved
+      int j = mi - 2 >= 0 ? mi - 2 : 0;
+      T qv = V[j], qd = D[j], qb = B[j], qa = A[j], qc = C[j + 1];
+      for (int i = mi - 2; i >= 0; --i) {
+        const T vi = qv, di = qd, bi = qb, ai = qa, ci1 = qc;
+        j = i > 0 ? i - 1 : 0;
+        qv = V[j];
+        qd = D[j];
+        qb = B[j];
+        qa = A[j];
+        qc = C[j + 1];
+        const T u2 = ((swaps >> i) & 1ull) && i + 2 < mi ? ci1 : T(0);
+        T r = fma(-vi, sp, di);
+        if (i == mi - 2) r = fma(-w_prev, st, r);
+        const T xi = fma(-u2, x2, fma(-bi, x1, r)) * ai;
+        D[i] = xi;
+        xmax = max(xmax, mag(xi));
+        bad |= !finite_val(xi);
+        x2 = x1;
+        x1 = xi;
+      }
+      bad |= !finite_val(st);
+      D[mi] = st;
+      XF[t] = D[0];
+      if (pass == 0) atomicMax(c_xmax, xmax);
+    }
+    cluster.sync();
+    {
+      T x_next = T(0);
+      if (t + 1 < NT) x_next = XF[t + 1];
+      else if (rank + 1 < CL) x_next = cluster.map_shared_rank(XF, rank + 1)[0];
+      const double r = fma(-(double)cs, (double)x_next,
+                           fma(-(double)bs, (double)st, fma(-(double)as, (double)x_last, (double)ds)));
+      const T amx = Fmt<T>::from_mag(*c_amax), xmx = Fmt<T>::from_mag(*c_xmax), dmx = Fmt<T>::from_mag(*c_dmax);
+      if (pass == 0) bad |= !(fabs(r) <= Fmt<T>::SEP_TOL * fma((double)amx, (double)xmx, (double)dmx));
+    }
+    if (__syncthreads_or(bad) && t == 0) atomicOr(c_bad, 1);
+    cluster.sync();
+    const bool pass_bad = *c_bad != 0;
+    cluster.sync();  // everyone has read the flag
+    if (rank == 0 && t == 0) s_bad = 0;
+    if (pass == 0 && !pass_bad) {
+      accepted = true;
+      break;
+    }
+    // x of a neighbouring row that may live in another CTA (staging array `arr`)
+    auto xat = [&](const T* arr, int r) -> T {
+      const int lr = r - row0;
+      if (lr >= 0 && lr < rows) return arr[sidx(lr)];
+      const int rk = r / rows;
+      return cluster.map_shared_rank(arr, rk)[sidx(r - rk * rows)];
+    };
+    if (pass > 0 && !pass_bad) {
+      for (int r = t; r < rows; r += NT)
+        if (row0 + r < n) SD[sidx(r)] += SX[sidx(r)];
+      cluster.sync();
+    }
+    if (pass_bad && pass > 0) break;  // a correction pass broke down
+    // exact normwise backward error of the current x (cluster-wide maxima)
+    {
+      unsigned long long rmax = 0ull, anorm = 0ull, xn = 0ull, dn = 0ull;
+      bool nonfinite = false;
+      for (int lr = t; lr < rows; lr += NT) {
+        const int r = row0 + lr;
+        if (r >= n) break;
+        const double ar = r > 0 ? (double)ga[base + r] : 0.0, br = (double)gb[base + r];
+        const double cr = r < n - 1 ? (double)gc[base + r] : 0.0, dr = (double)gd[base + r];
+        const double xr = (double)SD[sidx(lr)];
+        double res = fma(-br, xr, dr);
+        if (r > 0) res = fma(-ar, (double)xat(SD, r - 1), res);
+        if (r < n - 1) res = fma(-cr, (double)xat(SD, r + 1), res);
+        nonfinite |= !finite_val(res);
+        rmax = max(rmax, mag(res));
+        anorm = max(anorm, mag(fabs(ar) + fabs(br) + fabs(cr)));
+        xn = max(xn, mag(xr));
+        dn = max(dn, mag(dr));
+      }
+      atomicMax(c_rmax, rmax);
+      atomicMax(c_anorm, anorm);
+      atomicMax(c_xn, xn);
+      atomicMax(c_dn, dn);
+      if (nonfinite) atomicOr(c_nf, 1);
+      cluster.sync();
+      const double eta = __longlong_as_double((long long)*c_rmax) /
+                         fma(__longlong_as_double((long long)*c_anorm), __longlong_as_double((long long)*c_xn),
+                             __longlong_as_double((long long)*c_dn));
+      const bool ok = *c_nf == 0 && eta <= Fmt<T>::SEP_TOL;
+      cluster.sync();  // everyone has read the accumulators
+      if (rank == 0 && t == 0) {
+        s_rmax = s_anorm = s_xn = s_dn = 0ull;
+        s_nf = 0;
+      }
+      if (ok) {
+        accepted = true;
+        break;
+      }
+    }
+    if (pass == PGE_REFINE_CL) break;
+    // keep x in SX; the FP64 residual becomes the next right-hand side
+    for (int lr = t; lr < rows; lr += NT)
+      if (row0 + lr < n) SX[sidx(lr)] = SD[sidx(lr)];
+    cluster.sync();
+    for (int lr = t; lr < rows; lr += NT) {
+      const int r = row0 + lr;
+      const int q = sidx(lr);
+      if (r < n) {
+        const T ar = r > 0 ? ga[base + r] : T(0), br = gb[base + r], cr = r < n - 1 ? gc[base + r] : T(0);
+        double res = fma(-(double)br, (double)SX[q], (double)gd[base + r]);
+        if (r > 0) res = fma(-(double)ar, (double)xat(SX, r - 1), res);
+        if (r < n - 1) res = fma(-(double)cr, (double)xat(SX, r + 1), res);
+        SA[q] = ar;
+        SB[q] = br;
+        SC[q] = cr;
+        SD[q] = (T)res;
+      } else {
+        SA[q] = T(0);
+        SB[q] = T(1);
+        SC[q] = T(0);
+        SD[q] = T(0);
+      }
+    }
+    cluster.sync();
+  }  // passes
+  if (info && rank == 0 && t == 0) info[blockIdx.x / CL] = accepted ? 0 : n + 1;
+  if (!accepted && rank == 0 && t == 0) atomicAdd(&g_pge_fallbacks, 1ull);
+#pragma unroll 4
+  for (int p = warp; p < NT; p += NW) {
+    for (int i = lane; i < m; i += 32) {
+      const int r = row0 + p * m + i;
+      if (r < n) gx[base + r] = SD[p * ms + i];
+    }
+  }
+  cluster.sync();  // no CTA leaves while others may still read its shared memory
+}
+
 template <typename T, int NT>
 static size_t pge_smem_bytes(int ms) {
   return ((size_t)6 * NT * ms + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
@@ -610,11 +1043,47 @@ static cudaError_t pge_launch(const T* a, const T* b, const T* c, const T* d, T*
   return cudaGetLastError();
 }
 
+template <typename T, int NT, int CL>
+static size_t pgc_smem_bytes(int ms) {
+  return ((size_t)6 * NT * ms + PgcLayout<T, NT, CL>::END) * sizeof(T);
+}
+
+template <typename T, int NT, int CL>
+static bool pgc_fits(int n, int* m_out, int* ms_out) {
+  const int m = (n + CL * NT - 1) / (CL * NT);
+  if (m < 2 || m > 64) return false;
+  const int ms = m | 1;
+  if (pgc_smem_bytes<T, NT, CL>(ms) > PGE_SMEM_MAX) return false;
+  *m_out = m;
+  *ms_out = ms;
+  return true;
+}
+
+template <typename T, int NT, int CL>
+static cudaError_t pgc_launch(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                              int m, int ms, size_t stride, cudaStream_t s) {
+  const size_t smem = pgc_smem_bytes<T, NT, CL>(ms);
+  cudaError_t e = cudaFuncSetAttribute(pgc_kernel<T, NT, CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  pgc_kernel<T, NT, CL><<<(unsigned)batch * CL, NT, smem, s>>>(a, b, c, d, x, info, n, m, ms, stride);
+  return cudaGetLastError();
+}
+
+// Cluster sizes tried, smallest first.
+template <typename T>
+static int pgc_choice(int n, int* m, int* ms) {
+  if (pgc_fits<T, 128, 2>(n, m, ms)) return 2;
+  if (pgc_fits<T, 128, 4>(n, m, ms)) return 4;
+  if (pgc_fits<T, 128, 8>(n, m, ms)) return 8;
+  return 0;
+}
+
 template <typename T>
 bool pge_eligible(int layout, int n) {
   int m, ms;
   if (layout != CONTIG && layout != PACKED) return false;
-  return pge_fits<T, 128>(n, &m, &ms) || pge_fits<T, 64>(n, &m, &ms) || pge_fits<T, 256>(n, &m, &ms);
+  return pge_fits<T, 128>(n, &m, &ms) || pge_fits<T, 64>(n, &m, &ms) || pge_fits<T, 256>(n, &m, &ms) ||
+         pgc_choice<T>(n, &m, &ms) != 0;
 }
 
 template <typename T>
@@ -637,6 +1106,20 @@ cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* 
   if (pge_fits<T, 256>(n, &m, &ms)) {
     *used = true;
     return pge_launch<T, 256>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+  }
+  // longer systems: a cluster of 2, 4 or 8 CTAs per system
+  switch (pgc_choice<T>(n, &m, &ms)) {
+    case 2:
+      *used = true;
+      return pgc_launch<T, 128, 2>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+    case 4:
+      *used = true;
+      return pgc_launch<T, 128, 4>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+    case 8:
+      *used = true;
+      return pgc_launch<T, 128, 8>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+    default:
+      break;
   }
   return cudaSuccess;
 }

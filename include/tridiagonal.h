@@ -235,6 +235,54 @@ int tridiag_pge_single(int layout, const float *a, const float *b, const float *
 int tridiag_pge_double(int layout, const double *a, const double *b, const double *c, const double *d, double *x,
                        int *info, int n_eqt, int n_batch, void *stream);
 
+/* Adjoint through the partitioned solve (no pivot record needed): solves
+ * A^T lambda = xbar with tridiag_pge_* on the transposed coefficients
+ * (sub-diagonal c_{i-1}, super-diagonal a_{i+1}) and writes gd = lambda,
+ * ga_i = -lambda_i x_{i-1}, gb_i = -lambda_i x_i, gc_i = -lambda_i x_{i+1}
+ * (ga_0 = gc_{n-1} = 0); x is the forward solution.  Sizes as tridiag_pge_*;
+ * info (may be NULL) refers to A^T. */
+int tridiag_pge_adjoint_single(int layout, const float *a, const float *b, const float *c, const float *x,
+                               const float *xbar, float *ga, float *gb, float *gc, float *gd, int *info, int n_eqt,
+                               int n_batch, void *stream);
+int tridiag_pge_adjoint_double(int layout, const double *a, const double *b, const double *c, const double *x,
+                               const double *xbar, double *ga, double *gb, double *gc, double *gd, int *info,
+                               int n_eqt, int n_batch, void *stream);
+
+/* Ragged batches (no counterpart in the reference): n_batch systems of
+ * different sizes packed back to back in a, b, c, d (and x): system s is
+ * rows [offsets[s], offsets[s+1]) with 1 <= size <= 2^(TRIDIAG_RAGGED_CLASSES-1).
+ * A plan, built on the host from the offsets, groups the systems into size
+ * classes (class k: 2^(k-1) < n <= 2^k) and picks a kernel variant per class:
+ * 0 = thread-per-system sequential partial pivoting (n <= 64), 1/2/3 = the
+ * partitioned solve in one CTA with 64/128/256 partitions, 4/5/6 = in a
+ * cluster of 2/4/8 CTAs.  variant_by_class (may be NULL; entries < 0 mean
+ * "default") overrides the choice per class -- the autotuner's output; an
+ * entry that cannot serve its class's sizes makes the call return
+ * TRIDIAG_ERR_NOT_SUPPORTED.
+ * tridiag_ragged_solve_* / _adjoint_* issue one launch per non-empty class
+ * on the stream (capturable in one CUDA graph); offsets is the device copy of
+ * the offsets used to build the plan.  info (may be NULL) per system. */
+#define TRIDIAG_RAGGED_CLASSES 18
+typedef struct tridiag_ragged_plan tridiag_ragged_plan;
+int tridiag_ragged_plan_create(tridiag_ragged_plan **plan, int precision, const long long *offsets_host, int n_batch,
+                               const int *variant_by_class, int n_classes);
+void tridiag_ragged_plan_destroy(tridiag_ragged_plan *plan);
+/* Buckets of a plan, longest first: 4 ints each (class, variant, systems,
+ * largest n); returns the number of buckets. */
+int tridiag_ragged_plan_buckets(const tridiag_ragged_plan *plan, int *out, int max_buckets);
+/* Largest n a variant serves (0: none). */
+int tridiag_ragged_variant_max_n(int precision, int variant);
+int tridiag_ragged_solve_single(const tridiag_ragged_plan *plan, const float *a, const float *b, const float *c,
+                                const float *d, float *x, int *info, const long long *offsets, void *stream);
+int tridiag_ragged_solve_double(const tridiag_ragged_plan *plan, const double *a, const double *b, const double *c,
+                                const double *d, double *x, int *info, const long long *offsets, void *stream);
+int tridiag_ragged_adjoint_single(const tridiag_ragged_plan *plan, const float *a, const float *b, const float *c,
+                                  const float *x, const float *xbar, float *ga, float *gb, float *gc, float *gd,
+                                  int *info, const long long *offsets, void *stream);
+int tridiag_ragged_adjoint_double(const tridiag_ragged_plan *plan, const double *a, const double *b,
+                                  const double *c, const double *x, const double *xbar, double *ga, double *gb,
+                                  double *gc, double *gd, int *info, const long long *offsets, void *stream);
+
 /* Diagnostics: how many systems the partitioned partial-pivoting solve (used
  * by tridiag_gtsv_* without a pivot record, tridiag_solve_out_* with
  * TRIDIAG_ALGO_GTSV and the WM entry points on long systems) handed to its

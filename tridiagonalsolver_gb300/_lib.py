@@ -57,6 +57,16 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_partition_fallbacks": (ctypes.c_longlong, [_I]),
     "tridiag_pge_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_pge_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_ragged_plan_create": (_I, [_P, _I, _P, _I, _P, _I]),
+    "tridiag_ragged_plan_destroy": (None, [_P]),
+    "tridiag_ragged_plan_buckets": (_I, [_P, _P, _I]),
+    "tridiag_ragged_variant_max_n": (_I, [_I, _I]),
+    "tridiag_ragged_solve_single": (_I, [_P] * 9),
+    "tridiag_ragged_solve_double": (_I, [_P] * 9),
+    "tridiag_ragged_adjoint_single": (_I, [_P] * 13),
+    "tridiag_ragged_adjoint_double": (_I, [_P] * 13),
+    "tridiag_pge_adjoint_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_pge_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
 REFERENCE_SOLVERS = [

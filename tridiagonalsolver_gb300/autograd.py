@@ -1,9 +1,12 @@
 """torch.autograd wrapper of the pivoted solve and its adjoint kernel.
 
 ``x = solve_ad(a, b, c, d)`` solves the batch of tridiagonal systems
-A x = d with partial pivoting (``tridiag_gtsv_*``), keeping the pivot record;
-``x.backward(xbar)`` then runs ``tridiag_gtsv_adjoint_*``, which solves
-A^T lambda = xbar with the same factorisation and pivots and returns
+A x = d with partial pivoting: the partitioned solve (``tridiag_pge_*``)
+where it applies (contiguous layout, 65 <= n <= its size limit), else the
+thread-per-system sweep (``tridiag_gtsv_*``) keeping its pivot record.
+``x.backward(xbar)`` solves A^T lambda = xbar -- with the partitioned solve
+on the transposed coefficients (``tridiag_pge_adjoint_*``), or with the
+sweep's factorisation and pivots (``tridiag_gtsv_adjoint_*``) -- and returns
 
     grad_d = lambda,  grad_a[i] = -lambda[i] x[i-1],  grad_b[i] = -lambda[i] x[i],
     grad_c[i] = -lambda[i] x[i+1]
@@ -17,24 +20,44 @@ from __future__ import annotations
 import torch
 
 from . import ops
+from ._lib import ERR_NOT_SUPPORTED as NOT_SUPPORTED
+from ._lib import TridiagError
 
 
 class TridiagonalSolve(torch.autograd.Function):
     @staticmethod
     def forward(ctx, a, b, c, d, n, layout):
         a, b, c, d = (t.contiguous() for t in (a, b, c, d))
-        piv = ops.pivot_record(a, n, layout)
-        work = ops.gtsv_workspace(a, n, layout)
-        x = ops.gtsv(a, b, c, d, n, layout=layout, pivots=piv, work=work)
-        ctx.save_for_backward(a, b, c, x, piv, work)
-        ctx.n, ctx.layout = n, layout
+        method = "pge" if layout == "contiguous" else "gtsv"
+        x = None
+        if method == "pge":
+            # the partitioned solve: no pivot record, its adjoint is the same
+            # solver on A^T
+            try:
+                x = ops.pge(a, b, c, d, n, layout=layout)
+            except TridiagError as e:
+                if e.status != NOT_SUPPORTED:
+                    raise
+                method = "gtsv"
+        if method == "pge":
+            ctx.save_for_backward(a, b, c, x)
+        else:
+            piv = ops.pivot_record(a, n, layout)
+            work = ops.gtsv_workspace(a, n, layout)
+            x = ops.gtsv(a, b, c, d, n, layout=layout, pivots=piv, work=work)
+            ctx.save_for_backward(a, b, c, x, piv, work)
+        ctx.n, ctx.layout, ctx.method = n, layout, method
         return x
 
     @staticmethod
     def backward(ctx, xbar):
-        a, b, c, x, piv, work = ctx.saved_tensors
-        ga, gb, gc, gd = ops.gtsv_adjoint(a, b, c, x, piv, xbar.contiguous(), ctx.n, layout=ctx.layout,
-                                          work=work)
+        if ctx.method == "pge":
+            a, b, c, x = ctx.saved_tensors
+            ga, gb, gc, gd = ops.pge_adjoint(a, b, c, x, xbar.contiguous(), ctx.n, layout=ctx.layout)
+        else:
+            a, b, c, x, piv, work = ctx.saved_tensors
+            ga, gb, gc, gd = ops.gtsv_adjoint(a, b, c, x, piv, xbar.contiguous(), ctx.n, layout=ctx.layout,
+                                              work=work)
         need = ctx.needs_input_grad
         return (ga if need[0] else None, gb if need[1] else None, gc if need[2] else None,
                 gd if need[3] else None, None, None)

@@ -72,6 +72,33 @@ template <typename T>
 cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
                        cudaStream_t s, bool* used);
 
+// Adjoint with the partitioned solve: lambda = A^{-T} xbar (written to gd)
+// and ga = -lambda x_{i-1}, gb = -lambda x_i, gc = -lambda x_{i+1}, xf being
+// the forward solution.  No pivot record needed.
+template <typename T>
+cudaError_t launch_pge_adjoint(int layout, const T* a, const T* b, const T* c, const T* xf, const T* xbar, T* ga,
+                               T* gb, T* gc, T* gd, int* info, int n, int batch, cudaStream_t s, bool* used);
+// Variants of the partitioned solve (1-3: one CTA with 64/128/256
+// partitions, 4-6: a cluster of 2/4/8 CTAs), their largest n, the default
+// variant for n (0: none) -- used by the ragged planner.
+inline int pge_variant_partitions(int v) {
+  return v == 1 ? 64 : v == 2 ? 128 : v == 3 || v == 4 ? 256 : v == 5 ? 512 : v == 6 ? 1024 : 0;
+}
+template <typename T>
+int pge_default_variant(int n);
+template <typename T>
+int pge_variant_max_n(int v);
+template <typename T>
+int pge_variant_mmax(int v);
+// One size bucket of a ragged batch: `count` systems list[0..count) of the
+// packed arrays (system s = rows [offsets[s], offsets[s+1])), variant v, shared
+// memory for m_max rows per partition; mode 0 solves, mode 1 is the adjoint
+// (d = xbar, x = lambda, gradients to ga/gb/gc, xf = forward solution).
+template <typename T>
+cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, const T* c, const T* d, T* x,
+                              const T* xf, T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
+                              int count, int m_max, cudaStream_t s);
+
 // Number of systems the partitioned solve handed to its sequential fallback
 // (synchronous read; optionally reset).
 cudaError_t pge_fallback_count(unsigned long long* out, bool reset);

@@ -235,11 +235,66 @@ __device__ bool sep_solve_pivoted(const T* SEP, T* sx, T* tmp, int lane) {
   return bad;
 }
 
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, const T* __restrict__ gb,
-                                                    const T* __restrict__ gc, const T* gd, T* gx, int* info, int n,
-                                                    int m, int ms, size_t sys_stride) {
+// Arguments of the partitioned kernels.  Systems are uniform (system j at
+// j*stride, n rows) or ragged (system s = rows [offsets[s], offsets[s+1]) of
+// the packed arrays); `list` maps a CTA (cluster) to its system when a launch
+// serves one size bucket of a ragged batch.  MODE 0 writes x; MODE 1 is the
+// adjoint: the coefficient pointers describe A^T (a -> c - 1, c -> a + 1),
+// d is xbar, and the epilogue writes lambda to x and the gradients
+// ga = -lambda x_{i-1}, gb = -lambda x_i, gc = -lambda x_{i+1} using the
+// forward solution xf.
+template <typename T>
+struct PgeIO {
+  const T *a, *b, *c, *d;
+  T* x;
+  const T* xf;
+  T *ga, *gb, *gc;
+  int* info;
+  const long long* offsets;
+  const int* list;
+  size_t stride;
+  int n;
+};
+
+template <typename T, int MODE>
+__device__ __forceinline__ void pge_store(const PgeIO<T>& io, size_t base, int n, int r, T v) {
+  io.x[base + r] = v;
+  if (MODE == 1) {
+    io.ga[base + r] = r > 0 ? -v * io.xf[base + r - 1] : T(0);
+    io.gb[base + r] = -v * io.xf[base + r];
+    io.gc[base + r] = r < n - 1 ? -v * io.xf[base + r + 1] : T(0);
+  }
+}
+
+// System addressing of CTA (or cluster) `bid`; m = rows per partition for R
+// partitions (at least 2, so the last partitions may be identity rows).
+template <typename T>
+__device__ __forceinline__ void pge_system(const PgeIO<T>& io, int bid, int R, int& sys, size_t& base, int& n, int& m,
+                                           int& ms) {
+  sys = io.list ? io.list[bid] : bid;
+  if (io.offsets) {
+    base = (size_t)io.offsets[sys];
+    n = (int)(io.offsets[sys + 1] - io.offsets[sys]);
+  } else {
+    base = (size_t)sys * io.stride;
+    n = io.n;
+  }
+  m = (n + R - 1) / R;
+  if (m < 2) m = 2;
+  ms = m | 1;
+}
+
+template <typename T, int NT, int MODE>
+__global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   constexpr int NW = NT / 32;
+  int sys, n, m, ms;
+  size_t base;
+  pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
+  const T* __restrict__ ga = io.a;
+  const T* __restrict__ gb = io.b;
+  const T* __restrict__ gc = io.c;
+  const T* gd = io.d;
+  int* info = io.info;
   extern __shared__ __align__(16) unsigned char pge_smem[];
   T* SA = reinterpret_cast<T*>(pge_smem);
   T* SB = SA + NT * ms;
@@ -251,7 +306,6 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
   T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
   T* TMP = FST + 3 * NT;  // [PGE_TMP]: the FP32 separator solve's top level
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const size_t base = (size_t)blockIdx.x * sys_stride;
   using MagT = decltype(mag(T(0)));
   __shared__ MagT s_amax, s_dmax, s_xmax;
   MagT amax = 0, dmax = 0;
@@ -607,19 +661,19 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const T* __restrict__ ga, co
     if (t == 0) {
       atomicAdd(&g_pge_fallbacks, 1ull);
       s_info = seq_pivoted_inplace<T>(FA, FB, FC, FD, n);
-      if (info) info[blockIdx.x] = s_info;
+      if (info) info[sys] = s_info;
     }
     __syncthreads();
     if (s_info == 0)
-      for (int r = t; r < n; r += NT) gx[base + r] = FD[r];
+      for (int r = t; r < n; r += NT) pge_store<T, MODE>(io, base, n, r, FD[r]);
     return;
   }
-  if (info && t == 0) info[blockIdx.x] = 0;
+  if (info && t == 0) info[sys] = 0;
 #pragma unroll 4
   for (int p = warp; p < NT; p += NW) {
     for (int i = lane; i < m; i += 32) {
       const int r = p * m + i;
-      if (r < n) gx[base + r] = SD[p * ms + i];
+      if (r < n) pge_store<T, MODE>(io, base, n, r, SD[p * ms + i]);
     }
   }
 }
@@ -647,16 +701,17 @@ struct PgcLayout {
                        TSOL = TOP + 4 * NT, TMP = TSOL + NT, END = TMP + PGE_TMP;
 };
 
-template <typename T, int NT, int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1)
-    pgc_kernel(const T* __restrict__ ga, const T* __restrict__ gb, const T* __restrict__ gc, const T* gd, T* gx,
-               int* info, int n, int m, int ms, size_t sys_stride) {
+template <typename T, int NT, int CL, int MODE>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(const PgeIO<T> io) {
   namespace cg = cooperative_groups;
   using Lay = PgcLayout<T, NT, CL>;
   constexpr int R = Lay::R;
   constexpr int NW = NT / 32;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
+  int sys, n, m, ms;
+  size_t base;
+  pge_system(io, blockIdx.x / CL, R, sys, base, n, m, ms);
   extern __shared__ __align__(16) unsigned char pge_smem[];
   T* SA = reinterpret_cast<T*>(pge_smem);
   T* SB = SA + NT * ms;
@@ -675,7 +730,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1)
   T* TMP = EXT + Lay::TMP;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int P = rank * NT + t;
-  const size_t base = (size_t)(blockIdx.x / CL) * sys_stride;
+  const T* __restrict__ ga = io.a;
+  const T* __restrict__ gb = io.b;
+  const T* __restrict__ gc = io.c;
+  const T* gd = io.d;
+  int* info = io.info;
   const int rows = NT * m;  // rows per CTA
   const int row0 = rank * rows;
   using MagT = decltype(mag(T(0)));
@@ -1003,13 +1062,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1)
     }
     cluster.sync();
   }  // passes
-  if (info && rank == 0 && t == 0) info[blockIdx.x / CL] = accepted ? 0 : n + 1;
+  if (info && rank == 0 && t == 0) info[sys] = accepted ? 0 : n + 1;
   if (!accepted && rank == 0 && t == 0) atomicAdd(&g_pge_fallbacks, 1ull);
 #pragma unroll 4
   for (int p = warp; p < NT; p += NW) {
     for (int i = lane; i < m; i += 32) {
       const int r = row0 + p * m + i;
-      if (r < n) gx[base + r] = SD[p * ms + i];
+      if (r < n) pge_store<T, MODE>(io, base, n, r, SD[p * ms + i]);
     }
   }
   cluster.sync();  // no CTA leaves while others may still read its shared memory
@@ -1020,27 +1079,14 @@ static size_t pge_smem_bytes(int ms) {
   return ((size_t)6 * NT * ms + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
 }
 
-constexpr size_t PGE_SMEM_MAX = 227 * 1024 - 64;  // dynamic + the kernel's few static bytes
+constexpr size_t PGE_SMEM_MAX = 227 * 1024 - 128;  // dynamic + the kernels' few static bytes
 
+// Largest rows-per-partition m for which a variant's shared memory fits.
 template <typename T, int NT>
-static bool pge_fits(int n, int* m_out, int* ms_out) {
-  const int m = (n + NT - 1) / NT;
-  if (m < 2 || m > 64) return false;
-  const int ms = m | 1;  // odd stride: a warp's rows fall into distinct banks
-  if (pge_smem_bytes<T, NT>(ms) > PGE_SMEM_MAX) return false;
-  *m_out = m;
-  *ms_out = ms;
-  return true;
-}
-
-template <typename T, int NT>
-static cudaError_t pge_launch(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
-                              int m, int ms, size_t stride, cudaStream_t s) {
-  const size_t smem = pge_smem_bytes<T, NT>(ms);
-  cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  pge_kernel<T, NT><<<batch, NT, smem, s>>>(a, b, c, d, x, info, n, m, ms, stride);
-  return cudaGetLastError();
+static int pge_mmax() {
+  int m = 2;
+  while (m + 1 <= 64 && pge_smem_bytes<T, NT>((m + 1) | 1) <= PGE_SMEM_MAX) ++m;
+  return pge_smem_bytes<T, NT>(m | 1) <= PGE_SMEM_MAX ? m : 0;
 }
 
 template <typename T, int NT, int CL>
@@ -1049,79 +1095,158 @@ static size_t pgc_smem_bytes(int ms) {
 }
 
 template <typename T, int NT, int CL>
-static bool pgc_fits(int n, int* m_out, int* ms_out) {
-  const int m = (n + CL * NT - 1) / (CL * NT);
-  if (m < 2 || m > 64) return false;
-  const int ms = m | 1;
-  if (pgc_smem_bytes<T, NT, CL>(ms) > PGE_SMEM_MAX) return false;
-  *m_out = m;
-  *ms_out = ms;
-  return true;
+static int pgc_mmax() {
+  int m = 2;
+  while (m + 1 <= 64 && pgc_smem_bytes<T, NT, CL>((m + 1) | 1) <= PGE_SMEM_MAX) ++m;
+  return pgc_smem_bytes<T, NT, CL>(m | 1) <= PGE_SMEM_MAX ? m : 0;
 }
 
-template <typename T, int NT, int CL>
-static cudaError_t pgc_launch(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
-                              int m, int ms, size_t stride, cudaStream_t s) {
-  const size_t smem = pgc_smem_bytes<T, NT, CL>(ms);
-  cudaError_t e = cudaFuncSetAttribute(pgc_kernel<T, NT, CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// Variants: 0 = none, 1/2/3 = one CTA with 64/128/256 partitions,
+// 4/5/6 = a cluster of 2/4/8 CTAs with 128 partitions each
+// (pge_variant_partitions in kernels.h).
+
+template <typename T>
+int pge_variant_mmax(int v) {
+  switch (v) {
+    case 1: return pge_mmax<T, 64>();
+    case 2: return pge_mmax<T, 128>();
+    case 3: return pge_mmax<T, 256>();
+    case 4: return pgc_mmax<T, 128, 2>();
+    case 5: return pgc_mmax<T, 128, 4>();
+    case 6: return pgc_mmax<T, 128, 8>();
+    default: return 0;
+  }
+}
+
+template <typename T>
+int pge_variant_max_n(int v) {
+  if (v < 1 || v > 6) return 0;
+  return pge_variant_partitions(v) * pge_variant_mmax<T>(v);
+}
+
+template <typename T, int NT, int MODE>
+static cudaError_t pge_launch(const PgeIO<T>& io, int grid, int ms, cudaStream_t s) {
+  const size_t smem = pge_smem_bytes<T, NT>(ms);
+  cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, NT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  pgc_kernel<T, NT, CL><<<(unsigned)batch * CL, NT, smem, s>>>(a, b, c, d, x, info, n, m, ms, stride);
+  pge_kernel<T, NT, MODE><<<grid, NT, smem, s>>>(io);
   return cudaGetLastError();
 }
 
-// Cluster sizes tried, smallest first.
+template <typename T, int NT, int CL, int MODE>
+static cudaError_t pgc_launch(const PgeIO<T>& io, int grid, int ms, cudaStream_t s) {
+  const size_t smem = pgc_smem_bytes<T, NT, CL>(ms);
+  cudaError_t e =
+      cudaFuncSetAttribute(pgc_kernel<T, NT, CL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  pgc_kernel<T, NT, CL, MODE><<<(unsigned)grid * CL, NT, smem, s>>>(io);
+  return cudaGetLastError();
+}
+
+// Launch `grid` systems with variant v, shared memory sized for m_max rows
+// per partition.
+template <typename T, int MODE>
+static cudaError_t pge_launch_variant(int v, const PgeIO<T>& io, int grid, int m_max, cudaStream_t s) {
+  const int ms = (m_max < 2 ? 2 : m_max) | 1;
+  switch (v) {
+    case 1: return pge_launch<T, 64, MODE>(io, grid, ms, s);
+    case 2: return pge_launch<T, 128, MODE>(io, grid, ms, s);
+    case 3: return pge_launch<T, 256, MODE>(io, grid, ms, s);
+    case 4: return pgc_launch<T, 128, 2, MODE>(io, grid, ms, s);
+    case 5: return pgc_launch<T, 128, 4, MODE>(io, grid, ms, s);
+    case 6: return pgc_launch<T, 128, 8, MODE>(io, grid, ms, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Default variant for n rows: one CTA with 128 partitions where it fits
+// (64 for short systems, 256 for the longest single-CTA ones), else the
+// smallest cluster.  0 when no variant covers n.
 template <typename T>
-static int pgc_choice(int n, int* m, int* ms) {
-  if (pgc_fits<T, 128, 2>(n, m, ms)) return 2;
-  if (pgc_fits<T, 128, 4>(n, m, ms)) return 4;
-  if (pgc_fits<T, 128, 8>(n, m, ms)) return 8;
+int pge_default_variant(int n) {
+  if (n < 65) return 0;
+  const int v128 = pge_variant_max_n<T>(2);
+  if (n <= 128) return 1;
+  if (n <= v128) return 2;
+  if (n <= pge_variant_max_n<T>(3)) return 3;
+  for (int v = 4; v <= 6; ++v)
+    if (n <= pge_variant_max_n<T>(v)) return v;
   return 0;
 }
 
 template <typename T>
 bool pge_eligible(int layout, int n) {
-  int m, ms;
   if (layout != CONTIG && layout != PACKED) return false;
-  return pge_fits<T, 128>(n, &m, &ms) || pge_fits<T, 64>(n, &m, &ms) || pge_fits<T, 256>(n, &m, &ms) ||
-         pgc_choice<T>(n, &m, &ms) != 0;
+  return pge_default_variant<T>(n) != 0;
+}
+
+template <typename T>
+static PgeIO<T> uniform_io(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n) {
+  PgeIO<T> io{};
+  io.a = a;
+  io.b = b;
+  io.c = c;
+  io.d = d;
+  io.x = x;
+  io.info = info;
+  io.stride = layout == PACKED ? 4 * (size_t)n : (size_t)n;
+  io.n = n;
+  return io;
 }
 
 template <typename T>
 cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
                        cudaStream_t s, bool* used) {
   *used = false;
-  if (layout != CONTIG && layout != PACKED) return cudaSuccess;
-  const size_t stride = layout == PACKED ? 4 * (size_t)n : (size_t)n;
-  int m, ms;
-  // 128 partitions where the system fits (four warps: one per SM
-  // sub-partition), else fewer for short systems or more for long ones
-  if (pge_fits<T, 128>(n, &m, &ms)) {
-    *used = true;
-    return pge_launch<T, 128>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
+  if (!pge_eligible<T>(layout, n)) return cudaSuccess;
+  const int v = pge_default_variant<T>(n);
+  *used = true;
+  const int m = (n + pge_variant_partitions(v) - 1) / pge_variant_partitions(v);
+  return pge_launch_variant<T, 0>(v, uniform_io<T>(layout, a, b, c, d, x, info, n), batch, m, s);
+}
+
+template <typename T>
+cudaError_t launch_pge_adjoint(int layout, const T* a, const T* b, const T* c, const T* xf, const T* xbar, T* ga,
+                               T* gb, T* gc, T* gd, int* info, int n, int batch, cudaStream_t s, bool* used) {
+  *used = false;
+  if (!pge_eligible<T>(layout, n)) return cudaSuccess;
+  const int v = pge_default_variant<T>(n);
+  *used = true;
+  // A^T: sub-diagonal c_{i-1}, super-diagonal a_{i+1} (the shifted pointers
+  // are only dereferenced at rows 1..n-1 and 0..n-2 respectively)
+  PgeIO<T> io = uniform_io<T>(layout, c - 1, b, a + 1, xbar, gd, info, n);
+  io.xf = xf;
+  io.ga = ga;
+  io.gb = gb;
+  io.gc = gc;
+  const int m = (n + pge_variant_partitions(v) - 1) / pge_variant_partitions(v);
+  return pge_launch_variant<T, 1>(v, io, batch, m, s);
+}
+
+template <typename T>
+cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, const T* c, const T* d, T* x,
+                              const T* xf, T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
+                              int count, int m_max, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  PgeIO<T> io{};
+  io.b = b;
+  io.d = d;
+  io.x = x;
+  io.info = info;
+  io.offsets = offsets;
+  io.list = list;
+  if (mode == 0) {
+    io.a = a;
+    io.c = c;
+    return pge_launch_variant<T, 0>(variant, io, count, m_max, s);
   }
-  if (n < 256 && pge_fits<T, 64>(n, &m, &ms)) {
-    *used = true;
-    return pge_launch<T, 64>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
-  }
-  if (pge_fits<T, 256>(n, &m, &ms)) {
-    *used = true;
-    return pge_launch<T, 256>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
-  }
-  // longer systems: a cluster of 2, 4 or 8 CTAs per system
-  switch (pgc_choice<T>(n, &m, &ms)) {
-    case 2:
-      *used = true;
-      return pgc_launch<T, 128, 2>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
-    case 4:
-      *used = true;
-      return pgc_launch<T, 128, 4>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
-    case 8:
-      *used = true;
-      return pgc_launch<T, 128, 8>(a, b, c, d, x, info, n, batch, m, ms, stride, s);
-    default:
-      break;
-  }
-  return cudaSuccess;
+  io.a = c - 1;
+  io.c = a + 1;
+  io.xf = xf;
+  io.ga = ga;
+  io.gb = gb;
+  io.gc = gc;
+  return pge_launch_variant<T, 1>(variant, io, count, m_max, s);
 }
 
 cudaError_t pge_fallback_count(unsigned long long* out, bool reset) {
@@ -1135,8 +1260,15 @@ cudaError_t pge_fallback_count(unsigned long long* out, bool reset) {
 
 #define INST(T)                                                                                                   \
   template bool pge_eligible<T>(int, int);                                                                        \
+  template int pge_default_variant<T>(int);                                                                       \
+  template int pge_variant_max_n<T>(int);                                                                         \
+  template int pge_variant_mmax<T>(int);                                                                          \
   template cudaError_t launch_pge<T>(int, const T*, const T*, const T*, const T*, T*, int*, int, int, cudaStream_t, \
-                                     bool*);
+                                     bool*);                                                                      \
+  template cudaError_t launch_pge_adjoint<T>(int, const T*, const T*, const T*, const T*, const T*, T*, T*, T*, T*, \
+                                             int*, int, int, cudaStream_t, bool*);                                \
+  template cudaError_t launch_pge_ragged<T>(int, int, const T*, const T*, const T*, const T*, T*, const T*, T*, T*, \
+                                            T*, int*, const long long*, const int*, int, int, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

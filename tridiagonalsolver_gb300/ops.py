@@ -156,6 +156,20 @@ def pge(a, b, c, d, n: int, layout: str = "contiguous", info=None, out=None, str
     return x
 
 
+def pge_adjoint(a, b, c, x, xbar, n: int, layout: str = "contiguous", info=None, stream=None):
+    """Gradients (ga, gb, gc, gd) of L with dL/dx = xbar through x = A^-1 d,
+    by the partitioned solve of A^T lambda = xbar (no pivot record)."""
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    a, b, c, x, xbar = _al(a), _al(b), _al(c), _al(x), _al(xbar)
+    ga, gb, gc, gd = (torch.empty_like(a) for _ in range(4))
+    st = getattr(lib(), f"tridiag_pge_adjoint_{p}")(
+        LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), _ptr(x, a.dtype),
+        _ptr(xbar, a.dtype), _ptr(ga), _ptr(gb), _ptr(gc), _ptr(gd), _ptr(info), n, batch, _stream_ptr(stream))
+    check(st, f"tridiag_pge_adjoint_{p}")
+    return ga, gb, gc, gd
+
+
 def refine_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
     batch = _dims(a, n, layout)
     return torch.empty(lib().tridiag_refine_workspace_size(LAYOUTS[layout], n, batch), dtype=torch.uint8,

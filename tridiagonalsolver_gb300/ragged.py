@@ -1,0 +1,208 @@
+"""Ragged batches and the per-size-class autotuner.
+
+A ragged batch packs systems of different sizes back to back: system s is
+rows ``offsets[s] .. offsets[s+1]-1`` of the 1-D tensors a, b, c, d.  A
+:class:`RaggedPlan` (built once on the host from the offsets) groups the
+systems into size classes and picks a kernel variant per class; its
+:meth:`~RaggedPlan.solve` and :meth:`~RaggedPlan.adjoint` issue one launch
+per class on the current stream, so the whole call can be captured in one
+CUDA graph.  :func:`autotune` measures the variants on synthetic batches of
+each class and returns the fastest per class (the table a plan takes).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from ._lib import TridiagError, check, lib
+from .ops import _ptr, _stream_ptr
+
+CLASSES = 18            # TRIDIAG_RAGGED_CLASSES: class k holds 2^(k-1) < n <= 2^k
+VARIANTS = {0: "sequential (thread per system)", 1: "partitioned, 1 CTA x 64", 2: "partitioned, 1 CTA x 128",
+            3: "partitioned, 1 CTA x 256", 4: "partitioned, cluster of 2", 5: "partitioned, cluster of 4",
+            6: "partitioned, cluster of 8"}
+_P = ctypes.c_void_p
+
+
+def _sig():
+    return lib()
+
+
+def size_class(n: int) -> int:
+    return max(0, math.ceil(math.log2(n))) if n > 1 else 0
+
+
+def variant_max_n(precision: int, variant: int) -> int:
+    return _sig().tridiag_ragged_variant_max_n(precision, variant)
+
+
+class RaggedPlan:
+    """Plan for a ragged batch; ``offsets`` (int64, batch+1 entries) on the
+    host or device; ``table`` maps size class -> variant (None: defaults)."""
+
+    def __init__(self, offsets, dtype=torch.float32, table: dict | None = None, device=None):
+        L = _sig()
+        off = offsets.detach().cpu().numpy() if isinstance(offsets, torch.Tensor) else np.asarray(offsets)
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        self.batch = off.size - 1
+        self.precision = 1 if dtype == torch.float64 else 0
+        self.dtype = dtype
+        tab = np.full(CLASSES, -1, dtype=np.int32)
+        for k, v in (table or {}).items():
+            tab[int(k)] = int(v)
+        self._tab = tab
+        h = _P()
+        st = L.tridiag_ragged_plan_create(ctypes.addressof(h), self.precision, off.ctypes.data, self.batch,
+                                          tab.ctypes.data, CLASSES)
+        check(st, "tridiag_ragged_plan_create")
+        self._h = h
+        dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.offsets = torch.from_numpy(off).to(dev)
+        self.rows = int(off[-1] - off[0])
+
+    def buckets(self):
+        """[(class, variant, systems, largest n)], longest class first."""
+        L = _sig()
+        out = np.zeros(4 * CLASSES, dtype=np.int32)
+        nb = L.tridiag_ragged_plan_buckets(self._h, out.ctypes.data, CLASSES)
+        return [tuple(int(v) for v in out[4 * i:4 * i + 4]) for i in range(nb)]
+
+    def solve(self, a, b, c, d, out=None, info=None, stream=None):
+        p = "double" if self.precision else "single"
+        x = out if out is not None else torch.empty_like(d)
+        st = getattr(_sig(), f"tridiag_ragged_solve_{p}")(self._h, _ptr(a, self.dtype), _ptr(b, self.dtype),
+                                                          _ptr(c, self.dtype), _ptr(d, self.dtype),
+                                                          _ptr(x, self.dtype), _ptr(info), _ptr(self.offsets),
+                                                          _stream_ptr(stream))
+        check(st, f"tridiag_ragged_solve_{p}")
+        return x
+
+    def adjoint(self, a, b, c, x, xbar, grads=None, info=None, stream=None):
+        """(ga, gb, gc, gd) of L with dL/dx = xbar through x = A^-1 d."""
+        p = "double" if self.precision else "single"
+        ga, gb, gc, gd = grads if grads is not None else (torch.empty_like(x) for _ in range(4))
+        st = getattr(_sig(), f"tridiag_ragged_adjoint_{p}")(
+            self._h, _ptr(a, self.dtype), _ptr(b, self.dtype), _ptr(c, self.dtype), _ptr(x, self.dtype),
+            _ptr(xbar, self.dtype), _ptr(ga), _ptr(gb), _ptr(gc), _ptr(gd), _ptr(info), _ptr(self.offsets),
+            _stream_ptr(stream))
+        check(st, f"tridiag_ragged_adjoint_{p}")
+        return ga, gb, gc, gd
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _sig().tridiag_ragged_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+def synthetic_batch(sizes, dtype=torch.float32, nondominant_fraction=0.2, seed=0, device="cuda"):
+    """Packed arrays for systems of the given sizes: a, c, d ~ U[-1, 1]
+    (a_0 = c_{n-1} = 0); b = |a| + |c| + U[1, 2] for dominant systems, b ~
+    U[-1, 1] for the non-dominant fraction (chosen per system)."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    off = np.zeros(sizes.size + 1, dtype=np.int64)
+    np.cumsum(sizes, out=off[1:])
+    N = int(off[-1])
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+
+    def u(lo, hi):
+        return torch.rand(N, dtype=dtype, device=device, generator=g) * (hi - lo) + lo
+
+    a, c, d = u(-1, 1), u(-1, 1), u(-1, 1)
+    offs = torch.from_numpy(off).to(device)
+    a[offs[:-1]] = 0
+    c[offs[1:] - 1] = 0
+    rng = np.random.default_rng(seed + 1)
+    nondom = rng.random(sizes.size) < nondominant_fraction
+    row_sys = torch.repeat_interleave(torch.arange(sizes.size, device=device), torch.from_numpy(sizes).to(device))
+    nd_rows = torch.from_numpy(nondom).to(device)[row_sys]
+    b = torch.where(nd_rows, u(-1, 1), a.abs() + c.abs() + u(1, 2))
+    return a, b, c, d, off, nondom
+
+
+def log_uniform_sizes(count: int, lo: int = 32, hi: int = 65536, seed: int = 0):
+    rng = np.random.default_rng(seed)
+    return np.rint(np.exp(rng.uniform(math.log(lo), math.log(hi), count))).astype(np.int64)
+
+
+def _time(fn, reps=3):
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        fn()
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        s.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def candidates(precision: int, cls: int):
+    """Variants that serve every n of size class cls (2^(cls-1) < n <= 2^cls)."""
+    lo, hi = 2 ** (cls - 1) + 1 if cls > 0 else 1, 2 ** cls
+    out = [0] if hi <= 64 else []
+    if lo >= 65:
+        out += [v for v in range(1, 7) if variant_max_n(precision, v) >= hi]
+    return out
+
+
+def autotune(classes, dtype=torch.float32, systems_per_class=None, rows_per_class=2 ** 24, seed=0, reps=3,
+             verbose=False):
+    """Time every candidate variant on a synthetic batch of each size class
+    (sizes log-uniform inside the class, 20% non-dominant systems) and
+    return {class: fastest variant} plus the timings."""
+    precision = 1 if dtype == torch.float64 else 0
+    table, timings = {}, {}
+    for k in classes:
+        cands = candidates(precision, k)
+        if len(cands) <= 1:
+            if cands:
+                table[k] = cands[0]
+            continue
+        lo, hi = max(2 ** (k - 1) + 1, 2), 2 ** k
+        count = systems_per_class or max(64, min(20000, rows_per_class // hi))
+        sizes = log_uniform_sizes(count, lo, hi, seed=seed + k)
+        a, b, c, d, off, _ = synthetic_batch(sizes, dtype=dtype, seed=seed + k)
+        x = torch.empty_like(d)
+        res = {}
+        for v in cands:
+            plan = RaggedPlan(off, dtype=dtype, table={k: v})
+            if plan.buckets()[0][1] != v:
+                continue
+            res[v] = _time(lambda: plan.solve(a, b, c, d, out=x), reps)
+            del plan
+        if res:
+            table[k] = min(res, key=res.get)
+            timings[k] = res
+            if verbose:
+                print(f"class {k:2d} (n <= {hi:6d}, {count} systems): " +
+                      ", ".join(f"v{v} {t:.3f} ms" for v, t in sorted(res.items())) + f" -> v{table[k]}")
+        del a, b, c, d, x
+    return table, timings
+
+
+def save_table(path, table, dtype=torch.float32, timings=None):
+    doc = {"device": torch.cuda.get_device_name(), "dtype": str(dtype).replace("torch.", ""),
+           "table": {str(k): int(v) for k, v in table.items()},
+           "timings_ms": {str(k): {str(v): t for v, t in r.items()} for k, r in (timings or {}).items()}}
+    Path(path).write_text(json.dumps(doc, indent=1))
+
+
+def load_table(path):
+    doc = json.loads(Path(path).read_text())
+    return {int(k): int(v) for k, v in doc["table"].items()}
+
+
+__all__ = ["RaggedPlan", "autotune", "candidates", "load_table", "log_uniform_sizes", "save_table",
+           "synthetic_batch", "size_class", "variant_max_n", "TridiagError", "CLASSES", "VARIANTS"]

@@ -33,6 +33,8 @@ from __future__ import annotations
 
 import argparse
 import json
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -453,6 +455,370 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Further workloads (--workload): the other benchmark configurations, each
+# measured on its own and printed as one JSON line with the same keys.
+
+
+def _graph_time(torch, stream, fn, steps, warmup):
+    """Capture fn in a CUDA graph; time `steps` replays (CUDA events on the
+    launching stream, synchronised on both sides); return ms per replay."""
+    with torch.cuda.stream(stream):
+        for _ in range(max(warmup, 3)):
+            fn()
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        fn()
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(steps):
+            g.replay()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, g
+
+
+def _e2e_generic(torch, stream, dev_inputs, dev_outputs, fn, steps, unit_count):
+    """Pinned host -> device copies of the inputs, fn, device -> host copies
+    of the outputs, all inside the timed region."""
+    hin = [torch.empty_like(t, device="cpu").pin_memory() for t in dev_inputs]
+    hout = [torch.empty_like(t, device="cpu").pin_memory() for t in dev_outputs]
+    for h, t in zip(hin, dev_inputs):
+        h.copy_(t)
+    torch.cuda.synchronize()
+
+    def one():
+        for t, h in zip(dev_inputs, hin):
+            t.copy_(h, non_blocking=True)
+        fn()
+        for h, t in zip(hout, dev_outputs):
+            h.copy_(t, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        one()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            one()
+        e1.record(stream)
+        stream.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": unit_count / (ms * 1e-3), "unit": UNIT,
+            "h2d_bytes_per_step": sum(t.numel() * t.element_size() for t in dev_inputs),
+            "d2h_bytes_per_step": sum(t.numel() * t.element_size() for t in dev_outputs), "ms_per_step": ms,
+            "steps": steps}
+
+
+def _line(args, workload, value, ms_step, dtype, config, parts, roof_bytes, roof_ms, cpu, e2e, clocks, launches,
+          note=None):
+    peak, peak_kind = _measured_peaks()
+    achieved = roof_bytes / (roof_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "kernel": config.get("dominant", "step"),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s"}
+    if note:
+        roofline["note"] = note
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic (seeded, distributions of the workload)", "config": dict(config, workload=workload),
+            "parts": parts, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+
+
+def _cpu_sample(fn_sample, total_units, target_s=8.0, start=8):
+    """Time fn_sample(k) (k units) growing k until ~target_s/4; extrapolate."""
+    from oracle import oracle as O
+
+    O.set_threads(0)
+    k = start
+    t = fn_sample(k)
+    while t < target_s / 4 and k < total_units:
+        k = min(total_units, k * 4)
+        t = fn_sample(k)
+    return k / t, k, t, O.threads()
+
+
+def run_thomas_fp64(args):
+    """Plain Thomas, FP64, n = 4096 x 4096 dominant systems, interleaved layout."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+    from tridiagonalsolver_gb300 import inputs
+
+    T.lib()
+    n, batch = 4096, 4096
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    u = lambda lo, hi: torch.rand((n, batch), dtype=torch.float64, device=dev, generator=g) * (hi - lo) + lo
+    a, c, d = u(-1, 1), u(-1, 1), u(-1, 1)
+    a[0] = 0
+    c[-1] = 0
+    b = a.abs() + c.abs() + u(1, 2)
+    x = torch.empty_like(d)
+    work = T.solve_out_workspace(a, n, "thomas", layout="interleaved")
+    stream = torch.cuda.Stream(device=dev)
+    step = lambda: T.solve_out(a, b, c, d, n, algo="thomas", layout="interleaved", out=x, work=work, stream=stream)
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.6)
+    sampler.mark("begin")
+    ms, _ = _graph_time(torch, stream, step, args.steps, args.warmup)
+    sampler.mark("end")
+    clocks = sampler.stop()
+    idx = torch.arange(0, batch, batch // 16, device=dev)
+    hs = [t.index_select(1, idx).T.contiguous().cpu().numpy() for t in (a, b, c, d, x)]
+    _, eta = O.backward_error(*hs, n)
+    e2e = _e2e_generic(torch, stream, [a, b, c, d], [x], step, max(3, min(args.steps // 10, 10)), batch)
+
+    def cpu(k):
+        aa, bb, cc, dd = inputs.dominant(n, k, seed=3)
+        t0 = time.perf_counter()
+        O.thomas(aa, bb, cc, dd, n)
+        return time.perf_counter() - t0
+
+    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, batch)
+    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                      "sample": f"{k} of {batch} systems in {t:.2f} s (reference Thomas restated)"}
+    bytes_ = 5 * n * batch * 8
+    _line(args, "Thomas FP64 n=4096 x 4096, interleaved layout, dominant", batch / (ms * 1e-3), ms, "f64",
+          {"n": n, "batch": batch, "layout": "interleaved", "dominant": "tw_kernel<double, INTERLEAVED, ThomasOp>",
+           "l2": "inputs larger than L2 (537 MB)"},
+          [{"name": "thomas_fp64", "ms_per_launch": ms, "backward_error_max": eta}], bytes_, ms, cpu_b, e2e, clocks,
+          args.steps, note="FP64 pipe bound (two chains per system; ~0.5 Tops/s FP64 per GB300)")
+
+
+def run_adjoint(args):
+    """Forward + adjoint, FP32, n = 1024 x 16384 dominant, loss = sum(w x)."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+    from tridiagonalsolver_gb300 import inputs
+
+    T.lib()
+    n, batch = 1024, 16384
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(12)
+    u = lambda lo, hi: torch.rand((batch, n), dtype=torch.float32, device=dev, generator=g) * (hi - lo) + lo
+    a, c, d, w = u(-1, 1), u(-1, 1), u(-1, 1), u(-1, 1)
+    a[:, 0] = 0
+    c[:, -1] = 0
+    b = a.abs() + c.abs() + u(1, 2)
+    x = torch.empty_like(d)
+    grads = [torch.empty_like(d) for _ in range(4)]
+    L = T.lib()
+    stream = torch.cuda.Stream(device=dev)
+
+    def step():
+        sp = int(stream.cuda_stream)
+        T.check(L.tridiag_pge_single(0, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), None,
+                                     n, batch, sp), "pge")
+        T.check(L.tridiag_pge_adjoint_single(0, a.data_ptr(), b.data_ptr(), c.data_ptr(), x.data_ptr(),
+                                             w.data_ptr(), *[t.data_ptr() for t in grads], None, n, batch, sp),
+                "pge adjoint")
+
+    def fwd():
+        T.check(L.tridiag_pge_single(0, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), None,
+                                     n, batch, int(stream.cuda_stream)), "pge")
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.6)
+    sampler.mark("begin")
+    ms, _ = _graph_time(torch, stream, step, args.steps, args.warmup)
+    sampler.mark("end")
+    clocks = sampler.stop()
+    ms_f, _ = _graph_time(torch, stream, fwd, max(10, args.steps // 5), 3)
+    idx = torch.arange(0, batch, batch // 16, device=dev)
+    hs = [t.index_select(0, idx).double().cpu().numpy() for t in (a, b, c, d, x, w)]
+    _, eta = O.backward_error(*hs[:5], n)
+    ref = O.adjoint_f64(hs[0], hs[1], hs[2], hs[4], hs[5], n)
+    gerr = max(float(np.max(np.abs(gg.index_select(0, idx).double().cpu().numpy() - r.reshape(16, n))) /
+                     np.max(np.abs(r))) for gg, r in zip(grads, ref))
+    e2e = _e2e_generic(torch, stream, [a, b, c, d, w], [x] + grads, step, max(3, min(args.steps // 10, 10)), batch)
+
+    def cpu(k):
+        aa, bb, cc, dd = inputs.dominant(n, k, seed=3)
+        ww = np.random.default_rng(1).uniform(-1, 1, (k, n))
+        t0 = time.perf_counter()
+        xx = O.gtsv(aa, bb, cc, dd, n)
+        O.adjoint_f64(aa, bb, cc, xx, ww, n)
+        return time.perf_counter() - t0
+
+    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, batch)
+    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                      "sample": f"{k} of {batch} systems forward+adjoint in {t:.2f} s (FP64 port)"}
+    _line(args, "forward+adjoint FP32 WM-pGE n=1024 x 16384, dominant, loss=sum(w*x)", batch / (ms * 1e-3), ms,
+          "f32", {"n": n, "batch": batch, "dominant": "pge_kernel<float,128> forward + adjoint (transposed)",
+                  "l2": "inputs larger than L2 (336 MB)"},
+          [{"name": "forward", "ms_per_launch": ms_f, "backward_error_max": eta},
+           {"name": "adjoint", "ms_per_launch": ms - ms_f, "gradient_rel_err_vs_fp64": gerr}],
+          14 * n * batch * 4, ms, cpu_b, e2e, clocks, 2 * args.steps)
+
+
+def run_ragged(args):
+    """100000 systems, n log-uniform in [32, 65536], FP32, 20% non-dominant:
+    forward + adjoint through the autotuned size-class plan."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+    from tridiagonalsolver_gb300 import ragged
+
+    T.lib()
+    dev = torch.device("cuda", 0)
+    sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
+    w = torch.rand_like(d) * 2 - 1
+    classes = sorted({ragged.size_class(int(v)) for v in sizes})
+    t0 = time.time()
+    table, timings = ragged.autotune(classes, dtype=torch.float32, reps=2)
+    tune_s = time.time() - t0
+    plan = T.RaggedPlan(off, table=table)
+    x = torch.empty_like(d)
+    grads = [torch.empty_like(d) for _ in range(4)]
+    stream = torch.cuda.Stream(device=dev)
+
+    def step():
+        plan.solve(a, b, c, d, out=x, stream=stream)
+        plan.adjoint(a, b, c, x, w, grads=grads, stream=stream)
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.6)
+    sampler.mark("begin")
+    steps = max(3, min(args.steps, 20))
+    ms, _ = _graph_time(torch, stream, step, steps, args.warmup)
+    sampler.mark("end")
+    clocks = sampler.stop()
+    ms_f, _ = _graph_time(torch, stream, lambda: plan.solve(a, b, c, d, out=x, stream=stream), steps, 3)
+    rng = np.random.default_rng(5)
+    worst = 0.0
+    for s_ in rng.choice(len(sizes), 16, replace=False):
+        lo, hi = int(off[s_]), int(off[s_ + 1])
+        hs = [t[lo:hi].double().cpu().numpy()[None] for t in (a, b, c, d, x)]
+        worst = max(worst, O.backward_error(*hs, hi - lo)[1])
+    rows = int(off[-1])
+    e2e = _e2e_generic(torch, stream, [a, b, c, d, w], [x] + grads, step, 3, len(sizes))
+
+    def cpu(k):
+        sel = np.random.default_rng(9).choice(len(sizes), k, replace=False)
+        tt = 0.0
+        for s_ in sel:
+            n_ = int(sizes[s_])
+            aa, bb, cc, dd = (np.random.default_rng(int(s_)).uniform(-1, 1, (1, n_)) for _ in range(4))
+            bb = np.abs(aa) + np.abs(cc) + 1.5
+            t1 = time.perf_counter()
+            O.gtsv(aa, bb, cc, dd, n_)
+            tt += time.perf_counter() - t1
+        return tt
+
+    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, len(sizes), target_s=4.0, start=64)
+    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                      "sample": f"{k} random systems of the batch, forward only, one thread, {t:.2f} s"}
+    bk = [{"class": cl, "variant": v, "systems": cnt, "max_n": mx} for cl, v, cnt, mx in plan.buckets()]
+    _line(args, "ragged: 100000 systems, n log-uniform [32, 65536], FP32, 20% non-dominant, forward+adjoint",
+          len(sizes) / (ms * 1e-3), ms, "f32",
+          {"systems": len(sizes), "rows": rows, "buckets": bk, "autotune_table": {str(k_): v for k_, v in table.items()},
+           "autotune_seconds": round(tune_s, 1), "l2": "inputs larger than L2 (13.8 GB)",
+           "timing": "CUDA graph of the whole ragged forward+adjoint (one launch per size class and direction)"},
+          [{"name": "forward", "ms_per_launch": ms_f, "backward_error_max": worst},
+           {"name": "adjoint", "ms_per_launch": ms - ms_f}],
+          14 * rows * 4 + 16 * len(sizes), ms, cpu_b, e2e, clocks, 2 * steps * len(bk))
+
+
+def run_refined(args):
+    """n = 65536 x 1024, b = s (1+delta)(|a|+|c|): FP32 partitioned solve +
+    FP64-residual refinement (2 steps) vs the plain FP64 solve, delta sweep."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+
+    T.lib()
+    n, batch = 65536, 1024
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(13)
+    u = lambda lo, hi: torch.rand((batch, n), dtype=torch.float64, device=dev, generator=g) * (hi - lo) + lo
+    a, c, d = u(-1, 1), u(-1, 1), u(-1, 1)
+    a[:, 0] = 0
+    c[:, -1] = 0
+    sgn = torch.where(u(0, 1) < 0.5, -1.0, 1.0)
+    base_b = sgn * (a.abs() + c.abs())
+    del sgn
+    x = torch.empty_like(d)
+    work = T.refine_workspace(a, n)
+    stream = torch.cuda.Stream(device=dev)
+    parts = []
+    ms_main = None
+    clocks = None
+    idx = torch.arange(0, batch, batch // 8, device=dev)
+    for delta in (1.0, 1e-2, 1e-4, 1e-6):
+        b = base_b * (1 + delta)
+        fn = lambda: T.refine(a, b, c, d, n, iters=2, work=work, out=x, stream=stream)
+        sampler = None
+        if delta == 1e-6:
+            sampler = ClockSampler(0)
+            sampler.start()
+            time.sleep(0.6)
+            sampler.mark("begin")
+        ms, _ = _graph_time(torch, stream, fn, max(3, min(args.steps, 20)), args.warmup)
+        if sampler:
+            sampler.mark("end")
+            clocks = sampler.stop()
+            ms_main = ms
+            bmain = b
+        hs = [t.index_select(0, idx).cpu().numpy() for t in (a, b, c, d, x)]
+        _, eta = O.backward_error(*hs, n)
+        parts.append({"name": f"refined delta={delta:g}", "ms_per_launch": ms, "systems_per_s": batch / (ms * 1e-3),
+                      "backward_error_max": eta})
+    # plain FP64 solve on the same GPU (hardest delta)
+    wg = T.gtsv_workspace(a, n)
+    xp = torch.empty_like(d)
+    ms_p, _ = _graph_time(torch, stream, lambda: T.gtsv(a, bmain, c, d, n, work=wg, out=xp, stream=stream), 3, 3)
+    hs = [t.index_select(0, idx).cpu().numpy() for t in (a, bmain, c, d, xp)]
+    _, eta_p = O.backward_error(*hs, n)
+    parts.append({"name": "plain FP64 pivoted solve delta=1e-06", "ms_per_launch": ms_p,
+                  "systems_per_s": batch / (ms_p * 1e-3), "backward_error_max": eta_p})
+    del wg
+    e2e = _e2e_generic(torch, stream, [a, bmain, c, d], [x],
+                       lambda: T.refine(a, bmain, c, d, n, iters=2, work=work, out=x, stream=stream), 3, batch)
+    cpu_b = None
+    if not args.no_cpu:
+        def cpu(k):
+            hs_ = [t[:k].cpu().numpy() for t in (a, bmain, c, d)]
+            t0 = time.perf_counter()
+            O.gtsv(*hs_, n)
+            return time.perf_counter() - t0
+
+        rate, k, t, cores = _cpu_sample(cpu, batch, start=16)
+        cpu_b = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                 "sample": f"{k} of {batch} systems, plain FP64 partial pivoting, {t:.2f} s"}
+    _line(args, "refined: FP32 WM-pGE + FP64-residual refinement, n=65536 x 1024, delta sweep",
+          batch / (ms_main * 1e-3), ms_main, "f32+f64 residual",
+          {"n": n, "batch": batch, "iters": 2, "dominant": "pgc_kernel<float,128,8> (cluster of 8)",
+           "l2": "inputs larger than L2 (2.1 GB)", "headline_case": "delta=1e-6"},
+          parts, 5 * n * batch * 8, ms_main, cpu_b, e2e, clocks, 7 * max(3, min(args.steps, 20)),
+          note="algorithmic bytes counted as 5*n*8 (FP64 in/out), as for the plain FP64 solve")
+
+
+WORKLOADS = {"config2": None, "thomas-fp64": run_thomas_fp64, "adjoint": run_adjoint, "ragged": run_ragged,
+             "refined": run_refined}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -460,13 +826,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2",
+                    help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
+                         "remaining benchmark configurations, one JSON line each")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif WORKLOADS[args.workload] is None:
         run_ours(args)
+    else:
+        WORKLOADS[args.workload](args)
 
 
 if __name__ == "__main__":

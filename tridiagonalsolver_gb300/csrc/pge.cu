@@ -1159,16 +1159,18 @@ static cudaError_t pge_launch_variant(int v, const PgeIO<T>& io, int grid, int m
   }
 }
 
-// Default variant for n rows: one CTA with 128 partitions where it fits
-// (64 for short systems, 256 for the longest single-CTA ones), else the
-// smallest cluster.  0 when no variant covers n.
+// Default variant for n rows: about 32 rows per partition where one CTA
+// holds the system -- 64 partitions up to n = 2048, 128 up to 4096, 256
+// beyond (shorter partitions make the log2(NT)-step separator solve the
+// larger part of the work; measured on GB300 by the ragged autotuner) --
+// else the smallest cluster.  0 when no variant covers n.
 template <typename T>
 int pge_default_variant(int n) {
   if (n < 65) return 0;
-  const int v128 = pge_variant_max_n<T>(2);
-  if (n <= 128) return 1;
-  if (n <= v128) return 2;
+  if (n <= 2048 && n <= pge_variant_max_n<T>(1)) return 1;
+  if (n <= 4096 && n <= pge_variant_max_n<T>(2)) return 2;
   if (n <= pge_variant_max_n<T>(3)) return 3;
+  if (n <= pge_variant_max_n<T>(2)) return 2;
   for (int v = 4; v <= 6; ++v)
     if (n <= pge_variant_max_n<T>(v)) return v;
   return 0;

@@ -293,9 +293,16 @@ def run_ours(args):
                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                     else "fallback 6.8 TB/s"}
         if dom["dtype"] == "float64":
-            # the FP64 solve is bound by the FP64 pipe on GB300, not by HBM
-            roofline["note"] = ("FP64 arithmetic bound: ~11 FP64 ops/row at ~0.5 Tops/s FP64 per GB300 "
-                                "(measured, profiles/fp64_rates_microbench.txt)")
+            # the FP64 solve is bound by the FP64 pipe on GB300, not by HBM: report that roofline too
+            # (FP64 operations per row from ncu's instruction counts, profiles/pge_fp64_n4096.md;
+            # peak = measured DFMA rate, profiles/fp64_rates_microbench.txt)
+            ops_per_row, fp64_peak = 25.4, 503.0
+            gops = dom["n"] * dom["batch"] * ops_per_row / (dom["ms_per_launch"] * 1e-3) / 1e9
+            roofline["compute"] = {"bound": "fp64", "achieved": round(gops, 1), "peak": fp64_peak,
+                                   "unit": "Gop/s", "frac": round(gops / fp64_peak, 4),
+                                   "ops_per_row": ops_per_row, "peak_source": "measured DFMA microbenchmark"}
+            roofline["note"] = ("the pivoted FP64 solve is bound by GB300's FP64 issue rate (one FP64 warp "
+                                "instruction per 80 cycles per SM sub-partition), not by HBM; see roofline.compute")
         cpu = _cpu_baseline() if (world == 1 and not args.no_cpu) else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

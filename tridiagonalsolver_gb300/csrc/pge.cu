@@ -50,6 +50,13 @@ __device__ __forceinline__ unsigned long long mag(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 __device__ __forceinline__ unsigned mag(float v) { return (unsigned)__float_as_int(v) & 0x7fffffffu; }
+// Magnitude key in 32 bits (FP64: the high word, which orders |v| up to a
+// relative 2^-20 -- enough for the acceptance test's maxima -- and keeps
+// the running maxima single 32-bit integer instructions).
+__device__ __forceinline__ unsigned magh(double v) {
+  return (unsigned)((unsigned long long)__double_as_longlong(v) >> 32) & 0x7fffffffu;
+}
+__device__ __forceinline__ unsigned magh(float v) { return mag(v); }
 __device__ __forceinline__ int expo(double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff; }
 __device__ __forceinline__ int expo(float v) { return (int)((unsigned)__float_as_int(v) >> 23) & 0xff; }
 template <typename T>
@@ -58,7 +65,7 @@ template <>
 struct Fmt<double> {
   static constexpr int BIAS = 1023;
   static constexpr double SEP_TOL = 2.5e-13;  // backward error accepted (separator rows, then all rows)
-  __device__ static double from_mag(unsigned long long m) { return __longlong_as_double((long long)m); }
+  __device__ static double from_mag(unsigned m) { return __longlong_as_double((long long)m << 32); }
 };
 template <>
 struct Fmt<float> {
@@ -306,7 +313,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
   T* TMP = FST + 3 * NT;  // [PGE_TMP]: the FP32 separator solve's top level
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  using MagT = decltype(mag(T(0)));
+  using MagT = unsigned;
   __shared__ MagT s_amax, s_dmax, s_xmax;
   MagT amax = 0, dmax = 0;
   if (t == 0) {
@@ -340,20 +347,6 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
-  // magnitudes for the acceptance test: max |a|, |b|, |c| and max |d| over
-  // the partition's rows (integer pipe)
-  {
-    const T* A0 = SA + t * ms;
-    const T* B0 = SB + t * ms;
-    const T* C0 = SC + t * ms;
-    const T* D0 = SD + t * ms;
-    for (int i = 0; i < m; ++i) {
-      amax = max(amax, max(mag(A0[i]), max(mag(B0[i]), mag(C0[i]))));
-      dmax = max(dmax, mag(D0[i]));
-    }
-  }
-  atomicMax(&s_amax, amax);
-  atomicMax(&s_dmax, dmax);
 
   bool accepted = false;
 #pragma unroll 1
@@ -377,8 +370,11 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   bool bad = false;  // this pass: breakdown, non-finite or (pass 0) separator residual
   unsigned long long swaps = 0ull;
   T cb = B[0], cc = mi > 1 ? C[0] : T(0), cy = D[0], cv = A[0], cw = mi == 1 ? C[0] : T(0);
+  amax = max(amax, max(magh(cv), max(magh(cb), magh(C[0]))));  // magnitudes for the acceptance test
+  dmax = max(dmax, magh(cy));
   T w_prev = T(0);                             // w' of U row mi-2 (the only other nonzero w')
   T om1 = T(0), om2 = T(0);                    // omega_{i-1}, omega_{i-2}
+  T kro = T(1);                                // [i = 0] of the omega recurrence
   T pu1 = T(0), pu2a = T(0), pu2b = T(0);      // u1_{i-1}, u2_{i-1}, u2_{i-2}
   T Y0 = T(0), V0 = T(0);                      // omega . y', omega . v'
   // software-pipelined: row i+2 (at most the separator row, which always
@@ -386,6 +382,8 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   T pa = A[1], pb = B[1], pc = C[1], py = D[1];
   for (int i = 0; i + 1 < mi; ++i) {
     const T na = pa, nb = pb, cn = pc, ny = py;
+    amax = max(amax, max(magh(na), max(magh(nb), magh(cn))));
+    dmax = max(dmax, magh(ny));
     pa = A[i + 2];
     pb = B[i + 2];
     pc = C[i + 2];
@@ -401,7 +399,8 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     const T u2 = sw ? nc : T(0);
     const T uy = sw ? ny : cy;
     const T uv = sw ? T(0) : cv;
-    const T om = fma(-om2, pu2b, fma(-om1, pu1, i == 0 ? T(1) : T(0))) * inv;
+    const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv;
+    kro = T(0);
     Y0 = fma(om, uy, Y0);
     V0 = fma(om, uv, V0);
     om2 = om1;
@@ -427,7 +426,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   bad |= is_zero(cb);
   const T inv_last = Div<T>(cb).inv();
   {
-    const T om = fma(-om2, pu2b, fma(-om1, pu1, mi == 1 ? T(1) : T(0))) * inv_last;
+    const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv_last;
     Y0 = fma(om, cy, Y0);
     V0 = fma(om, cv, V0);
     const T W0 = fma(om1, w_prev, om * cw);
@@ -445,6 +444,12 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   // ---- separator system: row m-1 of partition t couples to the last
   // interior row of t and the first row of t+1
   const T as = A[mi], bs = B[mi], cs = C[mi], ds = D[mi];
+  amax = max(amax, max(magh(as), max(magh(bs), magh(cs))));
+  dmax = max(dmax, magh(ds));
+  if (pass == 0) {
+    atomicMax(&s_amax, amax);
+    atomicMax(&s_dmax, dmax);
+  }
   {
     const bool has_next = t + 1 < NT;
     const T Yf = has_next ? FST[t + 1] : T(0);
@@ -516,13 +521,13 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   // too) the sequential partial-pivoting solve.
   const T sp = t > 0 ? FST[t - 1] : T(0);
   const T st = FST[t];
-  MagT xmax = mag(st);
+  MagT xmax = magh(st);
   T x_last;
   {
     T x1 = (fma(-cw, st, fma(-V[mi - 1], sp, D[mi - 1]))) * inv_last;
     T x2 = T(0);
     D[mi - 1] = x1;
-    xmax = max(xmax, mag(x1));
+    xmax = max(xmax, magh(x1));
     bad |= !finite_val(x1);
     x_last = x1;
     // software-pipelined: row i-1's factors are loaded while row i is solved
@@ -541,7 +546,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
       if (i == mi - 2) r = fma(-w_prev, st, r);
       const T xi = fma(-u2, x2, fma(-bi, x1, r)) * ai;
       D[i] = xi;
-      xmax = max(xmax, mag(xi));
+      xmax = max(xmax, magh(xi));
       bad |= !finite_val(xi);
       x2 = x1;
       x1 = xi;
@@ -737,7 +742,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   int* info = io.info;
   const int rows = NT * m;  // rows per CTA
   const int row0 = rank * rows;
-  using MagT = decltype(mag(T(0)));
+  using MagT = unsigned;
   __shared__ MagT s_amax, s_dmax, s_xmax;
   __shared__ unsigned long long s_rmax, s_anorm, s_xn, s_dn;
   __shared__ int s_bad, s_nf;
@@ -784,19 +789,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   cluster.sync();  // staging done everywhere, CTA 0's accumulators initialised
-  {
-    MagT amax = 0, dmax = 0;
-    const T* A0 = SA + t * ms;
-    const T* B0 = SB + t * ms;
-    const T* C0 = SC + t * ms;
-    const T* D0 = SD + t * ms;
-    for (int i = 0; i < m; ++i) {
-      amax = max(amax, max(mag(A0[i]), max(mag(B0[i]), mag(C0[i]))));
-      dmax = max(dmax, mag(D0[i]));
-    }
-    atomicMax(c_amax, amax);
-    atomicMax(c_dmax, dmax);
-  }
+  MagT amax = 0, dmax = 0;
 
   const int mi = m - 1;
   T* A = SA + t * ms;
@@ -811,8 +804,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     bool bad = false;
     unsigned long long swaps = 0ull;
     T cb = B[0], cc = mi > 1 ? C[0] : T(0), cy = D[0], cv = A[0], cw = mi == 1 ? C[0] : T(0);
+    amax = max(amax, max(magh(cv), max(magh(cb), magh(C[0]))));  // magnitudes for the acceptance test
+    dmax = max(dmax, magh(cy));
     T w_prev = T(0);
     T om1 = T(0), om2 = T(0);
+    T kro = T(1);
     T pu1 = T(0), pu2a = T(0), pu2b = T(0);
     T Y0 = T(0), V0 = T(0);
     // software-pipelined: row i+2 (at most the separator row, which always
@@ -820,6 +816,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     T pa = A[1], pb = B[1], pc = C[1], py = D[1];
     for (int i = 0; i + 1 < mi; ++i) {
       const T na = pa, nb = pb, cn = pc, ny = py;
+      amax = max(amax, max(magh(na), max(magh(nb), magh(cn))));
+      dmax = max(dmax, magh(ny));
       pa = A[i + 2];
       pb = B[i + 2];
       pc = C[i + 2];
@@ -835,7 +833,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       const T u2 = sw ? nc : T(0);
       const T uy = sw ? ny : cy;
       const T uv = sw ? T(0) : cv;
-      const T om = fma(-om2, pu2b, fma(-om1, pu1, i == 0 ? T(1) : T(0))) * inv;
+      const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv;
+      kro = T(0);
       Y0 = fma(om, uy, Y0);
       V0 = fma(om, uv, V0);
       om2 = om1;
@@ -860,7 +859,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     bad |= is_zero(cb);
     const T inv_last = Div<T>(cb).inv();
     {
-      const T om = fma(-om2, pu2b, fma(-om1, pu1, mi == 1 ? T(1) : T(0))) * inv_last;
+      const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv_last;
       Y0 = fma(om, cy, Y0);
       V0 = fma(om, cv, V0);
       FST[t] = Y0;
@@ -876,6 +875,12 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
 
     // ---- separator row of partition P, into CTA 0's gather buffer
     const T as = A[mi], bs = B[mi], cs = C[mi], ds = D[mi];
+    amax = max(amax, max(magh(as), max(magh(bs), magh(cs))));
+    dmax = max(dmax, magh(ds));
+    if (pass == 0) {
+      atomicMax(c_amax, amax);
+      atomicMax(c_dmax, dmax);
+    }
     {
       T Yf = T(0), Vf = T(0), Wf = T(0);
       if (t + 1 < NT) {
@@ -930,13 +935,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     // ---- back substitution with the separators in place (as pge_kernel)
     const T sp = P > 0 ? SOL0[P - 1] : T(0);
     const T st = SOL0[P];
-    MagT xmax = mag(st);
+    MagT xmax = magh(st);
     T x_last;
     {
       T x1 = (fma(-cw, st, fma(-V[mi - 1], sp, D[mi - 1]))) * inv_last;
       T x2 = T(0);
       D[mi - 1] = x1;
-      xmax = max(xmax, mag(x1));
+      xmax = max(xmax, magh(x1));
       bad |= !finite_val(x1);
       x_last = x1;
       // software-pipelined: row i-1's factors are loaded while row i is solved
@@ -955,7 +960,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
         if (i == mi - 2) r = fma(-w_prev, st, r);
         const T xi = fma(-u2, x2, fma(-bi, x1, r)) * ai;
         D[i] = xi;
-        xmax = max(xmax, mag(xi));
+        xmax = max(xmax, magh(xi));
         bad |= !finite_val(xi);
         x2 = x1;
         x1 = xi;

@@ -59,8 +59,9 @@ void BPLG_PCR(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt,
  * 17-884).  One kernel family serves all four variants of each precision:
  * systems that fit one warp (n <= 1024 FP32, 512 FP64) run the on-chip
  * version without pivoting, as the reference does; longer systems run the
- * partitioned solve with partial pivoting inside each partition (one CTA per
- * system, up to 8960 rows FP32 / 4480 FP64), beyond that the Thomas sweep. */
+ * partitioned solve with partial pivoting inside each partition (one CTA,
+ * or a cluster of up to 8 CTAs, per system: up to 65536 rows FP32 / 27648
+ * FP64), beyond that the Thomas sweep. */
 void WM5_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 void WM4_shmem_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
 void WM5_reg_single(float *a_gbl, float *b_gbl, float *c_gbl, float *d_gbl, int n_eqt, int n_batch);
@@ -132,7 +133,7 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 #define TRIDIAG_ALGO_CR 2     /* CR-PCR hybrid, one warp per system */
 #define TRIDIAG_ALGO_PCR 3    /* PCR-pThomas, one warp per system */
 #define TRIDIAG_ALGO_WM 4     /* WM-pGE, one warp per system, unpivoted */
-#define TRIDIAG_ALGO_GTSV 5   /* partial pivoting: PGE for n >= 1024 where it fits, else one thread per system */
+#define TRIDIAG_ALGO_GTSV 5   /* partial pivoting: PGE for n >= 512 where it fits, else one thread per system */
 #define TRIDIAG_ALGO_PGE 6    /* WM-pGE with partial pivoting inside partitions, one CTA per system */
 
 /* Status of the last library call made by the calling host thread. */
@@ -219,17 +220,18 @@ int tridiag_refine_double(int layout, const double *a, const double *b, const do
  * in[k], back[k] = (double)out[k].  For tests of that conversion. */
 int tridiag_convert_check(const double *in, float *out, double *back, size_t count, void *stream);
 
-/* WM-pGE with partial pivoting inside each partition, one CTA per system
- * staged in shared memory (contiguous or packed layout; n from 65 up to
- * 8960 rows FP32, 4480 FP64, else TRIDIAG_ERR_NOT_SUPPORTED).  The NT
- * threads of a CTA each eliminate one partition (three right-hand sides);
+/* WM-pGE with partial pivoting inside each partition, the system staged in
+ * shared memory of one CTA (n up to 8960 FP32 / 4736 FP64) or of a cluster
+ * of 2, 4 or 8 CTAs (n up to 65536 FP32 / 27648 FP64); contiguous or packed
+ * layout, n >= 65, else TRIDIAG_ERR_NOT_SUPPORTED.  The NT threads of a CTA
+ * each eliminate one partition (three right-hand sides);
  * the separator system is solved by PCR, or with partial pivoting when
  * PCR's result fails a backward-error check; results whose separator rows
  * miss the residual bound and then an exact backward-error check are
  * refined in the kernel (FP64 residual, up to two correction passes) and,
  * if that does not reach the bound, recomputed by a sequential
- * partial-pivoting solve.  a, b, c, d are read
- * only (x may alias d); info (may be NULL) as tridiag_gtsv_*. */
+ * partial-pivoting solve (clusters: info = n + 1 instead).  a, b, c, d are
+ * read only (x may alias d); info (may be NULL) as tridiag_gtsv_*. */
 int tridiag_pge_single(int layout, const float *a, const float *b, const float *c, const float *d, float *x,
                        int *info, int n_eqt, int n_batch, void *stream);
 int tridiag_pge_double(int layout, const double *a, const double *b, const double *c, const double *d, double *x,

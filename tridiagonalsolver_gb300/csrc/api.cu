@@ -29,8 +29,9 @@ bool valid_layout(int layout) {
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 // Below this size the thread-per-system sweeps beat the partitioned solve
-// (measured on GB300 at batch 2^25 / n, FP32 and FP64).
-constexpr int PGE_MIN_N = 1024;
+// (measured on GB300 at batch 2^24 / n: the partitioned solve is faster
+// from n = 512 in both precisions, the two-ended sweep below).
+constexpr int PGE_MIN_N = 512;
 
 // Expand the four array pointers of a packed (layout 1) base pointer.
 template <typename T>

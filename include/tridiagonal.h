@@ -285,6 +285,58 @@ int tridiag_ragged_adjoint_double(const tridiag_ragged_plan *plan, const double 
                                   const double *c, const double *x, const double *xbar, double *ga, double *gb,
                                   double *gc, double *gd, int *info, const long long *offsets, void *stream);
 
+/* Layout conversion (no counterpart in the reference): copies a, b, c, d of
+ * n_batch systems from from_layout to to_layout (TRIDIAG_LAYOUT_*) in one
+ * pass over memory, coalesced on both sides (32 x 32 tiles through shared
+ * memory).  For the packed layout only the first pointer of the side is used
+ * (the others may be NULL).  Source and destination must not overlap.  Lets
+ * callers of the reference's layout-0 entry points reach the kernels that
+ * prefer another layout (e.g. the interleaved Thomas sweep) and back. */
+int tridiag_relayout_single(int from_layout, int to_layout, const float *a, const float *b, const float *c,
+                            const float *d, float *a2, float *b2, float *c2, float *d2, int n_eqt, int n_batch,
+                            void *stream);
+int tridiag_relayout_double(int from_layout, int to_layout, const double *a, const double *b, const double *c,
+                            const double *d, double *a2, double *b2, double *c2, double *d2, int n_eqt,
+                            int n_batch, void *stream);
+
+/* cuSPARSE-shaped entry points (no counterpart in the reference's own code:
+ * the argument lists of cusparse?gtsv2StridedBatch / ?gtsvInterleavedBatch,
+ * the library behind the reference's vendor row, Tridiagonal_CUDA/
+ * tridiagonal_basic.cu:207-246), served by this library's kernels; no
+ * handle.  Query the buffer size first; pBuffer may be NULL when it is 0.
+ *   ?gtsv2StridedBatch: dl, d, du read only (dl[0] and du[m-1] ignored), x
+ *   holds the right-hand side on entry and the solution on exit, system j at
+ *   j*batchStride.  batchStride == m: WM-pGE (on chip for short systems, the
+ *   partitioned pivoted solve for longer ones, the Thomas sweep beyond);
+ *   batchStride > m: the partitioned solve (65 <= m <= its limits, else
+ *   TRIDIAG_ERR_NOT_SUPPORTED).
+ *   ?gtsvInterleavedBatch: interleaved layout (row i of system j at
+ *   i*batchCount + j); algo 0 or 1 -> partial pivoting (tridiag_gtsv_*),
+ *   algo 2 -> Thomas without pivoting, which overwrites du. */
+size_t tridiag_gtsv2StridedBatch_bufferSize(int precision, int m, int batchCount, int batchStride);
+int tridiag_Sgtsv2StridedBatch(int m, const float *dl, const float *d, const float *du, float *x, int batchCount,
+                               int batchStride, void *pBuffer, void *stream);
+int tridiag_Dgtsv2StridedBatch(int m, const double *dl, const double *d, const double *du, double *x, int batchCount,
+                               int batchStride, void *pBuffer, void *stream);
+size_t tridiag_gtsvInterleavedBatch_bufferSize(int precision, int algo, int m, int batchCount);
+int tridiag_SgtsvInterleavedBatch(int algo, int m, float *dl, float *d, float *du, float *x, int batchCount,
+                                  void *pBuffer, void *stream);
+int tridiag_DgtsvInterleavedBatch(int algo, int m, double *dl, double *d, double *du, double *x, int batchCount,
+                                  void *pBuffer, void *stream);
+
+/* Periodic (cyclic) systems (no counterpart in the reference): row 0 also
+ * couples x_{n-1} with coefficient a_0 and row n-1 couples x_0 with c_{n-1}.
+ * Contiguous layout, n >= 3.  Sherman-Morrison over two tridiagonal solves
+ * with `algo` (TRIDIAG_ALGO_GTSV / AUTO: partial pivoting; TRIDIAG_ALGO_WM or
+ * TRIDIAG_ALGO_THOMAS: without pivoting, for diagonally dominant systems).
+ * a, b, c, d read only; x receives the solution (must not alias a, b, c);
+ * work: tridiag_periodic_workspace_size() bytes. */
+size_t tridiag_periodic_workspace_size(int precision, int algo, int n_eqt, int n_batch);
+int tridiag_periodic_single(int algo, const float *a, const float *b, const float *c, const float *d, float *x,
+                            void *work, size_t work_bytes, int n_eqt, int n_batch, void *stream);
+int tridiag_periodic_double(int algo, const double *a, const double *b, const double *c, const double *d, double *x,
+                            void *work, size_t work_bytes, int n_eqt, int n_batch, void *stream);
+
 /* Diagnostics: how many systems the partitioned partial-pivoting solve (used
  * by tridiag_gtsv_* without a pivot record, tridiag_solve_out_* with
  * TRIDIAG_ALGO_GTSV and the WM entry points on long systems) handed to its

@@ -57,6 +57,17 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_partition_fallbacks": (ctypes.c_longlong, [_I]),
     "tridiag_pge_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_pge_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_relayout_single": (_I, [_I, _I] + [_P] * 8 + [_I, _I, _P]),
+    "tridiag_relayout_double": (_I, [_I, _I] + [_P] * 8 + [_I, _I, _P]),
+    "tridiag_gtsv2StridedBatch_bufferSize": (_SZ, [_I, _I, _I, _I]),
+    "tridiag_Sgtsv2StridedBatch": (_I, [_I, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "tridiag_Dgtsv2StridedBatch": (_I, [_I, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "tridiag_gtsvInterleavedBatch_bufferSize": (_SZ, [_I, _I, _I, _I]),
+    "tridiag_SgtsvInterleavedBatch": (_I, [_I, _I, _P, _P, _P, _P, _I, _P, _P]),
+    "tridiag_DgtsvInterleavedBatch": (_I, [_I, _I, _P, _P, _P, _P, _I, _P, _P]),
+    "tridiag_periodic_workspace_size": (_SZ, [_I, _I, _I, _I]),
+    "tridiag_periodic_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_periodic_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_ragged_plan_create": (_I, [_P, _I, _P, _I, _P, _I]),
     "tridiag_ragged_plan_destroy": (None, [_P]),
     "tridiag_ragged_plan_buckets": (_I, [_P, _P, _I]),

@@ -554,3 +554,132 @@ extern "C" int tridiag_pge_adjoint_double(int layout, const double* a, const dou
   return set_status(pge_adjoint_entry<double>(layout, a, b, c, x, xbar, ga, gb, gc, gd, info, n, batch,
                                               (cudaStream_t)stream));
 }
+
+// ---------------------------------------------------------------------------
+// cuSPARSE-shaped entry points: the argument lists of cusparse?gtsv2StridedBatch
+// and cusparse?gtsvInterleavedBatch (the reference's vendor row,
+// Tridiagonal_CUDA/tridiagonal_basic.cu:207-246), served by this library's
+// kernels, so code written against those calls switches by renaming them.
+namespace {
+
+template <typename T>
+size_t gtsv2_strided_ws(int m, int batch, int stride) {
+  if (m <= 0 || batch <= 0 || stride < m) return 0;
+  return stride == m ? solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, m, batch) : 0;
+}
+
+template <typename T>
+int gtsv2_strided_impl(int m, const T* dl, const T* d, const T* du, T* x, int batch, int stride, void* buf,
+                       cudaStream_t s) {
+  if (m <= 0 || batch <= 0 || stride < m || !dl || !d || !du || !x) return TRIDIAG_ERR_INVALID_VALUE;
+  if (stride == m)
+    return solve_out_impl<T>(TRIDIAG_ALGO_WM, TRIDIAG_LAYOUT_CONTIGUOUS, dl, d, du, x, x, buf,
+                             gtsv2_strided_ws<T>(m, batch, stride), m, batch, s);
+  bool used = false;
+  cudaError_t e = tdg::launch_pge_strided<T>(dl, d, du, x, x, nullptr, m, batch, (size_t)stride, s, &used);
+  if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_NOT_SUPPORTED;
+}
+
+template <typename T>
+size_t gtsv_interleaved_ws(int algo, int m, int batch) {
+  if (m <= 0 || batch <= 0) return 0;
+  return algo == 2 ? 0 : gtsv_ws_bytes<T>(m, batch);
+}
+
+template <typename T>
+int gtsv_interleaved_impl(int algo, int m, T* dl, T* d, T* du, T* x, int batch, void* buf, cudaStream_t s) {
+  if (m <= 0 || batch <= 0 || !dl || !d || !du || !x || algo < 0 || algo > 2) return TRIDIAG_ERR_INVALID_VALUE;
+  if (algo == 2) return solve_impl<T>(TRIDIAG_ALGO_THOMAS, TRIDIAG_LAYOUT_INTERLEAVED, dl, d, du, x, m, batch, s);
+  return gtsv_impl<T>(TRIDIAG_LAYOUT_INTERLEAVED, dl, d, du, x, nullptr, nullptr, buf,
+                      gtsv_interleaved_ws<T>(algo, m, batch), m, batch, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t tridiag_gtsv2StridedBatch_bufferSize(int precision, int m, int batchCount, int batchStride) {
+  return precision ? gtsv2_strided_ws<double>(m, batchCount, batchStride)
+                   : gtsv2_strided_ws<float>(m, batchCount, batchStride);
+}
+int tridiag_Sgtsv2StridedBatch(int m, const float* dl, const float* d, const float* du, float* x, int batchCount,
+                               int batchStride, void* pBuffer, void* stream) {
+  return set_status(gtsv2_strided_impl<float>(m, dl, d, du, x, batchCount, batchStride, pBuffer, (cudaStream_t)stream));
+}
+int tridiag_Dgtsv2StridedBatch(int m, const double* dl, const double* d, const double* du, double* x, int batchCount,
+                               int batchStride, void* pBuffer, void* stream) {
+  return set_status(
+      gtsv2_strided_impl<double>(m, dl, d, du, x, batchCount, batchStride, pBuffer, (cudaStream_t)stream));
+}
+size_t tridiag_gtsvInterleavedBatch_bufferSize(int precision, int algo, int m, int batchCount) {
+  return precision ? gtsv_interleaved_ws<double>(algo, m, batchCount) : gtsv_interleaved_ws<float>(algo, m, batchCount);
+}
+int tridiag_SgtsvInterleavedBatch(int algo, int m, float* dl, float* d, float* du, float* x, int batchCount,
+                                  void* pBuffer, void* stream) {
+  return set_status(gtsv_interleaved_impl<float>(algo, m, dl, d, du, x, batchCount, pBuffer, (cudaStream_t)stream));
+}
+int tridiag_DgtsvInterleavedBatch(int algo, int m, double* dl, double* d, double* du, double* x, int batchCount,
+                                  void* pBuffer, void* stream) {
+  return set_status(gtsv_interleaved_impl<double>(algo, m, dl, d, du, x, batchCount, pBuffer, (cudaStream_t)stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Periodic systems (Sherman-Morrison over two tridiagonal solves; see
+// periodic.cu).
+namespace {
+
+template <typename T>
+size_t periodic_solver_ws(int algo, int n, int batch) {
+  const size_t w = solve_out_ws<T>(algo == TRIDIAG_ALGO_GTSV ? TRIDIAG_ALGO_GTSV : TRIDIAG_ALGO_THOMAS, n, batch);
+  return w;
+}
+
+template <typename T>
+size_t periodic_ws(int algo, int n, int batch) {
+  if (n < 3 || batch <= 0) return 0;
+  return 3 * align_up((size_t)n * (size_t)batch * sizeof(T)) + periodic_solver_ws<T>(algo, n, batch);
+}
+
+template <typename T>
+int periodic_impl(int algo, const T* a, const T* b, const T* c, const T* d, T* x, void* work, size_t work_bytes, int n,
+                  int batch, cudaStream_t s) {
+  if (n < 3 || batch <= 0 || !a || !b || !c || !d || !x) return TRIDIAG_ERR_INVALID_VALUE;
+  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_GTSV;
+  if (algo != TRIDIAG_ALGO_GTSV && algo != TRIDIAG_ALGO_WM && algo != TRIDIAG_ALGO_THOMAS) return TRIDIAG_ERR_NOT_SUPPORTED;
+  if (!work || work_bytes < periodic_ws<T>(algo, n, batch)) return TRIDIAG_ERR_WORKSPACE;
+  const size_t one = align_up((size_t)n * (size_t)batch * sizeof(T));
+  char* p = static_cast<char*>(work);
+  T* bp = reinterpret_cast<T*>(p);
+  T* u = reinterpret_cast<T*>(p + one);
+  T* y = reinterpret_cast<T*>(p + 2 * one);
+  void* sw = p + 3 * one;
+  const size_t sw_bytes = periodic_solver_ws<T>(algo, n, batch);
+  if (tdg::launch_periodic_prep<T>(a, b, c, bp, u, n, batch, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  int st = solve_out_impl<T>(algo, TRIDIAG_LAYOUT_CONTIGUOUS, a, bp, c, d, y, sw, sw_bytes, n, batch, s);
+  if (st != TRIDIAG_SUCCESS) return st;
+  st = solve_out_impl<T>(algo, TRIDIAG_LAYOUT_CONTIGUOUS, a, bp, c, u, u, sw, sw_bytes, n, batch, s);
+  if (st != TRIDIAG_SUCCESS) return st;
+  return cuda_status(tdg::launch_periodic_combine<T>(a, b, y, u, x, n, batch, s));
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t tridiag_periodic_workspace_size(int precision, int algo, int n, int batch) {
+  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_GTSV;
+  return precision ? periodic_ws<double>(algo, n, batch) : periodic_ws<float>(algo, n, batch);
+}
+int tridiag_periodic_single(int algo, const float* a, const float* b, const float* c, const float* d, float* x,
+                            void* work, size_t work_bytes, int n, int batch, void* stream) {
+  return set_status(periodic_impl<float>(algo, a, b, c, d, x, work, work_bytes, n, batch, (cudaStream_t)stream));
+}
+int tridiag_periodic_double(int algo, const double* a, const double* b, const double* c, const double* d, double* x,
+                            void* work, size_t work_bytes, int n, int batch, void* stream) {
+  return set_status(periodic_impl<double>(algo, a, b, c, d, x, work, work_bytes, n, batch, (cudaStream_t)stream));
+}
+
+}  // extern "C"

@@ -72,6 +72,11 @@ template <typename T>
 cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
                        cudaStream_t s, bool* used);
 
+// The partitioned solve on contiguous systems `stride` elements apart
+// (stride >= n; system j at j*stride).
+template <typename T>
+cudaError_t launch_pge_strided(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                               size_t stride, cudaStream_t s, bool* used);
 // Adjoint with the partitioned solve: lambda = A^{-T} xbar (written to gd)
 // and ga = -lambda x_{i-1}, gb = -lambda x_i, gc = -lambda x_{i+1}, xf being
 // the forward solution.  No pivot record needed.
@@ -98,6 +103,19 @@ template <typename T>
 cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, const T* c, const T* d, T* x,
                               const T* xf, T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
                               int count, int m_max, cudaStream_t s);
+
+// periodic.cu: Sherman-Morrison pieces of the periodic solve (contiguous).
+template <typename T>
+cudaError_t launch_periodic_prep(const T* a, const T* b, const T* c, T* bp, T* u, int n, int batch, cudaStream_t s);
+template <typename T>
+cudaError_t launch_periodic_combine(const T* a, const T* b, const T* y, const T* z, T* x, int n, int batch,
+                                    cudaStream_t s);
+
+// layout.cu: a, b, c, d from one layout to another in one pass (packed:
+// only src[0] / dst[0] is used).
+template <typename T>
+cudaError_t launch_relayout(int from, int to, const T* const src[4], T* const dst[4], int n, int batch,
+                            cudaStream_t s);
 
 // Number of systems the partitioned solve handed to its sequential fallback
 // (synchronous read; optionally reset).

@@ -1213,6 +1213,19 @@ cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* 
 }
 
 template <typename T>
+cudaError_t launch_pge_strided(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                               size_t stride, cudaStream_t s, bool* used) {
+  *used = false;
+  if (!pge_eligible<T>(CONTIG, n) || stride < (size_t)n) return cudaSuccess;
+  const int v = pge_default_variant<T>(n);
+  *used = true;
+  PgeIO<T> io = uniform_io<T>(CONTIG, a, b, c, d, x, info, n);
+  io.stride = stride;
+  const int m = (n + pge_variant_partitions(v) - 1) / pge_variant_partitions(v);
+  return pge_launch_variant<T, 0>(v, io, batch, m, s);
+}
+
+template <typename T>
 cudaError_t launch_pge_adjoint(int layout, const T* a, const T* b, const T* c, const T* xf, const T* xbar, T* ga,
                                T* gb, T* gc, T* gd, int* info, int n, int batch, cudaStream_t s, bool* used) {
   *used = false;
@@ -1272,6 +1285,8 @@ cudaError_t pge_fallback_count(unsigned long long* out, bool reset) {
   template int pge_variant_mmax<T>(int);                                                                          \
   template cudaError_t launch_pge<T>(int, const T*, const T*, const T*, const T*, T*, int*, int, int, cudaStream_t, \
                                      bool*);                                                                      \
+  template cudaError_t launch_pge_strided<T>(const T*, const T*, const T*, const T*, T*, int*, int, int, size_t,  \
+                                             cudaStream_t, bool*);                                                \
   template cudaError_t launch_pge_adjoint<T>(int, const T*, const T*, const T*, const T*, const T*, T*, T*, T*, T*, \
                                              int*, int, int, cudaStream_t, bool*);                                \
   template cudaError_t launch_pge_ragged<T>(int, int, const T*, const T*, const T*, const T*, T*, const T*, T*, T*, \

@@ -170,6 +170,44 @@ def pge_adjoint(a, b, c, x, xbar, n: int, layout: str = "contiguous", info=None,
     return ga, gb, gc, gd
 
 
+def periodic(a, b, c, d, n: int, algo: str = "gtsv", out=None, work=None, stream=None):
+    """Periodic (cyclic) systems: a_0 couples x_{n-1}, c_{n-1} couples x_0.
+    Contiguous layout; returns x."""
+    p = _prec(a)
+    batch = _dims(a, n, "contiguous")
+    a, b, c, d = _al(a), _al(b), _al(c), _al(d)
+    x = out if out is not None else torch.empty_like(d)
+    if work is None:
+        nbytes = lib().tridiag_periodic_workspace_size(1 if a.dtype == torch.float64 else 0, ALGOS[algo], n, batch)
+        work = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=a.device)
+    st = getattr(lib(), f"tridiag_periodic_{p}")(ALGOS[algo], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype),
+                                                 _ptr(d, a.dtype), _ptr(x, a.dtype), _ptr(work), work.numel(), n,
+                                                 batch, _stream_ptr(stream))
+    check(st, f"tridiag_periodic_{p}")
+    return x
+
+
+def relayout(arrays, n: int, from_layout: str, to_layout: str, out=None, stream=None):
+    """a, b, c, d (or one packed tensor) from one layout to another; returns
+    the four destination tensors (or one packed tensor)."""
+    src = list(arrays) if isinstance(arrays, (list, tuple)) else [arrays]
+    t0 = src[0]
+    p = _prec(t0)
+    batch = _dims(t0, n, from_layout)
+    if out is None:
+        if to_layout == "packed":
+            out = [torch.empty(batch * 4 * n, dtype=t0.dtype, device=t0.device)]
+        else:
+            out = [torch.empty(batch * n, dtype=t0.dtype, device=t0.device) for _ in range(4)]
+    dst = list(out) if isinstance(out, (list, tuple)) else [out]
+    sp = [_ptr(src[k]) if k < len(src) else None for k in range(4)]
+    dp = [_ptr(dst[k]) if k < len(dst) else None for k in range(4)]
+    st = getattr(lib(), f"tridiag_relayout_{p}")(LAYOUTS[from_layout], LAYOUTS[to_layout], *sp, *dp, n, batch,
+                                                 _stream_ptr(stream))
+    check(st, f"tridiag_relayout_{p}")
+    return dst if len(dst) > 1 else dst[0]
+
+
 def refine_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
     batch = _dims(a, n, layout)
     return torch.empty(lib().tridiag_refine_workspace_size(LAYOUTS[layout], n, batch), dtype=torch.uint8,

@@ -337,6 +337,24 @@ int tridiag_periodic_single(int algo, const float *a, const float *b, const floa
 int tridiag_periodic_double(int algo, const double *a, const double *b, const double *c, const double *d, double *x,
                             void *work, size_t work_bytes, int n_eqt, int n_batch, void *stream);
 
+/* Factor once, solve many right-hand sides (no counterpart in the
+ * reference; the algorithm of LAPACK ?gttrf / ?gttrs, one thread per
+ * system).  tridiag_factor_* factors the n_batch systems (any layout; a, b,
+ * c read only) into `factors` (tridiag_factor_size() bytes of device
+ * memory, the caller's); info (may be NULL) per system as tridiag_gtsv_*.
+ * tridiag_factored_solve_* then solves A x = r (transpose = 0) or
+ * A^T x = r (transpose = 1) for nrhs right-hand sides held in x (block k at
+ * k*n*batch elements, contiguous or interleaved layout), in place. */
+size_t tridiag_factor_size(int precision, int n_eqt, int n_batch);
+int tridiag_factor_single(int layout, const float *a, const float *b, const float *c, void *factors,
+                          size_t factor_bytes, int *info, int n_eqt, int n_batch, void *stream);
+int tridiag_factor_double(int layout, const double *a, const double *b, const double *c, void *factors,
+                          size_t factor_bytes, int *info, int n_eqt, int n_batch, void *stream);
+int tridiag_factored_solve_single(int layout, int transpose, const void *factors, size_t factor_bytes, float *x,
+                                  int nrhs, int n_eqt, int n_batch, void *stream);
+int tridiag_factored_solve_double(int layout, int transpose, const void *factors, size_t factor_bytes, double *x,
+                                  int nrhs, int n_eqt, int n_batch, void *stream);
+
 /* Diagnostics: how many systems the partitioned partial-pivoting solve (used
  * by tridiag_gtsv_* without a pivot record, tridiag_solve_out_* with
  * TRIDIAG_ALGO_GTSV and the WM entry points on long systems) handed to its

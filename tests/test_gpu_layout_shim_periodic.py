@@ -137,3 +137,44 @@ def test_periodic(cuda, dt, algo, n, batch):
             r = A @ x[j] - d_[j]
             scale = np.max(np.sum(np.abs(A), axis=1)) * np.max(np.abs(x[j])) + np.max(np.abs(d_[j]))
         assert np.max(np.abs(r)) / scale <= (1e-12 if dt == np.float64 else 1e-5), (j, algo)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("layout", ["contiguous", "interleaved"])
+@pytest.mark.parametrize("n,batch", [(1, 3), (2, 5), (9, 33), (300, 70), (4096, 16)])
+def test_factor_and_solve_many(cuda, dt, layout, n, batch):
+    """Factor once, then three right-hand sides and the transposed system."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    a, b, c, _ = inputs.nondominant(n, batch, seed=7 * n + batch)
+    rng = np.random.default_rng(n)
+    rhs = [rng.uniform(-1, 1, (batch, n)) for _ in range(3)]
+
+    def dev(v):
+        v = v.astype(dt)
+        return torch.from_numpy(np.ascontiguousarray(v.T if layout == "interleaved" else v).reshape(-1)).cuda()
+
+    def host(t):
+        v = t.double().cpu().numpy()
+        return v.reshape(n, batch).T if layout == "interleaved" else v.reshape(batch, n)
+
+    info = torch.full((batch,), -1, dtype=torch.int32, device="cuda")
+    F = T.Factorization(dev(a), dev(b), dev(c), n, layout=layout, info=info)
+    r = torch.cat([dev(v) for v in rhs])
+    F.solve(r)
+    rt = dev(rhs[0])
+    F.solve(rt, transpose=True)
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0
+    a_, b_, c_ = (v.astype(dt).astype(np.float64) for v in (a, b, c))
+    blk = n * batch
+    for k in range(3):
+        x = host(r[k * blk:(k + 1) * blk])
+        _, worst = O.backward_error(a_, b_, c_, rhs[k].astype(dt).astype(np.float64), x, n)
+        assert worst <= ETA[dt]
+    # A^T z = r0: the oracle's adjoint gives lambda = A^{-T} xbar (any x)
+    lam = O.adjoint_f64(a_, b_, c_, np.zeros((batch, n)), rhs[0].astype(dt).astype(np.float64), n)[3].reshape(batch, n)
+    z = host(rt)
+    rel = np.max(np.abs(z - lam), axis=1) / np.maximum(np.max(np.abs(lam), axis=1), 1e-300)
+    assert np.median(rel) <= (1e-10 if dt == np.float64 else 1e-3)

@@ -68,6 +68,11 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_periodic_workspace_size": (_SZ, [_I, _I, _I, _I]),
     "tridiag_periodic_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_periodic_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_factor_size": (_SZ, [_I, _I, _I]),
+    "tridiag_factor_single": (_I, [_I, _P, _P, _P, _P, _SZ, _P, _I, _I, _P]),
+    "tridiag_factor_double": (_I, [_I, _P, _P, _P, _P, _SZ, _P, _I, _I, _P]),
+    "tridiag_factored_solve_single": (_I, [_I, _I, _P, _SZ, _P, _I, _I, _I, _P]),
+    "tridiag_factored_solve_double": (_I, [_I, _I, _P, _SZ, _P, _I, _I, _I, _P]),
     "tridiag_ragged_plan_create": (_I, [_P, _I, _P, _I, _P, _I]),
     "tridiag_ragged_plan_destroy": (None, [_P]),
     "tridiag_ragged_plan_buckets": (_I, [_P, _P, _I]),

@@ -170,6 +170,36 @@ def pge_adjoint(a, b, c, x, xbar, n: int, layout: str = "contiguous", info=None,
     return ga, gb, gc, gd
 
 
+class Factorization:
+    """Partial-pivoting factors of a batch (LAPACK ?gttrf algorithm); solve
+    any number of right-hand sides, transposed or not, with :meth:`solve`."""
+
+    def __init__(self, a, b, c, n: int, layout: str = "contiguous", info=None, stream=None):
+        p = _prec(a)
+        self.n, self.layout, self.dtype = n, layout, a.dtype
+        self.batch = _dims(a, n, layout)
+        a, b, c = _al(a), _al(b), _al(c)
+        nbytes = lib().tridiag_factor_size(1 if a.dtype == torch.float64 else 0, n, self.batch)
+        self.factors = torch.empty(nbytes, dtype=torch.uint8, device=a.device)
+        st = getattr(lib(), f"tridiag_factor_{p}")(LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype),
+                                                   _ptr(c, a.dtype), _ptr(self.factors), nbytes, _ptr(info), n,
+                                                   self.batch, _stream_ptr(stream))
+        check(st, f"tridiag_factor_{p}")
+        self._p = p
+
+    def solve(self, r, transpose: bool = False, stream=None):
+        """Solve for r (nrhs blocks of n*batch elements, the factor's layout)
+        in place; returns r."""
+        nrhs = r.numel() // (self.n * self.batch)
+        if nrhs * self.n * self.batch != r.numel():
+            raise ValueError("r must hold whole right-hand sides")
+        st = getattr(lib(), f"tridiag_factored_solve_{self._p}")(
+            LAYOUTS[self.layout], int(transpose), _ptr(self.factors), self.factors.numel(), _ptr(r, self.dtype), nrhs,
+            self.n, self.batch, _stream_ptr(stream))
+        check(st, f"tridiag_factored_solve_{self._p}")
+        return r
+
+
 def periodic(a, b, c, d, n: int, algo: str = "gtsv", out=None, work=None, stream=None):
     """Periodic (cyclic) systems: a_0 couples x_{n-1}, c_{n-1} couples x_0.
     Contiguous layout; returns x."""

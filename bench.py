@@ -198,7 +198,9 @@ def run_ours(args):
         for item in data:
             solve_part(item, s)
 
-    # warm-up (also allocates the library's device error word, outside capture)
+    # warm-up (also allocates the library's device error word, outside capture); the
+    # inputs were made on the current stream, so the solve stream waits for them
+    stream.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(stream):
         for _ in range(max(args.warmup, 3)):
             step(stream)
@@ -469,7 +471,11 @@ def run_reference(args):
 
 def _graph_time(torch, stream, fn, steps, warmup):
     """Capture fn in a CUDA graph; time `steps` replays (CUDA events on the
-    launching stream, synchronised on both sides); return ms per replay."""
+    launching stream, synchronised on both sides); return ms per replay.  The
+    inputs were made on the current stream: `stream` waits for that work first
+    (otherwise buffers the caching allocator recycled from its temporaries
+    could be written while those temporaries are still being read)."""
+    stream.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(stream):
         for _ in range(max(warmup, 3)):
             fn()
@@ -822,8 +828,113 @@ def run_refined(args):
           note="algorithmic bytes counted as 5*n*8 (FP64 in/out), as for the plain FP64 solve")
 
 
+def run_block2(args):
+    """Block tridiagonal systems with 2 x 2 blocks, n = 512 block rows x 131072
+    systems, interleaved layout: the pivoted solve (FP64 and FP32, U[-1,1]
+    blocks) and block Thomas (FP64, block diagonally dominant).  The solve is
+    in place, so every step restores the inputs from a pristine copy outside
+    the timed region (as the reference's driver does) and the kernel alone is
+    timed with CUDA events on its stream."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+
+    T.lib()
+    n, batch = 512, 131072
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    parts, kernel_ms, eta_all = [], {}, {}
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.6)
+    sampler.mark("begin")
+    keep = None
+    for name, dt, algo in (("pivoted_fp64", torch.float64, "pivoted"), ("thomas_fp64", torch.float64, "thomas"),
+                           ("pivoted_fp32", torch.float32, "pivoted")):
+        g = torch.Generator(device=dev)
+        g.manual_seed(17)
+        src = [torch.rand(k * n * batch, dtype=dt, device=dev, generator=g) * 2 - 1 for k in (4, 4, 4, 2)]
+        if algo == "thomas":
+            bv = src[1].view(n, 4, batch)
+            rows = (src[0].view(n, 4, batch).abs() + src[2].view(n, 4, batch).abs() + bv.abs())
+            sgn = lambda t: torch.where(t >= 0, 1.0, -1.0).to(dt)
+            bv[:, 0] = sgn(bv[:, 0]) * (rows[:, 0] + rows[:, 1] + 1)
+            bv[:, 3] = sgn(bv[:, 3]) * (rows[:, 2] + rows[:, 3] + 1)
+        work = [t.clone() for t in src]
+        info = torch.zeros(batch, dtype=torch.int32, device=dev)
+        # inputs were built on the current stream (with temporaries the allocator may
+        # hand to `work`): the solve stream waits for that work before touching them
+        stream.wait_stream(torch.cuda.current_stream())
+        times = []
+        with torch.cuda.stream(stream):
+            for it in range(args.warmup + args.steps):
+                for w, s_ in zip(work, src):
+                    w.copy_(s_)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                T.block2(*work, n, algo=algo, layout="interleaved", info=info, stream=stream)
+                e1.record(stream)
+                stream.synchronize()
+                if it >= args.warmup:
+                    times.append(e0.elapsed_time(e1))
+        ms = sum(times) / len(times)
+        kernel_ms[name] = ms
+        # accuracy on 16 systems (FP64 residual against the inputs)
+        idx = torch.arange(0, batch, batch // 16, device=dev)
+        pick = lambda t, k: t.view(n * k, batch).index_select(1, idx).T.reshape(16, n, k).double().cpu().numpy()
+        x = pick(work[3], 2)
+        abc = [pick(t, 4).reshape(16, n, 2, 2) for t in src[:3]]
+        _, eta = O.block2_backward_error(*abc, pick(src[3], 2), x, n)
+        eta_all[name] = eta
+        es = 8 if dt == torch.float64 else 4
+        alg = 16 * n * batch * es
+        parts.append({"name": name, "dtype": str(dt).replace("torch.", ""), "algorithm": algo, "n": n,
+                      "batch": batch, "layout": "interleaved", "ms_per_launch": ms,
+                      "systems_per_s": batch / (ms * 1e-3), "block_rows_per_s": n * batch / (ms * 1e-3),
+                      "algorithmic_bytes": alg, "hbm_gbs": round(alg / (ms * 1e-3) / 1e9, 1),
+                      "backward_error_max": eta, "nonzero_info": int((info != 0).sum())})
+        if name == "pivoted_fp64":
+            keep = (src, work, info)
+        else:
+            del src, work
+        torch.cuda.empty_cache()
+    sampler.mark("end")
+    clocks = sampler.stop()
+    src, work, info = keep
+    for w, s_ in zip(work, src):
+        w.copy_(s_)
+    torch.cuda.synchronize()
+    e2e_step = lambda: T.block2(*work, n, algo="pivoted", layout="interleaved", info=info, stream=stream)
+    e2e = _e2e_generic(torch, stream, work, [work[3]], e2e_step, 3, batch)
+
+    def cpu(k):
+        rng = np.random.default_rng(3)
+        aa, bb, cc = (rng.uniform(-1, 1, (k, n, 2, 2)) for _ in range(3))
+        dd = rng.uniform(-1, 1, (k, n, 2))
+        t0 = time.perf_counter()
+        O.block2(aa, bb, cc, dd, n, "gbsv")
+        return time.perf_counter() - t0
+
+    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, batch, start=64)
+    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                      "sample": f"{k} of {batch} systems in {t:.2f} s (oracle ?gbsv restatement, FP64)"}
+    ms = kernel_ms["pivoted_fp64"]
+    # FP64 instructions per block row from ncu's counts (DFMA 43, DMUL 7, DADD 7;
+    # profiles/block2_fp64_n256.md)
+    ops_per_row, fp64_peak = 57.0, 503.0
+    gops = n * batch * ops_per_row / (ms * 1e-3) / 1e9
+    _line(args, "block tridiagonal (2 x 2 blocks) pivoted FP64, n=512 x 131072, interleaved", batch / (ms * 1e-3), ms,
+          "f64", {"n": n, "batch": batch, "layout": "interleaved",
+                  "dominant": "block2_pivoted_kernel<double, INTERLEAVED>",
+                  "l2": "inputs larger than L2 (3.8 GB FP64)", "timing": "kernel alone, inputs restored between steps"},
+          parts, 16 * n * batch * 8, ms, cpu_b, e2e, clocks, 3 * args.steps,
+          note=f"FP64 issue bound: {ops_per_row:.0f} FP64 instructions per block row -> {gops:.0f} Gop/s = "
+               f"{gops / fp64_peak:.0%} of the {fp64_peak:.0f} Gop/s DFMA microbenchmark rate")
+
+
 WORKLOADS = {"config2": None, "thomas-fp64": run_thomas_fp64, "adjoint": run_adjoint, "ragged": run_ragged,
-             "refined": run_refined}
+             "refined": run_refined, "block2": run_block2}
 
 
 def main():

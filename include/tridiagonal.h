@@ -355,6 +355,28 @@ int tridiag_factored_solve_single(int layout, int transpose, const void *factors
 int tridiag_factored_solve_double(int layout, int transpose, const void *factors, size_t factor_bytes, double *x,
                                   int nrhs, int n_eqt, int n_batch, void *stream);
 
+/* Block tridiagonal systems with 2 x 2 blocks (no counterpart in the
+ * reference):  A_i x_{i-1} + B_i x_i + C_i x_{i+1} = d_i for block rows
+ * i = 0..n_eqt-1 of each of n_batch systems, x_i and d_i in R^2, blocks
+ * row-major; A_0 and C_{n-1} are not read.  Layouts:
+ *   TRIDIAG_LAYOUT_CONTIGUOUS   block (i, j) at a[(j*n + i)*4 + k],
+ *                               right-hand side at d[(j*n + i)*2 + r];
+ *   TRIDIAG_LAYOUT_INTERLEAVED  a[(i*4 + k)*n_batch + j], d[(i*2 + r)*n_batch + j].
+ * algo TRIDIAG_BLOCK2_PIVOTED: partial pivoting over the scalar band of
+ * order 2n (the LAPACK ?gbsv algorithm); a, b, c are overwritten with the
+ * factors.  TRIDIAG_BLOCK2_THOMAS: block Thomas without pivoting (block
+ * diagonally dominant systems); a and b are kept, c is overwritten.  d
+ * receives x.  info (may be NULL) gets per system 0, or the first zero
+ * pivot (PIVOTED: scalar column, 1-based) / singular block (THOMAS: block
+ * row, 1-based).  One thread per system: batches of 20k systems or more
+ * fill the GPU. */
+#define TRIDIAG_BLOCK2_PIVOTED 0
+#define TRIDIAG_BLOCK2_THOMAS 1
+int tridiag_block2_single(int algo, int layout, float *a, float *b, float *c, float *d, int *info, int n_eqt,
+                          int n_batch, void *stream);
+int tridiag_block2_double(int algo, int layout, double *a, double *b, double *c, double *d, int *info, int n_eqt,
+                          int n_batch, void *stream);
+
 /* Diagnostics: how many systems the partitioned partial-pivoting solve (used
  * by tridiag_gtsv_* without a pivot record, tridiag_solve_out_* with
  * TRIDIAG_ALGO_GTSV and the WM entry points on long systems) handed to its

@@ -31,12 +31,14 @@ int orc_get_threads(void) {
 #define T float
 #define SFX f32
 #include "oracle_body.inc"
+#include "oracle_block2.inc"
 #undef T
 #undef SFX
 
 #define T double
 #define SFX f64
 #include "oracle_body.inc"
+#include "oracle_block2.inc"
 #undef T
 #undef SFX
 

@@ -67,6 +67,20 @@ int orc_wm_f64(double *a, double *b, double *c, double *d, int n, int batch, int
 int orc_gtsv_f32(float *a, float *b, float *c, float *d, int n, int batch);
 int orc_gtsv_f64(double *a, double *b, double *c, double *d, int n, int batch);
 
+/* Block tridiagonal systems with 2 x 2 blocks (no reference counterpart):
+ * A_i x_{i-1} + B_i x_i + C_i x_{i+1} = d_i, blocks row-major, block (i, j)
+ * at a[(j*n + i)*4], right-hand side at d[(j*n + i)*2].  gbsv = partial
+ * pivoting over the scalar band (the LAPACK ?gbsv algorithm, kl = ku = 3);
+ * thomas = block Thomas with 2 x 2 inverses, no pivoting.  x is returned in
+ * d; a, b, c are not modified; infos[j] (may be NULL) = 0 or the first
+ * zero-pivot scalar column (gbsv) / singular block row (thomas), 1-based.
+ * Returns the code of the first failing system, or 0. */
+int orc_block2_gbsv_f32(const float *a, const float *b, const float *c, float *d, int *infos, int n, int batch);
+int orc_block2_gbsv_f64(const double *a, const double *b, const double *c, double *d, int *infos, int n, int batch);
+int orc_block2_thomas_f32(const float *a, const float *b, const float *c, float *d, int *infos, int n, int batch);
+int orc_block2_thomas_f64(const double *a, const double *b, const double *c, double *d, int *infos, int n,
+                          int batch);
+
 /* Adjoint of x = A^{-1} d for L = sum(xbar * x) in FP64: lambda = A^{-T} xbar
  * from the pivoted LU of A, then grad_d = lambda, grad_a_i = -lambda_i x_{i-1},
  * grad_b_i = -lambda_i x_i, grad_c_i = -lambda_i x_{i+1}.  Inputs are not

@@ -30,6 +30,7 @@ _ref = None
 
 _F32P = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _F64P = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_I32P = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
 def build(force: bool = False) -> Path:
@@ -54,6 +55,10 @@ def lib():
             f = getattr(L, f"orc_gtsv_{t}")
             f.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int]
             f.restype = ctypes.c_int
+            for nm in ("gbsv", "thomas"):
+                f = getattr(L, f"orc_block2_{nm}_{t}")
+                f.argtypes = [P, P, P, P, _I32P, ctypes.c_int, ctypes.c_int]
+                f.restype = ctypes.c_int
         L.orc_adjoint_f64.argtypes = [_F64P] * 9 + [ctypes.c_int, ctypes.c_int]
         L.orc_adjoint_f64.restype = ctypes.c_int
         L.orc_residual_f64.argtypes = [_F64P] * 6 + [ctypes.c_int, ctypes.c_int]
@@ -123,6 +128,56 @@ def wm(a, b, c, d, n, rounds, half=0):
 def gtsv(a, b, c, d, n):
     """Partial-pivoting elimination (LAPACK ?gtsv algorithm); returns x."""
     return _call("gtsv", a, b, c, d, n)
+
+
+def block2(a, b, c, d, n, algo="gbsv"):
+    """Block tridiagonal solve with 2 x 2 blocks (a, b, c of shape
+    (batch, n, 2, 2) or flat, d of shape (batch, n, 2) or flat).  ``algo`` is
+    "gbsv" (partial pivoting, the LAPACK ?gbsv algorithm) or "thomas" (block
+    Thomas).  Returns (x flat, per-system info)."""
+    dt = np.result_type(a, b, c, d)
+    a_, b_, c_, d_ = (np.ascontiguousarray(np.array(v, dtype=dt, copy=True)).reshape(-1) for v in (a, b, c, d))
+    if n <= 0 or a_.size % (4 * n) or any(v.size != a_.size for v in (b_, c_)) or d_.size * 2 != a_.size:
+        raise ValueError("a, b, c need 4*n*batch values and d 2*n*batch")
+    batch = a_.size // (4 * n)
+    info = np.zeros(batch, dtype=np.int32)
+    getattr(lib(), f"orc_block2_{algo}_{_sfx(dt)}")(a_, b_, c_, d_, info, int(n), int(batch))
+    return d_, info
+
+
+def block2_dense(a, b, c, n):
+    """Dense matrices (batch, 2n, 2n) of block tridiagonal systems (FP64)."""
+    a, b, c = (np.asarray(v, dtype=np.float64).reshape(-1, n, 2, 2) for v in (a, b, c))
+    batch = a.shape[0]
+    M = np.zeros((batch, 2 * n, 2 * n))
+    for i in range(n):
+        M[:, 2 * i:2 * i + 2, 2 * i:2 * i + 2] = b[:, i]
+        if i > 0:
+            M[:, 2 * i:2 * i + 2, 2 * i - 2:2 * i] = a[:, i]
+        if i + 1 < n:
+            M[:, 2 * i:2 * i + 2, 2 * i + 2:2 * i + 4] = c[:, i]
+    return M
+
+
+def block2_backward_error(a, b, c, d, x, n):
+    """Per-system normwise backward error of block tridiagonal solves in FP64:
+    ||d - A x||_inf / (||A||_inf ||x||_inf + ||d||_inf); A_0 and C_{n-1} are
+    not part of the matrix."""
+    a, b, c = (np.array(v, dtype=np.float64).reshape(-1, n, 2, 2) for v in (a, b, c))
+    d, x = (np.asarray(v, dtype=np.float64).reshape(-1, n, 2) for v in (d, x))
+    a[:, 0] = 0
+    c[:, n - 1] = 0
+    xm = np.concatenate([np.zeros_like(x[:, :1]), x[:, :-1]], axis=1)
+    xp = np.concatenate([x[:, 1:], np.zeros_like(x[:, :1])], axis=1)
+    r = d - (np.einsum("bnij,bnj->bni", a, xm) + np.einsum("bnij,bnj->bni", b, x)
+             + np.einsum("bnij,bnj->bni", c, xp))
+    rown = np.abs(a).sum(axis=3) + np.abs(b).sum(axis=3) + np.abs(c).sum(axis=3)
+    nb = len(x)
+    den = rown.reshape(nb, -1).max(axis=1) * np.abs(x).reshape(nb, -1).max(axis=1) \
+        + np.abs(d).reshape(nb, -1).max(axis=1)
+    eta = np.abs(r).reshape(nb, -1).max(axis=1) / np.where(den > 0, den, 1.0)
+    eta = np.where(np.isfinite(x).reshape(nb, -1).all(axis=1), eta, np.inf)
+    return eta, float(eta.max()) if eta.size else 0.0
 
 
 def adjoint_f64(a, b, c, x, xbar, n):

@@ -97,11 +97,13 @@ def test_ragged_graph_capture(cuda):
     plan = T.RaggedPlan(off)
     x = torch.empty_like(d)
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # inputs were made on the current stream
     with torch.cuda.stream(s):
         plan.solve(a, b, c, d, out=x)
     s.synchronize()
     ref = x.clone()
     x.zero_()
+    s.wait_stream(torch.cuda.current_stream())
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g, stream=s):
         plan.solve(a, b, c, d, out=x)

@@ -73,6 +73,8 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_factor_double": (_I, [_I, _P, _P, _P, _P, _SZ, _P, _I, _I, _P]),
     "tridiag_factored_solve_single": (_I, [_I, _I, _P, _SZ, _P, _I, _I, _I, _P]),
     "tridiag_factored_solve_double": (_I, [_I, _I, _P, _SZ, _P, _I, _I, _I, _P]),
+    "tridiag_block2_single": (_I, [_I, _I, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_block2_double": (_I, [_I, _I, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_ragged_plan_create": (_I, [_P, _I, _P, _I, _P, _I]),
     "tridiag_ragged_plan_destroy": (None, [_P]),
     "tridiag_ragged_plan_buckets": (_I, [_P, _P, _I]),

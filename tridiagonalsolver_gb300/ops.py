@@ -200,6 +200,28 @@ class Factorization:
         return r
 
 
+BLOCK2_ALGOS = {"pivoted": 0, "thomas": 1}
+
+
+def block2(a, b, c, d, n: int, algo: str = "pivoted", layout: str = "contiguous", info=None, stream=None):
+    """Block tridiagonal systems with 2 x 2 blocks, in place: d receives x.
+    Contiguous layout: a, b, c hold (batch, n, 2, 2) blocks row-major and d
+    (batch, n, 2); interleaved: a[(i*4 + k)*batch + j], d[(i*2 + r)*batch + j].
+    "pivoted" (partial pivoting, the LAPACK ?gbsv algorithm) overwrites a, b,
+    c with the factors; "thomas" (block Thomas, no pivoting) overwrites c.
+    Returns d."""
+    p = _prec(a)
+    if n <= 0 or a.numel() % (4 * n) or d.numel() * 2 != a.numel() or b.numel() != a.numel() \
+            or c.numel() != a.numel():
+        raise ValueError("a, b, c need 4*n*batch elements and d 2*n*batch")
+    batch = a.numel() // (4 * n)
+    st = getattr(lib(), f"tridiag_block2_{p}")(BLOCK2_ALGOS[algo], LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype),
+                                               _ptr(c, a.dtype), _ptr(d, a.dtype), _ptr(info, torch.int32), n, batch,
+                                               _stream_ptr(stream))
+    check(st, f"tridiag_block2_{p}")
+    return d
+
+
 def periodic(a, b, c, d, n: int, algo: str = "gtsv", out=None, work=None, stream=None):
     """Periodic (cyclic) systems: a_0 couples x_{n-1}, c_{n-1} couples x_0.
     Contiguous layout; returns x."""

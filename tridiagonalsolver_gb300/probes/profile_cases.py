@@ -6,7 +6,9 @@ larger than L2, a few launches, one kernel family each).
 CASE: pge64 (partitioned pivoted solve, FP64, n = 4096 x 2048 non-dominant),
 pgc32 (cluster version, FP32, n = 65536 x 256 dominant), pge32 (FP32,
 n = 4096 x 4096 dominant), gtsv64 (thread-per-system pivoted sweep, FP64,
-n = 4096 x 1024).  Each solves its case three times.
+n = 4096 x 1024), block2_64 (2 x 2 block systems, FP64, interleaved,
+n = 256 x 32768: the pivoted solve, then block Thomas on dominant systems).
+Each solves its case three times.
 """
 import sys
 
@@ -18,7 +20,28 @@ CASES = {"pge64": (4096, 2048, torch.float64, False), "pgc32": (65536, 256, torc
          "pge32": (4096, 4096, torch.float32, True), "gtsv64": (4096, 1024, torch.float64, False)}
 
 
+def block2_case() -> None:
+    n, batch = 256, 32768
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    src = [torch.rand(k * n * batch, dtype=torch.float64, device="cuda", generator=g) * 2 - 1 for k in (4, 4, 4, 2)]
+    dom = src[1].clone().view(n, 4, batch)
+    dom[:, 0] += 8
+    dom[:, 3] += 8
+    work = [t.clone() for t in src]
+    for algo, b in (("pivoted", src[1]), ("thomas", dom.view(-1))):
+        for _ in range(3):
+            for w, s in zip(work, (src[0], b, src[2], src[3])):
+                w.copy_(s)
+            T.block2(*work, n, algo=algo, layout="interleaved")
+    torch.cuda.synchronize()
+    print("ok block2_64")
+
+
 def main(case: str) -> None:
+    if case == "block2_64":
+        block2_case()
+        return
     n, batch, dt, dominant = CASES[case]
     g = torch.Generator(device="cuda")
     g.manual_seed(3)

@@ -136,6 +136,7 @@ def log_uniform_sizes(count: int, lo: int = 32, hi: int = 65536, seed: int = 0):
 
 def _time(fn, reps=3):
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # the inputs were made on the caller's stream
     with torch.cuda.stream(s):
         fn()
         s.synchronize()

@@ -611,6 +611,70 @@ def run_thomas_fp64(args):
           args.steps, note="FP64 pipe bound (two chains per system; ~0.5 Tops/s FP64 per GB300)")
 
 
+def run_plain(args):
+    """Plain unpivoted solves at n = 4096 x 4096 on the dominant distribution,
+    contiguous layout, out of place: the partition method (one CTA per
+    system) in FP32 -- the headline of this workload -- and in FP64."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+    from tridiagonalsolver_gb300 import inputs
+
+    T.lib()
+    n, batch = 4096, 4096
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.6)
+    sampler.mark("begin")
+    parts, keep = [], None
+    for name, dt in (("partition_fp32", torch.float32), ("partition_fp64", torch.float64)):
+        g = torch.Generator(device=dev)
+        g.manual_seed(21)
+        u = lambda lo, hi: torch.rand((batch, n), dtype=dt, device=dev, generator=g) * (hi - lo) + lo
+        a, c, d = u(-1, 1), u(-1, 1), u(-1, 1)
+        b = a.abs() + c.abs() + u(1, 2)
+        x = torch.empty_like(d)
+        work = T.solve_out_workspace(a, n, "partition")
+        step = (lambda a=a, b=b, c=c, d=d, x=x, w=work:
+                T.solve_out(a, b, c, d, n, algo="partition", out=x, work=w, stream=stream))
+        ms, _ = _graph_time(torch, stream, step, args.steps, args.warmup)
+        idx = torch.arange(0, batch, batch // 16, device=dev)
+        hs = [t.index_select(0, idx).double().cpu().numpy() for t in (a, b, c, d, x)]
+        _, eta = O.backward_error(*hs, n)
+        es = 4 if dt == torch.float32 else 8
+        alg = 5 * n * batch * es
+        parts.append({"name": name, "dtype": str(dt).replace("torch.", ""), "algorithm": "partition", "n": n,
+                      "batch": batch, "layout": "contiguous", "ms_per_launch": ms, "systems_per_s": batch / (ms * 1e-3),
+                      "algorithmic_bytes": alg, "hbm_gbs": round(alg / (ms * 1e-3) / 1e9, 1),
+                      "backward_error_max": eta})
+        if keep is None:
+            keep = (a, b, c, d, x, step, ms)
+        else:
+            del a, b, c, d, x, work, step
+    sampler.mark("end")
+    clocks = sampler.stop()
+    a, b, c, d, x, step, ms = keep
+    e2e = _e2e_generic(torch, stream, [a, b, c, d], [x], step, max(3, min(args.steps // 10, 10)), batch)
+
+    def cpu(k):
+        aa, bb, cc, dd = (v.astype(np.float32) for v in inputs.dominant(n, k, seed=3))
+        t0 = time.perf_counter()
+        O.thomas(aa, bb, cc, dd, n)
+        return time.perf_counter() - t0
+
+    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, batch)
+    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                      "sample": f"{k} of {batch} systems in {t:.2f} s (reference Thomas restated, FP32)"}
+    _line(args, "plain unpivoted solve FP32 n=4096 x 4096, contiguous, dominant (partition method)",
+          batch / (ms * 1e-3), ms, "f32",
+          {"n": n, "batch": batch, "layout": "contiguous", "dominant": "wmc_kernel<float>",
+           "l2": "inputs larger than L2 (268 MB FP32)"},
+          parts, 5 * n * batch * 4, ms, cpu_b, e2e, clocks, args.steps * 2)
+
+
 def run_adjoint(args):
     """Forward + adjoint, FP32, n = 1024 x 16384 dominant, loss = sum(w x)."""
     import torch
@@ -934,7 +998,7 @@ def run_block2(args):
 
 
 WORKLOADS = {"config2": None, "thomas-fp64": run_thomas_fp64, "adjoint": run_adjoint, "ragged": run_ragged,
-             "refined": run_refined, "block2": run_block2}
+             "refined": run_refined, "block2": run_block2, "plain": run_plain}
 
 
 def main():

@@ -135,6 +135,8 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 #define TRIDIAG_ALGO_WM 4     /* WM-pGE, one warp per system, unpivoted */
 #define TRIDIAG_ALGO_GTSV 5   /* partial pivoting: PGE for n >= 512 where it fits, else one thread per system */
 #define TRIDIAG_ALGO_PGE 6    /* WM-pGE with partial pivoting inside partitions, one CTA per system */
+#define TRIDIAG_ALGO_PARTITION 7 /* partition method without pivoting, one CTA per system (contiguous / packed,
+                                    n a multiple of 32 (FP32) / 16 (FP64), 256 <= n <= 8192 / 128 <= n <= 4096) */
 
 /* Status of the last library call made by the calling host thread. */
 int tridiag_last_status(void);
@@ -149,18 +151,24 @@ int tridiag_device_error(int reset);
 /* In-place solve with the reference's contract (c may be overwritten, d <- x)
  * in any layout.  For TRIDIAG_LAYOUT_PACKED pass the packed base pointer as
  * a and NULL for b, c, d.  TRIDIAG_ALGO_GTSV allocates its workspace with
- * cudaMallocAsync on `stream`. */
+ * cudaMallocAsync on `stream`.  The unpivoted algorithms (AUTO, THOMAS, CR,
+ * PCR, PARTITION) assume systems that need no pivoting (e.g. diagonally
+ * dominant); AUTO picks TRIDIAG_ALGO_PARTITION where it applies and n > 1024,
+ * else Thomas; CR and PCR beyond one warp's reach use PARTITION where it
+ * applies.  WM keeps the pivoted partitioned solve beyond one warp. */
 int tridiag_solve_single(int algo, int layout, float *a, float *b, float *c, float *d, int n_eqt, int n_batch,
                          void *stream);
 int tridiag_solve_double(int algo, int layout, double *a, double *b, double *c, double *d, int n_eqt,
                          int n_batch, void *stream);
 
 /* Out-of-place solve: a, b, c, d are read only, x receives the solution.
- * TRIDIAG_ALGO_WM / AUTO run the on-chip WM-pGE where the shape allows
- * (contiguous layout) and need no workspace there; shapes it does not cover,
- * and TRIDIAG_ALGO_THOMAS / GTSV, use `work` of
- * tridiag_solve_out_workspace_size() bytes.  The packed layout is not
- * supported here. */
+ * TRIDIAG_ALGO_WM runs the on-chip WM-pGE where the shape allows (contiguous
+ * layout), the pivoted partitioned solve beyond it; AUTO runs the
+ * unpivoted TRIDIAG_ALGO_PARTITION where it applies and n > 1024, else as WM
+ * (CR and PCR beyond one warp: PARTITION where it applies).  These need no
+ * workspace; shapes none of them covers, and TRIDIAG_ALGO_THOMAS / GTSV, use
+ * `work` of tridiag_solve_out_workspace_size() bytes.  The packed layout is
+ * not supported here. */
 size_t tridiag_solve_out_workspace_size(int precision, int algo, int layout, int n_eqt, int n_batch);
 int tridiag_solve_out_single(int algo, int layout, const float *a, const float *b, const float *c, const float *d,
                              float *x, void *work, size_t work_bytes, int n_eqt, int n_batch, void *stream);

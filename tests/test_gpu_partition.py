@@ -1,0 +1,120 @@
+"""Partition method without pivoting, one CTA per system (TRIDIAG_ALGO_PARTITION),
+against the oracle on diagonally dominant systems, through the C ABI.
+
+Tolerances: normwise backward error <= 1e-12 (FP64) / 1e-6 (FP32); max |x -
+x_oracle| / max |x_oracle| <= 1e-12 (FP64) / 1e-5 (FP32) against the FP64
+pivoted oracle.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tridiagonalsolver_gb300 import inputs
+
+pytestmark = pytest.mark.gpu
+
+ETA = {np.float64: 1e-12, np.float32: 1e-6}
+FWD = {np.float64: 1e-12, np.float32: 1e-5}
+# eligible sizes: n = R * 128 / sizeof(T) rows, 8 <= R <= 256
+SIZES = {np.float32: [256, 1056, 2048, 4096, 8192], np.float64: [128, 528, 2048, 4096]}
+
+
+def _check(x, a, b, c, d, dt, n):
+    batch = x.size // n
+    a64, b64, c64, d64 = (v.astype(dt).astype(np.float64) for v in (a, b, c, d))
+    _, eta = O.backward_error(a64, b64, c64, d64, x, n)
+    assert eta <= ETA[dt], eta
+    xo = O.gtsv(a64, b64, c64, d64, n).reshape(batch, n)
+    rel = np.max(np.abs(x.reshape(batch, n) - xo), axis=1) / np.max(np.abs(xo), axis=1)
+    assert rel.max() <= FWD[dt], rel.max()
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("idx", range(5))
+@pytest.mark.parametrize("batch", [1, 7, 100])
+def test_partition_in_and_out_of_place(cuda, dt, idx, batch):
+    import tridiagonalsolver_gb300 as T
+
+    if idx >= len(SIZES[dt]):
+        pytest.skip("size list shorter for this precision")
+    n = SIZES[dt][idx]
+    a, b, c, d = inputs.dominant(n, batch, seed=n + batch)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    x = T.solve_out(*ts, n, algo="partition").double().cpu().numpy()
+    _check(x, a, b, c, d, dt, n)
+    # inputs untouched by the out-of-place solve
+    for t, v in zip(ts, (a, b, c, d)):
+        np.testing.assert_array_equal(t.cpu().numpy(), v.astype(dt))
+    T.solve(*ts, n, algo="partition")
+    x2 = ts[3].double().cpu().numpy()
+    assert np.array_equal(x, x2)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_partition_packed(cuda, dt):
+    import tridiagonalsolver_gb300 as T
+
+    n, batch = (2048 if dt == np.float32 else 1024), 9
+    a, b, c, d = inputs.dominant(n, batch, seed=5)
+    p = cuda.from_numpy(inputs.to_packed(a, b, c, d).astype(dt)).cuda()
+    T.solve(p, None, None, None, n, algo="partition", layout="packed")
+    x = p.double().cpu().numpy().reshape(batch, 4, n)[:, 3, :]
+    _check(x, a, b, c, d, dt, n)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_partition_ignores_a0_and_clast(cuda, dt):
+    import tridiagonalsolver_gb300 as T
+
+    n, batch = 4096, 5
+    a, b, c, d = inputs.dominant(n, batch, seed=9)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    x0 = T.solve_out(*ts, n, algo="partition").cpu().numpy()
+    a2, c2 = a.copy(), c.copy()
+    a2[:, 0] = np.nan
+    c2[:, -1] = np.nan
+    ts2 = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a2, b, c2, d)]
+    x1 = T.solve_out(*ts2, n, algo="partition").cpu().numpy()
+    assert np.array_equal(x0, x1)
+
+
+@pytest.mark.parametrize("dt,n", [(np.float32, 1000), (np.float32, 8224), (np.float64, 100), (np.float64, 4112),
+                                  (np.float32, 3000)])
+def test_partition_other_shapes_fall_back(cuda, dt, n):
+    """Shapes outside the CTA kernel's range are solved by the Thomas sweep."""
+    import tridiagonalsolver_gb300 as T
+
+    batch = 6
+    a, b, c, d = inputs.dominant(n, batch, seed=n)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    x = T.solve_out(*ts, n, algo="partition").double().cpu().numpy()
+    _check(x, a, b, c, d, dt, n)
+    T.solve(*ts, n, algo="partition")
+    _check(ts[3].double().cpu().numpy(), a, b, c, d, dt, n)
+
+
+@pytest.mark.parametrize("name,dt", [("PCR5_reg_single", np.float32), ("CR_reg8_single", np.float32),
+                                     ("PCR5_reg_double", np.float64), ("CR_reg8_double", np.float64)])
+def test_reference_cr_pcr_names_long_systems(cuda, name, dt):
+    """The reference's CR and PCR entry points beyond one warp's reach run
+    the partition kernel (in place, d <- x)."""
+    import tridiagonalsolver_gb300 as T
+
+    n, batch = 4096, 6
+    a, b, c, d = inputs.dominant(n, batch, seed=2)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    T.reference_call(name, *ts, n)
+    _check(ts[3].double().cpu().numpy(), a, b, c, d, dt, n)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_auto_uses_partition_and_is_exact_same(cuda, dt):
+    import tridiagonalsolver_gb300 as T
+
+    n, batch = 4096, 4
+    a, b, c, d = inputs.dominant(n, batch, seed=12)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    xa = T.solve_out(*ts, n, algo="auto").cpu().numpy()
+    xp = T.solve_out(*ts, n, algo="partition").cpu().numpy()
+    assert np.array_equal(xa, xp)
+    _check(xa.astype(np.float64), a, b, c, d, dt, n)

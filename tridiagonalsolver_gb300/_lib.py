@@ -22,7 +22,7 @@ ERR_SINGULAR = 5
 ERR_TIMEOUT = 6
 
 LAYOUTS = {"contiguous": 0, "packed": 1, "interleaved": 2}
-ALGOS = {"auto": 0, "thomas": 1, "cr": 2, "pcr": 3, "wm": 4, "gtsv": 5, "pge": 6}
+ALGOS = {"auto": 0, "thomas": 1, "cr": 2, "pcr": 3, "wm": 4, "gtsv": 5, "pge": 6, "partition": 7}
 
 _lock = threading.Lock()
 _lib = None

@@ -122,8 +122,18 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
   if (!valid_dims(n, batch) || !valid_layout(layout) || !a) return TRIDIAG_ERR_INVALID_VALUE;
   packed_ptrs(layout, a, b, c, d, n);
   if (!b || !c || !d) return TRIDIAG_ERR_INVALID_VALUE;
-  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_THOMAS;
+  if (algo == TRIDIAG_ALGO_AUTO)
+    algo = (n > 1024 && tdg::wmc_eligible<T>(layout, n)) ? TRIDIAG_ALGO_PARTITION : TRIDIAG_ALGO_THOMAS;
   switch (algo) {
+    case TRIDIAG_ALGO_PARTITION: {
+      bool used = false;
+      cudaError_t e = tdg::launch_wmc<T>(layout, a, b, c, d, d, n, batch, s, &used);
+      if (e == cudaSuccess && !used) {
+        e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
+        if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
+      }
+      return cuda_status(e);
+    }
     case TRIDIAG_ALGO_THOMAS: {
       bool used = false;
       cudaError_t e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
@@ -139,6 +149,8 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
                                                  : tdg::launch_wm_warp<T>(layout, a, b, c, d, d, n, batch, s, &used);
       if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM && n >= PGE_MIN_N)
         e = tdg::launch_pge<T>(layout, a, b, c, d, d, nullptr, n, batch, s, &used);
+      if (e == cudaSuccess && !used && algo != TRIDIAG_ALGO_WM)
+        e = tdg::launch_wmc<T>(layout, a, b, c, d, d, n, batch, s, &used);
       if (e == cudaSuccess && !used) {
         e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
         if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
@@ -182,10 +194,19 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
                    size_t work_bytes, int n, int batch, cudaStream_t s) {
   if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !b || !c || !d || !x) return TRIDIAG_ERR_INVALID_VALUE;
   if (layout == TRIDIAG_LAYOUT_PACKED) return TRIDIAG_ERR_NOT_SUPPORTED;
-  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_WM;
+  if (algo == TRIDIAG_ALGO_AUTO)
+    algo = (n > 1024 && tdg::wmc_eligible<T>(layout, n)) ? TRIDIAG_ALGO_PARTITION : TRIDIAG_ALGO_WM;
   if (work_bytes < solve_out_ws<T>(algo, n, batch) || (solve_out_ws<T>(algo, n, batch) && !work))
     return TRIDIAG_ERR_WORKSPACE;
   switch (algo) {
+    case TRIDIAG_ALGO_PARTITION: {
+      bool used = false;
+      cudaError_t e = tdg::launch_wmc<T>(layout, a, b, c, d, x, n, batch, s, &used);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      if (used) return TRIDIAG_SUCCESS;
+      if (!work || work_bytes < solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, n, batch)) return TRIDIAG_ERR_WORKSPACE;
+      return solve_out_impl<T>(TRIDIAG_ALGO_THOMAS, layout, a, b, c, d, x, work, work_bytes, n, batch, s);
+    }
     case TRIDIAG_ALGO_CR:
     case TRIDIAG_ALGO_PCR:
     case TRIDIAG_ALGO_WM: {
@@ -195,6 +216,8 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
                                                  : tdg::launch_wm_warp<T>(layout, a, b, c, d, x, n, batch, s, &used);
       if (e == cudaSuccess && !used && algo == TRIDIAG_ALGO_WM && n >= PGE_MIN_N)
         e = tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used);
+      if (e == cudaSuccess && !used && algo != TRIDIAG_ALGO_WM)
+        e = tdg::launch_wmc<T>(layout, a, b, c, d, x, n, batch, s, &used);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       if (!work || work_bytes < solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, n, batch)) return TRIDIAG_ERR_WORKSPACE;
@@ -418,7 +441,8 @@ int tridiag_solve_double(int algo, int layout, double* a, double* b, double* c, 
 size_t tridiag_solve_out_workspace_size(int precision, int algo, int layout, int n, int batch) {
   (void)layout;
   if (!valid_dims(n, batch)) return 0;
-  if (algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM || algo == TRIDIAG_ALGO_CR || algo == TRIDIAG_ALGO_PCR)
+  if (algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM || algo == TRIDIAG_ALGO_CR || algo == TRIDIAG_ALGO_PCR ||
+      algo == TRIDIAG_ALGO_PARTITION)
     algo = TRIDIAG_ALGO_THOMAS;  // possible fallback
   return precision ? solve_out_ws<double>(algo, n, batch) : solve_out_ws<float>(algo, n, batch);
 }

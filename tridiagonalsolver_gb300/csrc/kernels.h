@@ -51,6 +51,15 @@ template <typename T>
 cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                            cudaStream_t st, bool* used);
 
+// wmc.cu: partition method without pivoting, one CTA per system
+// (CONTIG / PACKED; n = R * 128 / sizeof(T) with 8 <= R <= 256).  x may alias
+// d (PACKED: must).  *used is false when the shape is not covered.
+template <typename T>
+bool wmc_eligible(int layout, int n);
+template <typename T>
+cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                       cudaStream_t s, bool* used);
+
 // wm.cu: CR-PCR hybrid on the same chunk layout (cyclic reduction in
 // registers down to one row per lane, warp PCR on those rows).
 template <typename T>

@@ -1,0 +1,303 @@
+// Partitioned solve without pivoting, one CTA per system (contiguous and
+// packed layouts): the partition method of the reference's WM-pGE
+// (Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884 partitions each system and
+// eliminates without pivoting) reorganised for a whole system per CTA.
+//
+// Shape: each thread owns one 128-byte row of the system, i.e. M = 32 (FP32)
+// or 16 (FP64) consecutive equations; n = R * M with R threads (R <= 256).
+// The four arrays arrive by TMA (one 2-D box of R x 128 bytes each, 128-byte
+// swizzle), so thread t's 16-byte units sit at t*128 + ((q ^ (t & 7)) * 16):
+// the eight threads of a quarter warp reading unit q hit eight different
+// 16-byte bank groups, and every shared-memory access is a conflict-free
+// vector access.
+//
+// Per partition (rows s .. s+M-1 of thread t), the last row is the
+// partition's separator y_t; the interior rows are eliminated top-down
+// without pivoting, each expressed as
+//     x_k = d'_k - c'_k x_{k+1} - v_k y_{t-1}
+// (v carries the coupling a_s y_{t-1} of the first row), while the same
+// sweep carries the first row's relation x_s = G + P x_{k+1} - L y_{t-1}
+// (P is the running product of -c').  At the last interior row x_{k+1} is
+// y_t, so each separator row gives one row of a tridiagonal system in
+// y_0 .. y_{R-1}:
+//     -a_r v_L y_{t-1} + (b_r - a_r c'_L - c_r L') y_t + c_r P' y_{t+1}
+//         = d_r - a_r d'_L - c_r G'
+// (primes: the next partition's first-row relation).  That system is solved
+// by parallel cyclic reduction across the CTA, then every thread substitutes
+// back bottom-up.  Stability: that of elimination without pivoting, i.e.
+// the contract of Thomas, CR and PCR -- diagonally dominant (or otherwise
+// pivoting-free) systems; the pivoted solves are tridiag_gtsv_* and
+// TRIDIAG_ALGO_GTSV / PGE.
+//
+// Shared-memory passes: read a, b, c, d and write v, c', d' over a, b, d
+// (top-down), read v, c', d' and write x over d (bottom-up); x leaves by one
+// TMA store.  HBM traffic is the algorithmic 5 n sizeof(T) per system.
+#include "../../include/tridiagonal.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "tma.cuh"
+#include "tw.cuh"
+
+namespace tdg {
+
+constexpr int WMC_MAX_R = 256;
+
+struct WmcMaps {
+  CUtensorMap m[5];  // a, b, c, d, x (PACKED: m[0] covers every array, x included)
+};
+
+template <typename T>
+struct WmcVec;
+template <>
+struct WmcVec<float> {
+  using V = float4;
+  static constexpr int N = 4;
+  __device__ static __forceinline__ void split(const V& v, float (&r)[4]) {
+    r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+  }
+  __device__ static __forceinline__ V join(const float (&r)[4]) { return make_float4(r[0], r[1], r[2], r[3]); }
+};
+template <>
+struct WmcVec<double> {
+  using V = double2;
+  static constexpr int N = 2;
+  __device__ static __forceinline__ void split(const V& v, double (&r)[2]) {
+    r[0] = v.x; r[1] = v.y;
+  }
+  __device__ static __forceinline__ V join(const double (&r)[2]) { return make_double2(r[0], r[1]); }
+};
+
+// byte offset of 16-byte unit q of 128-byte row t under the 128-byte swizzle
+__device__ __forceinline__ int wmc_swz(int t, int q) { return t * 128 + ((q ^ (t & 7)) << 4); }
+
+template <typename T>
+__host__ __device__ constexpr size_t wmc_array_bytes(int R) {
+  return ((size_t)R * 128 + 1023) / 1024 * 1024;
+}
+
+template <typename T>
+__host__ __device__ constexpr size_t wmc_smem_bytes(int R, int threads) {
+  return 1024 /* alignment slack */ + 4 * wmc_array_bytes<T>(R) + 8 * (size_t)threads * sizeof(T) + 16;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
+                                                        int packed, int* err) {
+  using W = WmcVec<T>;
+  constexpr int NV = W::N;     // values per 16-byte unit
+  constexpr int M = 8 * NV;    // rows per thread (128 bytes)
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const size_t ab = wmc_array_bytes<T>(R);
+  unsigned char* S[4] = {base, base + ab, base + 2 * ab, base + 3 * ab};
+  const int nt = blockDim.x;
+  T* red = reinterpret_cast<T*>(base + 4 * ab);  // 8 arrays of nt values
+  T *ra = red, *rb = red + nt, *rc = red + 2 * nt, *rd = red + 3 * nt;
+  T *xg = red + 4 * nt, *xp = red + 5 * nt, *xl = red + 6 * nt, *ys = red + 7 * nt;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(red + 8 * nt);
+
+  const int j = blockIdx.x;
+  const int t = threadIdx.x;
+  const bool active = t < R;
+  if (t == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (t == 0) {
+    mbar_arrive_expect_tx(bar, 4u * (unsigned)R * 128u);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const CUtensorMap* mp = &maps.m[packed ? 0 : k];
+      const int row = packed ? (j * 4 + k) * R : j * R;
+      tma_load_2d(S[k], mp, 0, row, bar);
+    }
+  }
+  const bool ok = mbar_wait(bar, 0, err);
+  if (!__syncthreads_and(ok)) return;
+
+  // ---- top-down elimination of the interior rows --------------------------
+  T cp = T(0), dp = T(0), vp = T(0);  // c', d', v of the previous row
+  T G = T(0), L = T(0), P = T(0);     // first-row relation
+  T sa = T(0), sb = T(1), sc = T(0), sd = T(0);  // separator row
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int off = wmc_swz(t, q);
+      T va[NV], vb[NV], vc[NV], vd[NV];
+      W::split(*reinterpret_cast<const typename W::V*>(S[0] + off), va);
+      W::split(*reinterpret_cast<const typename W::V*>(S[1] + off), vb);
+      W::split(*reinterpret_cast<const typename W::V*>(S[2] + off), vc);
+      W::split(*reinterpret_cast<const typename W::V*>(S[3] + off), vd);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const int k = q * NV + v;
+        const T a = (t == 0 && k == 0) ? T(0) : va[v];  // a_0 is not read
+        if (k < M - 1) {
+          const T den = k == 0 ? vb[v] : fma(-a, cp, vb[v]);
+          const T r = Div<T>(den).inv();
+          const T ncp = vc[v] * r;
+          const T ndp = (k == 0 ? vd[v] : fma(-a, dp, vd[v])) * r;
+          const T nvp = (k == 0 ? a : -a * vp) * r;
+          if (k == 0) {
+            G = ndp;
+            L = nvp;
+            P = -ncp;
+          } else {
+            G = fma(P, ndp, G);
+            L = fma(P, nvp, L);
+            P = -P * ncp;
+          }
+          cp = ncp;
+          dp = ndp;
+          vp = nvp;
+          va[v] = nvp;
+          vb[v] = ncp;
+          vd[v] = ndp;
+        } else {
+          sa = a;
+          sb = vb[v];
+          sc = (t == R - 1) ? T(0) : vc[v];  // c_{n-1} is not read
+          sd = vd[v];
+        }
+      }
+      *reinterpret_cast<typename W::V*>(S[0] + off) = W::join(va);
+      *reinterpret_cast<typename W::V*>(S[1] + off) = W::join(vb);
+      *reinterpret_cast<typename W::V*>(S[3] + off) = W::join(vd);
+    }
+    xg[t] = G;
+    xp[t] = P;
+    xl[t] = L;
+  }
+  __syncthreads();
+  // ---- the separators' tridiagonal system ---------------------------------
+  T al = T(0), be = T(1), ga = T(0), de = T(0);
+  if (active) {
+    const T Gn = t + 1 < R ? xg[t + 1] : T(0);
+    const T Pn = t + 1 < R ? xp[t + 1] : T(0);
+    const T Ln = t + 1 < R ? xl[t + 1] : T(0);
+    al = -sa * vp;
+    be = fma(-sc, Ln, fma(-sa, cp, sb));
+    ga = sc * Pn;
+    de = fma(-sc, Gn, fma(-sa, dp, sd));
+  }
+  // parallel cyclic reduction: row t combines rows t - s and t + s
+  for (int s = 1; s < R; s <<= 1) {
+    if (active) {
+      ra[t] = al;
+      rb[t] = be;
+      rc[t] = ga;
+      rd[t] = de;
+    }
+    __syncthreads();
+    if (active) {
+      T a1 = T(0), b1 = T(1), c1 = T(0), d1 = T(0), a2 = T(0), b2 = T(1), c2 = T(0), d2 = T(0);
+      if (t - s >= 0) {
+        a1 = ra[t - s];
+        b1 = rb[t - s];
+        c1 = rc[t - s];
+        d1 = rd[t - s];
+      }
+      if (t + s < R) {
+        a2 = ra[t + s];
+        b2 = rb[t + s];
+        c2 = rc[t + s];
+        d2 = rd[t + s];
+      }
+      const T k1 = al * Div<T>(b1).inv();
+      const T k2 = ga * Div<T>(b2).inv();
+      be = fma(-k2, a2, fma(-k1, c1, be));
+      de = fma(-k2, d2, fma(-k1, d1, de));
+      al = -k1 * a1;
+      ga = -k2 * c2;
+    }
+    __syncthreads();
+  }
+  if (active) ys[t] = de * Div<T>(be).inv();
+  __syncthreads();
+  // ---- bottom-up substitution ---------------------------------------------
+  if (active) {
+    const T y = ys[t];
+    const T yl = t > 0 ? ys[t - 1] : T(0);
+    T xn = y;
+#pragma unroll
+    for (int q = 7; q >= 0; --q) {
+      const int off = wmc_swz(t, q);
+      T va[NV], vb[NV], vd[NV];
+      W::split(*reinterpret_cast<const typename W::V*>(S[0] + off), va);
+      W::split(*reinterpret_cast<const typename W::V*>(S[1] + off), vb);
+      W::split(*reinterpret_cast<const typename W::V*>(S[3] + off), vd);
+#pragma unroll
+      for (int v = NV - 1; v >= 0; --v) {
+        const int k = q * NV + v;
+        if (k == M - 1) {
+          vd[v] = y;
+        } else {
+          xn = fma(-va[v], yl, fma(-vb[v], xn, vd[v]));
+          vd[v] = xn;
+        }
+      }
+      *reinterpret_cast<typename W::V*>(S[3] + off) = W::join(vd);
+    }
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (t == 0) {
+    const int row = packed ? (j * 4 + 3) * R : j * R;
+    tma_store_2d(&maps.m[packed ? 0 : 4], 0, row, S[3]);
+    bulk_commit();
+    bulk_wait_read<0>();
+  }
+}
+
+template <typename T>
+bool wmc_eligible(int layout, int n) {
+  constexpr int M = 128 / (int)sizeof(T);
+  if (layout != CONTIG && layout != PACKED) return false;
+  if (n % M != 0) return false;
+  const int R = n / M;
+  return R >= 8 && R <= WMC_MAX_R;
+}
+
+template <typename T>
+cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                       cudaStream_t s, bool* used) {
+  *used = false;
+  if (!wmc_eligible<T>(layout, n) || batch <= 0) return cudaSuccess;
+  constexpr int M = 128 / (int)sizeof(T);
+  const int R = n / M;
+  const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  WmcMaps maps;
+  const bool packed = layout == PACKED;
+  if (packed) {
+    // one tensor over the whole packed batch: rows of 128 bytes, 4 R rows per system
+    if (x != d) return cudaSuccess;
+    if (!encode_tmap_2d(&maps.m[0], a, dt, sizeof(T), (uint64_t)M, (uint64_t)4 * R * (uint64_t)batch, 128, M, R,
+                        CU_TENSOR_MAP_SWIZZLE_128B))
+      return cudaSuccess;
+  } else {
+    const T* ptrs[5] = {a, b, c, d, x};
+    for (int k = 0; k < 5; ++k)
+      if (!encode_tmap_2d(&maps.m[k], ptrs[k], dt, sizeof(T), (uint64_t)M, (uint64_t)R * (uint64_t)batch, 128, M, R,
+                          CU_TENSOR_MAP_SWIZZLE_128B))
+        return cudaSuccess;
+  }
+  const int threads = (R + 31) / 32 * 32;
+  const size_t smem = wmc_smem_bytes<T>(R, threads);
+  cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  wmc_kernel<T><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word());
+  e = cudaGetLastError();
+  if (e == cudaSuccess) *used = true;
+  return e;
+}
+
+template bool wmc_eligible<float>(int, int);
+template bool wmc_eligible<double>(int, int);
+template cudaError_t launch_wmc<float>(int, const float*, const float*, const float*, const float*, float*, int, int,
+                                       cudaStream_t, bool*);
+template cudaError_t launch_wmc<double>(int, const double*, const double*, const double*, const double*, double*,
+                                        int, int, cudaStream_t, bool*);
+
+}  // namespace tdg

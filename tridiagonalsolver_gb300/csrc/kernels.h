@@ -60,6 +60,12 @@ template <typename T>
 cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                        cudaStream_t s, bool* used);
 
+// wm.cu: PCR-pThomas on the persistent TMA-fed chunk kernel (CONTIG,
+// n = 512 FP32 / 256 FP64); *used is false for other shapes.
+template <typename T>
+cudaError_t launch_pcr_tma(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                           cudaStream_t st, bool* used);
+
 // wm.cu: CR-PCR hybrid on the same chunk layout (cyclic reduction in
 // registers down to one row per lane, warp PCR on those rows).
 template <typename T>

@@ -1,106 +1,117 @@
 // PCR-pThomas, one warp per system, everything on chip.
 //
-// Lane l holds rows l, l+32, l+64, ... (Q rows per lane, rows past n are
-// identity rows), so every global load and store of the warp is one
-// coalesced row of 32 consecutive elements.  Five PCR steps with strides
-// 1, 2, 4, 8, 16 couple each row to the rows 32 above and below it, which
-// splits the system into 32 independent chains -- chain l is exactly the
-// rows lane l holds -- and each lane then runs the Thomas algorithm on its
-// chain in registers.  A PCR step needs, from the rows s above and below,
-// a/b, c/b and d/b (three warp shuffles each way per row); a row that is s
-// above or below wraps into the neighbouring block of 32 rows, which one
-// shuffle of a per-lane selected block handles.
+// Five PCR steps with strides 1, 2, 4, 8, 16 couple each row to the rows 32
+// above and below it, which splits the system into 32 independent chains
+// (rows congruent mod 32); the Thomas algorithm then solves each chain.
+//
+// Placement.  Lane l holds the Q consecutive rows l*Q .. l*Q+Q-1 (rows past
+// n are identity rows), so a PCR step of stride s < Q finds most neighbours
+// in the lane's own registers: only the s rows at each end of the chunk
+// exchange their three normalised values (a/b, c/b, d/b) with the adjacent
+// lane, 6 s shuffles per step instead of 6 Q; strides s >= Q are a plain
+// shift by s/Q lanes.  At n = 512 (Q = 16) that is 186 shuffles per system
+// instead of the 480 a row-interleaved placement needs -- shuffles run on the
+// LSU pipe, one warp instruction per clock per SM, and bounded the kernel.
+// After the PCR steps the rows go through shared memory (an XOR-swizzled
+// index, conflict-free for the chunk-wise writes and the chain-wise reads)
+// and lane c runs Thomas on chain c (rows c, c+32, ...), whose solution it
+// stores with coalesced 32-row writes.  The step and chain code is in
+// pcr.cuh, shared with the persistent TMA-fed kernel of wm.cu that serves
+// n = 512 (FP32) / 256 (FP64) in the contiguous layout.
 //
 // Reference: PCR5_{reg,shmem}_kernel, Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:
 // 886-1282 (5 PCR steps over streamed 32-row chunks, then a per-lane Thomas
-// on the stride-32 chains, spilling c', d' to global memory), and the CPU
-// versions Tridiagonal_AVX512/tridiagonal_d_avx512.cpp:419-646.  The "half"
-// variants (4 steps, chains shared by two lanes) are served by the same
-// 5-step kernel.
+// on the stride-32 chains), and the CPU versions
+// Tridiagonal_AVX512/tridiagonal_d_avx512.cpp:419-646.  The "half" variants
+// (4 steps, chains shared by two lanes) are served by the same 5-step kernel.
 #include "common.cuh"
 #include "kernels.h"
+#include "pcr.cuh"
 #include "tw.cuh"
 
 namespace tdg {
 
-template <typename T, int Q>
-__global__ void __launch_bounds__(128) pcr_warp_kernel(const T* __restrict__ a, const T* __restrict__ b,
-                                                       const T* __restrict__ c, const T* d, T* x, int n, int batch,
-                                                       size_t sys_stride) {
-  const int lane = threadIdx.x & 31;
-  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+constexpr int PCR_WARPS = 4;
+
+template <typename T>
+struct PcrVec;
+template <>
+struct PcrVec<float> {
+  using V = float4;
+  static constexpr int N = 4;
+  __device__ static __forceinline__ float get(const V& v, int k) {
+    return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+  }
+};
+template <>
+struct PcrVec<double> {
+  using V = double2;
+  static constexpr int N = 2;
+  __device__ static __forceinline__ double get(const V& v, int k) { return k == 0 ? v.x : v.y; }
+};
+
+// Rows [r0, r0 + Q) of one array into registers; rows past n get `fill`, and
+// rows 0 / n-1 of a / c are not read (zero).  VEC: whole chunks inside the
+// system load as 16-byte vectors.
+template <typename T, int Q, bool VEC>
+__device__ __forceinline__ void pcr_load(const T* p, int r0, int n, int skip, T fill, T (&v)[Q]) {
+  constexpr int NV = PcrVec<T>::N;
+  if (VEC && Q % NV == 0 && r0 + Q <= n) {
+#pragma unroll
+    for (int u = 0; u < Q / NV; ++u) {
+      const typename PcrVec<T>::V w = __ldg(reinterpret_cast<const typename PcrVec<T>::V*>(p + r0) + u);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[u * NV + k] = PcrVec<T>::get(w, k);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q] = r0 + q < n ? __ldg(p + r0 + q) : fill;
+  }
+  if (skip >= 0) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+      if (r0 + q == skip) v[q] = T(0);
+  }
+}
+
+template <typename T, int Q, bool VEC>
+__global__ void __launch_bounds__(32 * PCR_WARPS) pcr_warp_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                                  const T* __restrict__ c, const T* d, T* x, int n,
+                                                                  int batch, size_t sys_stride) {
+  __shared__ T sh[PCR_WARPS][32 * Q];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * PCR_WARPS + w;
   if (j >= batch) return;
   const size_t base = (size_t)j * sys_stride;
-  T A[Q], B[Q], C[Q], D[Q];
+  const int r0 = lane * Q;
+  T A[Q], B[Q], C[Q], D[Q], X[Q];
+  pcr_load<T, Q, VEC>(a + base, r0, n, 0, T(0), A);
+  pcr_load<T, Q, VEC>(b + base, r0, n, -1, T(1), B);
+  pcr_load<T, Q, VEC>(c + base, r0, n, n - 1, T(0), C);
+  pcr_load<T, Q, VEC>(d + base, r0, n, -1, T(0), D);
+  pcr_chunk_steps<T, Q>(A, B, C, D, lane);
+  pcr_chain_thomas<T, Q>(A, B, C, D, X, lane, sh[w]);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const int r = q * 32 + lane;
-    const bool in = r < n;
-    A[q] = (in && r > 0) ? __ldg(a + base + r) : T(0);
-    B[q] = in ? __ldg(b + base + r) : T(1);
-    C[q] = (in && r < n - 1) ? __ldg(c + base + r) : T(0);
-    D[q] = in ? d[base + r] : T(0);
-  }
-  // PCR steps
-#pragma unroll
-  for (int s = 1; s < 32; s <<= 1) {
-    T al[Q], ga[Q], de[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const Div<T> q_(B[q]);
-      al[q] = q_.div(A[q]);
-      ga[q] = q_.div(C[q]);
-      de[q] = q_.div(D[q]);
-    }
-    const int srcL = (lane - s) & 31, srcR = (lane + s) & 31;
-    const bool lowL = lane < 32 - s;  // as a sender: my block feeds the same block on the left side
-    const bool lowR = lane >= s;      // as a sender: my block feeds the same block on the right side
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      // row s above: sender lane srcL gives block q if it lies in the same
-      // 32-row block, else block q-1 (identity above row 0)
-      const T sa = lowL ? al[q] : (q > 0 ? al[q - 1] : T(0));
-      const T sg = lowL ? ga[q] : (q > 0 ? ga[q - 1] : T(0));
-      const T sd = lowL ? de[q] : (q > 0 ? de[q - 1] : T(0));
-      const T aL = shfl(sa, srcL), gL = shfl(sg, srcL), dL = shfl(sd, srcL);
-      // row s below: block q, or block q+1 (identity past the last block)
-      const T ra = lowR ? al[q] : (q + 1 < Q ? al[q + 1] : T(0));
-      const T rg = lowR ? ga[q] : (q + 1 < Q ? ga[q + 1] : T(0));
-      const T rd = lowR ? de[q] : (q + 1 < Q ? de[q + 1] : T(0));
-      const T aR = shfl(ra, srcR), gR = shfl(rg, srcR), dR = shfl(rd, srcR);
-      const T a0 = A[q], c0 = C[q];
-      A[q] = -a0 * aL;
-      B[q] = fma(-c0, aR, fma(-a0, gL, B[q]));
-      C[q] = -c0 * gR;
-      D[q] = fma(-c0, dR, fma(-a0, dL, D[q]));
-    }
-  }
-  // Thomas on the lane's chain (rows lane, lane+32, ...)
-  T cp = T(0), dp = T(0);
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const Div<T> k(fma(-A[q], cp, B[q]));
-    cp = k.div(C[q]);
-    dp = k.div(fma(-A[q], dp, D[q]));
-    C[q] = cp;
-    D[q] = dp;
-  }
-  T xv = T(0);
-#pragma unroll
-  for (int qq = 0; qq < Q; ++qq) {
-    const int q = Q - 1 - qq;
-    xv = fma(-C[q], xv, D[q]);
-    const int r = q * 32 + lane;
-    if (r < n) x[base + r] = xv;
+  for (int k = 0; k < Q; ++k) {
+    const int r = lane + 32 * k;
+    if (r < n) x[base + r] = X[k];
   }
 }
 
 template <typename T, int Q>
 static cudaError_t launch_pcr_q(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                                 size_t stride, cudaStream_t st) {
-  const int wpb = 4;
-  dim3 grid((batch + wpb - 1) / wpb);
-  pcr_warp_kernel<T, Q><<<grid, 32 * wpb, 0, st>>>(a, b, c, d, x, n, batch, stride);
+  constexpr int WARPS = PCR_WARPS;
+  dim3 grid((batch + WARPS - 1) / WARPS);
+  constexpr int NV = PcrVec<T>::N;
+  const bool vec = Q % NV == 0 && stride % NV == 0 &&
+                   ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(c) |
+                     reinterpret_cast<uintptr_t>(d)) &
+                    15u) == 0;
+  if (vec)
+    pcr_warp_kernel<T, Q, true><<<grid, 32 * WARPS, 0, st>>>(a, b, c, d, x, n, batch, stride);
+  else
+    pcr_warp_kernel<T, Q, false><<<grid, 32 * WARPS, 0, st>>>(a, b, c, d, x, n, batch, stride);
   return cudaGetLastError();
 }
 
@@ -109,6 +120,8 @@ cudaError_t launch_pcr_warp(int layout, const T* a, const T* b, const T* c, cons
                             cudaStream_t st, bool* used) {
   *used = false;
   if (layout != CONTIG && layout != PACKED) return cudaSuccess;
+  cudaError_t e = launch_pcr_tma<T>(layout, a, b, c, d, x, n, batch, st, used);
+  if (e != cudaSuccess || *used) return e;
   const size_t stride = layout == PACKED ? 4 * (size_t)n : (size_t)n;
   const int q = (n + 31) / 32;
   const int qmax = sizeof(T) == 4 ? 32 : 16;

@@ -23,6 +23,7 @@
 // this version keeps the whole system in registers.
 #include "common.cuh"
 #include "kernels.h"
+#include "pcr.cuh"
 #include "tw.cuh"
 
 namespace tdg {
@@ -280,7 +281,7 @@ __device__ __forceinline__ void crpcr_lane_solve(T (&A)[M], T (&B)[M], T (&C)[M]
 }
 
 // Per-lane solve selector for the chunk-layout kernels.
-enum ChunkAlgo { CHUNK_WM = 0, CHUNK_CRPCR = 1 };
+enum ChunkAlgo { CHUNK_WM = 0, CHUNK_CRPCR = 1, CHUNK_PCR = 2 };
 
 template <int ALG, typename T, int M, int G>
 __device__ __forceinline__ void chunk_solve(T (&A)[M], T (&B)[M], T (&C)[M], T (&D)[M], T (&X)[M], int n, int s,
@@ -406,13 +407,30 @@ __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
     __syncwarp();
     // the slot is free again: refill it with the box WM_SLOTS ahead
     if (lane == 0 && i + WM_SLOTS < count) load(i + WM_SLOTS, q);
-    chunk_solve<ALG, T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
-    if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer
-    __syncwarp();
+    if constexpr (ALG == CHUNK_PCR) {
+      // PCR-pThomas (32 lanes per system): the PCR steps on the chunks, then
+      // the chains through the output buffer (free once the previous x
+      // store has read it), then x of rows lane + 32 k into the buffer's
+      // TMA layout
+      pcr_chunk_steps<T, M>(A, B, C, D, lane);
+      if (lane == 0) bulk_wait_read<0>();
+      __syncwarp();
+      pcr_chain_thomas<T, M>(A, B, C, D, X, lane, out->buf);
 #pragma unroll
-    for (int u = 0; u < M / NV; ++u) {
-      const int off = wm_swz<ROWB>(lane, u);
-      *reinterpret_cast<typename W::V*>(reinterpret_cast<unsigned char*>(out->buf) + off) = W::make(X, u * NV);
+      for (int k = 0; k < M; ++k) {
+        const int r = lane + 32 * k;
+        const int off = wm_swz<ROWB>(r / M, (r % M) / NV) + (r % NV) * (int)sizeof(T);
+        *reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(out->buf) + off) = X[k];
+      }
+    } else {
+      chunk_solve<ALG, T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
+      if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < M / NV; ++u) {
+        const int off = wm_swz<ROWB>(lane, u);
+        *reinterpret_cast<typename W::V*>(reinterpret_cast<unsigned char*>(out->buf) + off) = W::make(X, u * NV);
+      }
     }
     fence_async_smem();
     __syncwarp();
@@ -512,6 +530,19 @@ static cudaError_t launch_chunk(int layout, const T* a, const T* b, const T* c, 
   return cudaSuccess;
 }
 
+// PCR-pThomas for n = 32 * 16 (FP32) / 32 * 8 (FP64), contiguous layout,
+// on the persistent TMA-fed kernel; other shapes: pcr.cu.
+template <typename T>
+cudaError_t launch_pcr_tma(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                           cudaStream_t st, bool* used) {
+  *used = false;
+  constexpr int MP = sizeof(T) == 4 ? 16 : 8;
+  if (layout != CONTIG || n != 32 * MP) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  if (launch_wm_tma_m<CHUNK_PCR, T, MP, 32>(a, b, c, d, x, n, batch, st, &e)) *used = true;
+  return e;
+}
+
 template <typename T>
 cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                            cudaStream_t st, bool* used) {
@@ -524,6 +555,8 @@ cudaError_t launch_crpcr_warp(int layout, const T* a, const T* b, const T* c, co
 }
 
 #define INST(T)                                                                                                   \
+  template cudaError_t launch_pcr_tma<T>(int, const T*, const T*, const T*, const T*, T*, int, int, cudaStream_t, \
+                                         bool*);                                                                  \
   template cudaError_t launch_wm_warp<T>(int, const T*, const T*, const T*, const T*, T*, int, int, cudaStream_t, \
                                          bool*);                                                                  \
   template cudaError_t launch_crpcr_warp<T>(int, const T*, const T*, const T*, const T*, T*, int, int,            \

@@ -7,7 +7,8 @@ CASE: pge64 (partitioned pivoted solve, FP64, n = 4096 x 2048 non-dominant),
 pgc32 (cluster version, FP32, n = 65536 x 256 dominant), pge32 (FP32,
 n = 4096 x 4096 dominant), gtsv64 (thread-per-system pivoted sweep, FP64,
 n = 4096 x 1024), wmc32 (partition method without pivoting, FP32,
-n = 4096 x 4096 dominant), block2_64 (2 x 2 block systems, FP64, interleaved,
+n = 4096 x 4096 dominant), pcr32 (PCR-pThomas, FP32, n = 512 x 32768 dominant),
+block2_64 (2 x 2 block systems, FP64, interleaved,
 n = 256 x 32768: the pivoted solve, then block Thomas on dominant systems).
 Each solves its case three times.
 """
@@ -18,7 +19,7 @@ import torch
 import tridiagonalsolver_gb300 as T
 
 CASES = {"pge64": (4096, 2048, torch.float64, False), "pgc32": (65536, 256, torch.float32, True),
-         "wmc32": (4096, 4096, torch.float32, True),
+         "wmc32": (4096, 4096, torch.float32, True), "pcr32": (512, 32768, torch.float32, True),
          "pge32": (4096, 4096, torch.float32, True), "gtsv64": (4096, 1024, torch.float64, False)}
 
 
@@ -60,6 +61,8 @@ def main(case: str) -> None:
             T.gtsv(a, b, c, d, n, pivots=T.pivot_record(a, n), out=x)
         elif case == "wmc32":
             T.solve_out(a, b, c, d, n, algo="partition", out=x)
+        elif case == "pcr32":
+            T.solve_out(a, b, c, d, n, algo="pcr", out=x)
         else:
             T.pge(a, b, c, d, n, out=x)
     torch.cuda.synchronize()

@@ -676,7 +676,10 @@ def run_plain(args):
 
 
 def run_adjoint(args):
-    """Forward + adjoint, FP32, n = 1024 x 16384 dominant, loss = sum(w x)."""
+    """Forward + adjoint, FP32, n = 1024 x 16384 dominant, loss = sum(w x).
+    Main step: the unpivoted partition method (the reference's WM-pGE
+    eliminates without pivoting) forward and adjoint; the pivoted
+    partitioned solve and its adjoint are timed beside it as a part."""
     import torch
 
     import tridiagonalsolver_gb300 as T
@@ -697,18 +700,24 @@ def run_adjoint(args):
     grads = [torch.empty_like(d) for _ in range(4)]
     L = T.lib()
     stream = torch.cuda.Stream(device=dev)
-
-    def step():
-        sp = int(stream.cuda_stream)
-        T.check(L.tridiag_pge_single(0, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), None,
-                                     n, batch, sp), "pge")
-        T.check(L.tridiag_pge_adjoint_single(0, a.data_ptr(), b.data_ptr(), c.data_ptr(), x.data_ptr(),
-                                             w.data_ptr(), *[t.data_ptr() for t in grads], None, n, batch, sp),
-                "pge adjoint")
+    P = lambda t: t.data_ptr()
 
     def fwd():
-        T.check(L.tridiag_pge_single(0, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), None,
-                                     n, batch, int(stream.cuda_stream)), "pge")
+        T.check(L.tridiag_solve_out_single(7, 0, P(a), P(b), P(c), P(d), P(x), None, 0, n, batch,
+                                           int(stream.cuda_stream)), "partition")
+
+    def step():
+        fwd()
+        T.check(L.tridiag_partition_adjoint_single(0, P(a), P(b), P(c), P(x), P(w), *[P(t) for t in grads], n, batch,
+                                                   int(stream.cuda_stream)), "partition adjoint")
+
+    def fwd_piv():
+        T.check(L.tridiag_pge_single(0, P(a), P(b), P(c), P(d), P(x), None, n, batch, int(stream.cuda_stream)), "pge")
+
+    def step_piv():
+        fwd_piv()
+        T.check(L.tridiag_pge_adjoint_single(0, P(a), P(b), P(c), P(x), P(w), *[P(t) for t in grads], None, n, batch,
+                                             int(stream.cuda_stream)), "pge adjoint")
 
     sampler = ClockSampler(0)
     sampler.start()
@@ -719,11 +728,19 @@ def run_adjoint(args):
     clocks = sampler.stop()
     ms_f, _ = _graph_time(torch, stream, fwd, max(10, args.steps // 5), 3)
     idx = torch.arange(0, batch, batch // 16, device=dev)
-    hs = [t.index_select(0, idx).double().cpu().numpy() for t in (a, b, c, d, x, w)]
-    _, eta = O.backward_error(*hs[:5], n)
-    ref = O.adjoint_f64(hs[0], hs[1], hs[2], hs[4], hs[5], n)
-    gerr = max(float(np.max(np.abs(gg.index_select(0, idx).double().cpu().numpy() - r.reshape(16, n))) /
-                     np.max(np.abs(r))) for gg, r in zip(grads, ref))
+
+    def accuracy():
+        hs = [t.index_select(0, idx).double().cpu().numpy() for t in (a, b, c, d, x, w)]
+        _, eta = O.backward_error(*hs[:5], n)
+        ref = O.adjoint_f64(hs[0], hs[1], hs[2], hs[4], hs[5], n)
+        gerr = max(float(np.max(np.abs(gg.index_select(0, idx).double().cpu().numpy() - r.reshape(16, n))) /
+                         np.max(np.abs(r))) for gg, r in zip(grads, ref))
+        return eta, gerr
+
+    eta, gerr = accuracy()
+    ms_p, _ = _graph_time(torch, stream, step_piv, max(10, args.steps // 5), 3)
+    ms_pf, _ = _graph_time(torch, stream, fwd_piv, max(10, args.steps // 5), 3)
+    eta_p, gerr_p = accuracy()
     e2e = _e2e_generic(torch, stream, [a, b, c, d, w], [x] + grads, step, max(3, min(args.steps // 10, 10)), batch)
 
     def cpu(k):
@@ -737,12 +754,17 @@ def run_adjoint(args):
     rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, batch)
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                       "sample": f"{k} of {batch} systems forward+adjoint in {t:.2f} s (FP64 port)"}
+    bytes14 = 14 * n * batch * 4
     _line(args, "forward+adjoint FP32 WM-pGE n=1024 x 16384, dominant, loss=sum(w*x)", batch / (ms * 1e-3), ms,
-          "f32", {"n": n, "batch": batch, "dominant": "pge_kernel<float,128> forward + adjoint (transposed)",
+          "f32", {"n": n, "batch": batch, "dominant": "wmc_kernel<float,0> forward + wmc_kernel<float,1> adjoint",
+                  "algorithm": "partition method without pivoting (forward and transposed)",
                   "l2": "inputs larger than L2 (336 MB)"},
           [{"name": "forward", "ms_per_launch": ms_f, "backward_error_max": eta},
-           {"name": "adjoint", "ms_per_launch": ms - ms_f, "gradient_rel_err_vs_fp64": gerr}],
-          14 * n * batch * 4, ms, cpu_b, e2e, clocks, 2 * args.steps)
+           {"name": "adjoint", "ms_per_launch": ms - ms_f, "gradient_rel_err_vs_fp64": gerr},
+           {"name": "pivoted_forward_adjoint", "ms_per_step": ms_p, "forward_ms": ms_pf,
+            "hbm_gbs": round(bytes14 / (ms_p * 1e-3) / 1e9, 1), "backward_error_max": eta_p,
+            "gradient_rel_err_vs_fp64": gerr_p}],
+          bytes14, ms, cpu_b, e2e, clocks, 2 * args.steps)
 
 
 def run_ragged(args):

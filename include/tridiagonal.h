@@ -258,6 +258,21 @@ int tridiag_pge_adjoint_double(int layout, const double *a, const double *b, con
                                const double *xbar, double *ga, double *gb, double *gc, double *gd, int *info,
                                int n_eqt, int n_batch, void *stream);
 
+/* Adjoint through the unpivoted partition method (TRIDIAG_ALGO_PARTITION;
+ * no counterpart in the reference): solves A^T lambda = xbar with the
+ * partition kernel on the transposed coefficients and writes the gradients
+ * as tridiag_pge_adjoint_*.  Contiguous layout and the shapes
+ * TRIDIAG_ALGO_PARTITION covers (else TRIDIAG_ERR_NOT_SUPPORTED); systems that
+ * need no pivoting, as for the forward solve. */
+/* 1 if TRIDIAG_ALGO_PARTITION's CTA kernel covers (precision, layout, n). */
+int tridiag_partition_supported(int precision, int layout, int n_eqt);
+int tridiag_partition_adjoint_single(int layout, const float *a, const float *b, const float *c, const float *x,
+                                     const float *xbar, float *ga, float *gb, float *gc, float *gd, int n_eqt,
+                                     int n_batch, void *stream);
+int tridiag_partition_adjoint_double(int layout, const double *a, const double *b, const double *c,
+                                     const double *x, const double *xbar, double *ga, double *gb, double *gc,
+                                     double *gd, int n_eqt, int n_batch, void *stream);
+
 /* Ragged batches (no counterpart in the reference): n_batch systems of
  * different sizes packed back to back in a, b, c, d (and x): system s is
  * rows [offsets[s], offsets[s+1]) with 1 <= size <= 2^(TRIDIAG_RAGGED_CLASSES-1).

@@ -118,3 +118,51 @@ def test_auto_uses_partition_and_is_exact_same(cuda, dt):
     xp = T.solve_out(*ts, n, algo="partition").cpu().numpy()
     assert np.array_equal(xa, xp)
     _check(xa.astype(np.float64), a, b, c, d, dt, n)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("n,batch", [(256, 50), (1024, 33), (4096, 5)])
+def test_partition_adjoint_vs_oracle(cuda, dt, n, batch):
+    """Adjoint of the partition solve (A^T lambda = xbar and the gradients)
+    against the FP64 oracle adjoint: max |g - g_oracle| / max |g_oracle| <=
+    1e-12 (FP64) / 1e-5 (FP32), per gradient."""
+    import tridiagonalsolver_gb300 as T
+
+    if not T.partition_supported(cuda.zeros(1, dtype=cuda.float64 if dt == np.float64 else cuda.float32), n):
+        pytest.skip("shape outside the partition kernel")
+    a, b, c, d = inputs.dominant(n, batch, seed=n + 3)
+    w = np.random.default_rng(n).uniform(-1, 1, (batch, n))
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d, w)]
+    x = T.solve_out(*ts[:4], n, algo="partition")
+    grads = T.partition_adjoint(ts[0], ts[1], ts[2], x, ts[4], n)
+    h = [v.astype(dt).astype(np.float64) for v in (a, b, c)]
+    ref = O.adjoint_f64(*h, x.double().cpu().numpy(), w.astype(dt).astype(np.float64), n)
+    tol = 1e-12 if dt == np.float64 else 1e-5
+    for gg, r, name in zip(grads, ref, ("ga", "gb", "gc", "gd")):
+        g = gg.double().cpu().numpy().reshape(-1)
+        assert np.max(np.abs(g - r)) <= tol * np.max(np.abs(r)), name
+    # the boundary gradients vanish
+    assert float(grads[0].view(batch, n)[:, 0].abs().max()) == 0.0
+    assert float(grads[2].view(batch, n)[:, -1].abs().max()) == 0.0
+
+
+def test_partition_adjoint_unsupported_shape(cuda):
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import TridiagError
+
+    t = cuda.ones(1000 * 2, dtype=cuda.float32, device="cuda")
+    with pytest.raises(TridiagError):
+        T.partition_adjoint(t, t, t, t, t, 1000)
+
+
+def test_solve_ad_unpivoted_gradcheck(cuda):
+    """torch.autograd.gradcheck through the unpivoted partition method (FP64,
+    n = 128: the smallest shape the kernel covers)."""
+    import torch
+
+    from tridiagonalsolver_gb300 import solve_ad
+
+    n, batch = 128, 3
+    a, b, c, d = inputs.dominant(n, batch, seed=1)
+    ts = [torch.from_numpy(v).cuda().requires_grad_(True) for v in (a, b, c, d)]
+    assert torch.autograd.gradcheck(lambda *v: solve_ad(*v, pivoting=False), ts, eps=1e-6, atol=1e-5, rtol=1e-4)

@@ -85,6 +85,9 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_ragged_adjoint_double": (_I, [_P] * 13),
     "tridiag_pge_adjoint_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_pge_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_partition_supported": (_I, [_I, _I, _I]),
+    "tridiag_partition_adjoint_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "tridiag_partition_adjoint_double": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
 }
 # the reference's entry points: void f(T*, T*, T*, T*, int n_eqt, int n_batch)
 REFERENCE_SOLVERS = [

@@ -26,10 +26,18 @@ from ._lib import TridiagError
 
 class TridiagonalSolve(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, a, b, c, d, n, layout):
+    def forward(ctx, a, b, c, d, n, layout, pivoting=True):
         a, b, c, d = (t.contiguous() for t in (a, b, c, d))
-        method = "pge" if layout == "contiguous" else "gtsv"
+        if not pivoting and layout == "contiguous" and ops.partition_supported(a, n):
+            # the unpivoted partition method forward and adjoint (systems that
+            # need no pivoting, e.g. diagonally dominant)
+            method = "partition"
+        else:
+            method = "pge" if layout == "contiguous" else "gtsv"
         x = None
+        if method == "partition":
+            x = ops.solve_out(a, b, c, d, n, algo="partition")
+            ctx.save_for_backward(a, b, c, x)
         if method == "pge":
             # the partitioned solve: no pivot record, its adjoint is the same
             # solver on A^T
@@ -41,7 +49,7 @@ class TridiagonalSolve(torch.autograd.Function):
                 method = "gtsv"
         if method == "pge":
             ctx.save_for_backward(a, b, c, x)
-        else:
+        elif method == "gtsv":
             piv = ops.pivot_record(a, n, layout)
             work = ops.gtsv_workspace(a, n, layout)
             x = ops.gtsv(a, b, c, d, n, layout=layout, pivots=piv, work=work)
@@ -51,7 +59,10 @@ class TridiagonalSolve(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, xbar):
-        if ctx.method == "pge":
+        if ctx.method == "partition":
+            a, b, c, x = ctx.saved_tensors
+            ga, gb, gc, gd = ops.partition_adjoint(a, b, c, x, xbar.contiguous(), ctx.n)
+        elif ctx.method == "pge":
             a, b, c, x = ctx.saved_tensors
             ga, gb, gc, gd = ops.pge_adjoint(a, b, c, x, xbar.contiguous(), ctx.n, layout=ctx.layout)
         else:
@@ -60,14 +71,16 @@ class TridiagonalSolve(torch.autograd.Function):
                                               work=work)
         need = ctx.needs_input_grad
         return (ga if need[0] else None, gb if need[1] else None, gc if need[2] else None,
-                gd if need[3] else None, None, None)
+                gd if need[3] else None, None, None, None)
 
 
 def solve_ad(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor, d: torch.Tensor, n: int | None = None,
-             layout: str = "contiguous") -> torch.Tensor:
+             layout: str = "contiguous", pivoting: bool = True) -> torch.Tensor:
     """Differentiable batched solve.  ``a, b, c, d`` share one shape: (batch, n)
     for layout "contiguous" or (n, batch) for "interleaved"; ``n`` defaults to
-    the matching dimension."""
+    the matching dimension.  ``pivoting=False`` selects the unpivoted
+    partition method (forward and adjoint) where it covers the shape -- for
+    systems that need no pivoting, such as diagonally dominant ones."""
     if layout not in ("contiguous", "interleaved"):
         raise ValueError("solve_ad supports the contiguous and interleaved layouts")
     if not (a.shape == b.shape == c.shape == d.shape):
@@ -76,4 +89,4 @@ def solve_ad(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor, d: torch.Tensor,
         if a.dim() != 2:
             raise ValueError("pass n for flat tensors")
         n = a.shape[1] if layout == "contiguous" else a.shape[0]
-    return TridiagonalSolve.apply(a, b, c, d, n, layout)
+    return TridiagonalSolve.apply(a, b, c, d, n, layout, pivoting)

@@ -579,6 +579,36 @@ extern "C" int tridiag_pge_adjoint_double(int layout, const double* a, const dou
                                               (cudaStream_t)stream));
 }
 
+namespace {
+template <typename T>
+int partition_adjoint_entry(int layout, const T* a, const T* b, const T* c, const T* x, const T* xbar, T* ga, T* gb,
+                            T* gc, T* gd, int n, int batch, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout)) return TRIDIAG_ERR_INVALID_VALUE;
+  if (!a || !b || !c || !x || !xbar || !ga || !gb || !gc || !gd) return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout != TRIDIAG_LAYOUT_CONTIGUOUS) return TRIDIAG_ERR_NOT_SUPPORTED;
+  bool used = false;
+  cudaError_t e = tdg::launch_wmc_adjoint<T>(a, b, c, x, xbar, ga, gb, gc, gd, n, batch, s, &used);
+  if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_NOT_SUPPORTED;
+}
+}  // namespace
+
+extern "C" int tridiag_partition_supported(int precision, int layout, int n) {
+  return precision ? (int)tdg::wmc_eligible<double>(layout, n) : (int)tdg::wmc_eligible<float>(layout, n);
+}
+extern "C" int tridiag_partition_adjoint_single(int layout, const float* a, const float* b, const float* c,
+                                                const float* x, const float* xbar, float* ga, float* gb, float* gc,
+                                                float* gd, int n, int batch, void* stream) {
+  return set_status(
+      partition_adjoint_entry<float>(layout, a, b, c, x, xbar, ga, gb, gc, gd, n, batch, (cudaStream_t)stream));
+}
+extern "C" int tridiag_partition_adjoint_double(int layout, const double* a, const double* b, const double* c,
+                                                const double* x, const double* xbar, double* ga, double* gb,
+                                                double* gc, double* gd, int n, int batch, void* stream) {
+  return set_status(
+      partition_adjoint_entry<double>(layout, a, b, c, x, xbar, ga, gb, gc, gd, n, batch, (cudaStream_t)stream));
+}
+
 // ---------------------------------------------------------------------------
 // cuSPARSE-shaped entry points: the argument lists of cusparse?gtsv2StridedBatch
 // and cusparse?gtsvInterleavedBatch (the reference's vendor row,

@@ -59,6 +59,11 @@ bool wmc_eligible(int layout, int n);
 template <typename T>
 cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                        cudaStream_t s, bool* used);
+// wmc.cu: adjoint of the unpivoted partition solve (CONTIG): A^T lambda =
+// xbar and the gradients ga, gb, gc, gd = lambda.
+template <typename T>
+cudaError_t launch_wmc_adjoint(const T* a, const T* b, const T* c, const T* x, const T* xbar, T* ga, T* gb, T* gc,
+                               T* gd, int n, int batch, cudaStream_t s, bool* used);
 
 // wm.cu: PCR-pThomas on the persistent TMA-fed chunk kernel (CONTIG,
 // n = 512 FP32 / 256 FP64); *used is false for other shapes.

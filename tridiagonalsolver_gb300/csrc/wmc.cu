@@ -42,8 +42,10 @@ namespace tdg {
 
 constexpr int WMC_MAX_R = 256;
 
+// solve: a, b, c, d, x (PACKED: m[0] covers every array, x included);
+// adjoint: a, b, c, xbar, x, then the outputs ga, gb, gc, gd
 struct WmcMaps {
-  CUtensorMap m[5];  // a, b, c, d, x (PACKED: m[0] covers every array, x included)
+  CUtensorMap m[9];
 };
 
 template <typename T>
@@ -76,23 +78,36 @@ __host__ __device__ constexpr size_t wmc_array_bytes(int R) {
 }
 
 template <typename T>
-__host__ __device__ constexpr size_t wmc_smem_bytes(int R, int threads) {
-  return 1024 /* alignment slack */ + 4 * wmc_array_bytes<T>(R) + 8 * (size_t)threads * sizeof(T) + 16;
+__host__ __device__ constexpr size_t wmc_smem_bytes(int R, int threads, int arrays) {
+  return 1024 /* alignment slack */ + arrays * wmc_array_bytes<T>(R) + 8 * (size_t)threads * sizeof(T) + 16;
 }
 
+// element k of 128-byte row t of a staged array
 template <typename T>
+__device__ __forceinline__ T& wmc_elem(unsigned char* S, int t, int k) {
+  constexpr int NV = 16 / (int)sizeof(T);
+  return *reinterpret_cast<T*>(S + wmc_swz(t, k / NV) + (k % NV) * (int)sizeof(T));
+}
+
+// MODE 0: solve A x = d.  MODE 1 (adjoint of x = A^{-1} d for a loss with
+// dL/dx = xbar): solve A^T lambda = xbar -- A^T has sub-diagonal c_{i-1} and
+// super-diagonal a_{i+1}, formed in shared memory by a shift of the staged
+// c and a -- then write gd = lambda, ga_i = -lambda_i x_{i-1},
+// gb_i = -lambda_i x_i, gc_i = -lambda_i x_{i+1} (contiguous layout).
+template <typename T, int MODE>
 __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
                                                         int packed, int* err) {
   using W = WmcVec<T>;
   constexpr int NV = W::N;     // values per 16-byte unit
   constexpr int M = 8 * NV;    // rows per thread (128 bytes)
+  constexpr int NA = MODE == 1 ? 5 : 4;  // staged arrays
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const size_t ab = wmc_array_bytes<T>(R);
-  unsigned char* S[4] = {base, base + ab, base + 2 * ab, base + 3 * ab};
+  unsigned char* S[5] = {base, base + ab, base + 2 * ab, base + 3 * ab, base + 4 * ab};
   const int nt = blockDim.x;
-  T* red = reinterpret_cast<T*>(base + 4 * ab);  // 8 arrays of nt values
+  T* red = reinterpret_cast<T*>(base + NA * ab);  // 8 arrays of nt values
   T *ra = red, *rb = red + nt, *rc = red + 2 * nt, *rd = red + 3 * nt;
   T *xg = red + 4 * nt, *xp = red + 5 * nt, *xl = red + 6 * nt, *ys = red + 7 * nt;
   uint64_t* bar = reinterpret_cast<uint64_t*>(red + 8 * nt);
@@ -106,9 +121,9 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   }
   __syncthreads();
   if (t == 0) {
-    mbar_arrive_expect_tx(bar, 4u * (unsigned)R * 128u);
+    mbar_arrive_expect_tx(bar, (unsigned)NA * (unsigned)R * 128u);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < NA; ++k) {
       const CUtensorMap* mp = &maps.m[packed ? 0 : k];
       const int row = packed ? (j * 4 + k) * R : j * R;
       tma_load_2d(S[k], mp, 0, row, bar);
@@ -116,6 +131,37 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   }
   const bool ok = mbar_wait(bar, 0, err);
   if (!__syncthreads_and(ok)) return;
+
+  if constexpr (MODE == 1) {
+    // A^T: sub-diagonal c_{i-1} into the a slot, super-diagonal a_{i+1} into
+    // the c slot (the neighbours' boundary values are read before anyone
+    // writes)
+    const T cprev = (active && t > 0) ? wmc_elem<T>(S[2], t - 1, M - 1) : T(0);
+    const T anext = (active && t + 1 < R) ? wmc_elem<T>(S[0], t + 1, 0) : T(0);
+    __syncthreads();
+    if (active) {
+      T carry = cprev;
+      T av[NV], an[NV];
+      W::split(*reinterpret_cast<const typename W::V*>(S[0] + wmc_swz(t, 0)), av);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int off = wmc_swz(t, q);
+        if (q < 7) W::split(*reinterpret_cast<const typename W::V*>(S[0] + wmc_swz(t, q + 1)), an);
+        T cv[NV], sub[NV], sup[NV];
+        W::split(*reinterpret_cast<const typename W::V*>(S[2] + off), cv);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          sub[v] = v == 0 ? carry : cv[v - 1];
+          sup[v] = v + 1 < NV ? av[v + 1] : (q < 7 ? an[0] : anext);
+        }
+        carry = cv[NV - 1];
+        *reinterpret_cast<typename W::V*>(S[0] + off) = W::join(sub);
+        *reinterpret_cast<typename W::V*>(S[2] + off) = W::join(sup);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) av[v] = an[v];
+      }
+    }
+  }
 
   // ---- top-down elimination of the interior rows --------------------------
   T cp = T(0), dp = T(0), vp = T(0);  // c', d', v of the previous row
@@ -241,11 +287,48 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
       *reinterpret_cast<typename W::V*>(S[3] + off) = W::join(vd);
     }
   }
+  if constexpr (MODE == 1) {
+    // gradients: lambda (in the d slot) times the forward solution x
+    if (active) {
+      const T xprev = t > 0 ? wmc_elem<T>(S[4], t - 1, M - 1) : T(0);
+      const T xnext = t + 1 < R ? wmc_elem<T>(S[4], t + 1, 0) : T(0);
+      T carry = xprev;
+      T xv[NV], xn[NV];
+      W::split(*reinterpret_cast<const typename W::V*>(S[4] + wmc_swz(t, 0)), xv);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int off = wmc_swz(t, q);
+        if (q < 7) W::split(*reinterpret_cast<const typename W::V*>(S[4] + wmc_swz(t, q + 1)), xn);
+        T lam[NV], ga_[NV], gb_[NV], gc_[NV];
+        W::split(*reinterpret_cast<const typename W::V*>(S[3] + off), lam);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const int i = t * M + q * NV + v;
+          const T xl_ = v == 0 ? carry : xv[v - 1];
+          const T xr_ = v + 1 < NV ? xv[v + 1] : (q < 7 ? xn[0] : xnext);
+          ga_[v] = i > 0 ? -lam[v] * xl_ : T(0);
+          gb_[v] = -lam[v] * xv[v];
+          gc_[v] = i + 1 < n ? -lam[v] * xr_ : T(0);
+        }
+        carry = xv[NV - 1];
+        *reinterpret_cast<typename W::V*>(S[0] + off) = W::join(ga_);
+        *reinterpret_cast<typename W::V*>(S[1] + off) = W::join(gb_);
+        *reinterpret_cast<typename W::V*>(S[2] + off) = W::join(gc_);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) xv[v] = xn[v];
+      }
+    }
+  }
   fence_async_smem();
   __syncthreads();
   if (t == 0) {
-    const int row = packed ? (j * 4 + 3) * R : j * R;
-    tma_store_2d(&maps.m[packed ? 0 : 4], 0, row, S[3]);
+    if constexpr (MODE == 1) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) tma_store_2d(&maps.m[5 + k], 0, j * R, S[k]);
+    } else {
+      const int row = packed ? (j * 4 + 3) * R : j * R;
+      tma_store_2d(&maps.m[packed ? 0 : 4], 0, row, S[3]);
+    }
     bulk_commit();
     bulk_wait_read<0>();
   }
@@ -284,15 +367,44 @@ cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* 
         return cudaSuccess;
   }
   const int threads = (R + 31) / 32 * 32;
-  const size_t smem = wmc_smem_bytes<T>(R, threads);
-  cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = wmc_smem_bytes<T>(R, threads, 4);
+  cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  wmc_kernel<T><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word());
+  wmc_kernel<T, 0><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word());
   e = cudaGetLastError();
   if (e == cudaSuccess) *used = true;
   return e;
 }
 
+template <typename T>
+cudaError_t launch_wmc_adjoint(const T* a, const T* b, const T* c, const T* x, const T* xbar, T* ga, T* gb, T* gc,
+                               T* gd, int n, int batch, cudaStream_t s, bool* used) {
+  *used = false;
+  if (!wmc_eligible<T>(CONTIG, n) || batch <= 0) return cudaSuccess;
+  constexpr int M = 128 / (int)sizeof(T);
+  const int R = n / M;
+  const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  WmcMaps maps;
+  const T* ptrs[9] = {a, b, c, xbar, x, ga, gb, gc, gd};
+  for (int k = 0; k < 9; ++k)
+    if (!encode_tmap_2d(&maps.m[k], ptrs[k], dt, sizeof(T), (uint64_t)M, (uint64_t)R * (uint64_t)batch, 128, M, R,
+                        CU_TENSOR_MAP_SWIZZLE_128B))
+      return cudaSuccess;
+  const int threads = (R + 31) / 32 * 32;
+  const size_t smem = wmc_smem_bytes<T>(R, threads, 5);
+  cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  wmc_kernel<T, 1><<<batch, threads, smem, s>>>(maps, n, R, 0, error_word());
+  e = cudaGetLastError();
+  if (e == cudaSuccess) *used = true;
+  return e;
+}
+
+template cudaError_t launch_wmc_adjoint<float>(const float*, const float*, const float*, const float*, const float*,
+                                               float*, float*, float*, float*, int, int, cudaStream_t, bool*);
+template cudaError_t launch_wmc_adjoint<double>(const double*, const double*, const double*, const double*,
+                                                const double*, double*, double*, double*, double*, int, int,
+                                                cudaStream_t, bool*);
 template bool wmc_eligible<float>(int, int);
 template bool wmc_eligible<double>(int, int);
 template cudaError_t launch_wmc<float>(int, const float*, const float*, const float*, const float*, float*, int, int,

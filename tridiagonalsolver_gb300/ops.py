@@ -170,6 +170,26 @@ def pge_adjoint(a, b, c, x, xbar, n: int, layout: str = "contiguous", info=None,
     return ga, gb, gc, gd
 
 
+def partition_supported(a, n: int, layout: str = "contiguous") -> bool:
+    """Whether TRIDIAG_ALGO_PARTITION's CTA kernel covers (dtype of a, n, layout)."""
+    return bool(lib().tridiag_partition_supported(1 if a.dtype == torch.float64 else 0, LAYOUTS[layout], n))
+
+
+def partition_adjoint(a, b, c, x, xbar, n: int, stream=None):
+    """Gradients (ga, gb, gc, gd) of L with dL/dx = xbar through x = A^-1 d by
+    the unpivoted partition method on A^T (contiguous layout; systems that
+    need no pivoting)."""
+    p = _prec(a)
+    batch = _dims(a, n, "contiguous")
+    a, b, c, x, xbar = _al(a), _al(b), _al(c), _al(x), _al(xbar)
+    ga, gb, gc, gd = (torch.empty_like(a) for _ in range(4))
+    st = getattr(lib(), f"tridiag_partition_adjoint_{p}")(
+        LAYOUTS["contiguous"], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), _ptr(x, a.dtype),
+        _ptr(xbar, a.dtype), _ptr(ga), _ptr(gb), _ptr(gc), _ptr(gd), n, batch, _stream_ptr(stream))
+    check(st, f"tridiag_partition_adjoint_{p}")
+    return ga, gb, gc, gd
+
+
 class Factorization:
     """Partial-pivoting factors of a batch (LAPACK ?gttrf algorithm); solve
     any number of right-hand sides, transposed or not, with :meth:`solve`."""

@@ -222,6 +222,14 @@ size_t tridiag_refine_workspace_size(int layout, int n_eqt, int n_batch);
 int tridiag_refine_double(int layout, const double *a, const double *b, const double *c, const double *d,
                           double *x, int iters, int *info, void *work, size_t work_bytes, int n_eqt, int n_batch,
                           void *stream);
+/* The same with a choice of FP32 solver: TRIDIAG_ALGO_GTSV (or AUTO; partial
+ * pivoting, as tridiag_refine_double) or TRIDIAG_ALGO_PARTITION (the
+ * unpivoted partition method, for systems that need no pivoting such as
+ * diagonally dominant ones; contiguous layout where its kernels cover the
+ * shape, else the Thomas sweep; info is set to 0). */
+int tridiag_refine_ex_double(int algo, int layout, const double *a, const double *b, const double *c,
+                             const double *d, double *x, int iters, int *info, void *work, size_t work_bytes,
+                             int n_eqt, int n_batch, void *stream);
 
 /* FP64 -> FP32 narrowing (round to nearest even) and FP32 -> FP64 widening
  * as the refined solve performs them on the integer pipe: out[k] = (float)

@@ -78,10 +78,11 @@ def test_partition_ignores_a0_and_clast(cuda, dt):
     assert np.array_equal(x0, x1)
 
 
-@pytest.mark.parametrize("dt,n", [(np.float32, 1000), (np.float32, 8224), (np.float64, 100), (np.float64, 4112),
+@pytest.mark.parametrize("dt,n", [(np.float32, 1000), (np.float32, 8200), (np.float64, 100), (np.float64, 4100),
                                   (np.float32, 3000)])
 def test_partition_other_shapes_fall_back(cuda, dt, n):
-    """Shapes outside the CTA kernel's range are solved by the Thomas sweep."""
+    """Shapes the partition kernels do not cover (n not a multiple of the
+    128-byte row) are solved by the Thomas sweep."""
     import tridiagonalsolver_gb300 as T
 
     batch = 6
@@ -166,3 +167,43 @@ def test_solve_ad_unpivoted_gradcheck(cuda):
     a, b, c, d = inputs.dominant(n, batch, seed=1)
     ts = [torch.from_numpy(v).cuda().requires_grad_(True) for v in (a, b, c, d)]
     assert torch.autograd.gradcheck(lambda *v: solve_ad(*v, pivoting=False), ts, eps=1e-6, atol=1e-5, rtol=1e-4)
+
+
+@pytest.mark.parametrize("dt,n", [(np.float32, 8224), (np.float32, 20000), (np.float32, 65536),
+                                  (np.float64, 4112), (np.float64, 12288), (np.float64, 65536)])
+def test_partition_long_systems(cuda, dt, n):
+    """Systems beyond one CTA: chunks per CTA, the separators' system, chunks
+    again (last chunk shorter for 8224, 20000, 4112)."""
+    import tridiagonalsolver_gb300 as T
+
+    assert T.lib().tridiag_partition_supported(1 if dt == np.float64 else 0, 0, n) == 0
+    batch = 3
+    a, b, c, d = inputs.dominant(n, batch, seed=n % 1000)
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d)]
+    x = T.solve_out(*ts, n, algo="partition").double().cpu().numpy()
+    _check(x, a, b, c, d, dt, n)
+    xa = T.solve_out(*ts, n, algo="auto").double().cpu().numpy()
+    assert np.array_equal(x, xa)
+    T.solve(*ts, n, algo="partition")
+    assert np.array_equal(ts[3].double().cpu().numpy(), x)
+
+
+@pytest.mark.parametrize("delta", [1.0, 1e-6])
+def test_refine_with_partition_solves(cuda, delta):
+    """Refined solve with unpivoted FP32 partition solves on the refined
+    workload's distribution (diagonally dominant by construction): backward
+    error <= 1e-12 after two steps, as the pivoted version."""
+    import tridiagonalsolver_gb300 as T
+
+    n, batch = 65536, 4
+    rng = np.random.default_rng(7)
+    a, c, d = (rng.uniform(-1, 1, (batch, n)) for _ in range(3))
+    a[:, 0] = 0
+    c[:, -1] = 0
+    s_ = np.where(rng.uniform(-1, 1, (batch, n)) >= 0, 1.0, -1.0)
+    b = s_ * (1 + delta) * (np.abs(a) + np.abs(c))
+    b[b == 0] = 1.0
+    ts = [cuda.from_numpy(v).cuda() for v in (a, b, c, d)]
+    x = T.refine(*ts, n, iters=2, algo="partition").cpu().numpy()
+    _, eta = O.backward_error(a, b, c, d, x, n)
+    assert eta <= 1e-12

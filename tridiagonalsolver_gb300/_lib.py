@@ -53,6 +53,7 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_gtsv_noalloc_double": (_I, [_I, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_refine_workspace_size": (_SZ, [_I, _I, _I]),
     "tridiag_refine_double": (_I, [_I, _P, _P, _P, _P, _P, _I, _P, _P, _SZ, _I, _I, _P]),
+    "tridiag_refine_ex_double": (_I, [_I] + [_I, _P, _P, _P, _P, _P, _I, _P, _P, _SZ, _I, _I, _P]),
     "tridiag_convert_check": (_I, [_P, _P, _P, _SZ, _P]),
     "tridiag_partition_fallbacks": (ctypes.c_longlong, [_I]),
     "tridiag_pge_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),

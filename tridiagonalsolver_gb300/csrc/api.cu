@@ -123,11 +123,24 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
   packed_ptrs(layout, a, b, c, d, n);
   if (!b || !c || !d) return TRIDIAG_ERR_INVALID_VALUE;
   if (algo == TRIDIAG_ALGO_AUTO)
-    algo = (n > 1024 && tdg::wmc_eligible<T>(layout, n)) ? TRIDIAG_ALGO_PARTITION : TRIDIAG_ALGO_THOMAS;
+    algo = (n > 1024 && (tdg::wmc_eligible<T>(layout, n) || tdg::wml_eligible<T>(layout, n)))
+               ? TRIDIAG_ALGO_PARTITION
+               : TRIDIAG_ALGO_THOMAS;
   switch (algo) {
     case TRIDIAG_ALGO_PARTITION: {
       bool used = false;
       cudaError_t e = tdg::launch_wmc<T>(layout, a, b, c, d, d, n, batch, s, &used);
+      if (e == cudaSuccess && !used && tdg::wml_eligible<T>(layout, n)) {
+        // long systems: the chunked kernels with a stream-ordered workspace
+        const size_t bytes = tdg::wml_workspace_bytes<T>(n, batch);
+        void* work = nullptr;
+        e = cudaMallocAsync(&work, bytes, s);
+        if (e == cudaSuccess) {
+          e = tdg::launch_wml<T>(a, b, c, d, d, n, batch, work, bytes, s, &used);
+          const cudaError_t ef = cudaFreeAsync(work, s);
+          if (e == cudaSuccess) e = ef;
+        }
+      }
       if (e == cudaSuccess && !used) {
         e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
         if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
@@ -195,13 +208,16 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
   if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !b || !c || !d || !x) return TRIDIAG_ERR_INVALID_VALUE;
   if (layout == TRIDIAG_LAYOUT_PACKED) return TRIDIAG_ERR_NOT_SUPPORTED;
   if (algo == TRIDIAG_ALGO_AUTO)
-    algo = (n > 1024 && tdg::wmc_eligible<T>(layout, n)) ? TRIDIAG_ALGO_PARTITION : TRIDIAG_ALGO_WM;
+    algo = (n > 1024 && (tdg::wmc_eligible<T>(layout, n) || tdg::wml_eligible<T>(layout, n)))
+               ? TRIDIAG_ALGO_PARTITION
+               : TRIDIAG_ALGO_WM;
   if (work_bytes < solve_out_ws<T>(algo, n, batch) || (solve_out_ws<T>(algo, n, batch) && !work))
     return TRIDIAG_ERR_WORKSPACE;
   switch (algo) {
     case TRIDIAG_ALGO_PARTITION: {
       bool used = false;
       cudaError_t e = tdg::launch_wmc<T>(layout, a, b, c, d, x, n, batch, s, &used);
+      if (e == cudaSuccess && !used) e = tdg::launch_wml<T>(a, b, c, d, x, n, batch, work, work_bytes, s, &used);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       if (!work || work_bytes < solve_out_ws<T>(TRIDIAG_ALGO_THOMAS, n, batch)) return TRIDIAG_ERR_WORKSPACE;
@@ -287,7 +303,28 @@ RefineWs carve_refine(void* work, int n, int batch) {
   return w;
 }
 
-int refine_impl(int layout, const double* a, const double* b, const double* c, const double* d, double* x,
+// The FP32 solve of the refined solve, in place in v: pivoted (GTSV) or the
+// unpivoted partition method (PARTITION; the Thomas sweep where neither of
+// its kernels covers the shape).
+int refine_solve32(int algo, int layout, float* a32, float* b32, float* c32, float* v, int* info, void* gws,
+                   size_t gws_bytes, int n, int batch, cudaStream_t s) {
+  if (algo != TRIDIAG_ALGO_PARTITION)
+    return gtsv_impl<float>(layout, a32, b32, c32, v, nullptr, info, gws, gws_bytes, n, batch, s);
+  bool used = false;
+  cudaError_t e = tdg::launch_wmc<float>(layout, a32, b32, c32, v, v, n, batch, s, &used);
+  if (e == cudaSuccess && !used) e = tdg::launch_wml<float>(a32, b32, c32, v, v, n, batch, gws, gws_bytes, s, &used);
+  if (e == cudaSuccess && !used) {
+    // Thomas clobbers c: work on a copy (gws holds at least 2 n batch floats)
+    float* cs = static_cast<float*>(gws);
+    e = cudaMemcpyAsync(cs, c32, (size_t)n * batch * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = tdg::launch_thomas_tw<float>(layout, a32, b32, cs, v, n, batch, s, &used);
+    if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<float>(layout, a32, b32, cs, v, n, batch, s);
+  }
+  if (info && e == cudaSuccess) e = cudaMemsetAsync(info, 0, (size_t)batch * sizeof(int), s);
+  return cuda_status(e);
+}
+
+int refine_impl(int algo, int layout, const double* a, const double* b, const double* c, const double* d, double* x,
                 int iters, int* info, void* work, size_t work_bytes, int n, int batch, cudaStream_t s) {
   if (!valid_dims(n, batch) || !a || !b || !c || !d || !x || iters < 0 || iters > 8)
     return TRIDIAG_ERR_INVALID_VALUE;
@@ -297,8 +334,8 @@ int refine_impl(int layout, const double* a, const double* b, const double* c, c
   RefineWs w = carve_refine(work, n, batch);
   // FP32 copies; v0 <- d
   if (tdg::launch_narrow4(a, b, c, d, w.a32, w.b32, w.c32, w.v0, elems, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
-  // x0: FP32 pivoted solve in place in v0
-  int st = gtsv_impl<float>(layout, w.a32, w.b32, w.c32, w.v0, nullptr, info, w.gws, w.gws_bytes, n, batch, s);
+  // x0: FP32 solve in place in v0
+  int st = refine_solve32(algo, layout, w.a32, w.b32, w.c32, w.v0, info, w.gws, w.gws_bytes, n, batch, s);
   if (st != TRIDIAG_SUCCESS) return st;
   // The iterate lives in FP64 (x or w64, alternating so that the last step
   // lands in x); dx holds the latest FP32 solution or correction.
@@ -310,7 +347,7 @@ int refine_impl(int layout, const double* a, const double* b, const double* c, c
     double* xnew = xs[it % 2];
     if (tdg::launch_residual(layout, a, b, c, d, xcur, dx, xnew, spare, n, batch, s) != cudaSuccess)
       return TRIDIAG_ERR_CUDA;
-    st = gtsv_impl<float>(layout, w.a32, w.b32, w.c32, spare, nullptr, nullptr, w.gws, w.gws_bytes, n, batch, s);
+    st = refine_solve32(algo, layout, w.a32, w.b32, w.c32, spare, nullptr, w.gws, w.gws_bytes, n, batch, s);
     if (st != TRIDIAG_SUCCESS) return st;
     xcur = xnew;
     float* t = dx;
@@ -506,7 +543,17 @@ size_t tridiag_refine_workspace_size(int layout, int n, int batch) {
 int tridiag_refine_double(int layout, const double* a, const double* b, const double* c, const double* d,
                           double* x, int iters, int* info, void* work, size_t work_bytes, int n, int batch,
                           void* stream) {
-  return set_status(refine_impl(layout, a, b, c, d, x, iters, info, work, work_bytes, n, batch,
+  return set_status(refine_impl(TRIDIAG_ALGO_GTSV, layout, a, b, c, d, x, iters, info, work, work_bytes, n, batch,
+                                (cudaStream_t)stream));
+}
+
+int tridiag_refine_ex_double(int algo, int layout, const double* a, const double* b, const double* c,
+                             const double* d, double* x, int iters, int* info, void* work, size_t work_bytes, int n,
+                             int batch, void* stream) {
+  if (algo != TRIDIAG_ALGO_GTSV && algo != TRIDIAG_ALGO_PARTITION && algo != TRIDIAG_ALGO_AUTO)
+    return set_status(TRIDIAG_ERR_INVALID_VALUE);
+  if (algo == TRIDIAG_ALGO_AUTO) algo = TRIDIAG_ALGO_GTSV;
+  return set_status(refine_impl(algo, layout, a, b, c, d, x, iters, info, work, work_bytes, n, batch,
                                 (cudaStream_t)stream));
 }
 

@@ -59,6 +59,18 @@ bool wmc_eligible(int layout, int n);
 template <typename T>
 cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                        cudaStream_t s, bool* used);
+// wmc.cu: the same method for long systems (CONTIG, n a multiple of
+// 128 / sizeof(T) beyond one CTA's reach): chunks per CTA, the separators'
+// system by the single-CTA kernel, chunks again; `work` of
+// wml_workspace_bytes().  *used is false when not covered.
+template <typename T>
+bool wml_eligible(int layout, int n);
+template <typename T>
+size_t wml_workspace_bytes(int n, int batch);
+template <typename T>
+cudaError_t launch_wml(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch, void* work,
+                       size_t work_bytes, cudaStream_t s, bool* used);
+
 // wmc.cu: adjoint of the unpivoted partition solve (CONTIG): A^T lambda =
 // xbar and the gradients ga, gb, gc, gd = lambda.
 template <typename T>

@@ -43,9 +43,23 @@ namespace tdg {
 constexpr int WMC_MAX_R = 256;
 
 // solve: a, b, c, d, x (PACKED: m[0] covers every array, x included);
-// adjoint: a, b, c, xbar, x, then the outputs ga, gb, gc, gd
+// adjoint: a, b, c, xbar, x, then the outputs ga, gb, gc, gd; chunked
+// solve: a, b, c, d, x with boxes of the full chunk, then the same five with
+// boxes of the last (shorter) chunk
 struct WmcMaps {
-  CUtensorMap m[9];
+  CUtensorMap m[10];
+};
+
+// Chunked solve of long systems (MODE 2 / 3): a system of Rt partitions is
+// cut into chunks of Rfull partitions (the last one Rlast); MODE 2 writes
+// each partition's relations (WMC_REL values) to rel, MODE 3 reads the
+// separators' solution y (Ppad values per system) and substitutes back.
+constexpr int WMC_REL = 10;
+template <typename T>
+struct WmcChunk {
+  int nchunks, Rfull, Rlast, Rt, Ppad;
+  T* rel;
+  const T* ysol;
 };
 
 template <typename T>
@@ -94,9 +108,11 @@ __device__ __forceinline__ T& wmc_elem(unsigned char* S, int t, int k) {
 // super-diagonal a_{i+1}, formed in shared memory by a shift of the staged
 // c and a -- then write gd = lambda, ga_i = -lambda_i x_{i-1},
 // gb_i = -lambda_i x_i, gc_i = -lambda_i x_{i+1} (contiguous layout).
+// MODE 2 / 3: one chunk of a long system per CTA (see WmcChunk); the
+// separators' system between them is solved by a MODE 0 launch.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
-                                                        int packed, int* err) {
+                                                        int packed, int* err, const WmcChunk<T> ck) {
   using W = WmcVec<T>;
   constexpr int NV = W::N;     // values per 16-byte unit
   constexpr int M = 8 * NV;    // rows per thread (128 bytes)
@@ -112,20 +128,26 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   T *xg = red + 4 * nt, *xp = red + 5 * nt, *xl = red + 6 * nt, *ys = red + 7 * nt;
   uint64_t* bar = reinterpret_cast<uint64_t*>(red + 8 * nt);
 
-  const int j = blockIdx.x;
+  constexpr bool CHUNKED = MODE >= 2;
+  const int j = CHUNKED ? (int)(blockIdx.x / ck.nchunks) : (int)blockIdx.x;
+  const int ch = CHUNKED ? (int)(blockIdx.x % ck.nchunks) : 0;
+  const bool last_chunk = !CHUNKED || ch == ck.nchunks - 1;
+  const int Rc = CHUNKED && last_chunk ? ck.Rlast : R;     // partitions of this CTA
+  const int mset = CHUNKED && last_chunk && ck.Rlast != R ? 5 : 0;
+  const int row0 = CHUNKED ? j * ck.Rt + ch * R : j * R;  // first 128-byte row (non-packed)
   const int t = threadIdx.x;
-  const bool active = t < R;
+  const bool active = t < Rc;
   if (t == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
   if (t == 0) {
-    mbar_arrive_expect_tx(bar, (unsigned)NA * (unsigned)R * 128u);
+    mbar_arrive_expect_tx(bar, (unsigned)NA * (unsigned)Rc * 128u);
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
-      const CUtensorMap* mp = &maps.m[packed ? 0 : k];
-      const int row = packed ? (j * 4 + k) * R : j * R;
+      const CUtensorMap* mp = &maps.m[packed ? 0 : mset + k];
+      const int row = packed ? (j * 4 + k) * R : row0;
       tma_load_2d(S[k], mp, 0, row, bar);
     }
   }
@@ -179,7 +201,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         const int k = q * NV + v;
-        const T a = (t == 0 && k == 0) ? T(0) : va[v];  // a_0 is not read
+        const T a = (ch == 0 && t == 0 && k == 0) ? T(0) : va[v];  // a_0 is not read
         if (k < M - 1) {
           const T den = k == 0 ? vb[v] : fma(-a, cp, vb[v]);
           const T r = Div<T>(den).inv();
@@ -204,7 +226,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
         } else {
           sa = a;
           sb = vb[v];
-          sc = (t == R - 1) ? T(0) : vc[v];  // c_{n-1} is not read
+          sc = (last_chunk && t == Rc - 1) ? T(0) : vc[v];  // c_{n-1} is not read
           sd = vd[v];
         }
       }
@@ -216,8 +238,26 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
     xp[t] = P;
     xl[t] = L;
   }
+  if constexpr (MODE == 2) {
+    // the partition's relations for the separators' system
+    if (active) {
+      T* o = ck.rel + ((size_t)j * ck.Rt + (size_t)ch * R + t) * WMC_REL;
+      o[0] = G;
+      o[1] = P;
+      o[2] = L;
+      o[3] = vp;
+      o[4] = cp;
+      o[5] = dp;
+      o[6] = sa;
+      o[7] = sb;
+      o[8] = sc;
+      o[9] = sd;
+    }
+    return;
+  }
   __syncthreads();
   // ---- the separators' tridiagonal system ---------------------------------
+  if constexpr (MODE != 3) {
   T al = T(0), be = T(1), ga = T(0), de = T(0);
   if (active) {
     const T Gn = t + 1 < R ? xg[t + 1] : T(0);
@@ -261,11 +301,19 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
     __syncthreads();
   }
   if (active) ys[t] = de * Div<T>(be).inv();
+  }
+  if constexpr (MODE == 3) {
+    if (active) {
+      const size_t g = (size_t)j * ck.Ppad + (size_t)ch * R + t;
+      ys[t] = ck.ysol[g];
+      xl[t] = (ch > 0 || t > 0) ? ck.ysol[g - 1] : T(0);
+    }
+  }
   __syncthreads();
   // ---- bottom-up substitution ---------------------------------------------
   if (active) {
     const T y = ys[t];
-    const T yl = t > 0 ? ys[t - 1] : T(0);
+    const T yl = MODE == 3 ? xl[t] : (t > 0 ? ys[t - 1] : T(0));
     T xn = y;
 #pragma unroll
     for (int q = 7; q >= 0; --q) {
@@ -326,8 +374,8 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
 #pragma unroll
       for (int k = 0; k < 4; ++k) tma_store_2d(&maps.m[5 + k], 0, j * R, S[k]);
     } else {
-      const int row = packed ? (j * 4 + 3) * R : j * R;
-      tma_store_2d(&maps.m[packed ? 0 : 4], 0, row, S[3]);
+      const int row = packed ? (j * 4 + 3) * R : row0;
+      tma_store_2d(&maps.m[packed ? 0 : mset + 4], 0, row, S[3]);
     }
     bulk_commit();
     bulk_wait_read<0>();
@@ -370,7 +418,7 @@ cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* 
   const size_t smem = wmc_smem_bytes<T>(R, threads, 4);
   cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  wmc_kernel<T, 0><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word());
+  wmc_kernel<T, 0><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word(), WmcChunk<T>{});
   e = cudaGetLastError();
   if (e == cudaSuccess) *used = true;
   return e;
@@ -394,7 +442,7 @@ cudaError_t launch_wmc_adjoint(const T* a, const T* b, const T* c, const T* x, c
   const size_t smem = wmc_smem_bytes<T>(R, threads, 5);
   cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  wmc_kernel<T, 1><<<batch, threads, smem, s>>>(maps, n, R, 0, error_word());
+  wmc_kernel<T, 1><<<batch, threads, smem, s>>>(maps, n, R, 0, error_word(), WmcChunk<T>{});
   e = cudaGetLastError();
   if (e == cudaSuccess) *used = true;
   return e;
@@ -405,6 +453,124 @@ template cudaError_t launch_wmc_adjoint<float>(const float*, const float*, const
 template cudaError_t launch_wmc_adjoint<double>(const double*, const double*, const double*, const double*,
                                                 const double*, double*, double*, double*, double*, int, int,
                                                 cudaStream_t, bool*);
+// ---------------------------------------------------------------------------
+// Long systems: chunks of WMC_MAX_R partitions per CTA (MODE 2), the
+// separators' system (one row per partition, padded to a shape the
+// single-CTA kernel covers) assembled and solved by MODE 0, then the chunks
+// again (MODE 3).  Traffic: the four inputs twice, x once, plus ~14 values
+// per partition of workspace.
+
+template <typename T>
+static int wml_ppad(int Rt) {
+  constexpr int M = 128 / (int)sizeof(T);
+  int p = (Rt + M - 1) / M * M;
+  return p < 8 * M ? 8 * M : p;
+}
+
+template <typename T>
+bool wml_eligible(int layout, int n) {
+  constexpr int M = 128 / (int)sizeof(T);
+  if (layout != CONTIG || n % M != 0) return false;
+  const int Rt = n / M;
+  return Rt > WMC_MAX_R && wml_ppad<T>(Rt) <= WMC_MAX_R * M;
+}
+
+template <typename T>
+size_t wml_workspace_bytes(int n, int batch) {
+  constexpr int M = 128 / (int)sizeof(T);
+  const int Rt = n / M;
+  const size_t rel = ((size_t)WMC_REL * Rt * batch * sizeof(T) + 255) / 256 * 256;
+  const size_t red = ((size_t)wml_ppad<T>(Rt) * batch * sizeof(T) + 255) / 256 * 256;
+  return rel + 4 * red;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) wml_assemble(const T* __restrict__ rel, T* al, T* be, T* ga, T* de, int Rt,
+                                                    int Ppad, int batch) {
+  const size_t total = (size_t)Ppad * (size_t)batch;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t j = idx / (size_t)Ppad;
+    const int p = (int)(idx % (size_t)Ppad);
+    T a_ = T(0), b_ = T(1), g_ = T(0), d_ = T(0);
+    if (p < Rt) {
+      const T* o = rel + (j * Rt + p) * WMC_REL;
+      const T* on = o + WMC_REL;
+      const bool nx = p + 1 < Rt;
+      const T Gn = nx ? on[0] : T(0), Pn = nx ? on[1] : T(0), Ln = nx ? on[2] : T(0);
+      const T vL = o[3], cL = o[4], dL = o[5], sa = o[6], sb = o[7], sc = o[8], sd = o[9];
+      a_ = -sa * vL;
+      b_ = fma(-sc, Ln, fma(-sa, cL, sb));
+      g_ = sc * Pn;
+      d_ = fma(-sc, Gn, fma(-sa, dL, sd));
+    }
+    al[idx] = a_;
+    be[idx] = b_;
+    ga[idx] = g_;
+    de[idx] = d_;
+  }
+}
+
+template <typename T>
+cudaError_t launch_wml(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch, void* work,
+                       size_t work_bytes, cudaStream_t s, bool* used) {
+  *used = false;
+  if (!wml_eligible<T>(CONTIG, n) || batch <= 0 || !work || work_bytes < wml_workspace_bytes<T>(n, batch))
+    return cudaSuccess;
+  constexpr int M = 128 / (int)sizeof(T);
+  const int Rt = n / M, R = WMC_MAX_R;
+  const int nchunks = (Rt + R - 1) / R;
+  const int Rlast = Rt - (nchunks - 1) * R;
+  const int Ppad = wml_ppad<T>(Rt);
+  const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  WmcMaps maps;
+  const T* ptrs[5] = {a, b, c, d, x};
+  for (int set = 0; set < (Rlast != R ? 2 : 1); ++set)
+    for (int k = 0; k < 5; ++k)
+      if (!encode_tmap_2d(&maps.m[set * 5 + k], ptrs[k], dt, sizeof(T), (uint64_t)M, (uint64_t)Rt * (uint64_t)batch,
+                          128, M, set ? Rlast : R, CU_TENSOR_MAP_SWIZZLE_128B))
+        return cudaSuccess;
+  char* p = static_cast<char*>(work);
+  T* rel = reinterpret_cast<T*>(p);
+  p += ((size_t)WMC_REL * Rt * batch * sizeof(T) + 255) / 256 * 256;
+  const size_t red = ((size_t)Ppad * batch * sizeof(T) + 255) / 256 * 256;
+  T* ra = reinterpret_cast<T*>(p);
+  T* rb = reinterpret_cast<T*>(p + red);
+  T* rc = reinterpret_cast<T*>(p + 2 * red);
+  T* rd = reinterpret_cast<T*>(p + 3 * red);
+  const size_t smem = wmc_smem_bytes<T>(R, R, 4);
+  cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(wmc_kernel<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)nchunks * (unsigned)batch;
+  WmcChunk<T> ck{nchunks, R, Rlast, Rt, Ppad, rel, rd};
+  wmc_kernel<T, 2><<<grid, R, smem, s>>>(maps, n, R, 0, error_word(), ck);
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t total = (size_t)Ppad * batch;
+  const unsigned ag = (unsigned)((total + 255) / 256 < (size_t)sms * 8 ? (total + 255) / 256 : (size_t)sms * 8);
+  wml_assemble<T><<<ag, 256, 0, s>>>(rel, ra, rb, rc, rd, Rt, Ppad, batch);
+  bool inner = false;
+  e = launch_wmc<T>(CONTIG, ra, rb, rc, rd, rd, Ppad, batch, s, &inner);
+  if (e != cudaSuccess) return e;
+  if (!inner) return cudaErrorInvalidConfiguration;
+  wmc_kernel<T, 3><<<grid, R, smem, s>>>(maps, n, R, 0, error_word(), ck);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) *used = true;
+  return e;
+}
+
+template bool wml_eligible<float>(int, int);
+template bool wml_eligible<double>(int, int);
+template size_t wml_workspace_bytes<float>(int, int);
+template size_t wml_workspace_bytes<double>(int, int);
+template cudaError_t launch_wml<float>(const float*, const float*, const float*, const float*, float*, int, int,
+                                       void*, size_t, cudaStream_t, bool*);
+template cudaError_t launch_wml<double>(const double*, const double*, const double*, const double*, double*, int,
+                                        int, void*, size_t, cudaStream_t, bool*);
+
 template bool wmc_eligible<float>(int, int);
 template bool wmc_eligible<double>(int, int);
 template cudaError_t launch_wmc<float>(int, const float*, const float*, const float*, const float*, float*, int, int,

@@ -287,20 +287,22 @@ def refine_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> tor
 
 
 def refine(a, b, c, d, n: int, iters: int = 2, layout: str = "contiguous", info=None, work=None, out=None,
-           stream=None):
-    """Mixed-precision solve of FP64 systems: FP32 partial-pivoting solves,
-    ``iters`` refinement steps with the residual d - A x formed in FP64.
-    a, b, c, d (float64) are not modified; returns x (float64)."""
+           stream=None, algo: str = "gtsv"):
+    """Mixed-precision solve of FP64 systems: FP32 solves (``algo`` "gtsv":
+    partial pivoting; "partition": the unpivoted partition method, for
+    systems that need no pivoting), ``iters`` refinement steps with the
+    residual d - A x formed in FP64.  a, b, c, d (float64) are not modified;
+    returns x (float64)."""
     if a.dtype != torch.float64:
         raise TypeError("refine takes float64 arrays")
     batch = _dims(a, n, layout)
     a, b, c, d = _al(a), _al(b), _al(c), _al(d)
     x = out if out is not None else torch.empty_like(d)
     work = work if work is not None else refine_workspace(a, n, layout)
-    st = lib().tridiag_refine_double(LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype),
-                                     _ptr(d, a.dtype), _ptr(x, a.dtype), iters, _ptr(info), _ptr(work),
-                                     work.numel(), n, batch, _stream_ptr(stream))
-    check(st, "tridiag_refine_double")
+    st = lib().tridiag_refine_ex_double(ALGOS[algo], LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype),
+                                        _ptr(c, a.dtype), _ptr(d, a.dtype), _ptr(x, a.dtype), iters, _ptr(info),
+                                        _ptr(work), work.numel(), n, batch, _stream_ptr(stream))
+    check(st, "tridiag_refine_ex_double")
     return x
 
 

@@ -769,7 +769,8 @@ def run_adjoint(args):
 
 def run_ragged(args):
     """100000 systems, n log-uniform in [32, 65536], FP32, 20% non-dominant:
-    forward + adjoint through the autotuned size-class plan."""
+    forward + adjoint through the autotuned size-class plan, the dominant
+    systems marked as needing no pivoting."""
     import torch
 
     import tridiagonalsolver_gb300 as T
@@ -785,7 +786,11 @@ def run_ragged(args):
     t0 = time.time()
     table, timings = ragged.autotune(classes, dtype=torch.float32, reps=2)
     tune_s = time.time() - t0
-    plan = T.RaggedPlan(off, table=table)
+    # the dominant systems (80%) are marked as needing no pivoting: they run
+    # the unpivoted partition method up to 8192 rows; the rest, and longer
+    # ones, the autotuned pivoted variants
+    plan = T.RaggedPlan(off, table=table, no_pivoting=~nondom)
+    plan_piv = T.RaggedPlan(off, table=table)
     x = torch.empty_like(d)
     grads = [torch.empty_like(d) for _ in range(4)]
     stream = torch.cuda.Stream(device=dev)
@@ -803,6 +808,13 @@ def run_ragged(args):
     sampler.mark("end")
     clocks = sampler.stop()
     ms_f, _ = _graph_time(torch, stream, lambda: plan.solve(a, b, c, d, out=x, stream=stream), steps, 3)
+
+    def step_piv():
+        plan_piv.solve(a, b, c, d, out=x, stream=stream)
+        plan_piv.adjoint(a, b, c, x, w, grads=grads, stream=stream)
+
+    ms_piv, _ = _graph_time(torch, stream, step_piv, 3, 3)
+    _graph_time(torch, stream, step, 3, 3)  # leave this plan's results in x for the accuracy sample
     rng = np.random.default_rng(5)
     worst = 0.0
     for s_ in rng.choice(len(sizes), 16, replace=False):
@@ -834,7 +846,8 @@ def run_ragged(args):
            "autotune_seconds": round(tune_s, 1), "l2": "inputs larger than L2 (13.8 GB)",
            "timing": "CUDA graph of the whole ragged forward+adjoint (one launch per size class and direction)"},
           [{"name": "forward", "ms_per_launch": ms_f, "backward_error_max": worst},
-           {"name": "adjoint", "ms_per_launch": ms - ms_f}],
+           {"name": "adjoint", "ms_per_launch": ms - ms_f},
+           {"name": "forward+adjoint, every system pivoted", "ms_per_step": ms_piv}],
           14 * rows * 4 + 16 * len(sizes), ms, cpu_b, e2e, clocks, 2 * steps * len(bk))
 
 

@@ -135,8 +135,9 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 #define TRIDIAG_ALGO_WM 4     /* WM-pGE, one warp per system, unpivoted */
 #define TRIDIAG_ALGO_GTSV 5   /* partial pivoting: PGE for n >= 512 where it fits, else one thread per system */
 #define TRIDIAG_ALGO_PGE 6    /* WM-pGE with partial pivoting inside partitions, one CTA per system */
-#define TRIDIAG_ALGO_PARTITION 7 /* partition method without pivoting, one CTA per system (contiguous / packed,
-                                    n a multiple of 32 (FP32) / 16 (FP64), 256 <= n <= 8192 / 128 <= n <= 4096) */
+#define TRIDIAG_ALGO_PARTITION 7 /* partition method without pivoting: one CTA per system for n <= 8192 FP32 /
+                                    4096 FP64 (contiguous / packed); chunks of 8192 / 4096 rows per CTA for longer
+                                    systems whose n is a multiple of 32 / 16 (contiguous, up to 262144 / 65536) */
 
 /* Status of the last library call made by the calling host thread. */
 int tridiag_last_status(void);
@@ -272,7 +273,8 @@ int tridiag_pge_adjoint_double(int layout, const double *a, const double *b, con
  * as tridiag_pge_adjoint_*.  Contiguous layout and the shapes
  * TRIDIAG_ALGO_PARTITION covers (else TRIDIAG_ERR_NOT_SUPPORTED); systems that
  * need no pivoting, as for the forward solve. */
-/* 1 if TRIDIAG_ALGO_PARTITION's CTA kernel covers (precision, layout, n). */
+/* 1 if TRIDIAG_ALGO_PARTITION's single-CTA kernel (which the adjoint uses)
+ * covers (precision, layout, n). */
 int tridiag_partition_supported(int precision, int layout, int n_eqt);
 int tridiag_partition_adjoint_single(int layout, const float *a, const float *b, const float *c, const float *x,
                                      const float *xbar, float *ga, float *gb, float *gc, float *gd, int n_eqt,
@@ -299,6 +301,15 @@ int tridiag_partition_adjoint_double(int layout, const double *a, const double *
 typedef struct tridiag_ragged_plan tridiag_ragged_plan;
 int tridiag_ragged_plan_create(tridiag_ragged_plan **plan, int precision, const long long *offsets_host, int n_batch,
                                const int *variant_by_class, int n_classes);
+/* As tridiag_ragged_plan_create, with no_pivoting_host (may be NULL; one
+ * byte per system): systems marked 1 need no pivoting (diagonally dominant,
+ * say) and run variant 7, the unpivoted partition method (one CTA per
+ * system, n <= 8192 FP32 / 4096 FP64; longer ones keep their class's
+ * pivoted variant), in buckets of their own; info entries of those systems
+ * are set to 0. */
+int tridiag_ragged_plan_create_ex(tridiag_ragged_plan **plan, int precision, const long long *offsets_host,
+                                  int n_batch, const int *variant_by_class, int n_classes,
+                                  const unsigned char *no_pivoting_host);
 void tridiag_ragged_plan_destroy(tridiag_ragged_plan *plan);
 /* Buckets of a plan, longest first: 4 ints each (class, variant, systems,
  * largest n); returns the number of buckets. */

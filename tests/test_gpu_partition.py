@@ -79,10 +79,10 @@ def test_partition_ignores_a0_and_clast(cuda, dt):
 
 
 @pytest.mark.parametrize("dt,n", [(np.float32, 1000), (np.float32, 8200), (np.float64, 100), (np.float64, 4100),
-                                  (np.float32, 3000)])
-def test_partition_other_shapes_fall_back(cuda, dt, n):
-    """Shapes the partition kernels do not cover (n not a multiple of the
-    128-byte row) are solved by the Thomas sweep."""
+                                  (np.float32, 3000), (np.float32, 1), (np.float32, 33), (np.float64, 4095)])
+def test_partition_any_n(cuda, dt, n):
+    """n not a multiple of the 128-byte row: the element-wise staging up to
+    8192 (FP32) / 4096 (FP64) rows, the Thomas sweep beyond (8200, 4100)."""
     import tridiagonalsolver_gb300 as T
 
     batch = 6
@@ -151,9 +151,9 @@ def test_partition_adjoint_unsupported_shape(cuda):
     import tridiagonalsolver_gb300 as T
     from tridiagonalsolver_gb300 import TridiagError
 
-    t = cuda.ones(1000 * 2, dtype=cuda.float32, device="cuda")
+    t = cuda.ones(9000 * 2, dtype=cuda.float32, device="cuda")
     with pytest.raises(TridiagError):
-        T.partition_adjoint(t, t, t, t, t, 1000)
+        T.partition_adjoint(t, t, t, t, t, 9000)
 
 
 def test_solve_ad_unpivoted_gradcheck(cuda):
@@ -207,3 +207,24 @@ def test_refine_with_partition_solves(cuda, delta):
     x = T.refine(*ts, n, iters=2, algo="partition").cpu().numpy()
     _, eta = O.backward_error(a, b, c, d, x, n)
     assert eta <= 1e-12
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("n", [1, 77, 1000, 3001])
+def test_partition_adjoint_any_n(cuda, dt, n):
+    import tridiagonalsolver_gb300 as T
+
+    if dt == np.float64 and n > 4096:
+        pytest.skip("beyond the FP64 single-CTA reach")
+    batch = 9
+    a, b, c, d = inputs.dominant(n, batch, seed=n + 11)
+    w = np.random.default_rng(n).uniform(-1, 1, (batch, n))
+    ts = [cuda.from_numpy(v.astype(dt)).cuda() for v in (a, b, c, d, w)]
+    x = T.solve_out(*ts[:4], n, algo="partition")
+    grads = T.partition_adjoint(ts[0], ts[1], ts[2], x, ts[4], n)
+    h = [v.astype(dt).astype(np.float64) for v in (a, b, c)]
+    ref = O.adjoint_f64(*h, x.double().cpu().numpy(), w.astype(dt).astype(np.float64), n)
+    tol = 1e-12 if dt == np.float64 else 1e-5
+    for gg, r, name in zip(grads, ref, ("ga", "gb", "gc", "gd")):
+        g = gg.double().cpu().numpy().reshape(-1)
+        assert np.max(np.abs(g - r)) <= tol * max(np.max(np.abs(r)), 1e-300), name

@@ -70,3 +70,27 @@ def test_pgc_in_place_and_long_gtsv(cuda):
     _, worst = O.backward_error(*(v.astype(np.float32).astype(np.float64) for v in (a, b, c, d)),
                                 x.double().cpu().numpy().reshape(batch, n), n)
     assert worst <= 1e-6
+
+
+@pytest.mark.parametrize("variant,n", [(4, 10399), (5, 10399), (6, 40000)])
+def test_cluster_variants_are_deterministic(cuda, variant, n):
+    """Repeated solves of the same non-dominant systems through a cluster
+    variant give bit-identical results (the cluster-wide maxima of the
+    acceptance test are exact, whatever the timing of the CTAs)."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    batch = 120 if n < 20000 else 24
+    sizes = np.full(batch, n, dtype=np.int64)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, seed=9, nondominant_fraction=0.5)
+    plan = T.RaggedPlan(off, table={ragged.size_class(n): variant})
+    x = torch.empty_like(d)
+    plan.solve(a, b, c, d, out=x)
+    torch.cuda.synchronize()
+    ref = x.clone()
+    for _ in range(8):
+        x.fill_(float("nan"))
+        plan.solve(a, b, c, d, out=x)
+        torch.cuda.synchronize()
+        assert torch.equal(x, ref)

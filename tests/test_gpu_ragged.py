@@ -159,3 +159,33 @@ def test_ragged_full_workload(cuda):
         hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
         grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
         _check_system(hs, grads, n, not nondom[s], 1e-6, 2e-3)
+
+
+@pytest.mark.parametrize("dtype_name,max_n", [("float32", 65536), ("float64", 27648)])
+def test_ragged_unpivoted_buckets(cuda, dtype_name, max_n):
+    """Systems marked as needing no pivoting (the dominant ones here) run the
+    unpivoted partition method (variant 7) up to its size limit, the rest
+    the pivoted variants; forward and adjoint checked per system."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    dt = getattr(torch, dtype_name)
+    sizes = _sizes(max_n)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=dt, nondominant_fraction=0.3, seed=5)
+    plan = T.RaggedPlan(off, dtype=dt, no_pivoting=~nondom)
+    limit = T.lib().tridiag_ragged_variant_max_n(1 if dtype_name == "float64" else 0, 7)
+    buckets = plan.buckets()
+    assert any(v == 7 for _, v, _, _ in buckets)
+    assert all(mx <= limit for _, v, _, mx in buckets if v == 7)
+    info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+    x = plan.solve(a, b, c, d, info=info)
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    assert int((info != 0).sum()) == 0
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], ETA[dtype_name], GTOL[dtype_name])

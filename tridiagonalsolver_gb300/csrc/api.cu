@@ -123,7 +123,7 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
   packed_ptrs(layout, a, b, c, d, n);
   if (!b || !c || !d) return TRIDIAG_ERR_INVALID_VALUE;
   if (algo == TRIDIAG_ALGO_AUTO)
-    algo = (n > 1024 && (tdg::wmc_eligible<T>(layout, n) || tdg::wml_eligible<T>(layout, n)))
+    algo = (n > 1024 && (tdg::wmc_gen_eligible<T>(layout, n) || tdg::wml_eligible<T>(layout, n)))
                ? TRIDIAG_ALGO_PARTITION
                : TRIDIAG_ALGO_THOMAS;
   switch (algo) {
@@ -208,7 +208,7 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
   if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !b || !c || !d || !x) return TRIDIAG_ERR_INVALID_VALUE;
   if (layout == TRIDIAG_LAYOUT_PACKED) return TRIDIAG_ERR_NOT_SUPPORTED;
   if (algo == TRIDIAG_ALGO_AUTO)
-    algo = (n > 1024 && (tdg::wmc_eligible<T>(layout, n) || tdg::wml_eligible<T>(layout, n)))
+    algo = (n > 1024 && (tdg::wmc_gen_eligible<T>(layout, n) || tdg::wml_eligible<T>(layout, n)))
                ? TRIDIAG_ALGO_PARTITION
                : TRIDIAG_ALGO_WM;
   if (work_bytes < solve_out_ws<T>(algo, n, batch) || (solve_out_ws<T>(algo, n, batch) && !work))
@@ -641,7 +641,7 @@ int partition_adjoint_entry(int layout, const T* a, const T* b, const T* c, cons
 }  // namespace
 
 extern "C" int tridiag_partition_supported(int precision, int layout, int n) {
-  return precision ? (int)tdg::wmc_eligible<double>(layout, n) : (int)tdg::wmc_eligible<float>(layout, n);
+  return precision ? (int)tdg::wmc_gen_eligible<double>(layout, n) : (int)tdg::wmc_gen_eligible<float>(layout, n);
 }
 extern "C" int tridiag_partition_adjoint_single(int layout, const float* a, const float* b, const float* c,
                                                 const float* x, const float* xbar, float* ga, float* gb, float* gc,

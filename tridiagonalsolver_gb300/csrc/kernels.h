@@ -56,6 +56,17 @@ cudaError_t launch_wm_warp(int layout, const T* a, const T* b, const T* c, const
 // d (PACKED: must).  *used is false when the shape is not covered.
 template <typename T>
 bool wmc_eligible(int layout, int n);
+// any n up to 256 128-byte rows (element-wise staging), CONTIG / PACKED
+template <typename T>
+bool wmc_gen_eligible(int layout, int n);
+// ragged: mode 0 solve (a, b, c, d -> o0 = x), mode 1 adjoint (a, b, c,
+// d = xbar, xf = x -> o0..o3 = ga, gb, gc, gd) of systems list[0..count),
+// each at most Rmax 128-byte rows
+constexpr int WMC_GEN_MAX_ROWS = 256;  // 128-byte rows per system of the general staging
+template <typename T>
+cudaError_t launch_wmc_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
+                              T* o2, T* o3, const long long* offsets, const int* list, int count, int Rmax, int* info,
+                              cudaStream_t s);
 template <typename T>
 cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                        cudaStream_t s, bool* used);

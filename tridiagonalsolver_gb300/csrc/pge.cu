@@ -743,19 +743,23 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   const int rows = NT * m;  // rows per CTA
   const int row0 = rank * rows;
   using MagT = unsigned;
+  // Cluster-wide maxima and flags: every CTA accumulates into its own
+  // shared variables (CTA-local atomics), and after a cluster barrier the
+  // threads combine the CL values with plain distributed-shared-memory loads.
+  // (Atomics on another CTA's shared memory through map_shared_rank lost
+  // updates here: the maxima they produced depended on timing.)
   __shared__ MagT s_amax, s_dmax, s_xmax;
   __shared__ unsigned long long s_rmax, s_anorm, s_xn, s_dn;
   __shared__ int s_bad, s_nf;
-  // cluster-wide accumulators live in CTA 0
-  MagT* c_amax = cluster.map_shared_rank(&s_amax, 0);
-  MagT* c_dmax = cluster.map_shared_rank(&s_dmax, 0);
-  MagT* c_xmax = cluster.map_shared_rank(&s_xmax, 0);
-  unsigned long long* c_rmax = cluster.map_shared_rank(&s_rmax, 0);
-  unsigned long long* c_anorm = cluster.map_shared_rank(&s_anorm, 0);
-  unsigned long long* c_xn = cluster.map_shared_rank(&s_xn, 0);
-  unsigned long long* c_dn = cluster.map_shared_rank(&s_dn, 0);
-  int* c_bad = cluster.map_shared_rank(&s_bad, 0);
-  int* c_nf = cluster.map_shared_rank(&s_nf, 0);
+  auto cl_max = [&](auto& v) {
+    auto m = v;
+#pragma unroll
+    for (int r = 0; r < CL; ++r) {
+      const auto w = *cluster.map_shared_rank(&v, r);
+      m = w > m ? w : m;
+    }
+    return m;
+  };
   T* RED0 = cluster.map_shared_rank(RED, 0);
   T* SOL0 = cluster.map_shared_rank(SOL, 0);
   if (t == 0) {
@@ -788,7 +792,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
-  cluster.sync();  // staging done everywhere, CTA 0's accumulators initialised
+  cluster.sync();  // staging done everywhere, every CTA's accumulators initialised
   MagT amax = 0, dmax = 0;
 
   const int mi = m - 1;
@@ -878,8 +882,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     amax = max(amax, max(magh(as), max(magh(bs), magh(cs))));
     dmax = max(dmax, magh(ds));
     if (pass == 0) {
-      atomicMax(c_amax, amax);
-      atomicMax(c_dmax, dmax);
+      atomicMax(&s_amax, amax);
+      atomicMax(&s_dmax, dmax);
     }
     {
       T Yf = T(0), Vf = T(0), Wf = T(0);
@@ -968,7 +972,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       bad |= !finite_val(st);
       D[mi] = st;
       XF[t] = D[0];
-      if (pass == 0) atomicMax(c_xmax, xmax);
+      if (pass == 0) atomicMax(&s_xmax, xmax);
     }
     cluster.sync();
     {
@@ -977,14 +981,15 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       else if (rank + 1 < CL) x_next = cluster.map_shared_rank(XF, rank + 1)[0];
       const double r = fma(-(double)cs, (double)x_next,
                            fma(-(double)bs, (double)st, fma(-(double)as, (double)x_last, (double)ds)));
-      const T amx = Fmt<T>::from_mag(*c_amax), xmx = Fmt<T>::from_mag(*c_xmax), dmx = Fmt<T>::from_mag(*c_dmax);
+      const T amx = Fmt<T>::from_mag(cl_max(s_amax)), xmx = Fmt<T>::from_mag(cl_max(s_xmax)),
+              dmx = Fmt<T>::from_mag(cl_max(s_dmax));
       if (pass == 0) bad |= !(fabs(r) <= Fmt<T>::SEP_TOL * fma((double)amx, (double)xmx, (double)dmx));
     }
-    if (__syncthreads_or(bad) && t == 0) atomicOr(c_bad, 1);
+    if (__syncthreads_or(bad) && t == 0) s_bad = 1;
     cluster.sync();
-    const bool pass_bad = *c_bad != 0;
-    cluster.sync();  // everyone has read the flag
-    if (rank == 0 && t == 0) s_bad = 0;
+    const bool pass_bad = cl_max(s_bad) != 0;
+    cluster.sync();  // everyone has read the flags
+    if (t == 0) s_bad = 0;
     if (pass == 0 && !pass_bad) {
       accepted = true;
       break;
@@ -1021,18 +1026,18 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
         xn = max(xn, mag(xr));
         dn = max(dn, mag(dr));
       }
-      atomicMax(c_rmax, rmax);
-      atomicMax(c_anorm, anorm);
-      atomicMax(c_xn, xn);
-      atomicMax(c_dn, dn);
-      if (nonfinite) atomicOr(c_nf, 1);
+      atomicMax(&s_rmax, rmax);
+      atomicMax(&s_anorm, anorm);
+      atomicMax(&s_xn, xn);
+      atomicMax(&s_dn, dn);
+      if (nonfinite) s_nf = 1;
       cluster.sync();
-      const double eta = __longlong_as_double((long long)*c_rmax) /
-                         fma(__longlong_as_double((long long)*c_anorm), __longlong_as_double((long long)*c_xn),
-                             __longlong_as_double((long long)*c_dn));
-      const bool ok = *c_nf == 0 && eta <= Fmt<T>::SEP_TOL;
+      const double eta = __longlong_as_double((long long)cl_max(s_rmax)) /
+                         fma(__longlong_as_double((long long)cl_max(s_anorm)),
+                             __longlong_as_double((long long)cl_max(s_xn)), __longlong_as_double((long long)cl_max(s_dn)));
+      const bool ok = cl_max(s_nf) == 0 && eta <= Fmt<T>::SEP_TOL;
       cluster.sync();  // everyone has read the accumulators
-      if (rank == 0 && t == 0) {
+      if (t == 0) {
         s_rmax = s_anorm = s_xn = s_dn = 0ull;
         s_nf = 0;
       }

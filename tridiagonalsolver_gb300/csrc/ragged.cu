@@ -7,7 +7,10 @@
 // solve for n < 65 (variant 0), the partitioned solve with 64/128/256
 // partitions in one CTA (1-3) or in a cluster of 2/4/8 CTAs (4-6).  A
 // variant table (from the autotuner, or the defaults) overrides the choice
-// per class.  Within a bucket the systems run longest first.  Solving is one
+// per class.  Systems the caller marks as needing no pivoting (diagonally
+// dominant ones, say) form buckets of their own that run the unpivoted
+// partition method (variant 7, one CTA per system, up to 256 128-byte rows),
+// forward and adjoint.  Within a bucket the systems run longest first.  Solving is one
 // launch per non-empty bucket on the caller's stream, so the whole ragged
 // solve can be captured in one CUDA graph and replayed.
 #include <algorithm>
@@ -100,7 +103,7 @@ static cudaError_t launch_tiny(int mode, const T* a, const T* b, const T* c, con
 struct tridiag_ragged_plan {
   struct Bucket {
     int cls;      // size class
-    int variant;  // 0 tiny, 1-6 partitioned
+    int variant;  // 0 tiny, 1-6 partitioned, 7 unpivoted partition method
     int count;    // systems
     int m_max;    // rows per partition of the longest system
     int max_n;
@@ -123,21 +126,34 @@ int size_class(long long n) {
   return k;
 }
 
+constexpr int RAGGED_UNPIVOTED = 7;
+
 template <typename T>
-bool variant_serves(int v, int max_n) {
-  if (v == 0) return max_n <= tdg::RAGGED_TINY_MAX;
-  return max_n >= 65 && max_n <= tdg::pge_variant_max_n<T>(v);
+int unpivoted_max_n() {
+  return tdg::WMC_GEN_MAX_ROWS * (128 / (int)sizeof(T));
 }
 
 template <typename T>
-int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, const int* table, int table_len) {
+bool variant_serves(int v, int max_n) {
+  if (v == 0) return max_n <= tdg::RAGGED_TINY_MAX;
+  if (v == RAGGED_UNPIVOTED) return max_n <= unpivoted_max_n<T>();
+  return max_n >= 65 && max_n <= tdg::pge_variant_max_n<T>(v);
+}
+
+// no_pivoting (may be NULL): systems marked 1 need no pivoting and run the
+// unpivoted partition method (variant 7) where their class allows it.
+template <typename T>
+int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, const int* table, int table_len,
+                const unsigned char* no_pivoting = nullptr) {
   if (!out || !offsets || batch <= 0) return TRIDIAG_ERR_INVALID_VALUE;
   *out = nullptr;
-  std::vector<std::vector<int>> by_class(TRIDIAG_RAGGED_CLASSES);
+  // classes 0 .. CLASSES-1 pivoted, CLASSES .. 2 CLASSES-1 unpivoted
+  std::vector<std::vector<int>> by_class(2 * TRIDIAG_RAGGED_CLASSES);
   for (int s = 0; s < batch; ++s) {
     const long long n = offsets[s + 1] - offsets[s];
     if (n < 1 || n > (1ll << (TRIDIAG_RAGGED_CLASSES - 1))) return TRIDIAG_ERR_INVALID_VALUE;
-    by_class[size_class(n)].push_back(s);
+    const bool unp = no_pivoting && no_pivoting[s] && n <= unpivoted_max_n<T>();
+    by_class[size_class(n) + (unp ? TRIDIAG_RAGGED_CLASSES : 0)].push_back(s);
   }
   auto* plan = new (std::nothrow) tridiag_ragged_plan;
   if (!plan) return TRIDIAG_ERR_WORKSPACE;
@@ -146,16 +162,18 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   plan->total_rows = offsets[batch] - offsets[0];
   cudaGetDevice(&plan->device);
   std::vector<int> lists;
-  for (int k = 0; k < TRIDIAG_RAGGED_CLASSES; ++k) {
-    auto& sys = by_class[k];
+  for (int kk = 0; kk < 2 * TRIDIAG_RAGGED_CLASSES; ++kk) {
+    auto& sys = by_class[kk];
     if (sys.empty()) continue;
+    const bool unp = kk >= TRIDIAG_RAGGED_CLASSES;
+    const int k = kk % TRIDIAG_RAGGED_CLASSES;
     std::sort(sys.begin(), sys.end(), [&](int p, int q) {
       const long long np = offsets[p + 1] - offsets[p], nq = offsets[q + 1] - offsets[q];
       return np != nq ? np > nq : p < q;
     });
     const int max_n = (int)(offsets[sys[0] + 1] - offsets[sys[0]]);
-    int v = -1;
-    if (table && k < table_len && table[k] >= 0) {
+    int v = unp ? RAGGED_UNPIVOTED : -1;
+    if (!unp && table && k < table_len && table[k] >= 0) {
       if (!variant_serves<T>(table[k], max_n)) {  // an explicit choice that cannot serve the class
         delete plan;
         return TRIDIAG_ERR_NOT_SUPPORTED;
@@ -172,7 +190,11 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     bk.variant = v;
     bk.count = (int)sys.size();
     bk.max_n = max_n;
-    bk.m_max = v == 0 ? 0 : std::max(2, (max_n + tdg::pge_variant_partitions(v) - 1) / tdg::pge_variant_partitions(v));
+    constexpr int M = 128 / (int)sizeof(T);
+    bk.m_max = v == 0                  ? 0
+               : v == RAGGED_UNPIVOTED ? (max_n + M - 1) / M  // 128-byte rows of the longest system
+                                       : std::max(2, (max_n + tdg::pge_variant_partitions(v) - 1) /
+                                                         tdg::pge_variant_partitions(v));
     bk.rows = 0;
     for (int q : sys) bk.rows += offsets[q + 1] - offsets[q];
     bk.list_off = lists.size();
@@ -205,10 +227,17 @@ int plan_run(const tridiag_ragged_plan* plan, int mode, const T* a, const T* b, 
   if (mode == 1 && (!xf || !ga || !gb || !gc)) return TRIDIAG_ERR_INVALID_VALUE;
   for (const auto& bk : plan->buckets) {
     const int* list = plan->d_lists + bk.list_off;
-    cudaError_t e = bk.variant == 0
-                        ? tdg::launch_tiny<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count, s)
-                        : tdg::launch_pge_ragged<T>(bk.variant, mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets,
-                                                     list, bk.count, bk.m_max, s);
+    cudaError_t e;
+    if (bk.variant == 0)
+      e = tdg::launch_tiny<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count, s);
+    else if (bk.variant == RAGGED_UNPIVOTED)
+      e = mode == 0 ? tdg::launch_wmc_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets, list,
+                                                bk.count, bk.m_max, info, s)
+                    : tdg::launch_wmc_ragged<T>(1, a, b, c, d, xf, ga, gb, gc, x, offsets, list, bk.count, bk.m_max,
+                                                info, s);
+    else
+      e = tdg::launch_pge_ragged<T>(bk.variant, mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
+                                    bk.m_max, s);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
   }
   return TRIDIAG_SUCCESS;
@@ -222,6 +251,13 @@ int tridiag_ragged_plan_create(tridiag_ragged_plan** plan, int precision, const 
                                const int* variant_by_class, int n_classes) {
   return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes)
                    : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes);
+}
+
+int tridiag_ragged_plan_create_ex(tridiag_ragged_plan** plan, int precision, const long long* offsets_host,
+                                  int batch, const int* variant_by_class, int n_classes,
+                                  const unsigned char* no_pivoting_host) {
+  return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes, no_pivoting_host)
+                   : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes, no_pivoting_host);
 }
 
 void tridiag_ragged_plan_destroy(tridiag_ragged_plan* plan) {
@@ -246,6 +282,7 @@ int tridiag_ragged_plan_buckets(const tridiag_ragged_plan* plan, int* out, int m
 
 int tridiag_ragged_variant_max_n(int precision, int variant) {
   if (variant == 0) return tdg::RAGGED_TINY_MAX;
+  if (variant == RAGGED_UNPIVOTED) return precision ? unpivoted_max_n<double>() : unpivoted_max_n<float>();
   return precision ? tdg::pge_variant_max_n<double>(variant) : tdg::pge_variant_max_n<float>(variant);
 }
 

@@ -41,6 +41,7 @@
 namespace tdg {
 
 constexpr int WMC_MAX_R = 256;
+static_assert(WMC_GEN_MAX_ROWS == WMC_MAX_R, "general staging uses the single-CTA kernel");
 
 // solve: a, b, c, d, x (PACKED: m[0] covers every array, x included);
 // adjoint: a, b, c, xbar, x, then the outputs ga, gb, gc, gd; chunked
@@ -61,6 +62,31 @@ struct WmcChunk {
   T* rel;
   const T* ysol;
 };
+
+// General staging (any n, any offset; ragged batches): the CTA copies its
+// system element by element with cp.async into the same swizzled layout
+// and pads the last partition with identity rows (a = 0, b = 1, c = 0,
+// d = 0); results leave with coalesced stores.  System j of the launch is
+// list[j] (or j), rows [offsets[s], offsets[s+1]) (or s*stride .. + n).
+template <typename T>
+struct WmcGen {
+  const T* in[5];  // solve: a, b, c, d; adjoint: a, b, c, xbar, x
+  T* out[4];       // solve: x; adjoint: ga, gb, gc, gd
+  const long long* offsets;
+  const int* list;
+  int* info;  // may be NULL: 0 written per system
+  long long stride;
+  int n;
+};
+
+template <typename T>
+__device__ __forceinline__ void wmc_cp_async(T* smem, const T* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 
 template <typename T>
 struct WmcVec;
@@ -110,9 +136,10 @@ __device__ __forceinline__ T& wmc_elem(unsigned char* S, int t, int k) {
 // gb_i = -lambda_i x_i, gc_i = -lambda_i x_{i+1} (contiguous layout).
 // MODE 2 / 3: one chunk of a long system per CTA (see WmcChunk); the
 // separators' system between them is solved by a MODE 0 launch.
-template <typename T, int MODE>
+template <typename T, int MODE, bool GEN = false>
 __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
-                                                        int packed, int* err, const WmcChunk<T> ck) {
+                                                        int packed, int* err, const WmcChunk<T> ck,
+                                                        const WmcGen<T> gen) {
   using W = WmcVec<T>;
   constexpr int NV = W::N;     // values per 16-byte unit
   constexpr int M = 8 * NV;    // rows per thread (128 bytes)
@@ -129,37 +156,71 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   uint64_t* bar = reinterpret_cast<uint64_t*>(red + 8 * nt);
 
   constexpr bool CHUNKED = MODE >= 2;
-  const int j = CHUNKED ? (int)(blockIdx.x / ck.nchunks) : (int)blockIdx.x;
+  static_assert(!(GEN && CHUNKED), "general staging serves single-CTA systems");
+  int j = CHUNKED ? (int)(blockIdx.x / ck.nchunks) : (int)blockIdx.x;
   const int ch = CHUNKED ? (int)(blockIdx.x % ck.nchunks) : 0;
   const bool last_chunk = !CHUNKED || ch == ck.nchunks - 1;
-  const int Rc = CHUNKED && last_chunk ? ck.Rlast : R;     // partitions of this CTA
+  int Rc = CHUNKED && last_chunk ? ck.Rlast : R;  // partitions of this CTA
+  int nn = n;                                      // rows of this system
+  long long goff = 0;                              // its first row (GEN)
+  if constexpr (GEN) {
+    j = gen.list ? gen.list[blockIdx.x] : (int)blockIdx.x;
+    goff = gen.offsets ? gen.offsets[j] : (long long)j * gen.stride;
+    nn = gen.offsets ? (int)(gen.offsets[j + 1] - goff) : gen.n;
+    Rc = (nn + M - 1) / M;
+  }
   const int mset = CHUNKED && last_chunk && ck.Rlast != R ? 5 : 0;
   const int row0 = CHUNKED ? j * ck.Rt + ch * R : j * R;  // first 128-byte row (non-packed)
   const int t = threadIdx.x;
   const bool active = t < Rc;
-  if (t == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (t == 0) {
-    mbar_arrive_expect_tx(bar, (unsigned)NA * (unsigned)Rc * 128u);
+  if constexpr (GEN) {
+    const int rows = Rc * M;
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
-      const CUtensorMap* mp = &maps.m[packed ? 0 : mset + k];
-      const int row = packed ? (j * 4 + k) * R : row0;
-      tma_load_2d(S[k], mp, 0, row, bar);
+      const T* src = gen.in[k] + goff;
+      const T pad = k == 1 ? T(1) : T(0);
+      for (int i = t; i < rows; i += nt) {
+        T* dst = &wmc_elem<T>(S[k], i / M, i % M);
+        if (i < nn)
+          wmc_cp_async(dst, src + i);
+        else
+          *dst = pad;
+      }
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    // a_0 and c_{n-1} are not read
+    if (t == 0) {
+      wmc_elem<T>(S[0], 0, 0) = T(0);
+      wmc_elem<T>(S[2], (nn - 1) / M, (nn - 1) % M) = T(0);
+    }
+    __syncthreads();
+  } else {
+    if (t == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (t == 0) {
+      mbar_arrive_expect_tx(bar, (unsigned)NA * (unsigned)Rc * 128u);
+#pragma unroll
+      for (int k = 0; k < NA; ++k) {
+        const CUtensorMap* mp = &maps.m[packed ? 0 : mset + k];
+        const int row = packed ? (j * 4 + k) * R : row0;
+        tma_load_2d(S[k], mp, 0, row, bar);
+      }
+    }
+    const bool ok = mbar_wait(bar, 0, err);
+    if (!__syncthreads_and(ok)) return;
   }
-  const bool ok = mbar_wait(bar, 0, err);
-  if (!__syncthreads_and(ok)) return;
 
   if constexpr (MODE == 1) {
     // A^T: sub-diagonal c_{i-1} into the a slot, super-diagonal a_{i+1} into
     // the c slot (the neighbours' boundary values are read before anyone
     // writes)
     const T cprev = (active && t > 0) ? wmc_elem<T>(S[2], t - 1, M - 1) : T(0);
-    const T anext = (active && t + 1 < R) ? wmc_elem<T>(S[0], t + 1, 0) : T(0);
+    const T anext = (active && t + 1 < Rc) ? wmc_elem<T>(S[0], t + 1, 0) : T(0);
     __syncthreads();
     if (active) {
       T carry = cprev;
@@ -260,16 +321,16 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   if constexpr (MODE != 3) {
   T al = T(0), be = T(1), ga = T(0), de = T(0);
   if (active) {
-    const T Gn = t + 1 < R ? xg[t + 1] : T(0);
-    const T Pn = t + 1 < R ? xp[t + 1] : T(0);
-    const T Ln = t + 1 < R ? xl[t + 1] : T(0);
+    const T Gn = t + 1 < Rc ? xg[t + 1] : T(0);
+    const T Pn = t + 1 < Rc ? xp[t + 1] : T(0);
+    const T Ln = t + 1 < Rc ? xl[t + 1] : T(0);
     al = -sa * vp;
     be = fma(-sc, Ln, fma(-sa, cp, sb));
     ga = sc * Pn;
     de = fma(-sc, Gn, fma(-sa, dp, sd));
   }
   // parallel cyclic reduction: row t combines rows t - s and t + s
-  for (int s = 1; s < R; s <<= 1) {
+  for (int s = 1; s < Rc; s <<= 1) {
     if (active) {
       ra[t] = al;
       rb[t] = be;
@@ -285,7 +346,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
         c1 = rc[t - s];
         d1 = rd[t - s];
       }
-      if (t + s < R) {
+      if (t + s < Rc) {
         a2 = ra[t + s];
         b2 = rb[t + s];
         c2 = rc[t + s];
@@ -339,7 +400,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
     // gradients: lambda (in the d slot) times the forward solution x
     if (active) {
       const T xprev = t > 0 ? wmc_elem<T>(S[4], t - 1, M - 1) : T(0);
-      const T xnext = t + 1 < R ? wmc_elem<T>(S[4], t + 1, 0) : T(0);
+      const T xnext = t + 1 < Rc ? wmc_elem<T>(S[4], t + 1, 0) : T(0);
       T carry = xprev;
       T xv[NV], xn[NV];
       W::split(*reinterpret_cast<const typename W::V*>(S[4] + wmc_swz(t, 0)), xv);
@@ -356,7 +417,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
           const T xr_ = v + 1 < NV ? xv[v + 1] : (q < 7 ? xn[0] : xnext);
           ga_[v] = i > 0 ? -lam[v] * xl_ : T(0);
           gb_[v] = -lam[v] * xv[v];
-          gc_[v] = i + 1 < n ? -lam[v] * xr_ : T(0);
+          gc_[v] = i + 1 < nn ? -lam[v] * xr_ : T(0);
         }
         carry = xv[NV - 1];
         *reinterpret_cast<typename W::V*>(S[0] + off) = W::join(ga_);
@@ -366,6 +427,18 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
         for (int v = 0; v < NV; ++v) xv[v] = xn[v];
       }
     }
+  }
+  if constexpr (GEN) {
+    if (gen.info && t == 0) gen.info[j] = 0;
+    __syncthreads();
+    constexpr int NO = MODE == 1 ? 4 : 1;
+#pragma unroll
+    for (int k = 0; k < NO; ++k) {
+      unsigned char* src = S[MODE == 1 ? k : 3];
+      T* dst = gen.out[k] + goff;
+      for (int i = t; i < nn; i += nt) dst[i] = wmc_elem<T>(src, i / M, i % M);
+    }
+    return;
   }
   fence_async_smem();
   __syncthreads();
@@ -391,11 +464,47 @@ bool wmc_eligible(int layout, int n) {
   return R >= 8 && R <= WMC_MAX_R;
 }
 
+// the general staging: any n up to WMC_MAX_R 128-byte rows
+template <typename T>
+bool wmc_gen_eligible(int layout, int n) {
+  constexpr int M = 128 / (int)sizeof(T);
+  return (layout == CONTIG || layout == PACKED) && n >= 1 && n <= WMC_MAX_R * M;
+}
+
+template <typename T, int MODE>
+static cudaError_t wmc_gen_launch(const WmcGen<T>& gen, int count, int Rmax, cudaStream_t s) {
+  const int threads = (Rmax + 31) / 32 * 32;
+  const size_t smem = wmc_smem_bytes<T>(Rmax, threads, MODE == 1 ? 5 : 4);
+  cudaError_t e =
+      cudaFuncSetAttribute(wmc_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  WmcMaps maps{};
+  wmc_kernel<T, MODE, true><<<count, threads, smem, s>>>(maps, 0, Rmax, 0, error_word(), WmcChunk<T>{}, gen);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                        cudaStream_t s, bool* used) {
   *used = false;
-  if (!wmc_eligible<T>(layout, n) || batch <= 0) return cudaSuccess;
+  if (batch <= 0) return cudaSuccess;
+  if (!wmc_eligible<T>(layout, n)) {
+    if (!wmc_gen_eligible<T>(layout, n)) return cudaSuccess;
+    constexpr int M = 128 / (int)sizeof(T);
+    WmcGen<T> gen{};
+    const bool pk = layout == PACKED;
+    if (pk && x != d) return cudaSuccess;
+    gen.in[0] = a;
+    gen.in[1] = pk ? a + n : b;
+    gen.in[2] = pk ? a + 2 * (size_t)n : c;
+    gen.in[3] = pk ? a + 3 * (size_t)n : d;
+    gen.out[0] = pk ? const_cast<T*>(a) + 3 * (size_t)n : x;
+    gen.stride = pk ? 4 * (long long)n : (long long)n;
+    gen.n = n;
+    cudaError_t e = wmc_gen_launch<T, 0>(gen, batch, (n + M - 1) / M, s);
+    if (e == cudaSuccess) *used = true;
+    return e;
+  }
   constexpr int M = 128 / (int)sizeof(T);
   const int R = n / M;
   const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
@@ -418,7 +527,7 @@ cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* 
   const size_t smem = wmc_smem_bytes<T>(R, threads, 4);
   cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  wmc_kernel<T, 0><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word(), WmcChunk<T>{});
+  wmc_kernel<T, 0><<<batch, threads, smem, s>>>(maps, n, R, packed ? 1 : 0, error_word(), WmcChunk<T>{}, WmcGen<T>{});
   e = cudaGetLastError();
   if (e == cudaSuccess) *used = true;
   return e;
@@ -428,7 +537,21 @@ template <typename T>
 cudaError_t launch_wmc_adjoint(const T* a, const T* b, const T* c, const T* x, const T* xbar, T* ga, T* gb, T* gc,
                                T* gd, int n, int batch, cudaStream_t s, bool* used) {
   *used = false;
-  if (!wmc_eligible<T>(CONTIG, n) || batch <= 0) return cudaSuccess;
+  if (batch <= 0) return cudaSuccess;
+  if (!wmc_eligible<T>(CONTIG, n)) {
+    if (!wmc_gen_eligible<T>(CONTIG, n)) return cudaSuccess;
+    constexpr int M = 128 / (int)sizeof(T);
+    WmcGen<T> gen{};
+    const T* ins[5] = {a, b, c, xbar, x};
+    T* outs[4] = {ga, gb, gc, gd};
+    for (int k = 0; k < 5; ++k) gen.in[k] = ins[k];
+    for (int k = 0; k < 4; ++k) gen.out[k] = outs[k];
+    gen.stride = n;
+    gen.n = n;
+    cudaError_t e = wmc_gen_launch<T, 1>(gen, batch, (n + M - 1) / M, s);
+    if (e == cudaSuccess) *used = true;
+    return e;
+  }
   constexpr int M = 128 / (int)sizeof(T);
   const int R = n / M;
   const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
@@ -442,7 +565,7 @@ cudaError_t launch_wmc_adjoint(const T* a, const T* b, const T* c, const T* x, c
   const size_t smem = wmc_smem_bytes<T>(R, threads, 5);
   cudaError_t e = cudaFuncSetAttribute(wmc_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  wmc_kernel<T, 1><<<batch, threads, smem, s>>>(maps, n, R, 0, error_word(), WmcChunk<T>{});
+  wmc_kernel<T, 1><<<batch, threads, smem, s>>>(maps, n, R, 0, error_word(), WmcChunk<T>{}, WmcGen<T>{});
   e = cudaGetLastError();
   if (e == cudaSuccess) *used = true;
   return e;
@@ -545,7 +668,7 @@ cudaError_t launch_wml(const T* a, const T* b, const T* c, const T* d, T* x, int
   if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)nchunks * (unsigned)batch;
   WmcChunk<T> ck{nchunks, R, Rlast, Rt, Ppad, rel, rd};
-  wmc_kernel<T, 2><<<grid, R, smem, s>>>(maps, n, R, 0, error_word(), ck);
+  wmc_kernel<T, 2><<<grid, R, smem, s>>>(maps, n, R, 0, error_word(), ck, WmcGen<T>{});
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -556,7 +679,7 @@ cudaError_t launch_wml(const T* a, const T* b, const T* c, const T* d, T* x, int
   e = launch_wmc<T>(CONTIG, ra, rb, rc, rd, rd, Ppad, batch, s, &inner);
   if (e != cudaSuccess) return e;
   if (!inner) return cudaErrorInvalidConfiguration;
-  wmc_kernel<T, 3><<<grid, R, smem, s>>>(maps, n, R, 0, error_word(), ck);
+  wmc_kernel<T, 3><<<grid, R, smem, s>>>(maps, n, R, 0, error_word(), ck, WmcGen<T>{});
   e = cudaGetLastError();
   if (e == cudaSuccess) *used = true;
   return e;
@@ -571,6 +694,38 @@ template cudaError_t launch_wml<float>(const float*, const float*, const float*,
 template cudaError_t launch_wml<double>(const double*, const double*, const double*, const double*, double*, int,
                                         int, void*, size_t, cudaStream_t, bool*);
 
+// Ragged batches: `count` systems list[0..count) of the packed arrays, each
+// with n <= Rmax 128-byte rows (the caller groups systems by size).
+template <typename T>
+cudaError_t launch_wmc_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
+                              T* o2, T* o3, const long long* offsets, const int* list, int count, int Rmax, int* info,
+                              cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  if (Rmax < 1 || Rmax > WMC_MAX_R) return cudaErrorInvalidValue;
+  WmcGen<T> gen{};
+  gen.in[0] = a;
+  gen.in[1] = b;
+  gen.in[2] = c;
+  gen.in[3] = d;
+  gen.in[4] = xf;
+  gen.out[0] = o0;
+  gen.out[1] = o1;
+  gen.out[2] = o2;
+  gen.out[3] = o3;
+  gen.offsets = offsets;
+  gen.list = list;
+  gen.info = info;
+  return mode == 1 ? wmc_gen_launch<T, 1>(gen, count, Rmax, s) : wmc_gen_launch<T, 0>(gen, count, Rmax, s);
+}
+
+template cudaError_t launch_wmc_ragged<float>(int, const float*, const float*, const float*, const float*,
+                                              const float*, float*, float*, float*, float*, const long long*,
+                                              const int*, int, int, int*, cudaStream_t);
+template cudaError_t launch_wmc_ragged<double>(int, const double*, const double*, const double*, const double*,
+                                               const double*, double*, double*, double*, double*, const long long*,
+                                               const int*, int, int, int*, cudaStream_t);
+template bool wmc_gen_eligible<float>(int, int);
+template bool wmc_gen_eligible<double>(int, int);
 template bool wmc_eligible<float>(int, int);
 template bool wmc_eligible<double>(int, int);
 template cudaError_t launch_wmc<float>(int, const float*, const float*, const float*, const float*, float*, int, int,

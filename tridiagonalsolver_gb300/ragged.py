@@ -25,7 +25,7 @@ from .ops import _ptr, _stream_ptr
 CLASSES = 18            # TRIDIAG_RAGGED_CLASSES: class k holds 2^(k-1) < n <= 2^k
 VARIANTS = {0: "sequential (thread per system)", 1: "partitioned, 1 CTA x 64", 2: "partitioned, 1 CTA x 128",
             3: "partitioned, 1 CTA x 256", 4: "partitioned, cluster of 2", 5: "partitioned, cluster of 4",
-            6: "partitioned, cluster of 8"}
+            6: "partitioned, cluster of 8", 7: "unpivoted partition method (systems marked no_pivoting)"}
 _P = ctypes.c_void_p
 
 
@@ -43,9 +43,12 @@ def variant_max_n(precision: int, variant: int) -> int:
 
 class RaggedPlan:
     """Plan for a ragged batch; ``offsets`` (int64, batch+1 entries) on the
-    host or device; ``table`` maps size class -> variant (None: defaults)."""
+    host or device; ``table`` maps size class -> variant (None: defaults);
+    ``no_pivoting`` (bool per system, optional) marks systems that need no
+    pivoting (diagonally dominant, say), which then run the unpivoted
+    partition method where their size allows."""
 
-    def __init__(self, offsets, dtype=torch.float32, table: dict | None = None, device=None):
+    def __init__(self, offsets, dtype=torch.float32, table: dict | None = None, device=None, no_pivoting=None):
         L = _sig()
         off = offsets.detach().cpu().numpy() if isinstance(offsets, torch.Tensor) else np.asarray(offsets)
         off = np.ascontiguousarray(off, dtype=np.int64)
@@ -57,8 +60,15 @@ class RaggedPlan:
             tab[int(k)] = int(v)
         self._tab = tab
         h = _P()
-        st = L.tridiag_ragged_plan_create(ctypes.addressof(h), self.precision, off.ctypes.data, self.batch,
-                                          tab.ctypes.data, CLASSES)
+        if no_pivoting is None:
+            st = L.tridiag_ragged_plan_create(ctypes.addressof(h), self.precision, off.ctypes.data, self.batch,
+                                              tab.ctypes.data, CLASSES)
+        else:
+            mask = np.ascontiguousarray(np.asarray(no_pivoting, dtype=np.uint8).reshape(-1))
+            if mask.size != self.batch:
+                raise ValueError("no_pivoting needs one entry per system")
+            st = L.tridiag_ragged_plan_create_ex(ctypes.addressof(h), self.precision, off.ctypes.data, self.batch,
+                                                 tab.ctypes.data, CLASSES, mask.ctypes.data)
         check(st, "tridiag_ragged_plan_create")
         self._h = h
         dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -68,8 +78,8 @@ class RaggedPlan:
     def buckets(self):
         """[(class, variant, systems, largest n)], longest class first."""
         L = _sig()
-        out = np.zeros(4 * CLASSES, dtype=np.int32)
-        nb = L.tridiag_ragged_plan_buckets(self._h, out.ctypes.data, CLASSES)
+        out = np.zeros(4 * 2 * CLASSES, dtype=np.int32)  # pivoted and unpivoted buckets per class
+        nb = min(L.tridiag_ragged_plan_buckets(self._h, out.ctypes.data, 2 * CLASSES), 2 * CLASSES)
         return [tuple(int(v) for v in out[4 * i:4 * i + 4]) for i in range(nb)]
 
     def solve(self, a, b, c, d, out=None, info=None, stream=None):

@@ -303,9 +303,11 @@ int tridiag_ragged_plan_create(tridiag_ragged_plan **plan, int precision, const 
                                const int *variant_by_class, int n_classes);
 /* As tridiag_ragged_plan_create, with no_pivoting_host (may be NULL; one
  * byte per system): systems marked 1 need no pivoting (diagonally dominant,
- * say) and run variant 7, the unpivoted partition method (one CTA per
- * system, n <= 8192 FP32 / 4096 FP64; longer ones keep their class's
- * pivoted variant), in buckets of their own; info entries of those systems
+ * say) and run the unpivoted partition method in buckets of their own:
+ * variant 7, one CTA per system (n <= 4096 FP32 / 2048 FP64), and variant 8
+ * for longer ones (chunks of that size per CTA and the separators' system in
+ * between; n <= 262144 FP32 / 65536 FP64; the plan holds ~14 values of
+ * workspace per 32 (FP32) / 16 (FP64) rows); info entries of those systems
  * are set to 0. */
 int tridiag_ragged_plan_create_ex(tridiag_ragged_plan **plan, int precision, const long long *offsets_host,
                                   int n_batch, const int *variant_by_class, int n_classes,

@@ -136,16 +136,18 @@ def test_ragged_plan_table_and_autotune(cuda):
         T.RaggedPlan(np.array([0, 30000]), table={15: 1})
 
 
-def test_ragged_full_workload(cuda):
+@pytest.mark.parametrize("mark_dominant", [False, True])
+def test_ragged_full_workload(cuda, mark_dominant):
     """100000 systems, n log-uniform in [32, 65536] (~8.6e8 rows), FP32, 20%
-    non-dominant: forward and adjoint; 40 sampled systems checked."""
+    non-dominant: forward and adjoint; 40 sampled systems checked.  With
+    mark_dominant the dominant systems run the unpivoted partition method."""
     import tridiagonalsolver_gb300 as T
     from tridiagonalsolver_gb300 import ragged
 
     torch = cuda
     sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
     a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
-    plan = T.RaggedPlan(off)
+    plan = T.RaggedPlan(off, no_pivoting=~nondom if mark_dominant else None)
     info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
     x = plan.solve(a, b, c, d, info=info)
     w = torch.rand_like(d) * 2 - 1
@@ -177,6 +179,8 @@ def test_ragged_unpivoted_buckets(cuda, dtype_name, max_n):
     limit = T.lib().tridiag_ragged_variant_max_n(1 if dtype_name == "float64" else 0, 7)
     buckets = plan.buckets()
     assert any(v == 7 for _, v, _, _ in buckets)
+    if max_n > limit:
+        assert any(v == 8 for _, v, _, _ in buckets)
     assert all(mx <= limit for _, v, _, mx in buckets if v == 7)
     info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
     x = plan.solve(a, b, c, d, info=info)

@@ -63,6 +63,27 @@ bool wmc_gen_eligible(int layout, int n);
 // d = xbar, xf = x -> o0..o3 = ga, gb, gc, gd) of systems list[0..count),
 // each at most Rmax 128-byte rows
 constexpr int WMC_GEN_MAX_ROWS = 256;  // 128-byte rows per system of the general staging
+// partitions (128-byte rows) per CTA of the chunked kernels: ~68 KB of
+// shared memory, three CTAs per SM, so one CTA's loads overlap another's
+// arithmetic
+constexpr int WML_CHUNK_R = 128;
+// Long unpivoted systems of a ragged plan: L systems (l_sys), their
+// partitions' offsets roff (L+1, P in total, largest Pmax) and C chunks
+// (cl_li, cl_ch) of 256 128-byte rows.
+struct WmlRagged {
+  int L = 0, C = 0, Pmax = 0;
+  long long P = 0;
+  const int* l_sys = nullptr;
+  const long long* roff = nullptr;
+  const int* cl_li = nullptr;
+  const int* cl_ch = nullptr;
+};
+template <typename T>
+size_t wml_ragged_workspace_elems(long long total_partitions);
+template <typename T>
+cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
+                              T* o2, T* o3, const long long* offsets, const WmlRagged& lr, T* work, int* info,
+                              cudaStream_t s);
 template <typename T>
 cudaError_t launch_wmc_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
                               T* o2, T* o3, const long long* offsets, const int* list, int count, int Rmax, int* info,

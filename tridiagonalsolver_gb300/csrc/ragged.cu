@@ -9,8 +9,9 @@
 // variant table (from the autotuner, or the defaults) overrides the choice
 // per class.  Systems the caller marks as needing no pivoting (diagonally
 // dominant ones, say) form buckets of their own that run the unpivoted
-// partition method (variant 7, one CTA per system, up to 256 128-byte rows),
-// forward and adjoint.  Within a bucket the systems run longest first.  Solving is one
+// partition method: one CTA per system up to 128 128-byte rows (variant 7),
+// chunks of that size per CTA with the separators' system in between for
+// longer ones (variant 8), forward and adjoint.  Within a bucket the systems run longest first.  Solving is one
 // launch per non-empty bucket on the caller's stream, so the whole ragged
 // solve can be captured in one CUDA graph and replayed.
 #include <algorithm>
@@ -116,6 +117,11 @@ struct tridiag_ragged_plan {
   std::vector<Bucket> buckets;
   int* d_lists = nullptr;
   int device = 0;
+  // long systems marked as needing no pivoting (variant 8): chunk lists and
+  // the partition workspace, one device allocation
+  tdg::WmlRagged lr;
+  void* d_lr = nullptr;
+  void* lr_work = nullptr;
 };
 
 namespace {
@@ -127,10 +133,18 @@ int size_class(long long n) {
 }
 
 constexpr int RAGGED_UNPIVOTED = 7;
+constexpr int RAGGED_UNPIVOTED_LONG = 8;
 
 template <typename T>
 int unpivoted_max_n() {
-  return tdg::WMC_GEN_MAX_ROWS * (128 / (int)sizeof(T));
+  return tdg::WML_CHUNK_R * (128 / (int)sizeof(T));  // one chunk-sized CTA (three per SM)
+}
+
+// long unpivoted systems: beyond one CTA, their separators' system within one
+template <typename T>
+bool long_unpivoted_ok(long long n) {
+  constexpr int M = 128 / (int)sizeof(T);
+  return n > unpivoted_max_n<T>() && (n + M - 1) / M <= (long long)tdg::WMC_GEN_MAX_ROWS * M;
 }
 
 template <typename T>
@@ -147,12 +161,18 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
                 const unsigned char* no_pivoting = nullptr) {
   if (!out || !offsets || batch <= 0) return TRIDIAG_ERR_INVALID_VALUE;
   *out = nullptr;
-  // classes 0 .. CLASSES-1 pivoted, CLASSES .. 2 CLASSES-1 unpivoted
+  // classes 0 .. CLASSES-1 pivoted, CLASSES .. 2 CLASSES-1 unpivoted; long
+  // unpivoted systems apart
   std::vector<std::vector<int>> by_class(2 * TRIDIAG_RAGGED_CLASSES);
+  std::vector<int> longs;
   for (int s = 0; s < batch; ++s) {
     const long long n = offsets[s + 1] - offsets[s];
     if (n < 1 || n > (1ll << (TRIDIAG_RAGGED_CLASSES - 1))) return TRIDIAG_ERR_INVALID_VALUE;
     const bool unp = no_pivoting && no_pivoting[s] && n <= unpivoted_max_n<T>();
+    if (no_pivoting && no_pivoting[s] && !unp && long_unpivoted_ok<T>(n)) {
+      longs.push_back(s);
+      continue;
+    }
     by_class[size_class(n) + (unp ? TRIDIAG_RAGGED_CLASSES : 0)].push_back(s);
   }
   auto* plan = new (std::nothrow) tridiag_ragged_plan;
@@ -206,7 +226,66 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
                    [](const tridiag_ragged_plan::Bucket& p, const tridiag_ragged_plan::Bucket& q) {
                      return p.cls > q.cls;
                    });
-  if (cudaMalloc(&plan->d_lists, lists.size() * sizeof(int)) != cudaSuccess) {
+  if (!longs.empty()) {
+    constexpr int M = 128 / (int)sizeof(T);
+    const long long chunk_rows = (long long)tdg::WML_CHUNK_R * M;
+    std::sort(longs.begin(), longs.end(), [&](int p, int q) {
+      const long long np = offsets[p + 1] - offsets[p], nq = offsets[q + 1] - offsets[q];
+      return np != nq ? np > nq : p < q;
+    });
+    std::vector<long long> roff(longs.size() + 1, 0);
+    std::vector<int> cl_li, cl_ch;
+    int pmax = 0;
+    long long rows = 0;
+    for (size_t i = 0; i < longs.size(); ++i) {
+      const long long n = offsets[longs[i] + 1] - offsets[longs[i]];
+      const long long P = (n + M - 1) / M;
+      roff[i + 1] = roff[i] + P;
+      pmax = std::max(pmax, (int)P);
+      rows += n;
+      for (long long c = 0; c * chunk_rows < n; ++c) {
+        cl_li.push_back((int)i);
+        cl_ch.push_back((int)c);
+      }
+    }
+    plan->lr.L = (int)longs.size();
+    plan->lr.C = (int)cl_li.size();
+    plan->lr.P = roff.back();
+    plan->lr.Pmax = pmax;
+    const size_t b_lsys = longs.size() * sizeof(int), b_roff = roff.size() * sizeof(long long),
+                 b_cl = cl_li.size() * sizeof(int);
+    const size_t o_roff = (b_lsys + 255) / 256 * 256, o_li = o_roff + (b_roff + 255) / 256 * 256,
+                 o_ch = o_li + (b_cl + 255) / 256 * 256, o_end = o_ch + (b_cl + 255) / 256 * 256;
+    char* mem = nullptr;
+    if (cudaMalloc(&mem, o_end) != cudaSuccess ||
+        cudaMalloc(&plan->lr_work, tdg::wml_ragged_workspace_elems<T>(plan->lr.P) * sizeof(T)) != cudaSuccess) {
+      cudaFree(mem);
+      delete plan;
+      return TRIDIAG_ERR_CUDA;
+    }
+    plan->d_lr = mem;
+    cudaMemcpy(mem, longs.data(), b_lsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(mem + o_roff, roff.data(), b_roff, cudaMemcpyHostToDevice);
+    cudaMemcpy(mem + o_li, cl_li.data(), b_cl, cudaMemcpyHostToDevice);
+    cudaMemcpy(mem + o_ch, cl_ch.data(), b_cl, cudaMemcpyHostToDevice);
+    plan->lr.l_sys = reinterpret_cast<int*>(mem);
+    plan->lr.roff = reinterpret_cast<long long*>(mem + o_roff);
+    plan->lr.cl_li = reinterpret_cast<int*>(mem + o_li);
+    plan->lr.cl_ch = reinterpret_cast<int*>(mem + o_ch);
+    tridiag_ragged_plan::Bucket bk;
+    const int max_n = (int)(offsets[longs[0] + 1] - offsets[longs[0]]);
+    bk.cls = size_class(max_n);
+    bk.variant = RAGGED_UNPIVOTED_LONG;
+    bk.count = (int)longs.size();
+    bk.max_n = max_n;
+    bk.m_max = 0;
+    bk.rows = rows;
+    bk.list_off = 0;
+    plan->buckets.insert(plan->buckets.begin(), bk);  // longest work first
+  }
+  if (cudaMalloc(&plan->d_lists, std::max<size_t>(lists.size(), 1) * sizeof(int)) != cudaSuccess) {
+    cudaFree(plan->d_lr);
+    cudaFree(plan->lr_work);
     delete plan;
     return TRIDIAG_ERR_CUDA;
   }
@@ -228,7 +307,12 @@ int plan_run(const tridiag_ragged_plan* plan, int mode, const T* a, const T* b, 
   for (const auto& bk : plan->buckets) {
     const int* list = plan->d_lists + bk.list_off;
     cudaError_t e;
-    if (bk.variant == 0)
+    if (bk.variant == RAGGED_UNPIVOTED_LONG)
+      e = mode == 0 ? tdg::launch_wml_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets,
+                                                plan->lr, static_cast<T*>(plan->lr_work), info, s)
+                    : tdg::launch_wml_ragged<T>(1, a, b, c, d, xf, x, ga, gb, gc, offsets, plan->lr,
+                                                static_cast<T*>(plan->lr_work), info, s);
+    else if (bk.variant == 0)
       e = tdg::launch_tiny<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count, s);
     else if (bk.variant == RAGGED_UNPIVOTED)
       e = mode == 0 ? tdg::launch_wmc_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets, list,
@@ -263,6 +347,8 @@ int tridiag_ragged_plan_create_ex(tridiag_ragged_plan** plan, int precision, con
 void tridiag_ragged_plan_destroy(tridiag_ragged_plan* plan) {
   if (!plan) return;
   cudaFree(plan->d_lists);
+  cudaFree(plan->d_lr);
+  cudaFree(plan->lr_work);
   delete plan;
 }
 
@@ -283,6 +369,8 @@ int tridiag_ragged_plan_buckets(const tridiag_ragged_plan* plan, int* out, int m
 int tridiag_ragged_variant_max_n(int precision, int variant) {
   if (variant == 0) return tdg::RAGGED_TINY_MAX;
   if (variant == RAGGED_UNPIVOTED) return precision ? unpivoted_max_n<double>() : unpivoted_max_n<float>();
+  if (variant == RAGGED_UNPIVOTED_LONG)
+    return precision ? tdg::WMC_GEN_MAX_ROWS * 16 * 16 : tdg::WMC_GEN_MAX_ROWS * 32 * 32;
   return precision ? tdg::pge_variant_max_n<double>(variant) : tdg::pge_variant_max_n<float>(variant);
 }
 

@@ -61,6 +61,13 @@ struct WmcChunk {
   int nchunks, Rfull, Rlast, Rt, Ppad;
   T* rel;
   const T* ysol;
+  // element-wise staging of ragged long systems: CTA b serves chunk
+  // cl_ch[b] of long system cl_li[b] (= ragged system l_sys[cl_li[b]]), whose
+  // partitions start at roff[cl_li[b]] in rel and ysol
+  const int* cl_li;
+  const int* cl_ch;
+  const int* l_sys;
+  const long long* roff;
 };
 
 // General staging (any n, any offset; ragged batches): the CTA copies its
@@ -136,7 +143,10 @@ __device__ __forceinline__ T& wmc_elem(unsigned char* S, int t, int k) {
 // gb_i = -lambda_i x_i, gc_i = -lambda_i x_{i+1} (contiguous layout).
 // MODE 2 / 3: one chunk of a long system per CTA (see WmcChunk); the
 // separators' system between them is solved by a MODE 0 launch.
-template <typename T, int MODE, bool GEN = false>
+// GEN: element-wise staging (WmcGen); with TRANS the staged system is A^T
+// (sub-diagonal c_{i-1}, super-diagonal a_{i+1}, read shifted from global
+// memory) and MODE 3 writes lambda and the gradients (x from gen.in[4]).
+template <typename T, int MODE, bool GEN = false, bool TRANS = false>
 __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
                                                         int packed, int* err, const WmcChunk<T> ck,
                                                         const WmcGen<T> gen) {
@@ -156,45 +166,58 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   uint64_t* bar = reinterpret_cast<uint64_t*>(red + 8 * nt);
 
   constexpr bool CHUNKED = MODE >= 2;
-  static_assert(!(GEN && CHUNKED), "general staging serves single-CTA systems");
+  static_assert(!TRANS || (GEN && CHUNKED), "transposed staging serves the chunked element-wise path");
   int j = CHUNKED ? (int)(blockIdx.x / ck.nchunks) : (int)blockIdx.x;
-  const int ch = CHUNKED ? (int)(blockIdx.x % ck.nchunks) : 0;
-  const bool last_chunk = !CHUNKED || ch == ck.nchunks - 1;
+  int ch = CHUNKED ? (int)(blockIdx.x % ck.nchunks) : 0;
+  bool last_chunk = !CHUNKED || ch == ck.nchunks - 1;
   int Rc = CHUNKED && last_chunk ? ck.Rlast : R;  // partitions of this CTA
   int nn = n;                                      // rows of this system
-  long long goff = 0;                              // its first row (GEN)
+  long long goff = 0;                              // first row of this CTA (GEN)
+  int row_start = 0;                               // ... within its system
+  int rows_here = n;                               // rows this CTA holds
+  size_t rel_base = CHUNKED ? (size_t)j * ck.Rt + (size_t)ch * R : 0;     // partition index of t = 0
+  size_t y_base = CHUNKED ? (size_t)j * ck.Ppad + (size_t)ch * R : 0;
   if constexpr (GEN) {
-    j = gen.list ? gen.list[blockIdx.x] : (int)blockIdx.x;
-    goff = gen.offsets ? gen.offsets[j] : (long long)j * gen.stride;
-    nn = gen.offsets ? (int)(gen.offsets[j + 1] - goff) : gen.n;
-    Rc = (nn + M - 1) / M;
+    int li = 0;
+    if constexpr (CHUNKED) {
+      li = ck.cl_li[blockIdx.x];
+      ch = ck.cl_ch[blockIdx.x];
+      j = ck.l_sys[li];
+    } else {
+      j = gen.list ? gen.list[blockIdx.x] : (int)blockIdx.x;
+    }
+    const long long gsys = gen.offsets ? gen.offsets[j] : (long long)j * gen.stride;
+    nn = gen.offsets ? (int)(gen.offsets[j + 1] - gsys) : gen.n;
+    row_start = CHUNKED ? ch * R * M : 0;
+    rows_here = min(nn - row_start, R * M);
+    Rc = (rows_here + M - 1) / M;
+    last_chunk = row_start + R * M >= nn;
+    goff = gsys + row_start;
+    if constexpr (CHUNKED) rel_base = y_base = (size_t)ck.roff[li] + (size_t)ch * R;
   }
   const int mset = CHUNKED && last_chunk && ck.Rlast != R ? 5 : 0;
-  const int row0 = CHUNKED ? j * ck.Rt + ch * R : j * R;  // first 128-byte row (non-packed)
+  const int row0 = CHUNKED ? j * ck.Rt + ch * R : j * R;  // first 128-byte row (non-packed, TMA)
   const int t = threadIdx.x;
   const bool active = t < Rc;
   if constexpr (GEN) {
     const int rows = Rc * M;
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
-      const T* src = gen.in[k] + goff;
+      // TRANS: slot 0 <- c_{r-1}, slot 2 <- a_{r+1}; a_0 and c_{n-1} are not read
+      const T* src = TRANS && k == 0 ? gen.in[2] + goff - 1 : TRANS && k == 2 ? gen.in[0] + goff + 1 : gen.in[k] + goff;
       const T pad = k == 1 ? T(1) : T(0);
       for (int i = t; i < rows; i += nt) {
         T* dst = &wmc_elem<T>(S[k], i / M, i % M);
-        if (i < nn)
+        const int r = row_start + i;  // row within the system
+        const bool skip = (k == 0 && r == 0) || (k == 2 && r == nn - 1);
+        if (i < rows_here && !skip)
           wmc_cp_async(dst, src + i);
         else
-          *dst = pad;
+          *dst = i < rows_here ? T(0) : pad;
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_all;\n" ::: "memory");
-    __syncthreads();
-    // a_0 and c_{n-1} are not read
-    if (t == 0) {
-      wmc_elem<T>(S[0], 0, 0) = T(0);
-      wmc_elem<T>(S[2], (nn - 1) / M, (nn - 1) % M) = T(0);
-    }
     __syncthreads();
   } else {
     if (t == 0) {
@@ -302,7 +325,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   if constexpr (MODE == 2) {
     // the partition's relations for the separators' system
     if (active) {
-      T* o = ck.rel + ((size_t)j * ck.Rt + (size_t)ch * R + t) * WMC_REL;
+      T* o = ck.rel + (rel_base + t) * WMC_REL;
       o[0] = G;
       o[1] = P;
       o[2] = L;
@@ -365,7 +388,7 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   }
   if constexpr (MODE == 3) {
     if (active) {
-      const size_t g = (size_t)j * ck.Ppad + (size_t)ch * R + t;
+      const size_t g = y_base + t;
       ys[t] = ck.ysol[g];
       xl[t] = (ch > 0 || t > 0) ? ck.ysol[g - 1] : T(0);
     }
@@ -429,14 +452,28 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
     }
   }
   if constexpr (GEN) {
-    if (gen.info && t == 0) gen.info[j] = 0;
+    if (gen.info && t == 0 && (!CHUNKED || ch == 0)) gen.info[j] = 0;
     __syncthreads();
-    constexpr int NO = MODE == 1 ? 4 : 1;
+    if constexpr (TRANS) {
+      // lambda and the gradients ga = -lambda x_{i-1}, gb = -lambda x_i,
+      // gc = -lambda x_{i+1} (x of the forward solve in gen.in[4])
+      const T* xf = gen.in[4] + goff;
+      for (int i = t; i < rows_here; i += nt) {
+        const int r = row_start + i;
+        const T lam = wmc_elem<T>(S[3], i / M, i % M);
+        gen.out[0][goff + i] = lam;
+        gen.out[1][goff + i] = r > 0 ? -lam * xf[i - 1] : T(0);
+        gen.out[2][goff + i] = -lam * xf[i];
+        gen.out[3][goff + i] = r + 1 < nn ? -lam * xf[i + 1] : T(0);
+      }
+    } else {
+      constexpr int NO = MODE == 1 ? 4 : 1;
 #pragma unroll
-    for (int k = 0; k < NO; ++k) {
-      unsigned char* src = S[MODE == 1 ? k : 3];
-      T* dst = gen.out[k] + goff;
-      for (int i = t; i < nn; i += nt) dst[i] = wmc_elem<T>(src, i / M, i % M);
+      for (int k = 0; k < NO; ++k) {
+        unsigned char* src = S[MODE == 1 ? k : 3];
+        T* dst = gen.out[k] + goff;
+        for (int i = t; i < rows_here; i += nt) dst[i] = wmc_elem<T>(src, i / M, i % M);
+      }
     }
     return;
   }
@@ -577,7 +614,7 @@ template cudaError_t launch_wmc_adjoint<double>(const double*, const double*, co
                                                 const double*, double*, double*, double*, double*, int, int,
                                                 cudaStream_t, bool*);
 // ---------------------------------------------------------------------------
-// Long systems: chunks of WMC_MAX_R partitions per CTA (MODE 2), the
+// Long systems: chunks of WML_CHUNK_R partitions per CTA (MODE 2), the
 // separators' system (one row per partition, padded to a shape the
 // single-CTA kernel covers) assembled and solved by MODE 0, then the chunks
 // again (MODE 3).  Traffic: the four inputs twice, x once, plus ~14 values
@@ -595,7 +632,7 @@ bool wml_eligible(int layout, int n) {
   constexpr int M = 128 / (int)sizeof(T);
   if (layout != CONTIG || n % M != 0) return false;
   const int Rt = n / M;
-  return Rt > WMC_MAX_R && wml_ppad<T>(Rt) <= WMC_MAX_R * M;
+  return Rt > WMC_MAX_R && wml_ppad<T>(Rt) <= WMC_MAX_R * M;  // longer than one CTA holds
 }
 
 template <typename T>
@@ -641,7 +678,7 @@ cudaError_t launch_wml(const T* a, const T* b, const T* c, const T* d, T* x, int
   if (!wml_eligible<T>(CONTIG, n) || batch <= 0 || !work || work_bytes < wml_workspace_bytes<T>(n, batch))
     return cudaSuccess;
   constexpr int M = 128 / (int)sizeof(T);
-  const int Rt = n / M, R = WMC_MAX_R;
+  const int Rt = n / M, R = WML_CHUNK_R;
   const int nchunks = (Rt + R - 1) / R;
   const int Rlast = Rt - (nchunks - 1) * R;
   const int Ppad = wml_ppad<T>(Rt);
@@ -717,6 +754,112 @@ cudaError_t launch_wmc_ragged(int mode, const T* a, const T* b, const T* c, cons
   gen.info = info;
   return mode == 1 ? wmc_gen_launch<T, 1>(gen, count, Rmax, s) : wmc_gen_launch<T, 0>(gen, count, Rmax, s);
 }
+
+// Long systems of a ragged batch (more rows than one CTA holds), unpivoted:
+// chunks of WML_CHUNK_R 128-byte rows per CTA (MODE 2), the separators'
+// systems (one per long system, ragged) assembled and solved by the
+// element-wise single-CTA kernel, then the chunks again (MODE 3).  mode 1:
+// the adjoint, on A^T staged shifted, with the gradient epilogue.
+template <typename T>
+__global__ void __launch_bounds__(256) wml_assemble_ragged(const T* __restrict__ rel, T* al, T* be, T* ga, T* de,
+                                                           const long long* __restrict__ roff, int L,
+                                                           long long total) {
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = L;  // roff[lo] <= idx < roff[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (roff[mid] <= idx) lo = mid; else hi = mid;
+    }
+    const bool nx = idx + 1 < roff[lo + 1];
+    const T* o = rel + idx * WMC_REL;
+    const T* on = o + WMC_REL;
+    const T Gn = nx ? on[0] : T(0), Pn = nx ? on[1] : T(0), Ln = nx ? on[2] : T(0);
+    const T vL = o[3], cL = o[4], dL = o[5], sa = o[6], sb = o[7], sc = o[8], sd = o[9];
+    al[idx] = -sa * vL;
+    be[idx] = fma(-sc, Ln, fma(-sa, cL, sb));
+    ga[idx] = sc * Pn;
+    de[idx] = fma(-sc, Gn, fma(-sa, dL, sd));
+  }
+}
+
+template <typename T>
+size_t wml_ragged_workspace_elems(long long total_partitions) {
+  return (size_t)(WMC_REL + 4) * (size_t)total_partitions;
+}
+
+template <typename T>
+cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
+                              T* o2, T* o3, const long long* offsets, const WmlRagged& lr, T* work, int* info,
+                              cudaStream_t s) {
+  if (lr.L <= 0) return cudaSuccess;
+  constexpr int M = 128 / (int)sizeof(T);
+  const int R = WML_CHUNK_R;
+  T* rel = work;
+  T* ra = rel + (size_t)WMC_REL * lr.P;
+  T* rb = ra + lr.P;
+  T* rc = rb + lr.P;
+  T* rd = rc + lr.P;
+  WmcChunk<T> ck{};
+  ck.nchunks = 1;
+  ck.rel = rel;
+  ck.ysol = rd;
+  ck.cl_li = lr.cl_li;
+  ck.cl_ch = lr.cl_ch;
+  ck.l_sys = lr.l_sys;
+  ck.roff = lr.roff;
+  WmcGen<T> gen{};
+  gen.offsets = offsets;
+  gen.info = info;
+  gen.in[0] = a;
+  gen.in[1] = b;
+  gen.in[2] = c;
+  gen.in[3] = d;
+  gen.in[4] = xf;
+  gen.out[0] = o0;
+  gen.out[1] = o1;
+  gen.out[2] = o2;
+  gen.out[3] = o3;
+  const size_t smem = wmc_smem_bytes<T>(R, R, 4);
+  WmcMaps maps{};
+  cudaError_t e;
+  if (mode == 1) {
+    e = cudaFuncSetAttribute(wmc_kernel<T, 2, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(wmc_kernel<T, 3, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    wmc_kernel<T, 2, true, true><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen);
+  } else {
+    e = cudaFuncSetAttribute(wmc_kernel<T, 2, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(wmc_kernel<T, 3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    wmc_kernel<T, 2, true, false><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen);
+  }
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long blocks = (lr.P + 255) / 256;
+  const unsigned ag = (unsigned)(blocks < (long long)sms * 8 ? blocks : (long long)sms * 8);
+  wml_assemble_ragged<T><<<ag, 256, 0, s>>>(rel, ra, rb, rc, rd, lr.roff, lr.L, lr.P);
+  e = launch_wmc_ragged<T>(0, ra, rb, rc, rd, nullptr, rd, nullptr, nullptr, nullptr, lr.roff, nullptr, lr.L,
+                           (lr.Pmax + M - 1) / M, nullptr, s);
+  if (e != cudaSuccess) return e;
+  if (mode == 1)
+    wmc_kernel<T, 3, true, true><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen);
+  else
+    wmc_kernel<T, 3, true, false><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen);
+  return cudaGetLastError();
+}
+
+template size_t wml_ragged_workspace_elems<float>(long long);
+template size_t wml_ragged_workspace_elems<double>(long long);
+template cudaError_t launch_wml_ragged<float>(int, const float*, const float*, const float*, const float*,
+                                              const float*, float*, float*, float*, float*, const long long*,
+                                              const WmlRagged&, float*, int*, cudaStream_t);
+template cudaError_t launch_wml_ragged<double>(int, const double*, const double*, const double*, const double*,
+                                               const double*, double*, double*, double*, double*, const long long*,
+                                               const WmlRagged&, double*, int*, cudaStream_t);
 
 template cudaError_t launch_wmc_ragged<float>(int, const float*, const float*, const float*, const float*,
                                               const float*, float*, float*, float*, float*, const long long*,

@@ -25,7 +25,8 @@ from .ops import _ptr, _stream_ptr
 CLASSES = 18            # TRIDIAG_RAGGED_CLASSES: class k holds 2^(k-1) < n <= 2^k
 VARIANTS = {0: "sequential (thread per system)", 1: "partitioned, 1 CTA x 64", 2: "partitioned, 1 CTA x 128",
             3: "partitioned, 1 CTA x 256", 4: "partitioned, cluster of 2", 5: "partitioned, cluster of 4",
-            6: "partitioned, cluster of 8", 7: "unpivoted partition method (systems marked no_pivoting)"}
+            6: "partitioned, cluster of 8", 7: "unpivoted partition method (systems marked no_pivoting)",
+            8: "unpivoted partition method, chunked (long systems marked no_pivoting)"}
 _P = ctypes.c_void_p
 
 

@@ -261,6 +261,7 @@ struct PgeIO {
   const int* list;
   size_t stride;
   int n;
+  int pf_ahead;  // uniform batches: CTA b prefetches system b + pf_ahead into L2 (0: off)
 };
 
 template <typename T, int MODE>
@@ -346,6 +347,16 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+  // One CTA per SM fits: the CTA that runs here next (about one wave later)
+  // finds its system in L2 instead of HBM.
+  if (io.pf_ahead > 0 && t == 0 && (int)blockIdx.x + io.pf_ahead < (int)gridDim.x) {
+    const size_t nb = (size_t)(blockIdx.x + io.pf_ahead) * io.stride;
+    const unsigned bytes = (unsigned)((size_t)n * sizeof(T)) & ~15u;
+    const T* arr[4] = {ga, gb, gc, gd};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(arr[k] + nb), "r"(bytes) : "memory");
+  }
   __syncthreads();
 
   bool accepted = false;
@@ -1135,10 +1146,23 @@ int pge_variant_max_n(int v) {
 }
 
 template <typename T, int NT, int MODE>
-static cudaError_t pge_launch(const PgeIO<T>& io, int grid, int ms, cudaStream_t s) {
+static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int ms, cudaStream_t s) {
   const size_t smem = pge_smem_bytes<T, NT>(ms);
   cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, NT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  PgeIO<T> io = io_in;
+  io.pf_ahead = 0;
+  // L2 prefetch one wave ahead for uniform batches with 16-byte aligned systems
+  const uintptr_t al = reinterpret_cast<uintptr_t>(io.a) | reinterpret_cast<uintptr_t>(io.b) |
+                       reinterpret_cast<uintptr_t>(io.c) | reinterpret_cast<uintptr_t>(io.d);
+  if (!io.offsets && !io.list && (al & 15u) == 0 && (io.stride * sizeof(T)) % 16 == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE>, NT, smem) == cudaSuccess &&
+        per > 0 && grid > sms * per)
+      io.pf_ahead = sms * per;
+  }
   pge_kernel<T, NT, MODE><<<grid, NT, smem, s>>>(io);
   return cudaGetLastError();
 }

@@ -123,9 +123,15 @@ class ClockSampler:
                 self.proc.kill()
         mhz, maxmhz, reasons = [], None, set()
         names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for t, line in self.lines:
-            if self.t0 is None or not (self.t0 <= t <= (self.t1 or t)):
-                continue
+        t0 = self.t0
+        inside = [(t, l) for t, l in self.lines if t0 is not None and t0 <= t <= (self.t1 or t)]
+        window = "timed region"
+        if not inside and t0 is not None:
+            # a timed region shorter than the sampling period: the samples that
+            # follow it were taken while the same kernels ran again (per-part timing)
+            inside = [(t, l) for t, l in self.lines if t >= t0][:3]
+            window = "first samples after the timed region began (region shorter than the 100 ms period)"
+        for t, line in inside:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -138,7 +144,7 @@ class ClockSampler:
                 if v.lower() in ("active", "1"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": maxmhz,
-                "reasons": sorted(reasons), "samples": len(mhz)}
+                "reasons": sorted(reasons), "samples": len(mhz), "window": window}
 
 
 def make_inputs(torch, part, seed, device):

@@ -304,7 +304,7 @@ def run_ours(args):
             # the FP64 solve is bound by the FP64 pipe on GB300, not by HBM: report that roofline too
             # (FP64 operations per row from ncu's instruction counts, profiles/pge_fp64_n4096.md;
             # peak = measured DFMA rate, profiles/fp64_rates_microbench.txt)
-            ops_per_row, fp64_peak = 25.4, 503.0
+            ops_per_row, fp64_peak = 20.8, 503.0
             gops = dom["n"] * dom["batch"] * ops_per_row / (dom["ms_per_launch"] * 1e-3) / 1e9
             roofline["compute"] = {"bound": "fp64", "achieved": round(gops, 1), "peak": fp64_peak,
                                    "unit": "Gop/s", "frac": round(gops / fp64_peak, 4),

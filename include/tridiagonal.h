@@ -430,6 +430,16 @@ int tridiag_block2_double(int algo, int layout, double *a, double *b, double *c,
  * CUDA error. */
 long long tridiag_partition_fallbacks(int reset);
 
+/* Diagnostics of the same solve, per path taken since the last reset on the
+ * current device: counts[0] systems whose separator system, solved by
+ * parallel cyclic reduction, missed its residual bound and was solved again
+ * with partial pivoting; counts[1] systems whose separator rows missed the
+ * residual bound, so that the exact backward error of all rows was measured;
+ * counts[2] refinement passes run (FP64 residual as a new right-hand side);
+ * counts[3] sequential fallbacks (as tridiag_partition_fallbacks).
+ * Synchronous; reset != 0 clears all four.  Returns a TRIDIAG_* status. */
+int tridiag_partition_path_counts(long long *counts, int reset);
+
 /* Size of the static scratch array of tridiag_gtsv_noalloc_* (32 MiB). */
 #define TRIDIAG_NOALLOC_SCRATCH_BYTES (32u << 20)
 

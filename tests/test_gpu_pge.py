@@ -109,12 +109,15 @@ def test_pge_bench_shape_fp64(cuda):
     g.manual_seed(77)
     a, b, c, d = (torch.rand((batch, n), dtype=torch.float64, device="cuda", generator=g) * 2 - 1 for _ in range(4))
     info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
-    T.lib().tridiag_partition_fallbacks(1)
+    T.partition_path_counts(reset=True)
     x = T.gtsv(a, b, c, d, n, info=info)  # no pivot record requested: the partitioned solve
     assert int((info != 0).sum()) == 0
-    fb = T.lib().tridiag_partition_fallbacks(1)
-    print(f"partitioned solve: {fb} of {batch} systems took the sequential fallback")
+    paths = T.partition_path_counts(reset=True)
+    fb = paths["fallbacks"]
+    print(f"partitioned solve of {batch} systems: {paths}")
     assert fb <= batch // 256  # the fast path serves (nearly) every system
+    assert T.lib().tridiag_partition_fallbacks(0) == 0  # cleared with the path counts
+    assert paths["refinement_passes"] <= paths["exact_checks"] * 2
     idx = torch.arange(0, batch, batch // 64, device="cuda")
     host = [t.index_select(0, idx).cpu().numpy() for t in (a, b, c, d, x)]
     host[0][:, 0] = 0.0

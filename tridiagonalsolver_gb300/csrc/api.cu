@@ -571,6 +571,15 @@ extern "C" long long tridiag_partition_fallbacks(int reset) {
   return (long long)v;
 }
 
+extern "C" int tridiag_partition_path_counts(long long* counts, int reset) {
+  if (!counts) return set_status(TRIDIAG_ERR_INVALID_VALUE);
+  unsigned long long v[4] = {0ull, 0ull, 0ull, 0ull};
+  const cudaError_t e = tdg::pge_path_counts(v, reset != 0);
+  if (e != cudaSuccess) return set_status(cuda_status(e));
+  for (int k = 0; k < 4; ++k) counts[k] = (long long)v[k];
+  return set_status(TRIDIAG_SUCCESS);
+}
+
 namespace {
 template <typename T>
 int pge_entry(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,

@@ -58,22 +58,50 @@ __device__ __forceinline__ float rcp(float x) {
   return r;
 }
 
-// |x| >= |y| on the IEEE bit patterns (integer pipe; NaN compares as large).
-__device__ __forceinline__ bool abs_ge(double x, double y) {
-  unsigned long long ux = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-  unsigned long long uy = (unsigned long long)__double_as_longlong(y) & 0x7fffffffffffffffull;
-  return ux >= uy;
+// v when k, else +0, as a select the compiler cannot see through: an FMA
+// whose operand is a selected constant zero may otherwise be split into the
+// two cases (a separate multiply or add on the FP64 pipe for the zero one).
+__device__ __forceinline__ double keep_if(bool k, double v) {
+  double r;
+  asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\tselp.f64 %0, %1, 0d0000000000000000, p;\n\t}"
+      : "=d"(r)
+      : "d"(v), "r"((unsigned)k));
+  return r;
 }
-__device__ __forceinline__ bool abs_ge(float x, float y) {
-  unsigned ux = (unsigned)__float_as_int(x) & 0x7fffffffu;
-  unsigned uy = (unsigned)__float_as_int(y) & 0x7fffffffu;
-  return ux >= uy;
+__device__ __forceinline__ float keep_if(bool k, float v) {
+  float r;
+  asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\tselp.f32 %0, %1, 0f00000000, p;\n\t}"
+      : "=f"(r)
+      : "f"(v), "r"((unsigned)k));
+  return r;
 }
 
-__device__ __forceinline__ bool is_zero(double x) {
-  return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
+// The IEEE bit pattern of x through a move the compiler cannot see through,
+// so that tests written on it stay integer instructions: a test it
+// recognises (== 0 after dropping the sign, exponent all ones) may otherwise
+// be turned back into a floating-point compare, which for FP64 takes a slot
+// of the FP64 pipe.
+__device__ __forceinline__ unsigned long long bits_of(double x) {
+  unsigned long long r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
 }
-__device__ __forceinline__ bool is_zero(float x) { return ((unsigned)__float_as_int(x) << 1) == 0u; }
+__device__ __forceinline__ unsigned bits_of(float x) {
+  unsigned r;
+  asm("mov.b32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// |x| >= |y| on the IEEE bit patterns (integer pipe; NaN compares as large).
+__device__ __forceinline__ bool abs_ge(double x, double y) {
+  return (bits_of(x) & 0x7fffffffffffffffull) >= (bits_of(y) & 0x7fffffffffffffffull);
+}
+__device__ __forceinline__ bool abs_ge(float x, float y) {
+  return (bits_of(x) & 0x7fffffffu) >= (bits_of(y) & 0x7fffffffu);
+}
+
+__device__ __forceinline__ bool is_zero(double x) { return (bits_of(x) << 1) == 0ull; }
+__device__ __forceinline__ bool is_zero(float x) { return (bits_of(x) << 1) == 0u; }
 
 // ---------------------------------------------------------------------------
 // Streaming memory access with cache hints.  Inputs that are read once go

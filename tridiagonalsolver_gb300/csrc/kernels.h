@@ -184,6 +184,7 @@ cudaError_t launch_relayout(int from, int to, const T* const src[4], T* const ds
 // Number of systems the partitioned solve handed to its sequential fallback
 // (synchronous read; optionally reset).
 cudaError_t pge_fallback_count(unsigned long long* out, bool reset);
+cudaError_t pge_path_counts(unsigned long long* out, bool reset);  // out[4]
 
 // refine.cu: pieces of the mixed-precision refined solve (FP64 in/out).
 cudaError_t launch_narrow4(const double* a, const double* b, const double* c, const double* d, float* a32,

@@ -39,23 +39,17 @@
 
 namespace tdg {
 
-__device__ __forceinline__ bool finite_val(double v) {
-  return (((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffull) != 0x7ffull;
-}
-__device__ __forceinline__ bool finite_val(float v) { return (((unsigned)__float_as_int(v) >> 23) & 0xffu) != 0xffu; }
+__device__ __forceinline__ bool finite_val(double v) { return ((bits_of(v) >> 52) & 0x7ffull) != 0x7ffull; }
+__device__ __forceinline__ bool finite_val(float v) { return ((bits_of(v) >> 23) & 0xffu) != 0xffu; }
 
 // Magnitude bits (|v| as an unsigned pattern, ordered like |v|) and the
 // biased exponent, on the integer pipe.
-__device__ __forceinline__ unsigned long long mag(double v) {
-  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
-}
-__device__ __forceinline__ unsigned mag(float v) { return (unsigned)__float_as_int(v) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned long long mag(double v) { return bits_of(v) & 0x7fffffffffffffffull; }
+__device__ __forceinline__ unsigned mag(float v) { return bits_of(v) & 0x7fffffffu; }
 // Magnitude key in 32 bits (FP64: the high word, which orders |v| up to a
 // relative 2^-20 -- enough for the acceptance test's maxima -- and keeps
 // the running maxima single 32-bit integer instructions).
-__device__ __forceinline__ unsigned magh(double v) {
-  return (unsigned)((unsigned long long)__double_as_longlong(v) >> 32) & 0x7fffffffu;
-}
+__device__ __forceinline__ unsigned magh(double v) { return (unsigned)(bits_of(v) >> 32) & 0x7fffffffu; }
 __device__ __forceinline__ unsigned magh(float v) { return mag(v); }
 __device__ __forceinline__ int expo(double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff; }
 __device__ __forceinline__ int expo(float v) { return (int)((unsigned)__float_as_int(v) >> 23) & 0xff; }
@@ -132,6 +126,11 @@ __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
 
 // Systems that took the sequential fallback since the last reset (per device).
 __device__ unsigned long long g_pge_fallbacks = 0ull;
+// Per-path counts since the last reset (per device): [0] systems whose PCR
+// separator solution was rejected and re-solved with pivoting (first pass),
+// [1] systems whose separator rows missed the bound, so that the exact
+// backward error was measured, [2] refinement passes run.
+__device__ unsigned long long g_pge_paths[3] = {0ull, 0ull, 0ull};
 
 // A chunk of K consecutive rows of a tridiagonal system held in registers:
 // rows 0..K-2 are interior, row K-1 is the chunk's top-level row.  The
@@ -407,9 +406,9 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     const T inv = Div<T>(piv).inv();
     const T l = (sw ? cb : na) * inv;
     const T u1 = sw ? nb : cc;
-    const T u2 = sw ? nc : T(0);
+    const T u2 = keep_if(sw, nc);
     const T uy = sw ? ny : cy;
-    const T uv = sw ? T(0) : cv;
+    const T uv = keep_if(!sw, cv);
     const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv;
     kro = T(0);
     Y0 = fma(om, uy, Y0);
@@ -425,9 +424,12 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     V[i] = uv;
     swaps |= (unsigned long long)sw << i;
     cb = fma(-l, u1, sw ? cc : nb);
-    cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
+    // the row left behind keeps one of c_{i+2} (no swap) and the left spike
+    // (swap); the other is scaled by -l: one product for both
+    const T tq = -l * (sw ? nc : cv);
+    cc = sw ? tq : nc;
     cy = fma(-l, uy, sw ? cy : ny);
-    cv = sw ? cv : -l * cv;
+    cv = sw ? cv : tq;
     if (last) {  // the right spike enters with row mi-1
       w_prev = sw ? cn : cw;
       cw = fma(-l, w_prev, sw ? cw : cn);
@@ -518,6 +520,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     const T tol = sizeof(T) == 8 ? T(16 * 1.1102230246251565e-16) : T(4 * 5.9604645e-8);
     const bool reject = !(fabs(r) <= tol * scale);  // also catches NaN/Inf
     if (__syncthreads_or(reject)) {
+      if (pass == 0 && t == 0) atomicAdd(&g_pge_paths[0], 1ull);
       if (warp == 0) bad |= sep_solve_pivoted<T, NT>(SEP, FST, TMP, lane);
     }
   }
@@ -552,10 +555,10 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
       qb = B[j];
       qa = A[j];
       qc = C[j + 1];
-      const T u2 = ((swaps >> i) & 1ull) && i + 2 < mi ? ci1 : T(0);
+      const T u2 = keep_if(((swaps >> i) & 1ull) && i + 2 < mi, ci1);
       T r = fma(-vi, sp, di);
       if (i == mi - 2) r = fma(-w_prev, st, r);
-      const T xi = fma(-u2, x2, fma(-bi, x1, r)) * ai;
+      const T xi = fma(-bi, x1, fma(-u2, x2, r)) * ai;  // x_{i+2} term first: two ops depend on x_{i+1}
       D[i] = xi;
       xmax = max(xmax, magh(xi));
       bad |= !finite_val(xi);
@@ -588,6 +591,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     accepted = true;
     break;
   }
+  if (t == 0) atomicAdd(&g_pge_paths[pass == 0 ? 1 : 2], 1ull);
   auto sidx = [&](int r) { return (r / m) * ms + (r % m); };
   if (pass > 0 && !pass_bad) {
     // x = x_prev (held in SX) + correction
@@ -845,9 +849,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       const T inv = Div<T>(piv).inv();
       const T l = (sw ? cb : na) * inv;
       const T u1 = sw ? nb : cc;
-      const T u2 = sw ? nc : T(0);
+      const T u2 = keep_if(sw, nc);
       const T uy = sw ? ny : cy;
-      const T uv = sw ? T(0) : cv;
+      const T uv = keep_if(!sw, cv);
       const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv;
       kro = T(0);
       Y0 = fma(om, uy, Y0);
@@ -863,9 +867,12 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       V[i] = uv;
       swaps |= (unsigned long long)sw << i;
       cb = fma(-l, u1, sw ? cc : nb);
-      cc = fma(-l, sw ? nc : T(0), sw ? T(0) : nc);
+      // the row left behind keeps one of c_{i+2} (no swap) and the left spike
+      // (swap); the other is scaled by -l: one product for both
+      const T tq = -l * (sw ? nc : cv);
+      cc = sw ? tq : nc;
       cy = fma(-l, uy, sw ? cy : ny);
-      cv = sw ? cv : -l * cv;
+      cv = sw ? cv : tq;
       if (last) {
         w_prev = sw ? cn : cw;
         cw = fma(-l, w_prev, sw ? cw : cn);
@@ -970,10 +977,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
         qb = B[j];
         qa = A[j];
         qc = C[j + 1];
-        const T u2 = ((swaps >> i) & 1ull) && i + 2 < mi ? ci1 : T(0);
+        const T u2 = keep_if(((swaps >> i) & 1ull) && i + 2 < mi, ci1);
         T r = fma(-vi, sp, di);
         if (i == mi - 2) r = fma(-w_prev, st, r);
-        const T xi = fma(-u2, x2, fma(-bi, x1, r)) * ai;
+        const T xi = fma(-bi, x1, fma(-u2, x2, r)) * ai;  // x_{i+2} term first: two ops depend on x_{i+1}
         D[i] = xi;
         xmax = max(xmax, magh(xi));
         bad |= !finite_val(xi);
@@ -1005,6 +1012,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       accepted = true;
       break;
     }
+    if (rank == 0 && t == 0) atomicAdd(&g_pge_paths[pass == 0 ? 1 : 2], 1ull);
     // x of a neighbouring row that may live in another CTA (staging array `arr`)
     auto xat = [&](const T* arr, int r) -> T {
       const int lr = r - row0;
@@ -1303,6 +1311,17 @@ cudaError_t pge_fallback_count(unsigned long long* out, bool reset) {
   if (e == cudaSuccess && reset) {
     const unsigned long long zero = 0ull;
     e = cudaMemcpyToSymbol(g_pge_fallbacks, &zero, sizeof(zero));
+  }
+  return e;
+}
+
+cudaError_t pge_path_counts(unsigned long long* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_pge_paths, 3 * sizeof(*out));
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(out + 3, g_pge_fallbacks, sizeof(*out));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long zero[3] = {0ull, 0ull, 0ull};
+    e = cudaMemcpyToSymbol(g_pge_paths, zero, sizeof(zero));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_pge_fallbacks, zero, sizeof(zero[0]));
   }
   return e;
 }

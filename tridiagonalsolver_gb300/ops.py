@@ -11,6 +11,8 @@ layouts of include/tridiagonal.h:
 """
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from . import _lib
@@ -168,6 +170,15 @@ def pge_adjoint(a, b, c, x, xbar, n: int, layout: str = "contiguous", info=None,
         _ptr(xbar, a.dtype), _ptr(ga), _ptr(gb), _ptr(gc), _ptr(gd), _ptr(info), n, batch, _stream_ptr(stream))
     check(st, f"tridiag_pge_adjoint_{p}")
     return ga, gb, gc, gd
+
+
+def partition_path_counts(reset: bool = False) -> dict:
+    """Paths taken by the partitioned partial-pivoting solve on the current
+    device since the last reset: separator systems re-solved with pivoting,
+    exact backward-error checks, refinement passes, sequential fallbacks."""
+    buf = (ctypes.c_longlong * 4)()
+    check(lib().tridiag_partition_path_counts(ctypes.addressof(buf), int(reset)))
+    return dict(zip(("pivoted_separators", "exact_checks", "refinement_passes", "fallbacks"), list(buf)))
 
 
 def partition_supported(a, n: int, layout: str = "contiguous") -> bool:

@@ -114,6 +114,8 @@ constexpr int PGE_TMP = 4 * 32;
 // In-kernel refinement steps before the sequential fallback.
 constexpr int PGE_REFINE = 2;
 
+
+
 // One element global -> shared, asynchronously (cp.async, 4 or 8 bytes).
 template <typename T>
 __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
@@ -261,7 +263,18 @@ struct PgeIO {
   size_t stride;
   int n;
   int pf_ahead;  // uniform batches: CTA b prefetches system b + pf_ahead into L2 (0: off)
+  int* err;      // the library's device error word (bounded waits)
 };
+
+// Tensor maps of the TMA-staged FP64 kernel (pge_kernel with SWZ): a, b, c,
+// d, x of a uniform batch viewed as [partitions][2][16] elements, i.e. each
+// 32-row partition as two 128-byte rows.
+struct PgeMaps {
+  CUtensorMap m[5];
+};
+
+// Rows per partition of the TMA-staged kernel.
+constexpr int PGE_SWZ_M = 32;
 
 template <typename T, int MODE>
 __device__ __forceinline__ void pge_store(const PgeIO<T>& io, size_t base, int n, int r, T v) {
@@ -291,19 +304,36 @@ __device__ __forceinline__ void pge_system(const PgeIO<T>& io, int bid, int R, i
   ms = m | 1;
 }
 
-template <typename T, int NT, int MODE>
-__global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
+// Shared-memory position of row i of partition p.  Element staging: odd
+// partition stride ms (the sweeps' column accesses -- lane t, row i of
+// partition t -- are conflict-free).  TMA staging (SWZ, FP64, m = 32): each
+// array as [2][NT][16] elements, half h of partition p one 128-byte row whose
+// 16-byte pairs are XOR-swizzled by p mod 8 (the 128-byte swizzle of the
+// tensor maps); column accesses meet at most four-way bank conflicts.
+template <int NT, bool SWZ>
+__device__ __forceinline__ int pge_off(int p, int i, int ms) {
+  if constexpr (SWZ) return (i >> 4) * (NT * 16) + p * 16 + ((((i >> 1) & 7) ^ (p & 7)) << 1) + (i & 1);
+  else return p * ms + i;
+}
+
+template <typename T, int NT, int MODE, bool SWZ = false>
+__global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
   constexpr int NW = NT / 32;
   int sys, n, m, ms;
   size_t base;
   pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
+  if constexpr (SWZ) ms = PGE_SWZ_M;  // (the launch guarantees n = NT * 32)
   const T* __restrict__ ga = io.a;
   const T* __restrict__ gb = io.b;
   const T* __restrict__ gc = io.c;
   const T* gd = io.d;
   int* info = io.info;
+  auto off = [&](int p, int i) { return pge_off<NT, SWZ>(p, i, ms); };
+  __shared__ __align__(8) uint64_t s_bar[2];
   extern __shared__ __align__(16) unsigned char pge_smem[];
-  T* SA = reinterpret_cast<T*>(pge_smem);
+  unsigned char* sm = pge_smem;
+  if constexpr (SWZ) sm += (1024u - (smem_u32(pge_smem) & 1023u)) & 1023u;  // 128-byte swizzle: 1 KB aligned
+  T* SA = reinterpret_cast<T*>(sm);
   T* SB = SA + NT * ms;
   T* SC = SB + NT * ms;
   T* SD = SC + NT * ms;
@@ -322,30 +352,46 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     s_xmax = 0;
   }
 
-  // ---- stage the system with asynchronous element copies (cp.async): warp
-  // w copies partitions w, w+NW, ... (a partition's rows are contiguous in
-  // global memory, so each copy instruction moves 32 consecutive elements)
-  // into the odd-stride layout; every copy is in flight before the first
-  // wait.  a_0, c_{n-1} and the identity rows past n are stored directly.
-#pragma unroll 4
-  for (int p = warp; p < NT; p += NW) {
-    for (int i = lane; i < m; i += 32) {
-      const int r = p * m + i;
-      const int s = p * ms + i;
-      if (r < n) {
-        if (r > 0) cp_async_elem(SA + s, ga + base + r); else SA[s] = T(0);
-        cp_async_elem(SB + s, gb + base + r);
-        if (r < n - 1) cp_async_elem(SC + s, gc + base + r); else SC[s] = T(0);
-        cp_async_elem(SD + s, gd + base + r);
-      } else {
-        SA[s] = T(0);
-        SB[s] = T(1);
-        SC[s] = T(0);
-        SD[s] = T(0);
+  // ---- stage the system.  SWZ: one TMA box (16 rows x NT partitions) per
+  // array and half, each half counted on its own mbarrier, so that the
+  // forward sweep starts on rows 0-15 while rows 16-31 are in flight.
+  // Otherwise asynchronous element copies (cp.async): warp w copies
+  // partitions w, w+NW, ... (a partition's rows are contiguous in global
+  // memory, so each copy instruction moves 32 consecutive elements), every
+  // copy in flight before the first wait; a_0, c_{n-1} and the identity rows
+  // past n are stored directly.
+  if constexpr (SWZ) {
+    if (t == 0) {
+      mbar_init(&s_bar[0], 1);
+      mbar_init(&s_bar[1], 1);
+      fence_mbar_init();
+      for (int h = 0; h < 2; ++h) {
+        mbar_arrive_expect_tx(&s_bar[h], (unsigned)(4 * NT * 16 * sizeof(T)));
+        T* dst[4] = {SA, SB, SC, SD};
+        for (int k = 0; k < 4; ++k) tma_load_3d(dst[k] + h * NT * 16, &maps.m[k], 0, h, sys * NT, &s_bar[h]);
       }
     }
+  } else {
+#pragma unroll 4
+    for (int p = warp; p < NT; p += NW) {
+      for (int i = lane; i < m; i += 32) {
+        const int r = p * m + i;
+        const int s = off(p, i);
+        if (r < n) {
+          if (r > 0) cp_async_elem(SA + s, ga + base + r); else SA[s] = T(0);
+          cp_async_elem(SB + s, gb + base + r);
+          if (r < n - 1) cp_async_elem(SC + s, gc + base + r); else SC[s] = T(0);
+          cp_async_elem(SD + s, gd + base + r);
+        } else {
+          SA[s] = T(0);
+          SB[s] = T(1);
+          SC[s] = T(0);
+          SD[s] = T(0);
+        }
+      }
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
   }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
   // One CTA per SM fits: the CTA that runs here next (about one wave later)
   // finds its system in L2 instead of HBM.
   if (io.pf_ahead > 0 && t == 0 && (int)blockIdx.x + io.pf_ahead < (int)gridDim.x) {
@@ -372,32 +418,32 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   //   omega_i u0_i + omega_{i-1} u1_{i-1} + omega_{i-2} u2_{i-2} = [i = 0],
   // accumulated into omega . y', omega . v', omega . w' during the sweep.
   const int mi = m - 1;
-  T* A = SA + t * ms;
-  T* B = SB + t * ms;
-  T* C = SC + t * ms;
-  T* D = SD + t * ms;
-  T* V = SV + t * ms;
+  auto A = [&](int i) -> T& { return SA[off(t, i)]; };
+  auto B = [&](int i) -> T& { return SB[off(t, i)]; };
+  auto C = [&](int i) -> T& { return SC[off(t, i)]; };
+  auto D = [&](int i) -> T& { return SD[off(t, i)]; };
+  auto V = [&](int i) -> T& { return SV[off(t, i)]; };
   bool bad = false;  // this pass: breakdown, non-finite or (pass 0) separator residual
-  unsigned long long swaps = 0ull;
-  T cb = B[0], cc = mi > 1 ? C[0] : T(0), cy = D[0], cv = A[0], cw = mi == 1 ? C[0] : T(0);
-  amax = max(amax, max(magh(cv), max(magh(cb), magh(C[0]))));  // magnitudes for the acceptance test
-  dmax = max(dmax, magh(cy));
+  T cb, cc, cy, cv, cw;                        // the candidate row (b, c, y', v', w')
   T w_prev = T(0);                             // w' of U row mi-2 (the only other nonzero w')
   T om1 = T(0), om2 = T(0);                    // omega_{i-1}, omega_{i-2}
   T kro = T(1);                                // [i = 0] of the omega recurrence
   T pu1 = T(0), pu2a = T(0), pu2b = T(0);      // u1_{i-1}, u2_{i-1}, u2_{i-2}
   T Y0 = T(0), V0 = T(0);                      // omega . y', omega . v'
-  // software-pipelined: row i+2 (at most the separator row, which always
-  // exists) is loaded while row i+1 is eliminated
-  T pa = A[1], pb = B[1], pc = C[1], py = D[1];
-  for (int i = 0; i + 1 < mi; ++i) {
-    const T na = pa, nb = pb, cn = pc, ny = py;
+  T as, bs, cs, ds;                            // the separator row m-1
+  auto first_row = [&](T a0, T b0, T c0, T d0) {
+    cb = b0;
+    cc = mi > 1 ? c0 : T(0);
+    cy = d0;
+    cv = a0;
+    cw = mi == 1 ? c0 : T(0);
+    amax = max(amax, max(magh(a0), max(magh(b0), magh(c0))));  // magnitudes for the acceptance test
+    dmax = max(dmax, magh(d0));
+  };
+  // row i+1 (a, b, c, y) against the candidate row: U row i
+  auto eliminate = [&](int i, T na, T nb, T cn, T ny) {
     amax = max(amax, max(magh(na), max(magh(nb), magh(cn))));
     dmax = max(dmax, magh(ny));
-    pa = A[i + 2];
-    pb = B[i + 2];
-    pc = C[i + 2];
-    py = D[i + 2];
     const bool last = i + 2 == mi;  // row i+1 is the last interior row
     const T nc = last ? T(0) : cn;
     const bool sw = !abs_ge(cb, na);
@@ -418,11 +464,11 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     pu2b = pu2a;
     pu2a = u2;
     pu1 = u1;
-    A[i] = inv;
-    B[i] = u1;
-    D[i] = uy;
-    V[i] = uv;
-    swaps |= (unsigned long long)sw << i;
+    A(i) = inv;
+    B(i) = u1;
+    C(i) = u2;  // c_i was read two rows ago
+    D(i) = uy;
+    V(i) = uv;
     cb = fma(-l, u1, sw ? cc : nb);
     // the row left behind keeps one of c_{i+2} (no swap) and the left spike
     // (swap); the other is scaled by -l: one product for both
@@ -434,6 +480,31 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
       w_prev = sw ? cn : cw;
       cw = fma(-l, w_prev, sw ? cw : cn);
     }
+  };
+  {
+    // first pass of a TMA-staged system: wait for each half as the sweep
+    // reaches it (a timeout marks the pass bad: the system is then restaged
+    // and solved by the refinement passes)
+    if (SWZ && pass == 0) bad |= !mbar_wait(&s_bar[0], 0, io.err);
+    // a_0 and c_{n-1} are zero by definition (TMA staging copies whatever
+    // the arrays hold there)
+    first_row(t == 0 ? T(0) : A(0), B(0), C(0), D(0));
+    // software-pipelined: row i+2 (at most the separator row, which always
+    // exists) is loaded while row i+1 is eliminated
+    T pa = A(1), pb = B(1), pc = C(1), py = D(1);
+    for (int i = 0; i + 1 < mi; ++i) {
+      const T na = pa, nb = pb, cn = pc, ny = py;
+      if (SWZ && pass == 0 && i + 2 == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
+      pa = A(i + 2);
+      pb = B(i + 2);
+      pc = C(i + 2);
+      py = D(i + 2);
+      eliminate(i, na, nb, cn, ny);
+    }
+    as = A(mi);
+    bs = B(mi);
+    cs = t * m + mi == n - 1 ? T(0) : C(mi);
+    ds = D(mi);
   }
   // U row mi-1 is the remaining candidate row (u1 = u2 = 0)
   bad |= is_zero(cb);
@@ -448,15 +519,15 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     FST[2 * NT + t] = W0;
   }
   const T Ylast = cy * inv_last, Vlast = cv * inv_last, Wlast = cw * inv_last;
-  A[mi - 1] = inv_last;
-  B[mi - 1] = T(0);
-  D[mi - 1] = cy;
-  V[mi - 1] = cv;
+  A(mi - 1) = inv_last;
+  B(mi - 1) = T(0);
+  C(mi - 1) = T(0);
+  D(mi - 1) = cy;
+  V(mi - 1) = cv;
   __syncthreads();
 
   // ---- separator system: row m-1 of partition t couples to the last
   // interior row of t and the first row of t+1
-  const T as = A[mi], bs = B[mi], cs = C[mi], ds = D[mi];
   amax = max(amax, max(magh(as), max(magh(bs), magh(cs))));
   dmax = max(dmax, magh(ds));
   if (pass == 0) {
@@ -538,36 +609,35 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
   MagT xmax = magh(st);
   T x_last;
   {
-    T x1 = (fma(-cw, st, fma(-V[mi - 1], sp, D[mi - 1]))) * inv_last;
+    T x1 = (fma(-cw, st, fma(-V(mi - 1), sp, D(mi - 1)))) * inv_last;
     T x2 = T(0);
-    D[mi - 1] = x1;
+    D(mi - 1) = x1;
     xmax = max(xmax, magh(x1));
     bad |= !finite_val(x1);
     x_last = x1;
     // software-pipelined: row i-1's factors are loaded while row i is solved
     int j = mi - 2 >= 0 ? mi - 2 : 0;
-    T qv = V[j], qd = D[j], qb = B[j], qa = A[j], qc = C[j + 1];
+    T qv = V(j), qd = D(j), qb = B(j), qa = A(j), qc = C(j);
     for (int i = mi - 2; i >= 0; --i) {
-      const T vi = qv, di = qd, bi = qb, ai = qa, ci1 = qc;
+      const T vi = qv, di = qd, bi = qb, ai = qa, u2 = qc;
       j = i > 0 ? i - 1 : 0;
-      qv = V[j];
-      qd = D[j];
-      qb = B[j];
-      qa = A[j];
-      qc = C[j + 1];
-      const T u2 = keep_if(((swaps >> i) & 1ull) && i + 2 < mi, ci1);
+      qv = V(j);
+      qd = D(j);
+      qb = B(j);
+      qa = A(j);
+      qc = C(j);
       T r = fma(-vi, sp, di);
       if (i == mi - 2) r = fma(-w_prev, st, r);
       const T xi = fma(-bi, x1, fma(-u2, x2, r)) * ai;  // x_{i+2} term first: two ops depend on x_{i+1}
-      D[i] = xi;
+      D(i) = xi;
       xmax = max(xmax, magh(xi));
       bad |= !finite_val(xi);
       x2 = x1;
       x1 = xi;
     }
     bad |= !finite_val(st);
-    D[mi] = st;
-    FST[NT + t] = D[0];  // first x of the partition, for the separator residual of t-1
+    D(mi) = st;
+    FST[NT + t] = D(0);  // first x of the partition, for the separator residual of t-1
     if (pass == 0) atomicMax(&s_xmax, xmax);
     __syncthreads();
     const T x_next = t + 1 < NT ? FST[NT + t + 1] : T(0);
@@ -592,7 +662,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     break;
   }
   if (t == 0) atomicAdd(&g_pge_paths[pass == 0 ? 1 : 2], 1ull);
-  auto sidx = [&](int r) { return (r / m) * ms + (r % m); };
+  auto sidx = [&](int r) { return off(r / m, r % m); };
   if (pass > 0 && !pass_bad) {
     // x = x_prev (held in SX) + correction
     for (int r = t; r < n; r += NT) SD[sidx(r)] += SX[sidx(r)];
@@ -689,11 +759,24 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io) {
     return;
   }
   if (info && t == 0) info[sys] = 0;
+  if constexpr (SWZ) {
+    // x by two TMA stores (the rows were written by several threads in a
+    // refinement pass: fence, then barrier)
+    fence_async_smem();
+    __syncthreads();
+    if (t == 0) {
+      tma_store_3d(&maps.m[4], 0, 0, sys * NT, SD);
+      tma_store_3d(&maps.m[4], 0, 1, sys * NT, SD + NT * 16);
+      bulk_commit();
+      bulk_wait_read<0>();  // shared memory stays valid until the stores have read it
+    }
+  } else {
 #pragma unroll 4
-  for (int p = warp; p < NT; p += NW) {
-    for (int i = lane; i < m; i += 32) {
-      const int r = p * m + i;
-      if (r < n) pge_store<T, MODE>(io, base, n, r, SD[p * ms + i]);
+    for (int p = warp; p < NT; p += NW) {
+      for (int i = lane; i < m; i += 32) {
+        const int r = p * m + i;
+        if (r < n) pge_store<T, MODE>(io, base, n, r, SD[off(p, i)]);
+      }
     }
   }
 }
@@ -1153,13 +1236,12 @@ int pge_variant_max_n(int v) {
   return pge_variant_partitions(v) * pge_variant_mmax<T>(v);
 }
 
-template <typename T, int NT, int MODE>
-static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int ms, cudaStream_t s) {
-  const size_t smem = pge_smem_bytes<T, NT>(ms);
-  cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, NT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+template <typename T, int NT, int MODE, bool SWZ>
+static cudaError_t pge_launch_k(const PgeIO<T>& io_in, const PgeMaps& maps, int grid, size_t smem, cudaStream_t s) {
   PgeIO<T> io = io_in;
-  io.pf_ahead = 0;
+  cudaError_t e =
+      cudaFuncSetAttribute(pge_kernel<T, NT, MODE, SWZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   // L2 prefetch one wave ahead for uniform batches with 16-byte aligned systems
   const uintptr_t al = reinterpret_cast<uintptr_t>(io.a) | reinterpret_cast<uintptr_t>(io.b) |
                        reinterpret_cast<uintptr_t>(io.c) | reinterpret_cast<uintptr_t>(io.d);
@@ -1167,12 +1249,35 @@ static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int ms, cudaStrea
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE>, NT, smem) == cudaSuccess &&
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE, SWZ>, NT, smem) == cudaSuccess &&
         per > 0 && grid > sms * per)
       io.pf_ahead = sms * per;
   }
-  pge_kernel<T, NT, MODE><<<grid, NT, smem, s>>>(io);
+  pge_kernel<T, NT, MODE, SWZ><<<grid, NT, smem, s>>>(io, maps);
   return cudaGetLastError();
+}
+
+template <typename T, int NT, int MODE>
+static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int m_max, cudaStream_t s) {
+  PgeIO<T> io = io_in;
+  io.pf_ahead = 0;
+  io.err = error_word();
+  PgeMaps maps{};
+  // TMA staging: FP64 solve of a uniform contiguous batch with 32 rows per
+  // partition (n = 32 NT), arrays 16-byte aligned
+  if constexpr (MODE == 0 && sizeof(T) == 8) {
+    const size_t smem_swz = 1024 + pge_smem_bytes<T, NT>(PGE_SWZ_M);
+    if (!io.offsets && !io.list && io.n == PGE_SWZ_M * NT && io.stride == (size_t)io.n && smem_swz <= PGE_SMEM_MAX &&
+        (uint64_t)NT * grid < (1ull << 31)) {
+      const T* arr[5] = {io.a, io.b, io.c, io.d, io.x};
+      bool ok = true;
+      for (int k = 0; k < 5 && ok; ++k)
+        ok = encode_tmap_3d(&maps.m[k], arr[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, 16, 2, (uint64_t)NT * grid, 128,
+                            PGE_SWZ_M * 8, 16, 1, NT, CU_TENSOR_MAP_SWIZZLE_128B);
+      if (ok) return pge_launch_k<T, NT, MODE, true>(io, maps, grid, smem_swz, s);
+    }
+  }
+  return pge_launch_k<T, NT, MODE, false>(io, maps, grid, pge_smem_bytes<T, NT>(m_max | 1), s);
 }
 
 template <typename T, int NT, int CL, int MODE>
@@ -1189,11 +1294,12 @@ static cudaError_t pgc_launch(const PgeIO<T>& io, int grid, int ms, cudaStream_t
 // per partition.
 template <typename T, int MODE>
 static cudaError_t pge_launch_variant(int v, const PgeIO<T>& io, int grid, int m_max, cudaStream_t s) {
-  const int ms = (m_max < 2 ? 2 : m_max) | 1;
+  if (m_max < 2) m_max = 2;
+  const int ms = m_max | 1;
   switch (v) {
-    case 1: return pge_launch<T, 64, MODE>(io, grid, ms, s);
-    case 2: return pge_launch<T, 128, MODE>(io, grid, ms, s);
-    case 3: return pge_launch<T, 256, MODE>(io, grid, ms, s);
+    case 1: return pge_launch<T, 64, MODE>(io, grid, m_max, s);
+    case 2: return pge_launch<T, 128, MODE>(io, grid, m_max, s);
+    case 3: return pge_launch<T, 256, MODE>(io, grid, m_max, s);
     case 4: return pgc_launch<T, 128, 2, MODE>(io, grid, ms, s);
     case 5: return pgc_launch<T, 128, 4, MODE>(io, grid, ms, s);
     case 6: return pgc_launch<T, 128, 8, MODE>(io, grid, ms, s);

@@ -55,6 +55,31 @@ bool encode_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtyp
   return r == CUDA_SUCCESS;
 }
 
+bool encode_tmap_3d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype, int elem_bytes, uint64_t d0,
+                    uint64_t d1, uint64_t d2, uint64_t stride1_bytes, uint64_t stride2_bytes, uint32_t box0,
+                    uint32_t box1, uint32_t box2, CUtensorMapSwizzle swizzle) {
+  thread_local bool bound = false;
+  if (!bound) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) bound = true;
+  }
+  auto fn = encode_fn();
+  if (!fn || !base) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (stride1_bytes & 15u) != 0 || (stride2_bytes & 15u) != 0)
+    return false;
+  if (d0 == 0 || d1 == 0 || d2 == 0 || stride1_bytes < d0 * (uint64_t)elem_bytes || stride2_bytes < stride1_bytes)
+    return false;
+  cuuint64_t dims[3] = {d0, d1, d2};
+  cuuint64_t strides[2] = {stride1_bytes, stride2_bytes};
+  cuuint32_t box[3] = {box0, box1, box2};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, dtype, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS && std::getenv("TRIDIAG_DEBUG"))
+    std::fprintf(stderr, "tridiag: 3-D tensor map refused (CUresult %d)\n", (int)r);
+  return r == CUDA_SUCCESS;
+}
+
 static std::mutex g_err_mu;
 static int* g_err_words[64] = {};
 

@@ -177,6 +177,26 @@ int tridiag_solve_out_double(int algo, int layout, const double *a, const double
                              const double *d, double *x, void *work, size_t work_bytes, int n_eqt, int n_batch,
                              void *stream);
 
+/* Out-of-place solve with a, b, c, d and x in HOST memory (no counterpart in
+ * the reference, whose test harness, Tridiagonal_CUDA/utils.cu:259-281,
+ * copies each array to the device before the call).  The batch streams
+ * through device buffers in chunks of `chunk` systems (0: about 48 MB of
+ * inputs per chunk): host -> device copies, the solve of
+ * tridiag_solve_out_* with `algo`, device -> host copy of x, on three
+ * streams of the library's own, so that the copies of one chunk overlap the
+ * solve of another; the streams and a ring of three chunk buffers persist per
+ * device (grown on demand) and are shared by all such calls, so that calls
+ * made from independent caller streams keep the host link busy back to back.
+ * Layouts: contiguous and interleaved (2-D copies).  Ordered after the work
+ * queued on `stream`; work queued on `stream` afterwards runs after x is
+ * complete in host memory.  Returns once the copies are queued: x is valid
+ * after `stream` is synchronised.  Page-locked host memory moves at the
+ * link's rate; pageable memory works but the driver stages it. */
+int tridiag_solve_host_single(int algo, int layout, const float *a, const float *b, const float *c, const float *d,
+                              float *x, int n_eqt, int n_batch, int chunk, void *stream);
+int tridiag_solve_host_double(int algo, int layout, const double *a, const double *b, const double *c,
+                              const double *d, double *x, int n_eqt, int n_batch, int chunk, void *stream);
+
 /* Bytes of workspace tridiag_gtsv_* needs (precision: 0 = single, 1 = double). */
 size_t tridiag_gtsv_workspace_size(int precision, int layout, int n_eqt, int n_batch);
 /* Bytes of the pivot record written by tridiag_gtsv_* (one bit per row). */

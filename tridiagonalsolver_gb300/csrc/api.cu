@@ -2,6 +2,7 @@
 // the kernel launchers, and the per-thread status of the last call.
 // Declarations and contracts: include/tridiagonal.h.
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "../../include/tridiagonal.h"
@@ -790,6 +791,162 @@ int tridiag_periodic_single(int algo, const float* a, const float* b, const floa
 int tridiag_periodic_double(int algo, const double* a, const double* b, const double* c, const double* d, double* x,
                             void* work, size_t work_bytes, int n, int batch, void* stream) {
   return set_status(periodic_impl<double>(algo, a, b, c, d, x, work, work_bytes, n, batch, (cudaStream_t)stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Solves with the arrays in host memory: the batch streams through device
+// buffers in chunks, each chunk's host -> device copies, solve and
+// device -> host copy of x on three streams of the library's own, so that the
+// link carries one chunk while another is solved.  Streams, a ring of chunk
+// buffers and its events persist per device and are shared by all such calls
+// (enqueued under a lock): a call made while an earlier one is still in
+// flight -- from an independent caller stream -- queues its copies behind the
+// earlier ones and keeps the link busy across calls.
+namespace {
+
+constexpr int HOST_SLOTS = 3;
+// Systems per chunk: about 48 MB of coefficient and right-hand-side bytes.
+constexpr size_t HOST_CHUNK_BYTES = 48u << 20;
+
+struct HostPipe {
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  unsigned char* buf = nullptr;
+  size_t slot_bytes = 0;
+  cudaEvent_t ev_in[HOST_SLOTS] = {}, ev_comp[HOST_SLOTS] = {}, ev_out[HOST_SLOTS] = {};
+  bool used[HOST_SLOTS] = {};
+  int next = 0;
+};
+
+std::mutex g_pipe_mu;
+HostPipe g_pipes[64];
+
+cudaError_t host_pipe_init(HostPipe& q) {
+  if (q.in) return cudaSuccess;
+  cudaError_t e = cudaStreamCreateWithFlags(&q.in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&q.comp, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&q.out, cudaStreamNonBlocking);
+  for (int k = 0; k < HOST_SLOTS && e == cudaSuccess; ++k) {
+    e = cudaEventCreateWithFlags(&q.ev_in[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&q.ev_comp[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&q.ev_out[k], cudaEventDisableTiming);
+  }
+  return e;
+}
+
+// Grow the ring to slots of at least `bytes` (waits for the pipe's work).
+cudaError_t host_pipe_reserve(HostPipe& q, size_t bytes) {
+  if (q.slot_bytes >= bytes) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(q.in);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(q.comp);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(q.out);
+  if (e == cudaSuccess && q.buf) e = cudaFree(q.buf);
+  q.buf = nullptr;
+  q.slot_bytes = 0;
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&q.buf), HOST_SLOTS * bytes);
+  if (e == cudaSuccess) q.slot_bytes = bytes;
+  for (bool& u : q.used) u = false;
+  return e;
+}
+
+template <typename T>
+int solve_host_impl(int algo, int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
+                    int chunk, cudaStream_t s) {
+  if (!valid_dims(n, batch) || !valid_layout(layout) || !a || !b || !c || !d || !x || chunk < 0)
+    return TRIDIAG_ERR_INVALID_VALUE;
+  if (layout == TRIDIAG_LAYOUT_PACKED) return TRIDIAG_ERR_NOT_SUPPORTED;
+  const size_t row = (size_t)n * sizeof(T);  // one array of one system
+  int K = chunk;
+  if (K == 0) {
+    const size_t k = HOST_CHUNK_BYTES / (4 * row);
+    K = (int)(k < 1 ? 1 : k > (size_t)batch ? (size_t)batch : k);
+  }
+  if (K > batch) K = batch;
+  const int nchunks = (batch + K - 1) / K;
+  const size_t arr = align_up((size_t)K * row);
+  const int ws_algo = algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM || algo == TRIDIAG_ALGO_CR ||
+                              algo == TRIDIAG_ALGO_PCR || algo == TRIDIAG_ALGO_PARTITION
+                          ? TRIDIAG_ALGO_THOMAS  // possible fallback
+                          : algo;
+  const size_t ws = align_up(solve_out_ws<T>(ws_algo, n, K));
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TRIDIAG_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_pipe_mu);
+  HostPipe& p = g_pipes[dev];
+  cudaError_t e = host_pipe_init(p);
+  if (e == cudaSuccess) e = host_pipe_reserve(p, 5 * arr + ws);
+  if (e != cudaSuccess) return cuda_status(e);
+  cudaEvent_t ev_start = nullptr, ev_end = nullptr;
+  e = cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_end, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_start, s);
+  for (cudaStream_t q : {p.in, p.comp, p.out})
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(q, ev_start, 0);
+  const bool inter = layout == TRIDIAG_LAYOUT_INTERLEAVED;
+  // one array of the systems [j0, j0 + kc) between host and a device buffer
+  auto copy = [&](T* dst, const T* src, int j0, int kc, bool to_dev, cudaStream_t q) {
+    if (!inter) {
+      const size_t bytes = (size_t)kc * row;
+      return to_dev ? cudaMemcpyAsync(dst, src + (size_t)j0 * n, bytes, cudaMemcpyHostToDevice, q)
+                    : cudaMemcpyAsync(dst + (size_t)j0 * n, src, bytes, cudaMemcpyDeviceToHost, q);
+    }
+    const size_t w = (size_t)kc * sizeof(T), hp = (size_t)batch * sizeof(T);
+    return to_dev ? cudaMemcpy2DAsync(dst, w, src + j0, hp, w, n, cudaMemcpyHostToDevice, q)
+                  : cudaMemcpy2DAsync(dst + j0, hp, src, w, w, n, cudaMemcpyDeviceToHost, q);
+  };
+  int st = TRIDIAG_SUCCESS;
+  for (int ch = 0; ch < nchunks && e == cudaSuccess && st == TRIDIAG_SUCCESS; ++ch) {
+    const int k = p.next, j0 = ch * K, kc = batch - j0 < K ? batch - j0 : K;
+    p.next = (p.next + 1) % HOST_SLOTS;
+    unsigned char* sb = p.buf + k * p.slot_bytes;
+    T* da = reinterpret_cast<T*>(sb);
+    T* db = reinterpret_cast<T*>(sb + arr);
+    T* dc = reinterpret_cast<T*>(sb + 2 * arr);
+    T* dd = reinterpret_cast<T*>(sb + 3 * arr);
+    T* dx = reinterpret_cast<T*>(sb + 4 * arr);
+    void* dw = ws ? sb + 5 * arr : nullptr;
+    // inputs, once the slot's previous solve has read its own
+    if (p.used[k]) e = cudaStreamWaitEvent(p.in, p.ev_comp[k], 0);
+    const T* src[4] = {a, b, c, d};
+    T* dst[4] = {da, db, dc, dd};
+    for (int q = 0; q < 4 && e == cudaSuccess; ++q) e = copy(dst[q], src[q], j0, kc, true, p.in);
+    if (e == cudaSuccess) e = cudaEventRecord(p.ev_in[k], p.in);
+    // solve, once the inputs are in and the slot's previous x is out
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(p.comp, p.ev_in[k], 0);
+    if (e == cudaSuccess && p.used[k]) e = cudaStreamWaitEvent(p.comp, p.ev_out[k], 0);
+    if (e == cudaSuccess) st = solve_out_impl<T>(algo, layout, da, db, dc, dd, dx, dw, ws, n, kc, p.comp);
+    if (e == cudaSuccess && st == TRIDIAG_SUCCESS) e = cudaEventRecord(p.ev_comp[k], p.comp);
+    // x back to the host
+    if (e == cudaSuccess && st == TRIDIAG_SUCCESS) e = cudaStreamWaitEvent(p.out, p.ev_comp[k], 0);
+    if (e == cudaSuccess && st == TRIDIAG_SUCCESS) e = copy(x, dx, j0, kc, false, p.out);
+    if (e == cudaSuccess && st == TRIDIAG_SUCCESS) e = cudaEventRecord(p.ev_out[k], p.out);
+    p.used[k] = true;
+  }
+  // the copy-out stream has waited for every solve of this call: the
+  // caller's stream continues after its last copy
+  if (ev_end) {
+    const cudaError_t r = cudaEventRecord(ev_end, p.out);
+    const cudaError_t w = r == cudaSuccess ? cudaStreamWaitEvent(s, ev_end, 0) : r;
+    if (e == cudaSuccess) e = w;
+  }
+  if (ev_start) cudaEventDestroy(ev_start);
+  if (ev_end) cudaEventDestroy(ev_end);
+  if (st != TRIDIAG_SUCCESS) return st;
+  return cuda_status(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tridiag_solve_host_single(int algo, int layout, const float* a, const float* b, const float* c, const float* d,
+                              float* x, int n, int batch, int chunk, void* stream) {
+  return set_status(solve_host_impl<float>(algo, layout, a, b, c, d, x, n, batch, chunk, (cudaStream_t)stream));
+}
+int tridiag_solve_host_double(int algo, int layout, const double* a, const double* b, const double* c,
+                              const double* d, double* x, int n, int batch, int chunk, void* stream) {
+  return set_status(solve_host_impl<double>(algo, layout, a, b, c, d, x, n, batch, chunk, (cudaStream_t)stream));
 }
 
 }  // extern "C"

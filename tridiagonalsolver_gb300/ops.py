@@ -95,6 +95,26 @@ def solve_out(a, b, c, d, n: int, algo: str = "auto", layout: str = "contiguous"
     return x
 
 
+def solve_host(a, b, c, d, n: int, algo: str = "auto", layout: str = "contiguous", out=None, chunk: int = 0,
+               stream=None):
+    """Out-of-place solve of host (CPU) tensors through the chunked
+    host -> device -> host pipeline of tridiag_solve_host_*; returns x (a new
+    page-locked tensor or ``out``), valid once ``stream`` (default: the
+    current CUDA stream) has been synchronised."""
+    for t in (a, b, c, d):
+        if t.device.type != "cpu":
+            raise ValueError("solve_host takes host tensors")
+    p = _prec(a)
+    batch = _dims(a, n, layout)
+    a, b, c, d = (t.contiguous() for t in (a, b, c, d))
+    x = out if out is not None else torch.empty(d.shape, dtype=d.dtype).pin_memory()
+    st = getattr(lib(), f"tridiag_solve_host_{p}")(
+        ALGOS[algo], LAYOUTS[layout], a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), n,
+        batch, int(chunk), _stream_ptr(stream))
+    check(st, f"tridiag_solve_host_{p}({algo}, {layout})")
+    return x
+
+
 def gtsv_workspace(a: torch.Tensor, n: int, layout: str = "contiguous") -> torch.Tensor:
     batch = _dims(a, n, layout)
     nbytes = lib().tridiag_gtsv_workspace_size(1 if a.dtype == torch.float64 else 0, LAYOUTS[layout], n, batch)

@@ -807,8 +807,10 @@ int tridiag_periodic_double(int algo, const double* a, const double* b, const do
 namespace {
 
 constexpr int HOST_SLOTS = 3;
-// Systems per chunk: about 48 MB of coefficient and right-hand-side bytes.
-constexpr size_t HOST_CHUNK_BYTES = 48u << 20;
+// Systems per chunk: about 96 MB of coefficient and right-hand-side bytes
+// (measured on GB300: each copy adds a fixed gap on the link, so 12 MB chunks
+// cost 15% over 96 MB ones; larger chunks lengthen the pipeline's fill).
+constexpr size_t HOST_CHUNK_BYTES = 96u << 20;
 
 struct HostPipe {
   cudaStream_t in = nullptr, comp = nullptr, out = nullptr;

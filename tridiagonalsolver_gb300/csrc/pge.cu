@@ -304,42 +304,62 @@ __device__ __forceinline__ void pge_system(const PgeIO<T>& io, int bid, int R, i
   ms = m | 1;
 }
 
-// Shared-memory position of row i of partition p.  Element staging: odd
-// partition stride ms (the sweeps' column accesses -- lane t, row i of
-// partition t -- are conflict-free).  TMA staging (SWZ, FP64, m = 32): each
-// array as [2][NT][16] elements, half h of partition p one 128-byte row whose
-// 16-byte pairs are XOR-swizzled by p mod 8 (the 128-byte swizzle of the
-// tensor maps); column accesses meet at most four-way bank conflicts.
-template <int NT, bool SWZ>
-__device__ __forceinline__ int pge_off(int p, int i, int ms) {
-  if constexpr (SWZ) return (i >> 4) * (NT * 16) + p * 16 + ((((i >> 1) & 7) ^ (p & 7)) << 1) + (i & 1);
+// Staging modes of pge_kernel (template parameter LAY) and the shared-memory
+// position of row i of partition p in each:
+//  * PGE_ELEM: asynchronous element copies into an odd partition stride ms
+//    (the sweeps' column accesses -- lane t, row i of partition t -- are
+//    conflict-free);
+//  * PGE_DENSE: the system's rows in order (row r at delta + r, delta = the
+//    system's offset modulo 16 bytes), moved by one bulk copy per array; the
+//    partition size m is odd, so the column accesses are conflict-free;
+//  * PGE_SWZ (FP64, m = 32): each array as [2][NT][16] elements, half h of
+//    partition p one 128-byte row whose 16-byte pairs are XOR-swizzled by
+//    p mod 8 (the 128-byte swizzle of the tensor maps); column accesses meet
+//    at most four-way bank conflicts.
+constexpr int PGE_ELEM = 0, PGE_DENSE = 1, PGE_SWZ = 2;
+
+template <int NT, int LAY>
+__device__ __forceinline__ int pge_off(int p, int i, int ms, int m, int delta) {
+  if constexpr (LAY == PGE_SWZ) return (i >> 4) * (NT * 16) + p * 16 + ((((i >> 1) & 7) ^ (p & 7)) << 1) + (i & 1);
+  else if constexpr (LAY == PGE_DENSE) return delta + p * m + i;
   else return p * ms + i;
 }
 
-template <typename T, int NT, int MODE, bool SWZ = false>
+// Elements per staged array: NT partitions of stride ms, plus the dense
+// layout's shift, rounded to 16 bytes.
+template <typename T, int NT>
+__host__ __device__ constexpr int pge_array_elems(int ms) {
+  return (NT * ms + 2 * (16 / (int)sizeof(T)) - 1) / (16 / (int)sizeof(T)) * (16 / (int)sizeof(T));
+}
+
+template <typename T, int NT, int MODE, int LAY = PGE_ELEM>
 __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
   constexpr int NW = NT / 32;
+  constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
   pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
-  if constexpr (SWZ) ms = PGE_SWZ_M;  // (the launch guarantees n = NT * 32)
+  if constexpr (LAY == PGE_SWZ) ms = PGE_SWZ_M;  // (the launch guarantees n = NT * 32)
+  if constexpr (LAY == PGE_DENSE) m |= 1;        // odd partitions (ms = m)
+  const int delta = LAY == PGE_DENSE ? (int)(base % VE) : 0;
   const T* __restrict__ ga = io.a;
   const T* __restrict__ gb = io.b;
   const T* __restrict__ gc = io.c;
   const T* gd = io.d;
   int* info = io.info;
-  auto off = [&](int p, int i) { return pge_off<NT, SWZ>(p, i, ms); };
+  auto off = [&](int p, int i) { return pge_off<NT, LAY>(p, i, ms, m, delta); };
   __shared__ __align__(8) uint64_t s_bar[2];
   extern __shared__ __align__(16) unsigned char pge_smem[];
   unsigned char* sm = pge_smem;
-  if constexpr (SWZ) sm += (1024u - (smem_u32(pge_smem) & 1023u)) & 1023u;  // 128-byte swizzle: 1 KB aligned
+  if constexpr (LAY == PGE_SWZ) sm += (1024u - (smem_u32(pge_smem) & 1023u)) & 1023u;  // 128-byte swizzle: 1 KB aligned
+  const int astride = LAY == PGE_SWZ ? NT * PGE_SWZ_M : pge_array_elems<T, NT>(ms);
   T* SA = reinterpret_cast<T*>(sm);
-  T* SB = SA + NT * ms;
-  T* SC = SB + NT * ms;
-  T* SD = SC + NT * ms;
-  T* SV = SD + NT * ms;
-  T* SX = SV + NT * ms;   // x kept across refinement passes
-  T* SEP = SX + NT * ms;  // [3][4][NT] separator rows: original + ping-pong
+  T* SB = SA + astride;
+  T* SC = SB + astride;
+  T* SD = SC + astride;
+  T* SV = SD + astride;
+  T* SX = SV + astride;   // x kept across refinement passes
+  T* SEP = SX + astride;  // [3][4][NT] separator rows: original + ping-pong
   T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
   T* TMP = FST + 3 * NT;  // [PGE_TMP]: the FP32 separator solve's top level
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -351,16 +371,22 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     s_dmax = 0;
     s_xmax = 0;
   }
+  // dense layout: rows [r0, r1) start and end on 16-byte boundaries in
+  // global and shared memory and move in bulk; the rest element-wise
+  const int r0 = LAY == PGE_DENSE ? (n < (VE - delta) % VE ? n : (VE - delta) % VE) : 0;
+  const int r1 = LAY == PGE_DENSE ? r0 + (n - r0) / VE * VE : 0;
 
   // ---- stage the system.  SWZ: one TMA box (16 rows x NT partitions) per
   // array and half, each half counted on its own mbarrier, so that the
   // forward sweep starts on rows 0-15 while rows 16-31 are in flight.
-  // Otherwise asynchronous element copies (cp.async): warp w copies
-  // partitions w, w+NW, ... (a partition's rows are contiguous in global
-  // memory, so each copy instruction moves 32 consecutive elements), every
-  // copy in flight before the first wait; a_0, c_{n-1} and the identity rows
-  // past n are stored directly.
-  if constexpr (SWZ) {
+  // DENSE: one bulk copy per array (rows [r0, r1)), the few rows around it
+  // and the identity rows past n by plain copies.  ELEM: asynchronous
+  // element copies (cp.async): warp w copies partitions w, w+NW, ... (a
+  // partition's rows are contiguous in global memory, so each copy
+  // instruction moves 32 consecutive elements), every copy in flight before
+  // the first wait.  a_0, c_{n-1} and the identity rows past n are stored
+  // directly (bulk-staged: a_0 and c_{n-1} after the copies landed).
+  if constexpr (LAY == PGE_SWZ) {
     if (t == 0) {
       mbar_init(&s_bar[0], 1);
       mbar_init(&s_bar[1], 1);
@@ -370,6 +396,51 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
         T* dst[4] = {SA, SB, SC, SD};
         for (int k = 0; k < 4; ++k) tma_load_3d(dst[k] + h * NT * 16, &maps.m[k], 0, h, sys * NT, &s_bar[h]);
       }
+    }
+  } else if constexpr (LAY == PGE_DENSE) {
+    if (t == 0) {
+      mbar_init(&s_bar[0], 1);
+      fence_mbar_init();
+      const unsigned bytes = (unsigned)((r1 - r0) * sizeof(T));
+      mbar_arrive_expect_tx(&s_bar[0], 4 * bytes);
+      if (bytes) {
+        bulk_load_1d(SA + delta + r0, ga + base + r0, bytes, &s_bar[0]);
+        bulk_load_1d(SB + delta + r0, gb + base + r0, bytes, &s_bar[0]);
+        bulk_load_1d(SC + delta + r0, gc + base + r0, bytes, &s_bar[0]);
+        bulk_load_1d(SD + delta + r0, gd + base + r0, bytes, &s_bar[0]);
+      }
+    }
+    // rows [0, r0) and [r1, n) (fewer than 16 bytes each), identity past n
+    auto plain_row = [&](int r) {
+      const int q = delta + r;
+      SA[q] = r > 0 ? ga[base + r] : T(0);
+      SB[q] = gb[base + r];
+      SC[q] = r < n - 1 ? gc[base + r] : T(0);
+      SD[q] = gd[base + r];
+    };
+    if (t < r0) plain_row(t);
+    if (t < n - r1) plain_row(r1 + t);
+    for (int r = n + t; r < NT * m; r += NT) {
+      SA[delta + r] = T(0);
+      SB[delta + r] = T(1);
+      SC[delta + r] = T(0);
+      SD[delta + r] = T(0);
+    }
+    __syncthreads();  // (the mbarrier's initialisation, before anyone waits)
+    const bool landed = mbar_wait(&s_bar[0], 0, io.err);
+    if (t == 0) {
+      if (!landed) {
+        // a copy that never landed (the device error word has the timeout):
+        // solve identity rows there rather than stale shared memory
+        for (int r = r0; r < r1; ++r) {
+          SA[delta + r] = T(0);
+          SB[delta + r] = T(1);
+          SC[delta + r] = T(0);
+          SD[delta + r] = T(0);
+        }
+      }
+      if (r0 == 0 && r1 > 0) SA[delta] = T(0);
+      if (n - 1 >= r0 && n - 1 < r1) SC[delta + n - 1] = T(0);
     }
   } else {
 #pragma unroll 4
@@ -485,7 +556,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     // first pass of a TMA-staged system: wait for each half as the sweep
     // reaches it (a timeout marks the pass bad: the system is then restaged
     // and solved by the refinement passes)
-    if (SWZ && pass == 0) bad |= !mbar_wait(&s_bar[0], 0, io.err);
+    if (LAY == PGE_SWZ && pass == 0) bad |= !mbar_wait(&s_bar[0], 0, io.err);
     // a_0 and c_{n-1} are zero by definition (TMA staging copies whatever
     // the arrays hold there)
     first_row(t == 0 ? T(0) : A(0), B(0), C(0), D(0));
@@ -494,7 +565,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     T pa = A(1), pb = B(1), pc = C(1), py = D(1);
     for (int i = 0; i + 1 < mi; ++i) {
       const T na = pa, nb = pb, cn = pc, ny = py;
-      if (SWZ && pass == 0 && i + 2 == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
+      if (LAY == PGE_SWZ && pass == 0 && i + 2 == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
       pa = A(i + 2);
       pb = B(i + 2);
       pc = C(i + 2);
@@ -759,7 +830,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     return;
   }
   if (info && t == 0) info[sys] = 0;
-  if constexpr (SWZ) {
+  if constexpr (LAY == PGE_SWZ) {
     // x by two TMA stores (the rows were written by several threads in a
     // refinement pass: fence, then barrier)
     fence_async_smem();
@@ -770,6 +841,17 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       bulk_commit();
       bulk_wait_read<0>();  // shared memory stays valid until the stores have read it
     }
+  } else if constexpr (LAY == PGE_DENSE) {
+    // rows [r0, r1) of x by one bulk store, the rest element-wise
+    fence_async_smem();
+    __syncthreads();
+    if (t == 0 && r1 > r0) {
+      bulk_store_1d(io.x + base + r0, SD + delta + r0, (unsigned)((r1 - r0) * sizeof(T)));
+      bulk_commit();
+    }
+    if (t < r0) io.x[base + t] = SD[delta + t];
+    if (t < n - r1) io.x[base + r1 + t] = SD[delta + r1 + t];
+    if (t == 0 && r1 > r0) bulk_wait_read<0>();
   } else {
 #pragma unroll 4
     for (int p = warp; p < NT; p += NW) {
@@ -1188,7 +1270,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
 
 template <typename T, int NT>
 static size_t pge_smem_bytes(int ms) {
-  return ((size_t)6 * NT * ms + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
+  return ((size_t)6 * pge_array_elems<T, NT>(ms) + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
 }
 
 constexpr size_t PGE_SMEM_MAX = 227 * 1024 - 128;  // dynamic + the kernels' few static bytes
@@ -1236,11 +1318,11 @@ int pge_variant_max_n(int v) {
   return pge_variant_partitions(v) * pge_variant_mmax<T>(v);
 }
 
-template <typename T, int NT, int MODE, bool SWZ>
+template <typename T, int NT, int MODE, int LAY>
 static cudaError_t pge_launch_k(const PgeIO<T>& io_in, const PgeMaps& maps, int grid, size_t smem, cudaStream_t s) {
   PgeIO<T> io = io_in;
   cudaError_t e =
-      cudaFuncSetAttribute(pge_kernel<T, NT, MODE, SWZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(pge_kernel<T, NT, MODE, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // L2 prefetch one wave ahead for uniform batches with 16-byte aligned systems
   const uintptr_t al = reinterpret_cast<uintptr_t>(io.a) | reinterpret_cast<uintptr_t>(io.b) |
@@ -1249,11 +1331,11 @@ static cudaError_t pge_launch_k(const PgeIO<T>& io_in, const PgeMaps& maps, int 
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE, SWZ>, NT, smem) == cudaSuccess &&
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE, LAY>, NT, smem) == cudaSuccess &&
         per > 0 && grid > sms * per)
       io.pf_ahead = sms * per;
   }
-  pge_kernel<T, NT, MODE, SWZ><<<grid, NT, smem, s>>>(io, maps);
+  pge_kernel<T, NT, MODE, LAY><<<grid, NT, smem, s>>>(io, maps);
   return cudaGetLastError();
 }
 
@@ -1274,10 +1356,18 @@ static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int m_max, cudaSt
       for (int k = 0; k < 5 && ok; ++k)
         ok = encode_tmap_3d(&maps.m[k], arr[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, 16, 2, (uint64_t)NT * grid, 128,
                             PGE_SWZ_M * 8, 16, 1, NT, CU_TENSOR_MAP_SWIZZLE_128B);
-      if (ok) return pge_launch_k<T, NT, MODE, true>(io, maps, grid, smem_swz, s);
+      if (ok) return pge_launch_k<T, NT, MODE, PGE_SWZ>(io, maps, grid, smem_swz, s);
     }
   }
-  return pge_launch_k<T, NT, MODE, false>(io, maps, grid, pge_smem_bytes<T, NT>(m_max | 1), s);
+  const size_t smem = pge_smem_bytes<T, NT>(m_max | 1);
+  // bulk staging of each system's rows: all five arrays 16-byte aligned
+  if constexpr (MODE == 0) {
+    const uintptr_t al = reinterpret_cast<uintptr_t>(io.a) | reinterpret_cast<uintptr_t>(io.b) |
+                         reinterpret_cast<uintptr_t>(io.c) | reinterpret_cast<uintptr_t>(io.d) |
+                         reinterpret_cast<uintptr_t>(io.x);
+    if ((al & 15u) == 0) return pge_launch_k<T, NT, MODE, PGE_DENSE>(io, maps, grid, smem, s);
+  }
+  return pge_launch_k<T, NT, MODE, PGE_ELEM>(io, maps, grid, smem, s);
 }
 
 template <typename T, int NT, int CL, int MODE>

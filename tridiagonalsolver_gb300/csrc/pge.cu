@@ -306,23 +306,21 @@ __device__ __forceinline__ void pge_system(const PgeIO<T>& io, int bid, int R, i
 
 // Staging modes of pge_kernel (template parameter LAY) and the shared-memory
 // position of row i of partition p in each:
-//  * PGE_ELEM: asynchronous element copies into an odd partition stride ms
-//    (the sweeps' column accesses -- lane t, row i of partition t -- are
-//    conflict-free);
-//  * PGE_DENSE: the system's rows in order (row r at delta + r, delta = the
-//    system's offset modulo 16 bytes), moved by one bulk copy per array; the
-//    partition size m is odd, so the column accesses are conflict-free;
+//  * PGE_DENSE: the system's rows in order (row r of array k at delta_k + r,
+//    delta_k = the row's global address modulo 16 bytes, so that global and
+//    shared 16-byte boundaries coincide), moved by one bulk copy per array;
+//    the partition size m is odd, so the sweeps' column accesses -- lane t,
+//    row i of partition t -- are conflict-free;
 //  * PGE_SWZ (FP64, m = 32): each array as [2][NT][16] elements, half h of
 //    partition p one 128-byte row whose 16-byte pairs are XOR-swizzled by
 //    p mod 8 (the 128-byte swizzle of the tensor maps); column accesses meet
 //    at most four-way bank conflicts.
-constexpr int PGE_ELEM = 0, PGE_DENSE = 1, PGE_SWZ = 2;
+constexpr int PGE_DENSE = 1, PGE_SWZ = 2;
 
 template <int NT, int LAY>
-__device__ __forceinline__ int pge_off(int p, int i, int ms, int m, int delta) {
+__device__ __forceinline__ int pge_off(int p, int i, int m) {
   if constexpr (LAY == PGE_SWZ) return (i >> 4) * (NT * 16) + p * 16 + ((((i >> 1) & 7) ^ (p & 7)) << 1) + (i & 1);
-  else if constexpr (LAY == PGE_DENSE) return delta + p * m + i;
-  else return p * ms + i;
+  else return p * m + i;  // (each staged array's base shifted by its delta)
 }
 
 // Elements per staged array: NT partitions of stride ms, plus the dense
@@ -332,7 +330,7 @@ __host__ __device__ constexpr int pge_array_elems(int ms) {
   return (NT * ms + 2 * (16 / (int)sizeof(T)) - 1) / (16 / (int)sizeof(T)) * (16 / (int)sizeof(T));
 }
 
-template <typename T, int NT, int MODE, int LAY = PGE_ELEM>
+template <typename T, int NT, int MODE, int LAY>
 __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
   constexpr int NW = NT / 32;
   constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
@@ -341,23 +339,28 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
   if constexpr (LAY == PGE_SWZ) ms = PGE_SWZ_M;  // (the launch guarantees n = NT * 32)
   if constexpr (LAY == PGE_DENSE) m |= 1;        // odd partitions (ms = m)
-  const int delta = LAY == PGE_DENSE ? (int)(base % VE) : 0;
   const T* __restrict__ ga = io.a;
   const T* __restrict__ gb = io.b;
   const T* __restrict__ gc = io.c;
   const T* gd = io.d;
   int* info = io.info;
-  auto off = [&](int p, int i) { return pge_off<NT, LAY>(p, i, ms, m, delta); };
+  auto off = [&](int p, int i) { return pge_off<NT, LAY>(p, i, m); };
   __shared__ __align__(8) uint64_t s_bar[2];
   extern __shared__ __align__(16) unsigned char pge_smem[];
   unsigned char* sm = pge_smem;
   if constexpr (LAY == PGE_SWZ) sm += (1024u - (smem_u32(pge_smem) & 1023u)) & 1023u;  // 128-byte swizzle: 1 KB aligned
   const int astride = LAY == PGE_SWZ ? NT * PGE_SWZ_M : pge_array_elems<T, NT>(ms);
-  T* SA = reinterpret_cast<T*>(sm);
-  T* SB = SA + astride;
-  T* SC = SB + astride;
-  T* SD = SC + astride;
-  T* SV = SD + astride;
+  T* S0 = reinterpret_cast<T*>(sm);
+  // dense layout: each staged array shifted by its rows' 16-byte phase
+  auto phase = [&](const T* g) {
+    return LAY == PGE_DENSE ? (int)((reinterpret_cast<uintptr_t>(g + base) / sizeof(T)) % VE) : 0;
+  };
+  const int dl[4] = {phase(ga), phase(gb), phase(gc), phase(gd)};
+  T* SA = S0 + dl[0];
+  T* SB = S0 + astride + dl[1];
+  T* SC = S0 + 2 * astride + dl[2];
+  T* SD = S0 + 3 * astride + dl[3];
+  T* SV = S0 + 4 * astride;
   T* SX = SV + astride;   // x kept across refinement passes
   T* SEP = SX + astride;  // [3][4][NT] separator rows: original + ping-pong
   T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
@@ -371,21 +374,29 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     s_dmax = 0;
     s_xmax = 0;
   }
-  // dense layout: rows [r0, r1) start and end on 16-byte boundaries in
-  // global and shared memory and move in bulk; the rest element-wise
-  const int r0 = LAY == PGE_DENSE ? (n < (VE - delta) % VE ? n : (VE - delta) % VE) : 0;
-  const int r1 = LAY == PGE_DENSE ? r0 + (n - r0) / VE * VE : 0;
+  // dense layout: rows [r0[k], r1[k]) of array k start and end on 16-byte
+  // boundaries in global and shared memory and move in bulk; the rest
+  // element-wise.  Row 0 of a and row n-1 of c are never read (zero; the
+  // adjoint's shifted pointers would read outside the arrays there), so
+  // they stay out of the bulk ranges.
+  int r0[4] = {0, 0, 0, 0}, r1[4] = {0, 0, 0, 0};
+  if constexpr (LAY == PGE_DENSE) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      r0[k] = min(n, (VE - dl[k]) % VE);
+      r1[k] = r0[k] + (n - r0[k]) / VE * VE;
+    }
+    if (r0[0] == 0) r0[0] = min(VE, r1[0]);
+    if (r1[2] == n && r1[2] > r0[2]) r1[2] -= VE;
+  }
 
   // ---- stage the system.  SWZ: one TMA box (16 rows x NT partitions) per
   // array and half, each half counted on its own mbarrier, so that the
   // forward sweep starts on rows 0-15 while rows 16-31 are in flight.
   // DENSE: one bulk copy per array (rows [r0, r1)), the few rows around it
-  // and the identity rows past n by plain copies.  ELEM: asynchronous
-  // element copies (cp.async): warp w copies partitions w, w+NW, ... (a
-  // partition's rows are contiguous in global memory, so each copy
-  // instruction moves 32 consecutive elements), every copy in flight before
-  // the first wait.  a_0, c_{n-1} and the identity rows past n are stored
-  // directly (bulk-staged: a_0 and c_{n-1} after the copies landed).
+  // and the identity rows past n by plain copies.  (An SM issues about one
+  // bulk or element copy per 15 cycles: element copies of 4 or 8 bytes, or
+  // one bulk copy per partition, ran at 7-17 bytes per clock.)
   if constexpr (LAY == PGE_SWZ) {
     if (t == 0) {
       mbar_init(&s_bar[0], 1);
@@ -398,70 +409,39 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       }
     }
   } else if constexpr (LAY == PGE_DENSE) {
+    T* const Sk[4] = {SA, SB, SC, SD};
+    const T* const Gk[4] = {ga, gb, gc, gd};
     if (t == 0) {
       mbar_init(&s_bar[0], 1);
       fence_mbar_init();
-      const unsigned bytes = (unsigned)((r1 - r0) * sizeof(T));
-      mbar_arrive_expect_tx(&s_bar[0], 4 * bytes);
-      if (bytes) {
-        bulk_load_1d(SA + delta + r0, ga + base + r0, bytes, &s_bar[0]);
-        bulk_load_1d(SB + delta + r0, gb + base + r0, bytes, &s_bar[0]);
-        bulk_load_1d(SC + delta + r0, gc + base + r0, bytes, &s_bar[0]);
-        bulk_load_1d(SD + delta + r0, gd + base + r0, bytes, &s_bar[0]);
-      }
+      unsigned total = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) total += (unsigned)((r1[k] - r0[k]) * sizeof(T));
+      mbar_arrive_expect_tx(&s_bar[0], total);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (r1[k] > r0[k])
+          bulk_load_1d(Sk[k] + r0[k], Gk[k] + base + r0[k], (unsigned)((r1[k] - r0[k]) * sizeof(T)), &s_bar[0]);
     }
-    // rows [0, r0) and [r1, n) (fewer than 16 bytes each), identity past n
-    auto plain_row = [&](int r) {
-      const int q = delta + r;
-      SA[q] = r > 0 ? ga[base + r] : T(0);
-      SB[q] = gb[base + r];
-      SC[q] = r < n - 1 ? gc[base + r] : T(0);
-      SD[q] = gd[base + r];
-    };
-    if (t < r0) plain_row(t);
-    if (t < n - r1) plain_row(r1 + t);
-    for (int r = n + t; r < NT * m; r += NT) {
-      SA[delta + r] = T(0);
-      SB[delta + r] = T(1);
-      SC[delta + r] = T(0);
-      SD[delta + r] = T(0);
+    // rows outside the bulk ranges (fewer than 16 bytes at either end, plus
+    // row 0 of a and row n-1 of c), identity past n
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      auto plain = [&](int r) {
+        Sk[k][r] = (k == 0 && r == 0) || (k == 2 && r == n - 1) ? T(0) : Gk[k][base + r];
+      };
+      if (t < r0[k]) plain(t);
+      if (t < n - r1[k]) plain(r1[k] + t);
+      for (int r = n + t; r < NT * m; r += NT) Sk[k][r] = k == 1 ? T(1) : T(0);
     }
     __syncthreads();  // (the mbarrier's initialisation, before anyone waits)
-    const bool landed = mbar_wait(&s_bar[0], 0, io.err);
-    if (t == 0) {
-      if (!landed) {
-        // a copy that never landed (the device error word has the timeout):
-        // solve identity rows there rather than stale shared memory
-        for (int r = r0; r < r1; ++r) {
-          SA[delta + r] = T(0);
-          SB[delta + r] = T(1);
-          SC[delta + r] = T(0);
-          SD[delta + r] = T(0);
-        }
-      }
-      if (r0 == 0 && r1 > 0) SA[delta] = T(0);
-      if (n - 1 >= r0 && n - 1 < r1) SC[delta + n - 1] = T(0);
+    if (!mbar_wait(&s_bar[0], 0, io.err) && t == 0) {
+      // a copy that never landed (the device error word has the timeout):
+      // solve identity rows there rather than stale shared memory
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        for (int r = r0[k]; r < r1[k]; ++r) Sk[k][r] = k == 1 ? T(1) : T(0);
     }
-  } else {
-#pragma unroll 4
-    for (int p = warp; p < NT; p += NW) {
-      for (int i = lane; i < m; i += 32) {
-        const int r = p * m + i;
-        const int s = off(p, i);
-        if (r < n) {
-          if (r > 0) cp_async_elem(SA + s, ga + base + r); else SA[s] = T(0);
-          cp_async_elem(SB + s, gb + base + r);
-          if (r < n - 1) cp_async_elem(SC + s, gc + base + r); else SC[s] = T(0);
-          cp_async_elem(SD + s, gd + base + r);
-        } else {
-          SA[s] = T(0);
-          SB[s] = T(1);
-          SC[s] = T(0);
-          SD[s] = T(0);
-        }
-      }
-    }
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
   }
   // One CTA per SM fits: the CTA that runs here next (about one wave later)
   // finds its system in L2 instead of HBM.
@@ -841,17 +821,19 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       bulk_commit();
       bulk_wait_read<0>();  // shared memory stays valid until the stores have read it
     }
-  } else if constexpr (LAY == PGE_DENSE) {
-    // rows [r0, r1) of x by one bulk store, the rest element-wise
+  } else if (LAY == PGE_DENSE && MODE == 0 && phase(io.x) == dl[3]) {
+    // rows [q0, q1) of x by one bulk store (x in the same 16-byte phase as
+    // d), the rest element-wise
+    const int q0 = min(n, (VE - dl[3]) % VE), q1 = q0 + (n - q0) / VE * VE;
     fence_async_smem();
     __syncthreads();
-    if (t == 0 && r1 > r0) {
-      bulk_store_1d(io.x + base + r0, SD + delta + r0, (unsigned)((r1 - r0) * sizeof(T)));
+    if (t == 0 && q1 > q0) {
+      bulk_store_1d(io.x + base + q0, SD + q0, (unsigned)((q1 - q0) * sizeof(T)));
       bulk_commit();
     }
-    if (t < r0) io.x[base + t] = SD[delta + t];
-    if (t < n - r1) io.x[base + r1 + t] = SD[delta + r1 + t];
-    if (t == 0 && r1 > r0) bulk_wait_read<0>();
+    if (t < q0) io.x[base + t] = SD[t];
+    if (t < n - q1) io.x[base + q1 + t] = SD[q1 + t];
+    if (t == 0 && q1 > q0) bulk_wait_read<0>();
   } else {
 #pragma unroll 4
     for (int p = warp; p < NT; p += NW) {
@@ -1359,15 +1341,8 @@ static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int m_max, cudaSt
       if (ok) return pge_launch_k<T, NT, MODE, PGE_SWZ>(io, maps, grid, smem_swz, s);
     }
   }
-  const size_t smem = pge_smem_bytes<T, NT>(m_max | 1);
-  // bulk staging of each system's rows: all five arrays 16-byte aligned
-  if constexpr (MODE == 0) {
-    const uintptr_t al = reinterpret_cast<uintptr_t>(io.a) | reinterpret_cast<uintptr_t>(io.b) |
-                         reinterpret_cast<uintptr_t>(io.c) | reinterpret_cast<uintptr_t>(io.d) |
-                         reinterpret_cast<uintptr_t>(io.x);
-    if ((al & 15u) == 0) return pge_launch_k<T, NT, MODE, PGE_DENSE>(io, maps, grid, smem, s);
-  }
-  return pge_launch_k<T, NT, MODE, PGE_ELEM>(io, maps, grid, smem, s);
+  // every other shape: each system's rows in order, staged in bulk
+  return pge_launch_k<T, NT, MODE, PGE_DENSE>(io, maps, grid, pge_smem_bytes<T, NT>(m_max | 1), s);
 }
 
 template <typename T, int NT, int CL, int MODE>

@@ -114,18 +114,6 @@ constexpr int PGE_TMP = 4 * 32;
 // In-kernel refinement steps before the sequential fallback.
 constexpr int PGE_REFINE = 2;
 
-
-
-// One element global -> shared, asynchronously (cp.async, 4 or 8 bytes).
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  if constexpr (sizeof(T) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-
 // Systems that took the sequential fallback since the last reset (per device).
 __device__ unsigned long long g_pge_fallbacks = 0ull;
 // Per-path counts since the last reset (per device): [0] systems whose PCR
@@ -873,20 +861,30 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   namespace cg = cooperative_groups;
   using Lay = PgcLayout<T, NT, CL>;
   constexpr int R = Lay::R;
-  constexpr int NW = NT / 32;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
+  constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
   pge_system(io, blockIdx.x / CL, R, sys, base, n, m, ms);
+  // dense layout (as pge_kernel's PGE_DENSE): odd partitions, this CTA's
+  // rows in order, each staged array shifted by its rows' 16-byte phase
+  // (the same in every CTA: a CTA's rows span a multiple of 16 bytes)
+  m |= 1;
+  ms = m;
+  const int rows = NT * m;  // rows per CTA
+  const int row0 = rank * rows;
+  const int astride = pge_array_elems<T, NT>(ms);
   extern __shared__ __align__(16) unsigned char pge_smem[];
-  T* SA = reinterpret_cast<T*>(pge_smem);
-  T* SB = SA + NT * ms;
-  T* SC = SB + NT * ms;
-  T* SD = SC + NT * ms;
-  T* SV = SD + NT * ms;
-  T* SX = SV + NT * ms;
-  T* EXT = SX + NT * ms;
+  T* S0 = reinterpret_cast<T*>(pge_smem);
+  auto phase = [&](const T* g) { return (int)((reinterpret_cast<uintptr_t>(g + base + row0) / sizeof(T)) % VE); };
+  T* SA = S0 + phase(io.a);
+  T* SB = S0 + astride + phase(io.b);
+  T* SC = S0 + 2 * astride + phase(io.c);
+  T* SD = S0 + 3 * astride + phase(io.d);
+  T* SV = S0 + 4 * astride;
+  T* SX = SV + astride;
+  T* EXT = SX + astride;
   T* FST = EXT + Lay::FST;
   T* XF = EXT + Lay::XF;
   T* RED = EXT + Lay::RED;
@@ -902,8 +900,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   const T* __restrict__ gc = io.c;
   const T* gd = io.d;
   int* info = io.info;
-  const int rows = NT * m;  // rows per CTA
-  const int row0 = rank * rows;
   using MagT = unsigned;
   // Cluster-wide maxima and flags: every CTA accumulates into its own
   // shared variables (CTA-local atomics), and after a cluster barrier the
@@ -934,26 +930,53 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   }
   auto sidx = [&](int lr) { return (lr / m) * ms + (lr % m); };  // local row -> staging index
 
-  // ---- stage this CTA's rows
-#pragma unroll 4
-  for (int p = warp; p < NT; p += NW) {
-    for (int i = lane; i < m; i += 32) {
-      const int r = row0 + p * m + i;
-      const int q = p * ms + i;
-      if (r < n) {
-        if (r > 0) cp_async_elem(SA + q, ga + base + r); else SA[q] = T(0);
-        cp_async_elem(SB + q, gb + base + r);
-        if (r < n - 1) cp_async_elem(SC + q, gc + base + r); else SC[q] = T(0);
-        cp_async_elem(SD + q, gd + base + r);
-      } else {
-        SA[q] = T(0);
-        SB[q] = T(1);
-        SC[q] = T(0);
-        SD[q] = T(0);
-      }
+  // ---- stage this CTA's rows (local rows [0, hi) inside the system): one
+  // bulk copy per array of its 16-byte aligned rows [r0, r1), the rest and
+  // the identity rows past n by plain copies; the system's row 0 of a and
+  // row n-1 of c stay out of the bulk ranges (zero, and outside the arrays
+  // for the adjoint's shifted pointers)
+  const int hi = max(0, min(rows, n - row0));
+  __shared__ __align__(8) uint64_t s_bar;
+  {
+    T* const Sk[4] = {SA, SB, SC, SD};
+    const T* const Gk[4] = {ga, gb, gc, gd};
+    int r0[4], r1[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      r0[k] = min(hi, (VE - phase(Gk[k])) % VE);
+      r1[k] = r0[k] + (hi - r0[k]) / VE * VE;
+    }
+    if (row0 == 0 && r0[0] == 0) r0[0] = min(VE, r1[0]);
+    if (row0 + r1[2] == n && r1[2] > r0[2]) r1[2] -= VE;
+    if (t == 0) {
+      mbar_init(&s_bar, 1);
+      fence_mbar_init();
+      unsigned total = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) total += (unsigned)((r1[k] - r0[k]) * sizeof(T));
+      mbar_arrive_expect_tx(&s_bar, total);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (r1[k] > r0[k])
+          bulk_load_1d(Sk[k] + r0[k], Gk[k] + base + row0 + r0[k], (unsigned)((r1[k] - r0[k]) * sizeof(T)), &s_bar);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      auto plain = [&](int lr) {
+        const int r = row0 + lr;
+        Sk[k][lr] = (k == 0 && r == 0) || (k == 2 && r == n - 1) ? T(0) : Gk[k][base + r];
+      };
+      if (t < r0[k]) plain(t);
+      if (t < hi - r1[k]) plain(r1[k] + t);
+      for (int lr = hi + t; lr < rows; lr += NT) Sk[k][lr] = k == 1 ? T(1) : T(0);
+    }
+    __syncthreads();  // (the mbarrier's initialisation, before anyone waits)
+    if (!mbar_wait(&s_bar, 0, io.err) && t == 0) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        for (int lr = r0[k]; lr < r1[k]; ++lr) Sk[k][lr] = k == 1 ? T(1) : T(0);
     }
   }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
   cluster.sync();  // staging done everywhere, every CTA's accumulators initialised
   MagT amax = 0, dmax = 0;
 
@@ -1240,12 +1263,21 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   }  // passes
   if (info && rank == 0 && t == 0) info[sys] = accepted ? 0 : n + 1;
   if (!accepted && rank == 0 && t == 0) atomicAdd(&g_pge_fallbacks, 1ull);
-#pragma unroll 4
-  for (int p = warp; p < NT; p += NW) {
-    for (int i = lane; i < m; i += 32) {
-      const int r = row0 + p * m + i;
-      if (r < n) pge_store<T, MODE>(io, base, n, r, SD[p * ms + i]);
+  if (MODE == 0 && phase(io.x) == phase(io.d)) {
+    // this CTA's rows of x: the 16-byte aligned ones by one bulk store (x in
+    // the same phase as d), the rest element-wise
+    const int q0 = min(hi, (VE - phase(io.d)) % VE), q1 = q0 + (hi - q0) / VE * VE;
+    fence_async_smem();
+    __syncthreads();
+    if (t == 0 && q1 > q0) {
+      bulk_store_1d(io.x + base + row0 + q0, SD + q0, (unsigned)((q1 - q0) * sizeof(T)));
+      bulk_commit();
     }
+    if (t < q0) io.x[base + row0 + t] = SD[t];
+    if (t < hi - q1) io.x[base + row0 + q1 + t] = SD[q1 + t];
+    if (t == 0 && q1 > q0) bulk_wait_read<0>();
+  } else {
+    for (int lr = t; lr < hi; lr += NT) pge_store<T, MODE>(io, base, n, row0 + lr, SD[lr]);
   }
   cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
@@ -1267,7 +1299,7 @@ static int pge_mmax() {
 
 template <typename T, int NT, int CL>
 static size_t pgc_smem_bytes(int ms) {
-  return ((size_t)6 * NT * ms + PgcLayout<T, NT, CL>::END) * sizeof(T);
+  return ((size_t)6 * pge_array_elems<T, NT>(ms) + PgcLayout<T, NT, CL>::END) * sizeof(T);
 }
 
 template <typename T, int NT, int CL>

@@ -264,13 +264,43 @@ struct PgeMaps {
 // Rows per partition of the TMA-staged kernel.
 constexpr int PGE_SWZ_M = 32;
 
-template <typename T, int MODE>
-__device__ __forceinline__ void pge_store(const PgeIO<T>& io, size_t base, int n, int r, T v) {
-  io.x[base + r] = v;
-  if (MODE == 1) {
-    io.ga[base + r] = r > 0 ? -v * io.xf[base + r - 1] : T(0);
-    io.gb[base + r] = -v * io.xf[base + r];
-    io.gc[base + r] = r < n - 1 ? -v * io.xf[base + r + 1] : T(0);
+// Write rows r = lo + t, lo + t + nt, ... < hi of the result, value(r) from
+// shared memory.  MODE 1 also writes the gradients; the forward solution's
+// loads of U rows are issued before their stores (the outputs could alias
+// xf as far as the compiler knows, which would otherwise serialise one load
+// latency per row).
+template <typename T, int MODE, typename Val>
+__device__ __forceinline__ void pge_store_rows(const PgeIO<T>& io, size_t base, int n, int lo, int hi, int t, int nt,
+                                               Val value) {
+  if constexpr (MODE == 0) {
+    for (int r = lo + t; r < hi; r += nt) io.x[base + r] = value(r);
+  } else {
+    const T* __restrict__ xf = io.xf + base;
+    constexpr int U = 8;
+    for (int r0 = lo + t; r0 < hi; r0 += U * nt) {
+      T xl[U], xc[U], xr[U], v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + u * nt;
+        xl[u] = xc[u] = xr[u] = v[u] = T(0);
+        if (r < hi) {
+          if (r > 0) xl[u] = __ldg(xf + r - 1);
+          xc[u] = __ldg(xf + r);
+          if (r < n - 1) xr[u] = __ldg(xf + r + 1);
+          v[u] = value(r);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + u * nt;
+        if (r < hi) {
+          io.x[base + r] = v[u];
+          io.ga[base + r] = r > 0 ? -v[u] * xl[u] : T(0);
+          io.gb[base + r] = -v[u] * xc[u];
+          io.gc[base + r] = r < n - 1 ? -v[u] * xr[u] : T(0);
+        }
+      }
+    }
   }
 }
 
@@ -320,7 +350,6 @@ __host__ __device__ constexpr int pge_array_elems(int ms) {
 
 template <typename T, int NT, int MODE, int LAY>
 __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
-  constexpr int NW = NT / 32;
   constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
@@ -794,7 +823,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     }
     __syncthreads();
     if (s_info == 0)
-      for (int r = t; r < n; r += NT) pge_store<T, MODE>(io, base, n, r, FD[r]);
+      pge_store_rows<T, MODE>(io, base, n, 0, n, t, NT, [&](int r) { return FD[r]; });
     return;
   }
   if (info && t == 0) info[sys] = 0;
@@ -823,13 +852,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     if (t < n - q1) io.x[base + q1 + t] = SD[q1 + t];
     if (t == 0 && q1 > q0) bulk_wait_read<0>();
   } else {
-#pragma unroll 4
-    for (int p = warp; p < NT; p += NW) {
-      for (int i = lane; i < m; i += 32) {
-        const int r = p * m + i;
-        if (r < n) pge_store<T, MODE>(io, base, n, r, SD[off(p, i)]);
-      }
-    }
+    pge_store_rows<T, MODE>(io, base, n, 0, n, t, NT, [&](int r) { return SD[r]; });  // (dense: row r at r)
   }
 }
 
@@ -1277,7 +1300,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     if (t < hi - q1) io.x[base + row0 + q1 + t] = SD[q1 + t];
     if (t == 0 && q1 > q0) bulk_wait_read<0>();
   } else {
-    for (int lr = t; lr < hi; lr += NT) pge_store<T, MODE>(io, base, n, row0 + lr, SD[lr]);
+    pge_store_rows<T, MODE>(io, base, n, row0, row0 + hi, t, NT, [&](int r) { return SD[r - row0]; });
   }
   cluster.sync();  // no CTA leaves while others may still read its shared memory
 }

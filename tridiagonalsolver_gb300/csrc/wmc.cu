@@ -456,15 +456,39 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
     __syncthreads();
     if constexpr (TRANS) {
       // lambda and the gradients ga = -lambda x_{i-1}, gb = -lambda x_i,
-      // gc = -lambda x_{i+1} (x of the forward solve in gen.in[4])
-      const T* xf = gen.in[4] + goff;
-      for (int i = t; i < rows_here; i += nt) {
-        const int r = row_start + i;
-        const T lam = wmc_elem<T>(S[3], i / M, i % M);
-        gen.out[0][goff + i] = lam;
-        gen.out[1][goff + i] = r > 0 ? -lam * xf[i - 1] : T(0);
-        gen.out[2][goff + i] = -lam * xf[i];
-        gen.out[3][goff + i] = r + 1 < nn ? -lam * xf[i + 1] : T(0);
+      // gc = -lambda x_{i+1} (x of the forward solve in gen.in[4]).  The
+      // x loads of U rows per thread are issued before any store (the
+      // outputs could alias x as far as the compiler knows, which would
+      // otherwise serialise one load latency per row).
+      const T* __restrict__ xf = gen.in[4] + goff;
+      T* __restrict__ o0 = gen.out[0] + goff;
+      T* __restrict__ o1 = gen.out[1] + goff;
+      T* __restrict__ o2 = gen.out[2] + goff;
+      T* __restrict__ o3 = gen.out[3] + goff;
+      constexpr int U = 8;
+      for (int i0 = t; i0 < rows_here; i0 += U * nt) {
+        T xl_[U], xc_[U], xr_[U], lam[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * nt, r = row_start + i;
+          xl_[u] = xc_[u] = xr_[u] = lam[u] = T(0);
+          if (i < rows_here) {
+            if (r > 0) xl_[u] = __ldg(xf + i - 1);
+            xc_[u] = __ldg(xf + i);
+            if (r + 1 < nn) xr_[u] = __ldg(xf + i + 1);
+            lam[u] = wmc_elem<T>(S[3], i / M, i % M);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * nt, r = row_start + i;
+          if (i < rows_here) {
+            o0[i] = lam[u];
+            o1[i] = r > 0 ? -lam[u] * xl_[u] : T(0);
+            o2[i] = -lam[u] * xc_[u];
+            o3[i] = r + 1 < nn ? -lam[u] * xr_[u] : T(0);
+          }
+        }
       }
     } else {
       constexpr int NO = MODE == 1 ? 4 : 1;

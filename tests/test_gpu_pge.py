@@ -164,3 +164,43 @@ def test_bplg_packed_long(cuda):
     x = packed.double().cpu().numpy().reshape(batch, 4, n)[:, 3, :]
     _, worst = O.backward_error(*(v.astype(np.float32).astype(np.float64) for v in (a, b, c, d)), x, n)
     assert worst <= 1e-6
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,batch,shift", [(4096, 9, (0, 0, 0, 0, 1)), (1000, 7, (1, 2, 3, 1, 2)),
+                                           (3001, 5, (3, 0, 1, 2, 0)), (20000, 3, (0, 1, 0, 3, 2))])
+def test_pge_any_alignment(cuda, dt, n, batch, shift):
+    """Arrays at element offsets that put each one in its own 16-byte phase
+    (the bulk staging copies each array's aligned rows and the rest
+    element-wise; x in a phase other than d's leaves element-wise): the same
+    result as the aligned call, bit for bit, and the oracle's bar.  n = 20000
+    runs the cluster version.  At n = 4096 FP64 the aligned call runs the
+    TMA-staged kernel (32-row partitions) and the shifted x sends the call to
+    the dense layout (33-row partitions): the same bar, other roundings."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    a, b, c, d = inputs.nondominant(n, batch, seed=n + 5)
+    td = torch.float64 if dt == np.float64 else torch.float32
+    aligned = [torch.from_numpy(np.ascontiguousarray(v.astype(dt))).cuda() for v in (a, b, c, d)]
+    x0 = T.pge(*aligned, n)
+    shifted = []
+    for v, k in zip(aligned, shift[:4]):
+        buf = torch.empty(v.numel() + 8, dtype=td, device="cuda")
+        buf[k:k + v.numel()].copy_(v.reshape(-1))
+        shifted.append(buf[k:k + v.numel()])
+    xb = torch.empty(batch * n + 8, dtype=td, device="cuda")
+    x1 = xb[shift[4]:shift[4] + batch * n]
+    # through the C ABI: the Python front end copies inputs at odd offsets
+    p = "double" if dt == np.float64 else "single"
+    st = getattr(T.lib(), f"tridiag_pge_{p}")(0, *(v.data_ptr() for v in shifted), x1.data_ptr(), None, n, batch,
+                                            torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize()
+    if dt == np.float64 and n == 4096:
+        assert float((x0.reshape(-1) - x1).abs().max() / x0.abs().max()) <= 1e-10
+    else:
+        assert torch.equal(x0.reshape(-1), x1)
+    a_, b_, c_, d_ = (v.astype(dt).astype(np.float64) for v in (a, b, c, d))
+    _, worst = O.backward_error(a_, b_, c_, d_, x1.double().cpu().numpy(), n)
+    assert worst <= ETA[dt]

@@ -9,8 +9,11 @@ n = 4096 x 4096 dominant), gtsv64 (thread-per-system pivoted sweep, FP64,
 n = 4096 x 1024), wmc32 (partition method without pivoting, FP32,
 n = 4096 x 4096 dominant), pcr32 (PCR-pThomas, FP32, n = 512 x 32768 dominant),
 block2_64 (2 x 2 block systems, FP64, interleaved,
-n = 256 x 32768: the pivoted solve, then block Thomas on dominant systems).
-Each solves its case three times.
+n = 256 x 32768: the pivoted solve, then block Thomas on dominant systems),
+ragged_step (the ragged workload of `bench.py --workload ragged`: three
+forward + adjoint steps, then one between torch.cuda.profiler.start() and
+stop(), for `ncu --profile-from-start off`).
+Each other case solves its case three times.
 """
 import sys
 
@@ -41,9 +44,38 @@ def block2_case() -> None:
     print("ok block2_64")
 
 
+def ragged_step_case() -> None:
+    from tridiagonalsolver_gb300 import ragged
+
+    sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
+    w = torch.rand_like(d) * 2 - 1
+    classes = sorted({ragged.size_class(int(v)) for v in sizes})
+    table, _ = ragged.autotune(classes, dtype=torch.float32, reps=1)
+    plan = T.RaggedPlan(off, table=table, no_pivoting=~nondom)
+    x = torch.empty_like(d)
+    grads = [torch.empty_like(d) for _ in range(4)]
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            plan.solve(a, b, c, d, out=x, stream=s)
+            plan.adjoint(a, b, c, x, w, grads=grads, stream=s)
+        s.synchronize()
+        torch.cuda.profiler.start()
+        plan.solve(a, b, c, d, out=x, stream=s)
+        plan.adjoint(a, b, c, x, w, grads=grads, stream=s)
+        s.synchronize()
+        torch.cuda.profiler.stop()
+    print("ok ragged_step", int(off[-1]), "rows")
+
+
 def main(case: str) -> None:
     if case == "block2_64":
         block2_case()
+        return
+    if case == "ragged_step":
+        ragged_step_case()
         return
     n, batch, dt, dominant = CASES[case]
     g = torch.Generator(device="cuda")

@@ -520,7 +520,7 @@ def _graph_time(torch, stream, fn, steps, warmup):
     return e0.elapsed_time(e1) / steps, g
 
 
-def _e2e_host(torch, T, stream, dev_abcd, dev_x, n, algo, steps, unit_count):
+def _e2e_host(torch, T, stream, dev_abcd, dev_x, n, algo, steps, unit_count, layout="contiguous"):
     """End to end through the host-buffer entry point (tridiag_solve_host_*):
     every step copies a, b, c, d from page-locked host memory and x back,
     chunk by chunk, copies overlapping solves."""
@@ -529,7 +529,7 @@ def _e2e_host(torch, T, stream, dev_abcd, dev_x, n, algo, steps, unit_count):
     torch.cuda.synchronize()
 
     def one():
-        T.solve_host(*hin, n, algo=algo, out=hx, stream=stream)
+        T.solve_host(*hin, n, algo=algo, layout=layout, out=hx, stream=stream)
 
     with torch.cuda.stream(stream):
         one()
@@ -644,7 +644,8 @@ def run_thomas_fp64(args):
     idx = torch.arange(0, batch, batch // 16, device=dev)
     hs = [t.index_select(1, idx).T.contiguous().cpu().numpy() for t in (a, b, c, d, x)]
     _, eta = O.backward_error(*hs, n)
-    e2e = _e2e_generic(torch, stream, [a, b, c, d], [x], step, max(3, min(args.steps // 10, 10)), batch)
+    e2e = _e2e_host(torch, T, stream, [a, b, c, d], x, n, "thomas", max(3, min(args.steps // 10, 10)), batch,
+                    layout="interleaved")
 
     def cpu(k):
         aa, bb, cc, dd = inputs.dominant(n, k, seed=3)

@@ -44,10 +44,13 @@ void packed_ptrs(int layout, T*& a, T*& b, T*& c, T*& d, int n) {
   }
 }
 
+// Two arrays of n batch elements, the pivot words, and one int per system
+// (the chunked long-system solve's marks).
 template <typename T>
 size_t gtsv_ws_bytes(int n, int batch) {
   size_t elems = (size_t)n * (size_t)batch;
-  return 2 * align_up(elems * sizeof(T)) + align_up(tdg::pivot_words(n, batch) * sizeof(unsigned));
+  return 2 * align_up(elems * sizeof(T)) + align_up(tdg::pivot_words(n, batch) * sizeof(unsigned)) +
+         align_up((size_t)batch * sizeof(int));
 }
 
 template <typename T>
@@ -55,6 +58,7 @@ struct GtsvWs {
   T* w1;
   T* w2;
   unsigned* piv;
+  int* flag;
 };
 
 template <typename T>
@@ -67,6 +71,8 @@ GtsvWs<T> carve_gtsv(void* work, int n, int batch) {
   w.w2 = reinterpret_cast<T*>(p);
   p += align_up(elems * sizeof(T));
   w.piv = reinterpret_cast<unsigned*>(p);
+  p += align_up(tdg::pivot_words(n, batch) * sizeof(unsigned));
+  w.flag = reinterpret_cast<int*>(p);
   return w;
 }
 
@@ -89,6 +95,13 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
     if (used) return TRIDIAG_SUCCESS;
   }
   GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
+  if (!pivots && layout == TRIDIAG_LAYOUT_CONTIGUOUS && n >= PGE_MIN_N) {
+    // longer than the one-CTA and cluster solves reach: the chunked one
+    bool used = false;
+    cudaError_t e = tdg::launch_pge_long<T>(a, b, c, d, info, n, batch, w.w1, w.w2, w.piv, w.flag, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    if (used) return TRIDIAG_SUCCESS;
+  }
   unsigned* piv = pivots ? pivots : w.piv;
   if (tdg::tw_eligible(layout, n, batch, sizeof(T))) {
     bool used = false;

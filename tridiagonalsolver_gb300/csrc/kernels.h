@@ -11,6 +11,11 @@ cudaError_t launch_thomas_seq(int layout, T* a, T* b, T* c, T* d, int n, int bat
 template <typename T>
 cudaError_t launch_gtsv_seq(int layout, const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv,
                             int* info, int n, int batch, cudaStream_t s);
+// The sequential solve (contiguous) of the systems with mask[j] != 0 only;
+// info[j] = 0 for the others.
+template <typename T>
+cudaError_t launch_gtsv_seq_masked(const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv, int* info,
+                                   int n, int batch, const int* mask, cudaStream_t s);
 template <typename T>
 cudaError_t launch_gtsv_adjoint(int layout, const T* a, const T* b, const T* c, const T* x, const unsigned* piv,
                                 const T* g, T* ga, T* gb, T* gc, T* gd, T* wz, T* wm, int n, int batch,
@@ -183,6 +188,15 @@ cudaError_t launch_relayout(int from, int to, const T* const src[4], T* const ds
 
 // Number of systems the partitioned solve handed to its sequential fallback
 // (synchronous read; optionally reset).
+// Long systems (uniform contiguous batch, n beyond one chunk of 128 x 33
+// rows): the partitioned pivoted solve in chunks, in place on d.  w1, w2:
+// n batch elements each, piv: the pivot words of tridiag_gtsv's workspace,
+// flag: batch ints.  *used = false when n is not covered.
+template <typename T>
+bool pge_long_eligible(int n);
+template <typename T>
+cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info, int n, int batch, T* w1, T* w2,
+                            unsigned* piv, int* flag, cudaStream_t s, bool* used);
 cudaError_t pge_fallback_count(unsigned long long* out, bool reset);
 cudaError_t pge_path_counts(unsigned long long* out, bool reset);  // out[4]
 

@@ -252,6 +252,13 @@ struct PgeIO {
   int n;
   int pf_ahead;  // uniform batches: CTA b prefetches system b + pf_ahead into L2 (0: off)
   int* err;      // the library's device error word (bounded waits)
+  // chunked long systems (MODE 2 / 3, uniform contiguous batches): CTA b is
+  // chunk b % nchunks of system b / nchunks, chunk_rows rows of it
+  int nchunks, chunk_rows;
+  T* sep;        // [4][batch][nchunks NT]: the separator systems (sub, diag, super, rhs)
+  T* carry;      // [batch][nchunks][4]: Y, V, W of partition 0's first row, c of the last separator row
+  const T* xsep;  // [batch][nchunks NT]: the separators (MODE 3)
+  int* flag;     // [batch]: MODE 3 sets 1 where a separator row misses its bound
 };
 
 // Tensor maps of the TMA-staged FP64 kernel (pge_kernel with SWZ): a, b, c,
@@ -272,7 +279,7 @@ constexpr int PGE_SWZ_M = 32;
 template <typename T, int MODE, typename Val>
 __device__ __forceinline__ void pge_store_rows(const PgeIO<T>& io, size_t base, int n, int lo, int hi, int t, int nt,
                                                Val value) {
-  if constexpr (MODE == 0) {
+  if constexpr (MODE != 1) {
     for (int r = lo + t; r < hi; r += nt) io.x[base + r] = value(r);
   } else {
     const T* __restrict__ xf = io.xf + base;
@@ -353,7 +360,19 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
-  pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
+  int ch = 0;                       // chunk of a long system (MODE 2 / 3)
+  bool zero_a0 = true, zero_cl = true;  // this CTA holds the system's first / last row
+  if constexpr (MODE >= 2) {
+    sys = blockIdx.x / io.nchunks;
+    ch = blockIdx.x % io.nchunks;
+    base = (size_t)sys * io.stride + (size_t)ch * io.chunk_rows;
+    n = min(io.chunk_rows, io.n - ch * io.chunk_rows);
+    m = ms = io.chunk_rows / NT;  // odd (the launch's choice)
+    zero_a0 = ch == 0;
+    zero_cl = ch == io.nchunks - 1;
+  } else {
+    pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
+  }
   if constexpr (LAY == PGE_SWZ) ms = PGE_SWZ_M;  // (the launch guarantees n = NT * 32)
   if constexpr (LAY == PGE_DENSE) m |= 1;        // odd partitions (ms = m)
   const T* __restrict__ ga = io.a;
@@ -403,8 +422,8 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       r0[k] = min(n, (VE - dl[k]) % VE);
       r1[k] = r0[k] + (n - r0[k]) / VE * VE;
     }
-    if (r0[0] == 0) r0[0] = min(VE, r1[0]);
-    if (r1[2] == n && r1[2] > r0[2]) r1[2] -= VE;
+    if (zero_a0 && r0[0] == 0) r0[0] = min(VE, r1[0]);
+    if (zero_cl && r1[2] == n && r1[2] > r0[2]) r1[2] -= VE;
   }
 
   // ---- stage the system.  SWZ: one TMA box (16 rows x NT partitions) per
@@ -445,7 +464,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       auto plain = [&](int r) {
-        Sk[k][r] = (k == 0 && r == 0) || (k == 2 && r == n - 1) ? T(0) : Gk[k][base + r];
+        Sk[k][r] = (k == 0 && r == 0 && zero_a0) || (k == 2 && r == n - 1 && zero_cl) ? T(0) : Gk[k][base + r];
       };
       if (t < r0[k]) plain(t);
       if (t < n - r1[k]) plain(r1[k] + t);
@@ -556,7 +575,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     if (LAY == PGE_SWZ && pass == 0) bad |= !mbar_wait(&s_bar[0], 0, io.err);
     // a_0 and c_{n-1} are zero by definition (TMA staging copies whatever
     // the arrays hold there)
-    first_row(t == 0 ? T(0) : A(0), B(0), C(0), D(0));
+    first_row(t == 0 && zero_a0 ? T(0) : A(0), B(0), C(0), D(0));
     // software-pipelined: row i+2 (at most the separator row, which always
     // exists) is loaded while row i+1 is eliminated
     T pa = A(1), pb = B(1), pc = C(1), py = D(1);
@@ -571,7 +590,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     }
     as = A(mi);
     bs = B(mi);
-    cs = t * m + mi == n - 1 ? T(0) : C(mi);
+    cs = t * m + mi == n - 1 && zero_cl ? T(0) : C(mi);
     ds = D(mi);
   }
   // U row mi-1 is the remaining candidate row (u1 = u2 = 0)
@@ -611,8 +630,31 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     SEP[NT + t] = fma(-cs, Vf, fma(-as, Wlast, bs));
     SEP[2 * NT + t] = -cs * Wf;
     SEP[3 * NT + t] = fma(-cs, Yf, fma(-as, Ylast, ds));
+    if constexpr (MODE == 2) {
+      // a long system's chunk: its separator rows go to the system-wide
+      // separator system; the last one still lacks the next chunk's first
+      // row (added by pge_long_link from `carry`)
+      const size_t ptot = (size_t)io.nchunks * NT, bsz = ptot * gridDim.x / io.nchunks;
+      const size_t q = (size_t)sys * ptot + (size_t)ch * NT + t;
+      io.sep[q] = SEP[t];
+      io.sep[bsz + q] = SEP[NT + t];
+      io.sep[2 * bsz + q] = SEP[2 * NT + t];
+      io.sep[3 * bsz + q] = SEP[3 * NT + t];
+      T* cy_ = io.carry + ((size_t)sys * io.nchunks + ch) * 4;
+      if (t == 0) {
+        cy_[0] = FST[0];
+        cy_[1] = FST[NT];
+        cy_[2] = FST[2 * NT];
+      }
+      if (t == NT - 1) cy_[3] = cs;
+      return;
+    }
   }
   __syncthreads();
+  if constexpr (MODE == 3) {
+    // the separators from the system-wide solve
+    FST[t] = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT + t];
+  } else {
   // Parallel cyclic reduction of the separator system (SEP[0..4NT) keeps the
   // original rows, SEP[4NT..12NT) is the ping-pong pair) ...
   {
@@ -663,6 +705,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       if (warp == 0) bad |= sep_solve_pivoted<T, NT>(SEP, FST, TMP, lane);
     }
   }
+  }  // MODE != 3
   __syncthreads();
   // ---- back substitution of the interior block with the separators in
   // place: x_i = (y'_i - v'_i s_{t-1} - w'_i s_t - u1_i x_{i+1} - u2_i x_{i+2})
@@ -672,7 +715,9 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   // must meet SEP_TOL relative to max|A| max|x| + max|d|; a failing system
   // gets an exact backward-error check of all rows, then (if that fails
   // too) the sequential partial-pivoting solve.
-  const T sp = t > 0 ? FST[t - 1] : T(0);
+  T sp = t > 0 ? FST[t - 1] : T(0);
+  if constexpr (MODE == 3)
+    if (t == 0 && ch > 0) sp = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT - 1];
   const T st = FST[t];
   MagT xmax = magh(st);
   T x_last;
@@ -708,7 +753,15 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     FST[NT + t] = D(0);  // first x of the partition, for the separator residual of t-1
     if (pass == 0) atomicMax(&s_xmax, xmax);
     __syncthreads();
-    const T x_next = t + 1 < NT ? FST[NT + t + 1] : T(0);
+    T x_next = t + 1 < NT ? FST[NT + t + 1] : T(0);
+    if constexpr (MODE == 3) {
+      if (t + 1 == NT && !zero_cl) {
+        // the next chunk's first row: x = Y - V s_t - W s_{t+1}
+        const T* cy_ = io.carry + ((size_t)sys * io.nchunks + ch + 1) * 4;
+        const T s_next = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)(ch + 1) * NT];
+        x_next = fma(-cy_[2], s_next, fma(-cy_[1], st, cy_[0]));
+      }
+    }
     // (one row per partition: formed in FP64 for both precisions)
     const double r = fma(-(double)cs, (double)x_next,
                          fma(-(double)bs, (double)st, fma(-(double)as, (double)x_last, (double)ds)));
@@ -726,6 +779,13 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   // the sequential partial-pivoting solve takes over.
   const bool pass_bad = __syncthreads_or(bad);
   if (pass == 0 && !pass_bad) {
+    accepted = true;
+    break;
+  }
+  if constexpr (MODE == 3) {
+    // a chunk cannot refine alone: mark the system for the sequential solve
+    // (counted once per system)
+    if (t == 0 && atomicExch(&io.flag[sys], 1) == 0) atomicAdd(&g_pge_fallbacks, 1ull);
     accepted = true;
     break;
   }
@@ -826,7 +886,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       pge_store_rows<T, MODE>(io, base, n, 0, n, t, NT, [&](int r) { return FD[r]; });
     return;
   }
-  if (info && t == 0) info[sys] = 0;
+  if (MODE < 2 && info && t == 0) info[sys] = 0;
   if constexpr (LAY == PGE_SWZ) {
     // x by two TMA stores (the rows were written by several threads in a
     // refinement pass: fence, then barrier)
@@ -838,7 +898,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       bulk_commit();
       bulk_wait_read<0>();  // shared memory stays valid until the stores have read it
     }
-  } else if (LAY == PGE_DENSE && MODE == 0 && phase(io.x) == dl[3]) {
+  } else if (LAY == PGE_DENSE && (MODE == 0 || MODE == 3) && phase(io.x) == dl[3]) {
     // rows [q0, q1) of x by one bulk store (x in the same 16-byte phase as
     // d), the rest element-wise
     const int q0 = min(n, (VE - dl[3]) % VE), q1 = q0 + (n - q0) / VE * VE;
@@ -1475,6 +1535,119 @@ cudaError_t launch_pge(int layout, const T* a, const T* b, const T* c, const T* 
   return pge_launch_variant<T, 0>(v, uniform_io<T>(layout, a, b, c, d, x, info, n), batch, m, s);
 }
 
+// ---------------------------------------------------------------------------
+// Long systems (uniform contiguous batches beyond the one-CTA and cluster
+// sizes): the partitioned solve in chunks of PGE_LONG_NT partitions of
+// PGE_LONG_M rows, one CTA per chunk, in four launches --
+//   1. pge_kernel MODE 2: each chunk eliminates its partitions (as the
+//      one-CTA solve) and writes their separator rows into the system-wide
+//      separator system, plus the first-row relation of its first partition
+//      and the last separator's c for the link;
+//   2. pge_long_link: completes the separator row at each chunk boundary;
+//   3. the separator systems (PGE_LONG_NT rows per chunk), solved by the
+//      partitioned solve itself (one CTA or a cluster per system);
+//   4. pge_kernel MODE 3: each chunk eliminates again, back-substitutes with
+//      its separators and checks its separator rows' residuals (as pass 0 of
+//      the one-CTA solve, with the chunk's maxima: never a looser bound);
+// then x goes to d where every chunk passed, and the systems with a failing
+// chunk (a chunk cannot refine on its own) take the sequential
+// partial-pivoting solve.
+constexpr int PGE_LONG_NT = 128, PGE_LONG_M = 33;
+
+template <typename T>
+__global__ void __launch_bounds__(256) pge_long_link(T* sep, const T* carry, int nchunks, int batch) {
+  const size_t ptot = (size_t)nchunks * PGE_LONG_NT, bsz = ptot * batch;
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // (system, chunk boundary)
+  const int nb = nchunks - 1;
+  if (nb <= 0 || k >= (long long)batch * nb) return;
+  const int j = (int)(k / nb), c = (int)(k % nb);
+  const T cs = carry[((size_t)j * nchunks + c) * 4 + 3];  // c of chunk c's last separator row
+  const T* f = carry + ((size_t)j * nchunks + c + 1) * 4;  // Y, V, W of chunk c+1's first row
+  const size_t q = (size_t)j * ptot + (size_t)(c + 1) * PGE_LONG_NT - 1;
+  sep[bsz + q] = fma(-cs, f[1], sep[bsz + q]);
+  sep[2 * bsz + q] = -cs * f[2];
+  sep[3 * bsz + q] = fma(-cs, f[0], sep[3 * bsz + q]);
+}
+
+// x -> d for the systems without a mark; bps blocks per system.
+template <typename T>
+__global__ void __launch_bounds__(256) pge_long_commit(T* __restrict__ d, const T* __restrict__ x,
+                                                       const int* __restrict__ flag, int n, int bps) {
+  const int j = (int)(blockIdx.x / bps), k = (int)(blockIdx.x % bps);
+  if (flag[j]) return;
+  const size_t o = (size_t)j * n;
+  for (int i = k * blockDim.x + threadIdx.x; i < n; i += bps * blockDim.x) d[o + i] = x[o + i];
+}
+
+template <typename T>
+bool pge_long_eligible(int n) {
+  if (n <= PGE_LONG_NT * PGE_LONG_M) return false;
+  const int nchunks = (n + PGE_LONG_NT * PGE_LONG_M - 1) / (PGE_LONG_NT * PGE_LONG_M);
+  return pge_eligible<T>(CONTIG, nchunks * PGE_LONG_NT) &&
+         pge_smem_bytes<T, PGE_LONG_NT>(PGE_LONG_M) <= PGE_SMEM_MAX;
+}
+
+template <typename T>
+cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info, int n, int batch, T* w1, T* w2,
+                            unsigned* piv, int* flag, cudaStream_t s, bool* used) {
+  *used = false;
+  if (!pge_long_eligible<T>(n)) return cudaSuccess;
+  const int rows = PGE_LONG_NT * PGE_LONG_M;
+  const int nchunks = (n + rows - 1) / rows;
+  const size_t ptot = (size_t)nchunks * PGE_LONG_NT, bsz = ptot * batch;
+  // w1: the separator systems, their solution and the chunk links (about
+  // 0.15 n per system); w2: x until it is committed
+  if (5 * ptot + 4 * (size_t)nchunks > (size_t)n) return cudaSuccess;
+  T* sep = w1;
+  T* xsep = w1 + 4 * bsz;
+  T* carry = xsep + bsz;
+  *used = true;
+  PgeIO<T> io{};
+  io.a = a;
+  io.b = b;
+  io.c = c;
+  io.d = d;
+  io.stride = (size_t)n;
+  io.n = n;
+  io.err = error_word();
+  io.nchunks = nchunks;
+  io.chunk_rows = rows;
+  io.sep = sep;
+  io.carry = carry;
+  io.xsep = xsep;
+  io.flag = flag;
+  const size_t smem = pge_smem_bytes<T, PGE_LONG_NT>(PGE_LONG_M);
+  const PgeMaps maps{};
+  const int grid = batch * nchunks;
+  cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, PGE_LONG_NT, 2, PGE_DENSE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(pge_kernel<T, PGE_LONG_NT, 3, PGE_DENSE>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  pge_kernel<T, PGE_LONG_NT, 2, PGE_DENSE><<<grid, PGE_LONG_NT, smem, s>>>(io, maps);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (nchunks > 1) {
+    const long long links = (long long)batch * (nchunks - 1);
+    pge_long_link<T><<<(unsigned)((links + 255) / 256), 256, 0, s>>>(sep, carry, nchunks, batch);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  bool sep_used = false;
+  e = launch_pge<T>(CONTIG, sep, sep + bsz, sep + 2 * bsz, sep + 3 * bsz, xsep, nullptr, (int)ptot, batch, s,
+                    &sep_used);
+  if (e != cudaSuccess) return e;
+  if (!sep_used) return cudaErrorInvalidValue;  // (pge_long_eligible checked the size)
+  if ((e = cudaMemsetAsync(flag, 0, (size_t)batch * sizeof(int), s)) != cudaSuccess) return e;
+  io.x = w2;
+  pge_kernel<T, PGE_LONG_NT, 3, PGE_DENSE><<<grid, PGE_LONG_NT, smem, s>>>(io, maps);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int bps = (n + 255) / 256 < 64 ? (n + 255) / 256 : 64;
+  pge_long_commit<T><<<(unsigned)((size_t)bps * batch), 256, 0, s>>>(d, w2, flag, n, bps);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // the flagged systems: sequential partial pivoting in place on d (their
+  // right-hand side is still there), w1/w2 now free for its factors
+  return launch_gtsv_seq_masked<T>(a, b, c, d, w1, w2, piv, info, n, batch, flag, s);
+}
+
 template <typename T>
 cudaError_t launch_pge_strided(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
                                size_t stride, cudaStream_t s, bool* used) {
@@ -1559,6 +1732,9 @@ cudaError_t pge_path_counts(unsigned long long* out, bool reset) {
   template int pge_variant_mmax<T>(int);                                                                          \
   template cudaError_t launch_pge<T>(int, const T*, const T*, const T*, const T*, T*, int*, int, int, cudaStream_t, \
                                      bool*);                                                                      \
+  template bool pge_long_eligible<T>(int);                                                                        \
+  template cudaError_t launch_pge_long<T>(const T*, const T*, const T*, T*, int*, int, int, T*, T*, unsigned*, int*, \
+                                          cudaStream_t, bool*);                                                   \
   template cudaError_t launch_pge_strided<T>(const T*, const T*, const T*, const T*, T*, int*, int, int, size_t,  \
                                              cudaStream_t, bool*);                                                \
   template cudaError_t launch_pge_adjoint<T>(int, const T*, const T*, const T*, const T*, const T*, T*, T*, T*, T*, \

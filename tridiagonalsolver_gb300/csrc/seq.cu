@@ -119,9 +119,13 @@ __global__ void __launch_bounds__(128) gtsv_seq_kernel(const T* __restrict__ a, 
                                                        const T* __restrict__ c, T* __restrict__ d,
                                                        T* __restrict__ w1, T* __restrict__ w2,
                                                        unsigned* __restrict__ piv, int* __restrict__ info, int n,
-                                                       int batch) {
+                                                       int batch, const int* __restrict__ mask) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= batch) return;
+  if (mask && !mask[j]) {  // (masked launch: only the marked systems)
+    if (info) info[j] = 0;
+    return;
+  }
   // row i carried as (u0, u1, rhs); the next row is read from memory
   size_t o0 = idx<L>(0, j, n, batch);
   T u0 = ld_stream(b + o0), u1 = (n > 1) ? ld_stream(c + o0) : T(0), rhs = ld_stream(d + o0);
@@ -330,11 +334,17 @@ cudaError_t launch_thomas_seq(int layout, T* a, T* b, T* c, T* d, int n, int bat
 
 template <typename T, int L>
 cudaError_t launch_gtsv_seq_l(const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv, int* info,
-                              int n, int batch, cudaStream_t s) {
+                              int n, int batch, cudaStream_t s, const int* mask = nullptr) {
   int tpb = seq_block(batch);
   dim3 grid((batch + tpb - 1) / tpb);
-  gtsv_seq_kernel<T, L, 4><<<grid, tpb, 0, s>>>(a, b, c, d, w1, w2, piv, info, n, batch);
+  gtsv_seq_kernel<T, L, 4><<<grid, tpb, 0, s>>>(a, b, c, d, w1, w2, piv, info, n, batch, mask);
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_gtsv_seq_masked(const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv, int* info,
+                                   int n, int batch, const int* mask, cudaStream_t s) {
+  return launch_gtsv_seq_l<T, CONTIG>(a, b, c, d, w1, w2, piv, info, n, batch, s, mask);
 }
 
 template <typename T>
@@ -372,6 +382,8 @@ cudaError_t launch_gtsv_adjoint(int layout, const T* a, const T* b, const T* c, 
 
 #define INST(T)                                                                                                  \
   template cudaError_t launch_thomas_seq<T>(int, T*, T*, T*, T*, int, int, cudaStream_t);                        \
+  template cudaError_t launch_gtsv_seq_masked<T>(const T*, const T*, const T*, T*, T*, T*, unsigned*, int*, int,   \
+                                                 int, const int*, cudaStream_t);                                   \
   template cudaError_t launch_gtsv_seq<T>(int, const T*, const T*, const T*, T*, T*, T*, unsigned*, int*, int,   \
                                           int, cudaStream_t);                                                    \
   template cudaError_t launch_gtsv_adjoint<T>(int, const T*, const T*, const T*, const T*, const unsigned*,      \

@@ -1,5 +1,5 @@
-"""Pivoted solve of long systems in chunks (uniform contiguous batches beyond
-the one-CTA and cluster sizes: FP64 n > 27648, FP32 n > 65536), through
+"""Pivoted solve of long systems in chunks (uniform contiguous batches: FP64
+from 12288 rows, FP32 beyond the cluster sizes, n > 65536), through
 tridiag_gtsv_* without a pivot record, against the oracle.
 
 Tolerances: normwise backward error <= 1e-12 (FP64) / 1e-6 (FP32) computed in
@@ -42,6 +42,7 @@ def _check(arrs, x, dt, n, forward):
 
 
 @pytest.mark.parametrize("dt,n,batch", [(np.float64, 65536, 3), (np.float64, 30001, 4), (np.float64, 8448 * 4 + 7, 2),
+                                        (np.float64, 12288, 5), (np.float64, 16384, 3), (np.float64, 27648, 2),
                                         (np.float32, 70000, 3), (np.float32, 200000, 2)])
 @pytest.mark.parametrize("dominant", [False, True])
 def test_long_pivoted_matches_oracle(cuda, dt, n, batch, dominant):

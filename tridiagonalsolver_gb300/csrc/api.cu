@@ -33,6 +33,8 @@ inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 // (measured on GB300 at batch 2^24 / n: the partitioned solve is faster
 // from n = 512 in both precisions, the two-ended sweep below).
 constexpr int PGE_MIN_N = 512;
+// From this size on FP64 pivoted solves with a workspace run in chunks.
+constexpr int PGE_LONG_MIN_FP64 = 12288;
 
 // Expand the four array pointers of a packed (layout 1) base pointer.
 template <typename T>
@@ -87,18 +89,25 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
     return TRIDIAG_ERR_INVALID_VALUE;
   }
   if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
+  GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
+  // Long systems without a pivot record, contiguous: the chunked partitioned
+  // solve where the one-CTA and cluster solves do not reach, and for FP64
+  // from PGE_LONG_MIN_FP64 rows on (measured on GB300: n = 16384 / 27648 FP64
+  // 1.32 / 1.15 ms chunked vs 2.63 / 1.60 ms in clusters; FP32 chunks fail
+  // their separator checks too often -- 4-13% of systems -- to replace the
+  // clusters).
+  const bool chunked_first = sizeof(T) == 8 && n >= PGE_LONG_MIN_FP64;
+  if (!pivots && layout == TRIDIAG_LAYOUT_CONTIGUOUS && n >= PGE_MIN_N &&
+      (chunked_first || !tdg::pge_eligible<T>(layout, n))) {
+    bool used = false;
+    cudaError_t e = tdg::launch_pge_long<T>(a, b, c, d, info, n, batch, w.w1, w.w2, w.piv, w.flag, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    if (used) return TRIDIAG_SUCCESS;
+  }
   if (!pivots && n >= PGE_MIN_N && tdg::pge_eligible<T>(layout, n)) {
     // no pivot record wanted: the partitioned solve (many chains per system)
     bool used = false;
     cudaError_t e = tdg::launch_pge<T>(layout, a, b, c, d, d, info, n, batch, s, &used);
-    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
-    if (used) return TRIDIAG_SUCCESS;
-  }
-  GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
-  if (!pivots && layout == TRIDIAG_LAYOUT_CONTIGUOUS && n >= PGE_MIN_N) {
-    // longer than the one-CTA and cluster solves reach: the chunked one
-    bool used = false;
-    cudaError_t e = tdg::launch_pge_long<T>(a, b, c, d, info, n, batch, w.w1, w.w2, w.piv, w.flag, s, &used);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
     if (used) return TRIDIAG_SUCCESS;
   }

@@ -404,11 +404,14 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   using MagT = unsigned;
   __shared__ MagT s_amax, s_dmax, s_xmax;
+  __shared__ T s_xprev, s_xnext;  // x of the neighbouring chunks' adjacent rows (MODE 3)
   MagT amax = 0, dmax = 0;
   if (t == 0) {
     s_amax = 0;
     s_dmax = 0;
     s_xmax = 0;
+    s_xprev = T(0);
+    s_xnext = T(0);
   }
   // dense layout: rows [r0[k], r1[k]) of array k start and end on 16-byte
   // boundaries in global and shared memory and move in bulk; the rest
@@ -717,7 +720,10 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   // too) the sequential partial-pivoting solve.
   T sp = t > 0 ? FST[t - 1] : T(0);
   if constexpr (MODE == 3)
-    if (t == 0 && ch > 0) sp = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT - 1];
+    if (t == 0 && ch > 0) {
+      sp = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT - 1];
+      s_xprev = sp;  // (the previous chunk's last row is its last separator)
+    }
   const T st = FST[t];
   MagT xmax = magh(st);
   T x_last;
@@ -760,6 +766,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
         const T* cy_ = io.carry + ((size_t)sys * io.nchunks + ch + 1) * 4;
         const T s_next = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)(ch + 1) * NT];
         x_next = fma(-cy_[2], s_next, fma(-cy_[1], st, cy_[0]));
+        s_xnext = x_next;
       }
     }
     // (one row per partition: formed in FP64 for both precisions)
@@ -782,13 +789,6 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     accepted = true;
     break;
   }
-  if constexpr (MODE == 3) {
-    // a chunk cannot refine alone: mark the system for the sequential solve
-    // (counted once per system)
-    if (t == 0 && atomicExch(&io.flag[sys], 1) == 0) atomicAdd(&g_pge_fallbacks, 1ull);
-    accepted = true;
-    break;
-  }
   if (t == 0) atomicAdd(&g_pge_paths[pass == 0 ? 1 : 2], 1ull);
   auto sidx = [&](int r) { return off(r / m, r % m); };
   if (pass > 0 && !pass_bad) {
@@ -807,13 +807,15 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     __syncthreads();
     unsigned long long rmax = 0ull, anorm = 0ull, xn = 0ull, dn = 0ull;
     bool nonfinite = false;
+    // (a long system's chunk: its first and last rows couple to x of the
+    // neighbouring chunks, s_xprev / s_xnext)
     for (int r = t; r < n; r += NT) {
-      const double ar = r > 0 ? (double)ga[base + r] : 0.0, br = (double)gb[base + r];
-      const double cr = r < n - 1 ? (double)gc[base + r] : 0.0, dr = (double)gd[base + r];
+      const double ar = r > 0 || !zero_a0 ? (double)ga[base + r] : 0.0, br = (double)gb[base + r];
+      const double cr = r < n - 1 || !zero_cl ? (double)gc[base + r] : 0.0, dr = (double)gd[base + r];
       const double xr = (double)SD[sidx(r)];
       double res = fma(-br, xr, dr);
-      if (r > 0) res = fma(-ar, (double)SD[sidx(r - 1)], res);
-      if (r < n - 1) res = fma(-cr, (double)SD[sidx(r + 1)], res);
+      res = fma(-ar, r > 0 ? (double)SD[sidx(r - 1)] : (double)s_xprev, res);
+      res = fma(-cr, r < n - 1 ? (double)SD[sidx(r + 1)] : (double)s_xnext, res);
       nonfinite |= !finite_val(res);
       rmax = max(rmax, mag(res));
       anorm = max(anorm, mag(fabs(ar) + fabs(br) + fabs(cr)));
@@ -829,6 +831,13 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
                        fma(__longlong_as_double((long long)s_anorm), __longlong_as_double((long long)s_xn),
                            __longlong_as_double((long long)s_dn));
     if (!__syncthreads_or(nonfinite || !(eta <= Fmt<T>::SEP_TOL))) {
+      accepted = true;
+      break;
+    }
+    if constexpr (MODE == 3) {
+      // a chunk cannot refine alone: mark the system for the sequential
+      // solve (counted once per system)
+      if (t == 0 && atomicExch(&io.flag[sys], 1) == 0) atomicAdd(&g_pge_fallbacks, 1ull);
       accepted = true;
       break;
     }

@@ -203,11 +203,17 @@ size_t tridiag_gtsv_workspace_size(int precision, int layout, int n_eqt, int n_b
 size_t tridiag_pivot_record_size(int n_eqt, int n_batch);
 
 /* Gaussian elimination with partial pivoting (the algorithm of LAPACK ?gtsv,
- * the reference's MKL row: Tridiagonal_AVX512/tridiagonal_basic.cpp:131-143),
- * one thread per system.  a, b, c are read only; d holds the right-hand side
- * on entry and x on exit.  pivots (may be NULL) receives the pivot record for
- * tridiag_gtsv_adjoint_*; info (may be NULL) receives per system 0 or k+1 for
- * the first zero pivot U(k,k).  work: tridiag_gtsv_workspace_size() bytes. */
+ * the reference's MKL row: Tridiagonal_AVX512/tridiagonal_basic.cpp:131-143).
+ * a, b, c are read only; d holds the right-hand side on entry and x on exit.
+ * pivots (may be NULL) receives the pivot record for tridiag_gtsv_adjoint_*;
+ * info (may be NULL) receives per system 0 or k+1 for the first zero pivot
+ * U(k,k).  work: tridiag_gtsv_workspace_size() bytes.  With a pivot record:
+ * one thread per system (two from both ends where the layout allows).
+ * Without one, from n = 512 on: the partitioned solve with partial pivoting
+ * inside partitions (one CTA or a cluster per system; contiguous FP64 from
+ * 12288 rows and any longer contiguous system in chunks of 4224 rows, one CTA
+ * each), which checks every result's backward error and hands a system that
+ * misses it to the sequential solve. */
 int tridiag_gtsv_single(int layout, const float *a, const float *b, const float *c, float *d,
                         unsigned int *pivots, int *info, void *work, size_t work_bytes, int n_eqt, int n_batch,
                         void *stream);

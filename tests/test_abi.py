@@ -77,3 +77,21 @@ def test_argument_checks_need_no_device(lib):
     assert lib.tridiag_gtsv_workspace_size(1, 0, 0, 4) == 0
     assert lib.tridiag_gtsv_workspace_size(1, 0, 100, 7) >= 2 * 100 * 7 * 8
     assert lib.tridiag_pivot_record_size(64, 3) == 2 * 3 * 4
+
+
+def test_host_solve_and_path_count_checks_need_no_device(lib):
+    """The host-buffer solve and the path counters reject bad arguments
+    before any CUDA call; the gtsv workspace covers the chunked solve's one
+    int per system."""
+    from tridiagonalsolver_gb300 import _lib
+
+    p = ctypes.c_void_p(256)
+    assert lib.tridiag_solve_host_double(0, 0, None, p, p, p, p, 64, 4, 0, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_solve_host_single(0, 0, p, p, p, p, p, 0, 4, 0, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_solve_host_single(0, 0, p, p, p, p, p, 64, 4, -1, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_solve_host_single(0, 9, p, p, p, p, p, 64, 4, 0, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_solve_host_single(0, 1, p, p, p, p, p, 64, 4, 0, None) == _lib.ERR_NOT_SUPPORTED
+    assert lib.tridiag_partition_path_counts(None, 0) == _lib.ERR_INVALID_VALUE
+    n, batch = 100000, 5
+    need = 2 * n * batch * 8 + 4 * ((n + 31) // 32) * batch + 4 * batch
+    assert lib.tridiag_gtsv_workspace_size(1, 0, n, batch) >= need

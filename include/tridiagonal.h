@@ -181,7 +181,8 @@ int tridiag_solve_out_double(int algo, int layout, const double *a, const double
  * the reference, whose test harness, Tridiagonal_CUDA/utils.cu:259-281,
  * copies each array to the device before the call).  The batch streams
  * through device buffers in chunks of `chunk` systems (0: about 96 MB of
- * inputs per chunk): host -> device copies, the solve of
+ * inputs per chunk; interleaved batches in one piece, as 2-D copies of
+ * chunks move far below the link's rate): host -> device copies, the solve of
  * tridiag_solve_out_* with `algo`, device -> host copy of x, on three
  * streams of the library's own, so that the copies of one chunk overlap the
  * solve of another; the streams and a ring of three chunk buffers persist per

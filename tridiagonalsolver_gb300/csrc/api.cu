@@ -883,7 +883,10 @@ int solve_host_impl(int algo, int layout, const T* a, const T* b, const T* c, co
   const size_t row = (size_t)n * sizeof(T);  // one array of one system
   int K = chunk;
   if (K == 0) {
-    const size_t k = HOST_CHUNK_BYTES / (4 * row);
+    // interleaved: one contiguous copy per array (chunks of systems are 2-D
+    // copies of n short rows, which the copy engines move far below the
+    // link's rate: 6 KB rows measured at about half of it on GB300)
+    const size_t k = layout == TRIDIAG_LAYOUT_INTERLEAVED ? (size_t)batch : HOST_CHUNK_BYTES / (4 * row);
     K = (int)(k < 1 ? 1 : k > (size_t)batch ? (size_t)batch : k);
   }
   if (K > batch) K = batch;
@@ -916,6 +919,9 @@ int solve_host_impl(int algo, int layout, const T* a, const T* b, const T* c, co
                     : cudaMemcpyAsync(dst + (size_t)j0 * n, src, bytes, cudaMemcpyDeviceToHost, q);
     }
     const size_t w = (size_t)kc * sizeof(T), hp = (size_t)batch * sizeof(T);
+    if (kc == batch)  // the whole batch: one contiguous copy
+      return to_dev ? cudaMemcpyAsync(dst, src, w * n, cudaMemcpyHostToDevice, q)
+                    : cudaMemcpyAsync(dst, src, w * n, cudaMemcpyDeviceToHost, q);
     return to_dev ? cudaMemcpy2DAsync(dst, w, src + j0, hp, w, n, cudaMemcpyHostToDevice, q)
                   : cudaMemcpy2DAsync(dst + j0, hp, src, w, w, n, cudaMemcpyDeviceToHost, q);
   };

@@ -4,7 +4,8 @@ larger than L2, a few launches, one kernel family each).
     python -m tridiagonalsolver_gb300.probes.profile_cases CASE
 
 CASE: pge64 (partitioned pivoted solve, FP64, n = 4096 x 2048 non-dominant),
-pgc32 (cluster version, FP32, n = 65536 x 256 dominant), pge32 (FP32,
+pgc32 (cluster version, FP32, n = 65536 x 256 dominant), pgl64 (long
+systems in chunks through gtsv, FP64, n = 65536 x 128 non-dominant), pge32 (FP32,
 n = 4096 x 4096 dominant), gtsv64 (thread-per-system pivoted sweep, FP64,
 n = 4096 x 1024), wmc32 (partition method without pivoting, FP32,
 n = 4096 x 4096 dominant), pcr32 (PCR-pThomas, FP32, n = 512 x 32768 dominant),
@@ -22,6 +23,7 @@ import torch
 import tridiagonalsolver_gb300 as T
 
 CASES = {"pge64": (4096, 2048, torch.float64, False), "pgc32": (65536, 256, torch.float32, True),
+         "pgl64": (65536, 128, torch.float64, False),
          "wmc32": (4096, 4096, torch.float32, True), "pcr32": (512, 32768, torch.float32, True),
          "pge32": (4096, 4096, torch.float32, True), "gtsv64": (4096, 1024, torch.float64, False)}
 
@@ -95,6 +97,8 @@ def main(case: str) -> None:
             T.solve_out(a, b, c, d, n, algo="partition", out=x)
         elif case == "pcr32":
             T.solve_out(a, b, c, d, n, algo="pcr", out=x)
+        elif case == "pgl64":
+            T.gtsv(a, b, c, d, n, out=x)
         else:
             T.pge(a, b, c, d, n, out=x)
     torch.cuda.synchronize()

@@ -1605,8 +1605,10 @@ cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info,
   const int nchunks = (n + rows - 1) / rows;
   const size_t ptot = (size_t)nchunks * PGE_LONG_NT, bsz = ptot * batch;
   // w1: the separator systems, their solution and the chunk links (about
-  // 0.15 n per system); w2: x until it is committed
+  // 0.15 n per system); w2: x until it is committed.  (One CTA per chunk:
+  // the grid must stay an int.)
   if (5 * ptot + 4 * (size_t)nchunks > (size_t)n) return cudaSuccess;
+  if ((long long)batch * nchunks > 0x7fffffffLL || (long long)batch * 64 > 0x7fffffffLL) return cudaSuccess;
   T* sep = w1;
   T* xsep = w1 + 4 * bsz;
   T* carry = xsep + bsz;

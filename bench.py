@@ -253,9 +253,7 @@ def run_ours(args):
     sampler.mark("end")
     ms_total = ev0.elapsed_time(ev1)
     if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+        ms_total = max_over_ranks(torch, dist, ms_total, dev)
     ms_step = ms_total / args.steps
 
     # per-part launch times (same conditions, after the timed region)
@@ -277,7 +275,7 @@ def run_ours(args):
     e2e = _e2e(torch, T, data, stream, solve_part, steps=max(3, min(args.steps // 10, 20)))
 
     systems = sum(p["batch"] for p in PARTS)
-    value = world * systems / (ms_step * 1e-3)
+    value = job_value(world, systems, ms_step)
     if rank == 0:
         peak, peak_kind = _measured_peaks()
         traffic = _traffic_table()
@@ -326,6 +324,20 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def max_over_ranks(torch, dist, value: float, device) -> float:
+    """The largest of every rank's value (the slowest rank's time): an
+    all-reduce of one number, the same on every rank."""
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, systems_per_rank: int, ms_step: float) -> float:
+    """Whole-job systems/s: every rank solves its own systems (replicas), the
+    step lasts as long as the slowest rank's."""
+    return world * systems_per_rank / (ms_step * 1e-3)
 
 
 def _accuracy(torch, data, sample=16):

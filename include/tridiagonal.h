@@ -136,8 +136,9 @@ void Thomas_double(double *a_gbl, double *b_gbl, double *c_gbl, double *d_gbl, i
 #define TRIDIAG_ALGO_GTSV 5   /* partial pivoting: PGE for n >= 512 where it fits, else one thread per system */
 #define TRIDIAG_ALGO_PGE 6    /* WM-pGE with partial pivoting inside partitions, one CTA per system */
 #define TRIDIAG_ALGO_PARTITION 7 /* partition method without pivoting: one CTA per system for n <= 8192 FP32 /
-                                    4096 FP64 (contiguous / packed); chunks of 8192 / 4096 rows per CTA for longer
-                                    systems whose n is a multiple of 32 / 16 (contiguous, up to 262144 / 65536) */
+                                    4096 FP64 (contiguous / packed, any n); chunks of 4096 / 2048 rows per CTA for
+                                    longer systems whose n is a multiple of 32 / 16 (contiguous, up to 262144 /
+                                    65536) */
 
 /* Status of the last library call made by the calling host thread. */
 int tridiag_last_status(void);

@@ -1118,6 +1118,125 @@ def run_block2(args):
                f"{gops / fp64_peak:.0%} of the {fp64_peak:.0f} Gop/s DFMA microbenchmark rate")
 
 
+# ---------------------------------------------------------------------------
+# Small cases of single kernel families for ncu captures (--profile-case NAME):
+# inputs a little larger than L2 where the kernel allows, a few launches,
+# each case solving three times.
+
+PROFILE_CASES = {
+    # name: (n, batch, dtype, dominant, how)
+    "pge64": (4096, 2048, "float64", False, "pge"),        # partitioned pivoted solve, FP64
+    "pge32": (4096, 4096, "float32", True, "pge"),         # the same, FP32
+    "pgc32": (65536, 256, "float32", True, "pge"),         # cluster version, FP32
+    "pgl64": (65536, 128, "float64", False, "gtsv"),       # long systems in chunks, FP64
+    "gtsv64": (4096, 1024, "float64", False, "gtsv_piv"),  # thread-per-system pivoted sweep (pivot record)
+    "adj64": (4096, 1024, "float64", False, "adjoint"),    # its adjoint (AdjOp)
+    "wmc32": (4096, 4096, "float32", True, "partition"),   # partition method without pivoting, FP32
+    "pcr32": (512, 32768, "float32", True, "pcr"),         # PCR-pThomas at the config-2 shape
+    "crpcr32": (512, 32768, "float32", True, "cr"),        # CR-PCR at the config-2 shape
+    "wm32": (1024, 16384, "float32", True, "wm"),          # on-chip WM-pGE, one warp per system
+    "thomas64i": (4096, 2048, "float64", True, "thomas_i"),  # Thomas FP64, interleaved (config 1 kernel)
+    "refine64": (65536, 128, "float64", True, "refine"),   # refinement pieces + chunked FP32 solves
+    "factor64": (1024, 8192, "float64", False, "factor"),  # factor once / solve many
+    "relayout64": (1024, 16384, "float64", True, "relayout"),  # contiguous -> interleaved transposes
+    "periodic64": (1024, 8192, "float64", True, "periodic"),   # Sherman-Morrison periodic solve
+}
+
+
+def profile_case(name: str) -> None:
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+
+    T.lib()
+    if name == "block2_64":
+        n, batch = 256, 32768
+        g = torch.Generator(device="cuda")
+        g.manual_seed(5)
+        src = [torch.rand(k * n * batch, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+               for k in (4, 4, 4, 2)]
+        dom = src[1].clone().view(n, 4, batch)
+        dom[:, 0] += 8
+        dom[:, 3] += 8
+        work = [t.clone() for t in src]
+        for algo, b in (("pivoted", src[1]), ("thomas", dom.view(-1))):
+            for _ in range(3):
+                for w, s_ in zip(work, (src[0], b, src[2], src[3])):
+                    w.copy_(s_)
+                T.block2(*work, n, algo=algo, layout="interleaved")
+        torch.cuda.synchronize()
+        print("ok block2_64")
+        return
+    if name == "ragged_step":
+        # the ragged workload: three forward + adjoint steps, then one between
+        # torch.cuda.profiler.start() and stop() (ncu --profile-from-start off)
+        from tridiagonalsolver_gb300 import ragged
+
+        sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
+        a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
+        w = torch.rand_like(d) * 2 - 1
+        classes = sorted({ragged.size_class(int(v)) for v in sizes})
+        table, _ = ragged.autotune(classes, dtype=torch.float32, reps=1)
+        plan = T.RaggedPlan(off, table=table, no_pivoting=~nondom)
+        x = torch.empty_like(d)
+        grads = [torch.empty_like(d) for _ in range(4)]
+        s_ = torch.cuda.Stream()
+        s_.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s_):
+            for _ in range(3):
+                plan.solve(a, b, c, d, out=x, stream=s_)
+                plan.adjoint(a, b, c, x, w, grads=grads, stream=s_)
+            s_.synchronize()
+            torch.cuda.profiler.start()
+            plan.solve(a, b, c, d, out=x, stream=s_)
+            plan.adjoint(a, b, c, x, w, grads=grads, stream=s_)
+            s_.synchronize()
+            torch.cuda.profiler.stop()
+        print("ok ragged_step", int(off[-1]), "rows")
+        return
+    n, batch, dts, dominant, how = PROFILE_CASES[name]
+    dt = getattr(torch, dts)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    inter = how == "thomas_i"
+    shape = (n, batch) if inter else (batch, n)
+
+    def u(lo, hi):
+        return torch.rand(shape, dtype=dt, device="cuda", generator=g) * (hi - lo) + lo
+
+    a, b, c, d = u(-1, 1), u(-1, 1), u(-1, 1), u(-1, 1)
+    if dominant:
+        b = a.abs() + c.abs() + u(1, 2)
+    x = torch.empty_like(d)
+    piv = T.pivot_record(a, n) if how in ("gtsv_piv", "adjoint") else None
+    fac = T.Factorization(a, b, c, n) if how == "factor" else None
+    for _ in range(3):
+        if how == "gtsv_piv":
+            T.gtsv(a, b, c, d, n, pivots=piv, out=x)
+        elif how == "adjoint":
+            xf = T.gtsv(a, b, c, d, n, pivots=piv)
+            T.gtsv_adjoint(a, b, c, xf, piv, d, n)
+        elif how == "gtsv":
+            T.gtsv(a, b, c, d, n, out=x)
+        elif how in ("partition", "pcr", "cr", "wm"):
+            T.solve_out(a, b, c, d, n, algo=how, out=x)
+        elif how == "thomas_i":
+            T.solve_out(a, b, c, d, n, algo="thomas", layout="interleaved", out=x)
+        elif how == "refine":
+            T.refine(a, b, c, d, n, iters=2, out=x, algo="partition")
+        elif how == "factor":
+            fac = T.Factorization(a, b, c, n)
+            fac.solve(d)
+        elif how == "relayout":
+            T.relayout((a, b, c, d), n, "contiguous", "interleaved")
+        elif how == "periodic":
+            T.periodic(a, b, c, d, n, out=x)
+        else:
+            T.pge(a, b, c, d, n, out=x)
+    torch.cuda.synchronize()
+    print("ok", name)
+
+
 WORKLOADS = {"config2": None, "thomas-fp64": run_thomas_fp64, "adjoint": run_adjoint, "ragged": run_ragged,
              "refined": run_refined, "block2": run_block2, "plain": run_plain}
 
@@ -1132,7 +1251,12 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2",
                     help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
                          "remaining benchmark configurations, one JSON line each")
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step"], default=None,
+                    help="run one small case of one kernel family three times (for ncu captures) and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

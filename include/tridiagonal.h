@@ -215,7 +215,9 @@ size_t tridiag_pivot_record_size(int n_eqt, int n_batch);
  * inside partitions (one CTA or a cluster per system; contiguous FP64 from
  * 12288 rows and any longer contiguous system in chunks of 4224 rows, one CTA
  * each), which checks every result's backward error and hands a system that
- * misses it to the sequential solve. */
+ * misses it to the sequential solve.  Layout 1 (packed): a is the packed base
+ * pointer (b and c are ignored) and d points at the right-hand-side rows of
+ * system 0 with the packed stride 4n between systems (a + 3n solves in place). */
 int tridiag_gtsv_single(int layout, const float *a, const float *b, const float *c, float *d,
                         unsigned int *pivots, int *info, void *work, size_t work_bytes, int n_eqt, int n_batch,
                         void *stream);
@@ -480,7 +482,11 @@ int tridiag_partition_path_counts(long long *counts, int reset);
  * scratch is one static device array of TRIDIAG_NOALLOC_SCRATCH_BYTES that
  * every GPU loading the library holds until exit.  The first call on a
  * device looks up that array's device address; make it before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU
+ * capture.  After cudaDeviceReset the device's next call looks it up again
+ * (the array is new with the new context), so that call too belongs before
+ * any capture.  Layout 1: a is the packed base, b and c are ignored, d
+ * points at the right-hand-side rows (a + 3n in place), as for
+ * tridiag_gtsv_*.  All calls share the array, so calls that overlap on the GPU
  * race and must be serialised by the caller.  Returns TRIDIAG_ERR_WORKSPACE,
  * launching nothing, when 2*n*batch*sizeof(T) plus the pivot bits (each
  * rounded up to 256 bytes) exceed the array.  Returns its status directly

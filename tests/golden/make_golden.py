@@ -1,6 +1,6 @@
 """Generate the golden fixtures in this directory (run here, on x86-64).
 
-    make -C oracle ref             # builds oracle/_ref/libref_avx512.so from
+    make -C oracle ref REF_ROOT=<reference checkout>   # builds oracle/_ref/libref_avx512.so from
                                    # the reference's Tridiagonal_AVX512 sources
     python tests/golden/make_golden.py
 
@@ -54,7 +54,7 @@ def _gen(kind, n, batch, seed):
 
 def main() -> None:
     if not O.ref_available():
-        raise SystemExit("build the reference first: make -C oracle ref")
+        raise SystemExit("build the reference first: make -C oracle ref REF_ROOT=<reference checkout>")
     for dt, names in ROUTINES.items():
         out = {}
         tag = "f64" if dt == np.float64 else "f32"

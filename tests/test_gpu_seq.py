@@ -199,3 +199,72 @@ def test_gtsv_adjoint_central_differences_fp64(cuda):
             vm[k][:, i] -= h
             fd = (loss(vp) - loss(vm)) / (2 * h)
             np.testing.assert_allclose(grads[k][:, i], fd, rtol=1e-6, atol=1e-8)
+
+
+GUARD = 4 << 20  # bytes of guard region on each side of the workspace
+PATTERN = 0xA5
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("with_pivots", [True, False])
+@pytest.mark.parametrize("n,batch", [(3, 8), (33, 37), (300, 8), (511, 64), (1000, 9)])
+def test_gtsv_packed_guarded_workspace(cuda, dt, with_pivots, n, batch):
+    """Pivoted solve of packed systems ([batch][a|b|c|d][n], the reference's
+    layout 1, Tridiagonal_CUDA/utils.cu:254-260) through the C ABI with the
+    workspace between two guard regions of a byte pattern: the guard bytes
+    must be unchanged afterwards (no scratch write outside the workspace),
+    the packed a, b, c rows of the output untouched, and x within backward
+    error 1e-12 (FP64) / 1e-6 (FP32) of its system."""
+    import ctypes
+
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300._lib import SUCCESS
+
+    lib = T.lib()
+    a, b, c, d = inputs.nondominant(n, batch, seed=300 + n + batch)
+    packed = inputs.to_packed(a, b, c, d).astype(dt)
+    p = cuda.from_numpy(packed.copy()).cuda()
+    x = p.clone()
+    ws = lib.tridiag_gtsv_workspace_size(1 if dt == np.float64 else 0, 1, n, batch)
+    buf = cuda.full((GUARD + ws + GUARD,), PATTERN, dtype=cuda.uint8, device="cuda")
+    piv = T.pivot_record(p, n, "packed") if with_pivots else None
+    info = cuda.full((batch,), -1, dtype=cuda.int32, device="cuda")
+    fn = lib.tridiag_gtsv_double if dt == np.float64 else lib.tridiag_gtsv_single
+    es = np.dtype(dt).itemsize
+    st = fn(1, ctypes.c_void_p(p.data_ptr()), None, None, ctypes.c_void_p(x.data_ptr() + 3 * n * es),
+            ctypes.c_void_p(piv.data_ptr()) if piv is not None else None, ctypes.c_void_p(info.data_ptr()),
+            ctypes.c_void_p(buf.data_ptr() + GUARD), ctypes.c_size_t(ws), n, batch, None)
+    assert st == SUCCESS
+    cuda.cuda.synchronize()
+    g = buf.cpu().numpy()
+    assert np.all(g[:GUARD] == PATTERN), "workspace underrun"
+    assert np.all(g[GUARD + ws:] == PATTERN), "workspace overrun"
+    assert int(info.abs().sum()) == 0
+    xh = x.cpu().numpy().reshape(batch, 4, n)
+    np.testing.assert_array_equal(xh[:, :3, :], packed.reshape(batch, 4, n)[:, :3, :])
+    np.testing.assert_array_equal(p.cpu().numpy(), packed)
+    a_, b_, c_, d_ = (v.astype(dt).astype(np.float64) for v in (a, b, c, d))
+    xs = xh[:, 3, :].astype(np.float64)
+    _, worst = O.backward_error(a_, b_, c_, d_, xs, n)
+    assert worst <= ETA[dt]
+    xo = O.gtsv(a_, b_, c_, d_, n).reshape(batch, n)
+    assert np.median(_rel(xs, xo)) <= (1e-11 if dt == np.float64 else 1e-3)
+    # the Python front end gives the same bits
+    xt = T.gtsv(p, None, None, None, n, layout="packed", pivots=piv)
+    np.testing.assert_array_equal(xt.cpu().numpy(), x.cpu().numpy())
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_gtsv_packed_adjoint_refused(cuda, dt):
+    """The pivoted adjoint takes contiguous and interleaved systems only."""
+    import ctypes
+
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300._lib import ERR_NOT_SUPPORTED
+
+    lib = T.lib()
+    t = cuda.zeros(4 * 8 * 4, dtype=cuda.float64 if dt == np.float64 else cuda.float32, device="cuda")
+    ptr = ctypes.c_void_p(t.data_ptr())
+    fn = lib.tridiag_gtsv_adjoint_double if dt == np.float64 else lib.tridiag_gtsv_adjoint_single
+    st = fn(1, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ctypes.c_size_t(1 << 20), 8, 4, None)
+    assert st == ERR_NOT_SUPPORTED

@@ -3,11 +3,13 @@
 It exists for callers that cannot allocate device memory where they solve
 (hard latency budgets, memory owned by another allocator); its scratch is a
 static device array shared by all calls.  This test calls it through the C
-ABI twice in a row on different systems and compares each result with the
-existing pivoted entry point (tridiag_gtsv_*, caller-provided workspace):
+ABI twice in a row on different systems, in each layout, and compares each
+result with the existing pivoted entry point (tridiag_gtsv_*, caller-provided
+workspace):
 max |x_noalloc - x_gtsv| / max |x_gtsv| <= 1e-12 (FP64) / 1e-5 (FP32) per
 system, and normwise backward error <= 1e-12 / 1e-6.  It also checks that a
-problem larger than the static array is refused.  The file is named to be
+call after the first one leaves the device's free memory unchanged, and
+that a problem larger than the static array is refused.  The file is named to be
 collected last; it passes alone and after the other tests.
 """
 import ctypes
@@ -24,7 +26,7 @@ TOL = {np.float64: (1e-12, 1e-12), np.float32: (1e-5, 1e-6)}
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32])
-@pytest.mark.parametrize("layout", ["contiguous", "interleaved"])
+@pytest.mark.parametrize("layout", ["contiguous", "interleaved", "packed"])
 def test_noalloc_matches_gtsv_two_calls(cuda, dt, layout):
     import tridiagonalsolver_gb300 as T
     from tridiagonalsolver_gb300._lib import LAYOUTS, SUCCESS
@@ -33,6 +35,7 @@ def test_noalloc_matches_gtsv_two_calls(cuda, dt, layout):
     fn = lib.tridiag_gtsv_noalloc_double if dt == np.float64 else lib.tridiag_gtsv_noalloc_single
     rel_tol, eta_tol = TOL[dt]
     n, batch = 300, 96
+    es = np.dtype(dt).itemsize
     stream = cuda.cuda.current_stream().cuda_stream
     for call in range(2):
         # the second call solves different systems (another seed and
@@ -41,16 +44,23 @@ def test_noalloc_matches_gtsv_two_calls(cuda, dt, layout):
             a, b, c, d = (v.astype(dt) for v in inputs.dominant(n, batch, seed=41))
         else:
             a, b, c, d = (v.astype(dt) for v in inputs.reference(n, batch, seed=42)[:4])
-        host = (a, b, c, d)
-        if layout == "interleaved":
-            host = inputs.to_interleaved(*host)
-        ta, tb, tc, td = (cuda.from_numpy(np.ascontiguousarray(v)).cuda() for v in host)
-        x_ref = T.gtsv(ta, tb, tc, td, n, layout=layout)
-        x_new = td.clone()
+        if layout == "packed":
+            # one packed array [batch][a|b|c|d][n]; x in the d rows of a copy
+            tp = cuda.from_numpy(inputs.to_packed(a, b, c, d).astype(dt)).cuda()
+            x_ref = T.gtsv(tp, None, None, None, n, layout="packed")
+            x_new = tp.clone()
+            ptrs = (tp.data_ptr(), None, None, x_new.data_ptr() + 3 * n * es)
+        else:
+            host = (a, b, c, d)
+            if layout == "interleaved":
+                host = inputs.to_interleaved(*host)
+            ta, tb, tc, td = (cuda.from_numpy(np.ascontiguousarray(v)).cuda() for v in host)
+            x_ref = T.gtsv(ta, tb, tc, td, n, layout=layout)
+            x_new = td.clone()
+            ptrs = (ta.data_ptr(), tb.data_ptr(), tc.data_ptr(), x_new.data_ptr())
         info = cuda.full((batch,), -1, dtype=cuda.int32, device="cuda")
-        st = fn(LAYOUTS[layout], ctypes.c_void_p(ta.data_ptr()), ctypes.c_void_p(tb.data_ptr()),
-                ctypes.c_void_p(tc.data_ptr()), ctypes.c_void_p(x_new.data_ptr()), ctypes.c_void_p(info.data_ptr()),
-                n, batch, ctypes.c_void_p(stream))
+        st = fn(LAYOUTS[layout], *(ctypes.c_void_p(v) if v else None for v in ptrs),
+                ctypes.c_void_p(info.data_ptr()), n, batch, ctypes.c_void_p(stream))
         assert st == SUCCESS
         cuda.cuda.synchronize()
         assert int(info.abs().sum()) == 0
@@ -58,6 +68,11 @@ def test_noalloc_matches_gtsv_two_calls(cuda, dt, layout):
         xn = x_new.double().cpu().numpy()
         if layout == "interleaved":
             xr, xn = xr.T, xn.T
+        if layout == "packed":
+            xr, xn = xr.reshape(batch, 4, n)[:, 3, :], xn.reshape(batch, 4, n)[:, 3, :]
+            # the a, b, c rows of the copy are untouched
+            np.testing.assert_array_equal(x_new.cpu().numpy().reshape(batch, 4, n)[:, :3, :],
+                                          tp.cpu().numpy().reshape(batch, 4, n)[:, :3, :])
         xr, xn = xr.reshape(batch, n), xn.reshape(batch, n)
         rel = np.max(np.abs(xn - xr), axis=1) / np.max(np.abs(xr), axis=1)
         assert np.max(rel) <= rel_tol, (call, float(np.max(rel)))
@@ -77,3 +92,31 @@ def test_noalloc_refuses_oversized_problem(cuda):
     ptr = ctypes.c_void_p(p.data_ptr())
     st = lib.tridiag_gtsv_noalloc_double(0, ptr, ptr, ptr, ptr, None, n, batch, None)
     assert st == ERR_WORKSPACE
+
+
+def test_noalloc_leaves_free_memory_unchanged(cuda):
+    """After a first call on the device (which looks up the static array's
+    address), further calls take no device memory: cudaMemGetInfo's free
+    bytes are the same before and after."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300._lib import SUCCESS
+
+    lib = T.lib()
+    n, batch = 1000, 256
+    a, b, c, d = (cuda.from_numpy(v.copy()).cuda() for v in inputs.nondominant(n, batch, seed=43))
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    x = d.clone()
+    # warm-up: the first call of each kernel (this entry point's and torch's
+    # copy) may load its module, which takes device memory once
+    x.copy_(d)
+    assert lib.tridiag_gtsv_noalloc_double(0, P(a), P(b), P(c), P(x), None, n, batch, None) == SUCCESS
+    cuda.cuda.synchronize()
+    free0, _ = cuda.cuda.mem_get_info()
+    for _ in range(3):
+        x.copy_(d)
+        assert lib.tridiag_gtsv_noalloc_double(0, P(a), P(b), P(c), P(x), None, n, batch, None) == SUCCESS
+    cuda.cuda.synchronize()
+    free1, _ = cuda.cuda.mem_get_info()
+    assert free1 == free0
+    _, eta = O.backward_error(*(t.cpu().numpy() for t in (a, b, c, d, x)), n)
+    assert eta <= 1e-12

@@ -34,6 +34,16 @@ __host__ __device__ __forceinline__ size_t idx(int i, int j, int n, int batch) {
   return (size_t)j * (size_t)n + (size_t)i;
 }
 
+// Element offset of row i of system j in a kernel's own scratch array of
+// n * batch elements: batch-fastest for interleaved inputs (so the scratch
+// accesses coalesce like the inputs'), system-major otherwise.  Never the
+// packed stride: packed systems are 4n elements apart, which would run past
+// an n * batch array.
+template <int L>
+__host__ __device__ __forceinline__ size_t sidx(int i, int j, int n, int batch) {
+  return L == INTERLEAVED ? idx<INTERLEAVED>(i, j, n, batch) : idx<CONTIG>(i, j, n, batch);
+}
+
 // ---------------------------------------------------------------------------
 // Reciprocals.
 

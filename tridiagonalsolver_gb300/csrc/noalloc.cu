@@ -13,8 +13,10 @@
 //   * every GPU that loads this library holds the array until the process
 //     exits;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture;
+//     (cudaGetSymbolAddress, with that device current) and caches it with
+//     the device's context; make that first call before any stream capture.
+//     A later call in another context of the device (after cudaDeviceReset)
+//     looks the address up again, so it too belongs outside a capture;
 //   * all calls share the one array, which keeps the last call's contents;
 //     the kernel writes every scratch entry before it reads it, so nothing
 //     has to be cleared between calls, but calls that overlap on the GPU
@@ -24,6 +26,8 @@
 //     TRIDIAG_ERR_WORKSPACE before anything is launched.
 // The arithmetic is the one-ended pivoted sweep of seq.cu (the algorithm of
 // LAPACK ?gtsv), so results match tridiag_gtsv_* to rounding.
+#include <cuda.h>
+
 #include <cstdint>
 #include <mutex>
 
@@ -36,20 +40,47 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[TRIDIAG_NOALLOC
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[64] = {};
+CUcontext g_noalloc_ctx[64] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device; the host-side symbol itself is not a device address).
+// The calling thread's current driver context (cuCtxGetCurrent through the
+// runtime's driver entry point; no link-time dependency on libcuda).
+CUcontext current_context() {
+  using Fn = CUresult (*)(CUcontext*);
+  static Fn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<Fn>(p);
+  });
+  CUcontext ctx = nullptr;
+  if (fn && fn(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+  return ctx;
+}
+
+// Device address of g_noalloc_scratch on the current device (the host-side
+// symbol itself is not a device address).  Looked up on the first call on a
+// device and again whenever that device's context has changed since (after
+// cudaDeviceReset the primary context, and with it the array, is new).
 cudaError_t noalloc_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  // bind the device's primary context to this thread (a thread that has made
+  // no runtime call yet has none current)
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess) return e;
+  const CUcontext ctx = current_context();
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || ctx != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
     g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx[dev] = ctx;
   }
   *out = g_noalloc_ptr[dev];
   return cudaSuccess;

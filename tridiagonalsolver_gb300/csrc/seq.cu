@@ -108,7 +108,8 @@ __global__ void __launch_bounds__(128) thomas_seq_kernel(const T* __restrict__ a
 // Pivoted elimination.  Step i compares the running pivot u0 (row i) with the
 // sub-diagonal a_{i+1}; when |u0| < |a_{i+1}| rows i and i+1 are interchanged
 // (LAPACK's rule: ties keep the rows).  The finished row i is kept as
-//   RHS_i -> d[i], U1_i -> w1[i], 1/U0_i -> w2[i],
+//   RHS_i -> d[i], U1_i -> w1[i], 1/U0_i -> w2[i]
+// (w1, w2: n * batch elements each, indexed by sidx, for every layout),
 // and its second super-diagonal U2_i equals c_{i+1} when the rows were
 // swapped, else 0, so only the pivot bit is stored (bit i%32 of word i/32,
 // word w of system j at piv[w*batch + j]).  a, b, c are not modified.
@@ -173,10 +174,10 @@ __global__ void __launch_bounds__(128) gtsv_seq_kernel(const T* __restrict__ a, 
         const T nu0 = fma(-m, sw ? rb[u] : u1, sw ? u1 : rb[u]);
         const T nu1 = sw ? -m * rc[u] : rc[u];
         const T nrhs = fma(-m, sw ? rd[u] : rhs, sw ? rhs : rd[u]);
-        size_t o = idx<L>(i, j, n, batch);
-        st_keep(d + o, R);
-        st_keep(w1 + o, U1);
-        st_keep(w2 + o, r);
+        const size_t so = sidx<L>(i, j, n, batch);
+        st_keep(d + idx<L>(i, j, n, batch), R);
+        st_keep(w1 + so, U1);
+        st_keep(w2 + so, r);
         word |= (unsigned)sw << (i & 31);
         if ((i & 31) == 31) {
           if (piv) piv[(size_t)(i >> 5) * batch + j] = word;
@@ -210,7 +211,8 @@ __global__ void __launch_bounds__(128) gtsv_seq_kernel(const T* __restrict__ a, 
     T u2 = T(0);
     const bool sw = (wcur >> (i & 31)) & 1u;
     if (sw && i + 2 < n) u2 = ld_stream(c + idx<L>(i + 1, j, n, batch));
-    T R = ld_keep(d + o), U1v = ld_keep(w1 + o), rv = ld_keep(w2 + o);
+    const size_t so = sidx<L>(i, j, n, batch);
+    T R = ld_keep(d + o), U1v = ld_keep(w1 + so), rv = ld_keep(w2 + so);
     T x0 = fma(-U1v, x1, R);
     x0 = fma(-u2, x2, x0) * rv;
     st_stream(d + o, x0);
@@ -270,8 +272,9 @@ __global__ void __launch_bounds__(128) gtsv_adjoint_seq_kernel(
     s = fma(-U1p, z1, s);
     s = fma(-U2pp, z2, s);
     T z = s * r;
-    st_keep(wz + o, z);
-    st_keep(wm + o, m);
+    const size_t so = sidx<L>(i, j, n, batch);
+    st_keep(wz + so, z);
+    st_keep(wm + so, m);
     z2 = z1;
     z1 = z;
     U2pp = U2p;
@@ -286,7 +289,8 @@ __global__ void __launch_bounds__(128) gtsv_adjoint_seq_kernel(
     size_t o = idx<L>(i, j, n, batch);
     if (((i & 31) == 31) || i == n - 2) wcur = piv[(size_t)(i >> 5) * batch + j];
     const bool sw = (wcur >> (i & 31)) & 1u;
-    T zi = ld_keep(wz + o), mi = ld_keep(wm + o);
+    const size_t so = sidx<L>(i, j, n, batch);
+    T zi = ld_keep(wz + so), mi = ld_keep(wm + so);
     T ni = fma(-mi, carry, zi);
     T lam1 = sw ? ni : carry;  // final lambda_{i+1}
     carry = sw ? carry : ni;

@@ -132,16 +132,27 @@ def gtsv(a, b, c, d, n: int, layout: str = "contiguous", pivots=None, info=None,
     """Partial-pivoting solve; a, b, c, d are not modified.  Returns x (a new
     tensor, or ``out``).  ``pivots`` (from :func:`pivot_record`) receives the
     pivot record for :func:`gtsv_adjoint`; ``info`` (int32, batch) receives
-    0 or k+1 for the first zero pivot of each system."""
+    0 or k+1 for the first zero pivot of each system.  Layout "packed": pass
+    the packed tensor as ``a`` (None for b, c, d); the result is a packed
+    tensor with x in rows 3n..4n of each system."""
     p = _prec(a)
     batch = _dims(a, n, layout)
     a, b, c = _al(a), _al(b), _al(c)
-    x = out if out is not None else torch.empty_like(d, memory_format=torch.contiguous_format)
-    if x.data_ptr() != d.data_ptr():
-        x.copy_(d)
+    if layout == "packed":
+        # one packed tensor in (pass it as a, None for b, c, d); x is a copy of
+        # it whose right-hand-side rows (3n..4n of each system) receive the solution
+        x = out if out is not None else torch.empty_like(a, memory_format=torch.contiguous_format)
+        if x.data_ptr() != a.data_ptr():
+            x.copy_(a)
+        xp = _ptr(x, a.dtype) + 3 * n * x.element_size()
+    else:
+        x = out if out is not None else torch.empty_like(d, memory_format=torch.contiguous_format)
+        if x.data_ptr() != d.data_ptr():
+            x.copy_(d)
+        xp = _ptr(x, a.dtype)
     work = work if work is not None else gtsv_workspace(a, n, layout)
     st = getattr(lib(), f"tridiag_gtsv_{p}")(
-        LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), _ptr(x, a.dtype),
+        LAYOUTS[layout], _ptr(a, a.dtype), _ptr(b, a.dtype), _ptr(c, a.dtype), xp,
         _ptr(pivots), _ptr(info), _ptr(work), work.numel(), n, batch, _stream_ptr(stream))
     check(st, f"tridiag_gtsv_{p}")
     return x

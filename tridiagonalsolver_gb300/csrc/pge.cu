@@ -396,9 +396,8 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   T* SB = S0 + astride + dl[1];
   T* SC = S0 + 2 * astride + dl[2];
   T* SD = S0 + 3 * astride + dl[3];
-  T* SV = S0 + 4 * astride;
-  T* SX = SV + astride;   // x kept across refinement passes
-  T* SEP = SX + astride;  // [3][4][NT] separator rows: original + ping-pong
+  T* SX = S0 + 4 * astride;  // x kept across refinement passes
+  T* SEP = SX + astride;     // [3][4][NT] separator rows: original + ping-pong
   T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
   T* TMP = FST + 3 * NT;  // [PGE_TMP]: the FP32 separator solve's top level
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -500,8 +499,11 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   // ---- forward elimination of partition t's interior block (rows 0 ..
   // mi-1) with partial pivoting, for three right-hand sides: d, the left
   // spike a_0 e_0 and the right spike c_{mi-1} e_{mi-1}.  U row i is stored
-  // as (1/u0_i -> A, u1_i -> B, y'_i -> D, v'_i -> V); u2_i is c_{i+1} when
-  // rows i and i+1 were interchanged (swap bit), else 0.  The separator
+  // as (1/u0_i -> A, u1_i -> B, z_i -> C, y'_i -> D) and swap bit i of swm:
+  // when rows i and i+1 were interchanged, u2_i = z_i (= c_{i+1}) and
+  // v'_i = 0, else u2_i = 0 and v'_i = z_i -- one of the two is always zero,
+  // so one array holds both and the back substitution's term is
+  // z_i * (swap ? x_{i+2} : s_{t-1}).  The separator
   // system needs the first and last rows of U^{-1} applied to the three
   // eliminated right-hand sides: the last row is y'/u0 of the last U row;
   // the first row omega = e_0^T U^{-1} follows the recurrence
@@ -512,7 +514,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   auto B = [&](int i) -> T& { return SB[off(t, i)]; };
   auto C = [&](int i) -> T& { return SC[off(t, i)]; };
   auto D = [&](int i) -> T& { return SD[off(t, i)]; };
-  auto V = [&](int i) -> T& { return SV[off(t, i)]; };
+  unsigned long long swm = 0ull;  // swap bits of U rows 0 .. mi-2 (m <= 64)
   bool bad = false;  // this pass: breakdown, non-finite or (pass 0) separator residual
   T cb, cc, cy, cv, cw;                        // the candidate row (b, c, y', v', w')
   T w_prev = T(0);                             // w' of U row mi-2 (the only other nonzero w')
@@ -545,6 +547,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     const T u2 = keep_if(sw, nc);
     const T uy = sw ? ny : cy;
     const T uv = keep_if(!sw, cv);
+    const T zs = sw ? nc : cv;  // the nonzero one of u2 and v'
     const T om = fma(-om2, pu2b, fma(-om1, pu1, kro)) * inv;
     kro = T(0);
     Y0 = fma(om, uy, Y0);
@@ -556,13 +559,13 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     pu1 = u1;
     A(i) = inv;
     B(i) = u1;
-    C(i) = u2;  // c_i was read two rows ago
+    C(i) = zs;  // c_i was read two rows ago
     D(i) = uy;
-    V(i) = uv;
+    swm |= (unsigned long long)sw << i;
     cb = fma(-l, u1, sw ? cc : nb);
     // the row left behind keeps one of c_{i+2} (no swap) and the left spike
     // (swap); the other is scaled by -l: one product for both
-    const T tq = -l * (sw ? nc : cv);
+    const T tq = -l * zs;
     cc = sw ? tq : nc;
     cy = fma(-l, uy, sw ? cy : ny);
     cv = sw ? cv : tq;
@@ -611,9 +614,8 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   const T Ylast = cy * inv_last, Vlast = cv * inv_last, Wlast = cw * inv_last;
   A(mi - 1) = inv_last;
   B(mi - 1) = T(0);
-  C(mi - 1) = T(0);
+  C(mi - 1) = cv;  // z of the last U row: v' (no u2; its swap bit is 0)
   D(mi - 1) = cy;
-  V(mi - 1) = cv;
   __syncthreads();
 
   // ---- separator system: row m-1 of partition t couples to the last
@@ -659,36 +661,52 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     FST[t] = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT + t];
   } else {
   // Parallel cyclic reduction of the separator system (SEP[0..4NT) keeps the
-  // original rows, SEP[4NT..12NT) is the ping-pong pair) ...
+  // original rows, SEP[4NT..12NT) is the ping-pong pair) ...  Thread t owns
+  // row t through all steps and keeps it in registers; what its neighbours
+  // read is published as (a, 1/b, c, d), so each row's reciprocal is formed
+  // once per step by its owner instead of once by each of its two readers.
   {
-    const T* cur = SEP;
-    int ph = 1;
+    T ra = SEP[t], rb = SEP[NT + t], rc = SEP[2 * NT + t], rd = SEP[3 * NT + t];
+    T ri = Div<T>(rb).inv();
+    T* cur = SEP + 4 * NT;
+    cur[t] = ra;
+    cur[NT + t] = ri;
+    cur[2 * NT + t] = rc;
+    cur[3 * NT + t] = rd;
+    __syncthreads();
+    int ph = 2;
 #pragma unroll 1
     for (int s = 1; s < NT; s <<= 1) {
-      T* nxt = SEP + ph * 4 * NT;
-      const T a0 = cur[t], b0 = cur[NT + t], c0 = cur[2 * NT + t], d0 = cur[3 * NT + t];
-      T nb = b0, nd = d0, na = T(0), nc = T(0);
+      T nb = rb, nd = rd, na = T(0), nc = T(0);
       if (t >= s) {
-        const T al = Div<T>(cur[NT + t - s]).div(a0);
+        const T al = ra * cur[NT + t - s];
         nb = fma(-al, cur[2 * NT + t - s], nb);
         nd = fma(-al, cur[3 * NT + t - s], nd);
         na = -al * cur[t - s];
       }
       if (t + s < NT) {
-        const T gm = Div<T>(cur[NT + t + s]).div(c0);
+        const T gm = rc * cur[NT + t + s];
         nb = fma(-gm, cur[t + s], nb);
         nd = fma(-gm, cur[3 * NT + t + s], nd);
         nc = -gm * cur[2 * NT + t + s];
       }
-      nxt[t] = na;
-      nxt[NT + t] = nb;
-      nxt[2 * NT + t] = nc;
-      nxt[3 * NT + t] = nd;
-      cur = nxt;
-      ph = 3 - ph;
-      __syncthreads();
+      ra = na;
+      rb = nb;
+      rc = nc;
+      rd = nd;
+      ri = Div<T>(rb).inv();
+      if (2 * s < NT) {  // (after the last step every row stands alone)
+        T* nxt = SEP + ph * 4 * NT;
+        nxt[t] = ra;
+        nxt[NT + t] = ri;
+        nxt[2 * NT + t] = rc;
+        nxt[3 * NT + t] = rd;
+        cur = nxt;
+        ph = 3 - ph;
+        __syncthreads();
+      }
     }
-    FST[t] = Div<T>(cur[NT + t]).div(cur[3 * NT + t]);  // FST is free again: separator values
+    FST[t] = rd * ri;  // FST is free again: separator values
   }
   __syncthreads();
   // ... accepted when its normwise backward error on the separator system is
@@ -728,7 +746,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   MagT xmax = magh(st);
   T x_last;
   {
-    T x1 = (fma(-cw, st, fma(-V(mi - 1), sp, D(mi - 1)))) * inv_last;
+    T x1 = (fma(-cw, st, fma(-C(mi - 1), sp, D(mi - 1)))) * inv_last;
     T x2 = T(0);
     D(mi - 1) = x1;
     xmax = max(xmax, magh(x1));
@@ -736,18 +754,19 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     x_last = x1;
     // software-pipelined: row i-1's factors are loaded while row i is solved
     int j = mi - 2 >= 0 ? mi - 2 : 0;
-    T qv = V(j), qd = D(j), qb = B(j), qa = A(j), qc = C(j);
+    T qz = C(j), qd = D(j), qb = B(j), qa = A(j);
     for (int i = mi - 2; i >= 0; --i) {
-      const T vi = qv, di = qd, bi = qb, ai = qa, u2 = qc;
+      const T zi = qz, di = qd, bi = qb, ai = qa;
       j = i > 0 ? i - 1 : 0;
-      qv = V(j);
+      qz = C(j);
       qd = D(j);
       qb = B(j);
       qa = A(j);
-      qc = C(j);
-      T r = fma(-vi, sp, di);
+      // z_i multiplies x_{i+2} (swap) or the previous separator (no swap)
+      const T zx = (swm >> i) & 1ull ? x2 : sp;
+      T r = fma(-zi, zx, di);
       if (i == mi - 2) r = fma(-w_prev, st, r);
-      const T xi = fma(-bi, x1, fma(-u2, x2, r)) * ai;  // x_{i+2} term first: two ops depend on x_{i+1}
+      const T xi = fma(-bi, x1, r) * ai;  // one op on x_{i+1}, then the reciprocal
       D(i) = xi;
       xmax = max(xmax, magh(xi));
       bad |= !finite_val(xi);
@@ -870,7 +889,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   }  // passes
 
   if (!accepted) {
-    // restage the system densely (4 arrays of n rows fit in the 6 NT ms
+    // restage the system densely (4 arrays of n rows fit in the 5 NT ms
     // staging elements) and solve it in place by one thread
     T* FA = SA;
     T* FB = FA + n;
@@ -1376,7 +1395,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
 
 template <typename T, int NT>
 static size_t pge_smem_bytes(int ms) {
-  return ((size_t)6 * pge_array_elems<T, NT>(ms) + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
+  return ((size_t)5 * pge_array_elems<T, NT>(ms) + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
 }
 
 constexpr size_t PGE_SMEM_MAX = 227 * 1024 - 128;  // dynamic + the kernels' few static bytes

@@ -268,3 +268,29 @@ def test_gtsv_packed_adjoint_refused(cuda, dt):
     fn = lib.tridiag_gtsv_adjoint_double if dt == np.float64 else lib.tridiag_gtsv_adjoint_single
     st = fn(1, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ptr, ctypes.c_size_t(1 << 20), 8, 4, None)
     assert st == ERR_NOT_SUPPORTED
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,batch", [(96, 100), (100, 37), (257, 129), (1000, 500), (4096, 256), (2049, 4096),
+                                     (64, 8000), (513, 20000)])
+def test_thomas_interleaved_partitioned(cuda, dt, n, batch):
+    """Out-of-place Thomas on interleaved systems: the partitioned sweep
+    (several partitions per system, separators by one thread per system).
+    Against the oracle's sequential Thomas (the reference's algorithm,
+    Tridiagonal_AVX512/tridiagonal_basic.cpp:6-27): per system
+    max|x - x_oracle| / max|x_oracle| <= 1e-12 (FP64) / 2e-5 (FP32), backward
+    error <= 1e-12 / 1e-6, inputs untouched."""
+    import tridiagonalsolver_gb300 as T
+
+    a, b, c, d = inputs.dominant(n, batch, seed=7 * n + batch)
+    ts = _dev(cuda, (a, b, c, d), dt, "interleaved")
+    x_t = T.solve_out(*ts, n, algo="thomas", layout="interleaved")
+    cuda.cuda.synchronize()
+    x = _host(x_t, "interleaved", batch, n)
+    for t, v in zip(ts, (a, b, c, d)):
+        np.testing.assert_array_equal(_host(t, "interleaved", batch, n), v.astype(dt).astype(np.float64))
+    a_, b_, c_, d_ = (v.astype(dt).astype(np.float64) for v in (a, b, c, d))
+    _, worst = O.backward_error(a_, b_, c_, d_, x, n)
+    assert worst <= ETA[dt]
+    xo = O.thomas(a_, b_, c_, d_, n).reshape(batch, n)
+    assert np.max(_rel(x, xo)) <= (1e-12 if dt == np.float64 else 2e-5)

@@ -1,6 +1,7 @@
 // C ABI of libtridiag.so: argument checking, workspace carving, dispatch to
 // the kernel launchers, and the per-thread status of the last call.
 // Declarations and contracts: include/tridiagonal.h.
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <cuda_runtime.h>
@@ -218,9 +219,14 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
 // Out-of-place solve: a, b, c, d untouched, x receives the solution.  The
 // on-chip algorithms need no workspace; the sweeps that spill (Thomas) copy
 // d into x and use `work` for the c' spill.
+// Interleaved Thomas runs the partitioned sweep (ipt.cu), whose factors need
+// two n x batch arrays and the partitions' end relations.
 template <typename T>
-size_t solve_out_ws(int algo, int n, int batch) {
-  if (algo == TRIDIAG_ALGO_THOMAS) return align_up((size_t)n * (size_t)batch * sizeof(T));
+size_t solve_out_ws(int algo, int n, int batch, int layout = TRIDIAG_LAYOUT_CONTIGUOUS) {
+  if (algo == TRIDIAG_ALGO_THOMAS) {
+    const size_t w = align_up((size_t)n * (size_t)batch * sizeof(T));
+    return layout == TRIDIAG_LAYOUT_INTERLEAVED ? std::max(w, tdg::ipt_workspace_bytes<T>(n, batch)) : w;
+  }
   if (algo == TRIDIAG_ALGO_GTSV) return gtsv_ws_bytes<T>(n, batch);
   return 0;
 }
@@ -235,7 +241,7 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
                ? TRIDIAG_ALGO_PARTITION
                : TRIDIAG_ALGO_WM;
   if (work_bytes < solve_out_ws<T>(algo, n, batch) || (solve_out_ws<T>(algo, n, batch) && !work))
-    return TRIDIAG_ERR_WORKSPACE;
+    return TRIDIAG_ERR_WORKSPACE;  // (the interleaved Thomas sweep falls back when given less than it wants)
   switch (algo) {
     case TRIDIAG_ALGO_PARTITION: {
       bool used = false;
@@ -264,6 +270,13 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
     }
       // fall through: shapes beyond the on-chip kernel use the Thomas sweep
     case TRIDIAG_ALGO_THOMAS: {
+      if (layout == TRIDIAG_LAYOUT_INTERLEAVED) {
+        // partitioned sweep: every SM sub-partition busy for a few thousand systems
+        bool used = false;
+        const cudaError_t e = tdg::launch_ipt<T>(a, b, c, d, x, n, batch, work, work_bytes, s, &used);
+        if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+        if (used) return TRIDIAG_SUCCESS;
+      }
       T* cs = static_cast<T*>(work);
       size_t bytes = (size_t)n * (size_t)batch * sizeof(T);
       if (cudaMemcpyAsync(cs, c, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
@@ -499,12 +512,11 @@ int tridiag_solve_double(int algo, int layout, double* a, double* b, double* c, 
 }
 
 size_t tridiag_solve_out_workspace_size(int precision, int algo, int layout, int n, int batch) {
-  (void)layout;
   if (!valid_dims(n, batch)) return 0;
   if (algo == TRIDIAG_ALGO_AUTO || algo == TRIDIAG_ALGO_WM || algo == TRIDIAG_ALGO_CR || algo == TRIDIAG_ALGO_PCR ||
       algo == TRIDIAG_ALGO_PARTITION)
     algo = TRIDIAG_ALGO_THOMAS;  // possible fallback
-  return precision ? solve_out_ws<double>(algo, n, batch) : solve_out_ws<float>(algo, n, batch);
+  return precision ? solve_out_ws<double>(algo, n, batch, layout) : solve_out_ws<float>(algo, n, batch, layout);
 }
 
 int tridiag_solve_out_single(int algo, int layout, const float* a, const float* b, const float* c, const float* d,
@@ -896,7 +908,7 @@ int solve_host_impl(int algo, int layout, const T* a, const T* b, const T* c, co
                               algo == TRIDIAG_ALGO_PCR || algo == TRIDIAG_ALGO_PARTITION
                           ? TRIDIAG_ALGO_THOMAS  // possible fallback
                           : algo;
-  const size_t ws = align_up(solve_out_ws<T>(ws_algo, n, K));
+  const size_t ws = align_up(solve_out_ws<T>(ws_algo, n, K, layout));
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TRIDIAG_ERR_CUDA;
   std::lock_guard<std::mutex> lk(g_pipe_mu);

@@ -210,6 +210,18 @@ cudaError_t launch_residual(int layout, const double* a, const double* b, const 
 cudaError_t launch_update(const double* xold, const float* dx, double* xout, size_t count, cudaStream_t s);
 cudaError_t launch_convert_probe(const double* in, float* out, double* back, size_t count, cudaStream_t s);
 
+// ipt.cu: Thomas for batch-interleaved systems, P partitions per system
+// (top-down first, bottom-up last, spikes in between), the separators by one
+// thread per system, then the back substitution; out of place.  `work` of
+// ipt_workspace_bytes(); *used is false where fewer than three partitions
+// would fill the GPU (the two-ended sweep is as good there) or the workspace
+// is short.
+template <typename T>
+size_t ipt_workspace_bytes(int n, int batch);
+template <typename T>
+cudaError_t launch_ipt(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch, void* work,
+                       size_t work_bytes, cudaStream_t s, bool* used);
+
 // pivot record: one 32-bit word per 32 rows per system
 inline size_t pivot_words(int n, int batch) { return (size_t)((n + 31) / 32) * (size_t)batch; }
 

@@ -58,6 +58,9 @@ PARTS = [
 ]
 
 
+CONFIG = {"workload": WORKLOAD, "parts": [p["name"] for p in PARTS]}  # the same in both arms
+
+
 def _measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -314,16 +317,18 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded U[-1,1] systems, see config)",
-            "config": {"workload": WORKLOAD, "parts": [p["name"] for p in PARTS],
-                       "systems_per_step_per_gpu": systems, "l2": "inputs larger than L2 (1.2 GB per step)",
-                       "timing": "CUDA graph replay of one step, CUDA events on the launching stream",
-                       "parallelism": f"replicas x{world} (independent systems per GPU)"},
+            "config": CONFIG,
+            "run": {"systems_per_step_per_gpu": systems, "l2": "inputs larger than L2 (1.2 GB per step)",
+                    "timing": "CUDA graph replay of one step, CUDA events on the launching stream",
+                    "parallelism": f"replicas x{world} (independent systems per GPU)"},
             "parts": parts_out, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps * len(PARTS),
         }
-        print(json.dumps(line), flush=True)
+    else:
+        line = None
     if world > 1:
         dist.destroy_process_group()
+    return line
 
 
 def max_over_ranks(torch, dist, value: float, device) -> float:
@@ -490,7 +495,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded U[-1,1] systems)",
-        "config": {"workload": WORKLOAD, "parts": [p["name"] for p in PARTS]},
+        "config": CONFIG,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": "; ".join(f"{p['name']}: {s} of {p['batch']} systems per step"
                                              for p, s in zip(PARTS, samples))},
@@ -608,7 +613,7 @@ def _line(args, workload, value, ms_step, dtype, config, parts, roof_bytes, roof
             "data": "synthetic (seeded, distributions of the workload)", "config": dict(config, workload=workload),
             "parts": parts, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def _cpu_sample(fn_sample, total_units, target_s=8.0, start=8):
@@ -669,11 +674,15 @@ def run_thomas_fp64(args):
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                       "sample": f"{k} of {batch} systems in {t:.2f} s (reference Thomas restated)"}
     bytes_ = 5 * n * batch * 8
-    _line(args, "Thomas FP64 n=4096 x 4096, interleaved layout, dominant", batch / (ms * 1e-3), ms, "f64",
-          {"n": n, "batch": batch, "layout": "interleaved", "dominant": "tw_kernel<double, INTERLEAVED, ThomasOp>",
+    return _line(args, "Thomas FP64 n=4096 x 4096, interleaved layout, dominant", batch / (ms * 1e-3), ms, "f64",
+          {"n": n, "batch": batch, "layout": "interleaved",
+           "dominant": "ipt_forward_kernel<double> + ipt_separator_kernel + ipt_back_kernel (partitioned Thomas)",
            "l2": "inputs larger than L2 (537 MB)"},
-          [{"name": "thomas_fp64", "ms_per_launch": ms, "backward_error_max": eta}], bytes_, ms, cpu_b, e2e, clocks,
-          args.steps, note="FP64 pipe bound (two chains per system; ~0.5 Tops/s FP64 per GB300)")
+          [{"name": "thomas_fp64", "ms_per_launch": ms, "systems_per_s": batch / (ms * 1e-3),
+            "algorithmic_bytes": bytes_, "hbm_gbs": round(bytes_ / (ms * 1e-3) / 1e9, 1),
+            "backward_error_max": eta}], bytes_, ms, cpu_b, e2e, clocks,
+          3 * args.steps, note="FP64 issue bound: partitioned Thomas, about 13.4 FP64 instructions per row "
+                               "(7 + 1 in the end partitions, 12 + 2 in the others)")
 
 
 def run_plain(args):
@@ -733,7 +742,7 @@ def run_plain(args):
     rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, batch)
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                       "sample": f"{k} of {batch} systems in {t:.2f} s (reference Thomas restated, FP32)"}
-    _line(args, "plain unpivoted solve FP32 n=4096 x 4096, contiguous, dominant (partition method)",
+    return _line(args, "plain unpivoted solve FP32 n=4096 x 4096, contiguous, dominant (partition method)",
           batch / (ms * 1e-3), ms, "f32",
           {"n": n, "batch": batch, "layout": "contiguous", "dominant": "wmc_kernel<float>",
            "l2": "inputs larger than L2 (268 MB FP32)"},
@@ -820,7 +829,7 @@ def run_adjoint(args):
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                       "sample": f"{k} of {batch} systems forward+adjoint in {t:.2f} s (FP64 port)"}
     bytes14 = 14 * n * batch * 4
-    _line(args, "forward+adjoint FP32 WM-pGE n=1024 x 16384, dominant, loss=sum(w*x)", batch / (ms * 1e-3), ms,
+    return _line(args, "forward+adjoint FP32 WM-pGE n=1024 x 16384, dominant, loss=sum(w*x)", batch / (ms * 1e-3), ms,
           "f32", {"n": n, "batch": batch, "dominant": "wmc_kernel<float,0> forward + wmc_kernel<float,1> adjoint",
                   "algorithm": "partition method without pivoting (forward and transposed)",
                   "l2": "inputs larger than L2 (336 MB)"},
@@ -905,7 +914,7 @@ def run_ragged(args):
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                       "sample": f"{k} random systems of the batch, forward only, one thread, {t:.2f} s"}
     bk = [{"class": cl, "variant": v, "systems": cnt, "max_n": mx} for cl, v, cnt, mx in plan.buckets()]
-    _line(args, "ragged: 100000 systems, n log-uniform [32, 65536], FP32, 20% non-dominant, forward+adjoint",
+    return _line(args, "ragged: 100000 systems, n log-uniform [32, 65536], FP32, 20% non-dominant, forward+adjoint",
           len(sizes) / (ms * 1e-3), ms, "f32",
           {"systems": len(sizes), "rows": rows, "buckets": bk, "autotune_table": {str(k_): v for k_, v in table.items()},
            "autotune_seconds": round(tune_s, 1), "l2": "inputs larger than L2 (13.8 GB)",
@@ -1005,7 +1014,7 @@ def run_refined(args):
         rate, k, t, cores = _cpu_sample(cpu, batch, start=16)
         cpu_b = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                  "sample": f"{k} of {batch} systems, plain FP64 partial pivoting, {t:.2f} s"}
-    _line(args, "refined: FP32 WM-pGE + FP64-residual refinement, n=65536 x 1024, delta sweep",
+    return _line(args, "refined: FP32 WM-pGE + FP64-residual refinement, n=65536 x 1024, delta sweep",
           batch / (ms_main * 1e-3), ms_main, "f32+f64 residual",
           {"n": n, "batch": batch, "iters": 2, "fp32_solver": "partition method (unpivoted), chunked",
            "l2": "inputs larger than L2 (2.1 GB)", "headline_case": "delta=1e-6"},
@@ -1109,7 +1118,7 @@ def run_block2(args):
     # profiles/block2_fp64_n256.md)
     ops_per_row, fp64_peak = 57.0, 503.0
     gops = n * batch * ops_per_row / (ms * 1e-3) / 1e9
-    _line(args, "block tridiagonal (2 x 2 blocks) pivoted FP64, n=512 x 131072, interleaved", batch / (ms * 1e-3), ms,
+    return _line(args, "block tridiagonal (2 x 2 blocks) pivoted FP64, n=512 x 131072, interleaved", batch / (ms * 1e-3), ms,
           "f64", {"n": n, "batch": batch, "layout": "interleaved",
                   "dominant": "block2_pivoted_kernel<double, INTERLEAVED>",
                   "l2": "inputs larger than L2 (3.8 GB FP64)", "timing": "kernel alone, inputs restored between steps"},
@@ -1237,6 +1246,46 @@ def profile_case(name: str) -> None:
     print("ok", name)
 
 
+# The other benchmark configurations, measured after the headline in the
+# default run (one GPU) and reported under "configs" of its line.
+OTHER_CONFIGS = [
+    ("config1_thomas_fp64_interleaved", "thomas-fp64"),
+    ("plain_fp32_fp64_4096x4096", "plain"),
+    ("config3_forward_adjoint", "adjoint"),
+    ("config4_ragged", "ragged"),
+    ("config5_refined", "refined"),
+]
+
+
+def other_configs(args):
+    """Run each other configuration's workload (20 timed steps at most, no
+    CPU leg) and keep the figures of its line: systems/s, step time, HBM
+    fraction of its dominant kernel, worst backward error, its parts, the
+    end-to-end figure and its clocks."""
+    import torch
+
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, min(args.steps, 20))
+    sub.no_cpu = True
+    out = {}
+    for key, wl in OTHER_CONFIGS:
+        torch.cuda.empty_cache()
+        t0 = time.time()
+        try:
+            ln = WORKLOADS[wl](sub)
+        except Exception as exc:  # report, keep the headline
+            out[key] = {"workload": wl, "error": f"{type(exc).__name__}: {exc}"[:300]}
+            continue
+        etas = [p.get("backward_error_max") for p in ln.get("parts", []) if p.get("backward_error_max") is not None]
+        out[key] = {"workload": ln["config"]["workload"], "systems_per_s": ln["value"],
+                    "ms_per_step": ln["ms_per_step"], "dtype": ln["dtype"],
+                    "hbm_frac": ln["roofline"]["frac"], "achieved_gbs": ln["roofline"]["achieved"],
+                    "backward_error_max": max(etas) if etas else None, "parts": ln["parts"],
+                    "roofline": ln["roofline"], "e2e": ln["e2e"], "clocks": ln["clocks"],
+                    "gpu_launches": ln["gpu_launches"], "steps": sub.steps, "wall_s": round(time.time() - t0, 1)}
+    return out
+
+
 WORKLOADS = {"config2": None, "thomas-fp64": run_thomas_fp64, "adjoint": run_adjoint, "ragged": run_ragged,
              "refined": run_refined, "block2": run_block2, "plain": run_plain}
 
@@ -1248,6 +1297,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: measure configuration 2 only (no 'configs' entry)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2",
                     help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
                          "remaining benchmark configurations, one JSON line each")
@@ -1262,9 +1313,13 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif WORKLOADS[args.workload] is None:
-        run_ours(args)
+        line = run_ours(args)
+        if line is not None:
+            if line["n_gpus"] == 1 and not args.headline_only:
+                line["configs"] = other_configs(args)
+            print(json.dumps(line), flush=True)
     else:
-        WORKLOADS[args.workload](args)
+        print(json.dumps(WORKLOADS[args.workload](args)), flush=True)
 
 
 if __name__ == "__main__":

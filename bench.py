@@ -841,10 +841,48 @@ def run_adjoint(args):
           bytes14, ms, cpu_b, e2e, clocks, 2 * args.steps)
 
 
+RAGGED_TABLE = ROOT / "tridiagonalsolver_gb300" / "tuned" / "ragged_fp32_gb300.json"
+
+
+def _ragged_cpu_rate(O, sizes, nondom, target_s=8.0):
+    """The oracle's forward + adjoint (LAPACK-style pivoted solve, FP64
+    adjoint) of sampled systems of the ragged batch, one system per call on
+    all host threads (a thread pool; the oracle releases the GIL).  Returns
+    (systems/s, systems timed, seconds, threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    cores = os.cpu_count() or 1
+    O.set_threads(1)
+
+    def one(s_):
+        n_ = int(sizes[s_])
+        rng = np.random.default_rng(int(s_))
+        aa, cc, dd, ww = (rng.uniform(-1, 1, (1, n_)) for _ in range(4))
+        bb = rng.uniform(-1, 1, (1, n_)) if nondom[s_] else np.abs(aa) + np.abs(cc) + 1.5
+        xx = O.gtsv(aa, bb, cc, dd, n_)
+        O.adjoint_f64(aa, bb, cc, xx, ww, n_)
+
+    k, t = 64, 0.0
+    rng = np.random.default_rng(9)
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        while True:
+            sel = rng.choice(len(sizes), min(k, len(sizes)), replace=False)
+            t0 = time.perf_counter()
+            list(ex.map(one, sel))
+            t = time.perf_counter() - t0
+            if t >= target_s / 4 or k >= len(sizes):
+                break
+            k *= 4
+    O.set_threads(0)
+    return k / t, k, t, cores
+
+
 def run_ragged(args):
     """100000 systems, n log-uniform in [32, 65536], FP32, 20% non-dominant:
-    forward + adjoint through the autotuned size-class plan, the dominant
-    systems marked as needing no pivoting."""
+    forward + adjoint through the size-class plan, the library finding per
+    system (inside the timed step) which systems run without pivoting;
+    variants and chunk width from the committed autotuner table (re-tuned
+    here when it is absent)."""
     import torch
 
     import tridiagonalsolver_gb300 as T
@@ -856,14 +894,18 @@ def run_ragged(args):
     sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
     a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
     w = torch.rand_like(d) * 2 - 1
-    classes = sorted({ragged.size_class(int(v)) for v in sizes})
     t0 = time.time()
-    table, timings = ragged.autotune(classes, dtype=torch.float32, reps=2)
+    if RAGGED_TABLE.exists():
+        table, utab, chunk = ragged.load_table(RAGGED_TABLE, full=True)
+        tuned = f"loaded from {RAGGED_TABLE.relative_to(ROOT)}"
+    else:
+        classes = sorted({ragged.size_class(int(v)) for v in sizes})
+        table, _ = ragged.autotune(classes, dtype=torch.float32, reps=2)
+        utab, chunk, _ = ragged.autotune_unpivoted(classes, dtype=torch.float32, reps=2)
+        tuned = "autotuned in this run"
     tune_s = time.time() - t0
-    # the dominant systems (80%) are marked as needing no pivoting: they run
-    # the unpivoted partition method up to 8192 rows; the rest, and longer
-    # ones, the autotuned pivoted variants
-    plan = T.RaggedPlan(off, table=table, no_pivoting=~nondom)
+    plan = T.RaggedPlan(off, table=table, classify=True, unpivoted_table=utab, chunk_rows=chunk)
+    plan_mask = T.RaggedPlan(off, table=table, no_pivoting=~nondom)
     plan_piv = T.RaggedPlan(off, table=table)
     x = torch.empty_like(d)
     grads = [torch.empty_like(d) for _ in range(4)]
@@ -883,46 +925,48 @@ def run_ragged(args):
     clocks = sampler.stop()
     ms_f, _ = _graph_time(torch, stream, lambda: plan.solve(a, b, c, d, out=x, stream=stream), steps, 3)
 
-    def step_piv():
-        plan_piv.solve(a, b, c, d, out=x, stream=stream)
-        plan_piv.adjoint(a, b, c, x, w, grads=grads, stream=stream)
+    def step_with(p_):
+        def f():
+            p_.solve(a, b, c, d, out=x, stream=stream)
+            p_.adjoint(a, b, c, x, w, grads=grads, stream=stream)
+        return f
 
-    ms_piv, _ = _graph_time(torch, stream, step_piv, 3, 3)
+    ms_piv, _ = _graph_time(torch, stream, step_with(plan_piv), 3, 3)
+    ms_mask, _ = _graph_time(torch, stream, step_with(plan_mask), 3, 3)
     _graph_time(torch, stream, step, 3, 3)  # leave this plan's results in x for the accuracy sample
+    marks = plan.kinds()
+    marks_match = bool(np.array_equal(marks, ~nondom & (sizes > 64)))
     rng = np.random.default_rng(5)
     worst = 0.0
-    for s_ in rng.choice(len(sizes), 16, replace=False):
+    for s_ in list(rng.choice(len(sizes), 16, replace=False)) + list(np.argsort(sizes)[-2:]):
         lo, hi = int(off[s_]), int(off[s_ + 1])
         hs = [t[lo:hi].double().cpu().numpy()[None] for t in (a, b, c, d, x)]
         worst = max(worst, O.backward_error(*hs, hi - lo)[1])
     rows = int(off[-1])
     e2e = _e2e_generic(torch, stream, [a, b, c, d, w], [x] + grads, step, 3, len(sizes))
-
-    def cpu(k):
-        sel = np.random.default_rng(9).choice(len(sizes), k, replace=False)
-        tt = 0.0
-        for s_ in sel:
-            n_ = int(sizes[s_])
-            aa, bb, cc, dd = (np.random.default_rng(int(s_)).uniform(-1, 1, (1, n_)) for _ in range(4))
-            bb = np.abs(aa) + np.abs(cc) + 1.5
-            t1 = time.perf_counter()
-            O.gtsv(aa, bb, cc, dd, n_)
-            tt += time.perf_counter() - t1
-        return tt
-
-    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _cpu_sample(cpu, len(sizes), target_s=4.0, start=64)
-    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-                                      "sample": f"{k} random systems of the batch, forward only, one thread, {t:.2f} s"}
+    rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _ragged_cpu_rate(O, sizes, nondom)
+    cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                      "sample": f"{k} random systems of the batch, forward + adjoint (FP64 port), "
+                                                f"{cores} threads, {t:.2f} s"}
     bk = [{"class": cl, "variant": v, "systems": cnt, "max_n": mx} for cl, v, cnt, mx in plan.buckets()]
     return _line(args, "ragged: 100000 systems, n log-uniform [32, 65536], FP32, 20% non-dominant, forward+adjoint",
-          len(sizes) / (ms * 1e-3), ms, "f32",
-          {"systems": len(sizes), "rows": rows, "buckets": bk, "autotune_table": {str(k_): v for k_, v in table.items()},
-           "autotune_seconds": round(tune_s, 1), "l2": "inputs larger than L2 (13.8 GB)",
-           "timing": "CUDA graph of the whole ragged forward+adjoint (one launch per size class and direction)"},
-          [{"name": "forward", "ms_per_launch": ms_f, "backward_error_max": worst},
-           {"name": "adjoint", "ms_per_launch": ms - ms_f},
-           {"name": "forward+adjoint, every system pivoted", "ms_per_step": ms_piv}],
-          14 * rows * 4 + 16 * len(sizes), ms, cpu_b, e2e, clocks, 2 * steps * len(bk))
+                 len(sizes) / (ms * 1e-3), ms, "f32",
+                 {"systems": len(sizes), "rows": rows, "buckets": bk,
+                  "autotune_table": {str(k_): v for k_, v in table.items()},
+                  "unpivoted_table": {str(k_): v for k_, v in utab.items()}, "chunk_rows": chunk,
+                  "tuning": tuned, "tuning_seconds": round(tune_s, 1), "l2": "inputs larger than L2 (13.8 GB)",
+                  "routing": "found by the library in each solve (strict row dominance checked on the staged rows); "
+                             "the adjoint reuses the forward's marks",
+                  "timing": "CUDA graph of the whole ragged forward+adjoint (device-side resets, one launch per "
+                            "bucket, resident CTAs taking systems through atomic tickets)"},
+                 [{"name": "forward (classification included)", "ms_per_launch": ms_f,
+                   "backward_error_max": worst},
+                  {"name": "adjoint", "ms_per_launch": ms - ms_f},
+                  {"name": "forward+adjoint, every system pivoted", "ms_per_step": ms_piv},
+                  {"name": "forward+adjoint, the generator's dominance passed as a mask", "ms_per_step": ms_mask},
+                  {"name": "library marks", "systems_marked_unpivoted": int(marks.sum()),
+                   "equal_to_generator_dominance": marks_match}],
+                 14 * rows * 4 + 16 * len(sizes), ms, cpu_b, e2e, clocks, 2 * steps * len(bk))
 
 
 def run_refined(args):
@@ -1182,11 +1226,10 @@ def profile_case(name: str) -> None:
         from tridiagonalsolver_gb300 import ragged
 
         sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
-        a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
+        a, b, c, d, off, _ = ragged.synthetic_batch(sizes, seed=2024)
         w = torch.rand_like(d) * 2 - 1
-        classes = sorted({ragged.size_class(int(v)) for v in sizes})
-        table, _ = ragged.autotune(classes, dtype=torch.float32, reps=1)
-        plan = T.RaggedPlan(off, table=table, no_pivoting=~nondom)
+        table, utab, chunk = ragged.load_table(RAGGED_TABLE, full=True) if RAGGED_TABLE.exists() else ({}, {}, 0)
+        plan = T.RaggedPlan(off, table=table, classify=True, unpivoted_table=utab, chunk_rows=chunk)
         x = torch.empty_like(d)
         grads = [torch.empty_like(d) for _ in range(4)]
         s_ = torch.cuda.Stream()

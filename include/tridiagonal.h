@@ -324,9 +324,10 @@ int tridiag_partition_adjoint_double(int layout, const double *a, const double *
  * "default") overrides the choice per class -- the autotuner's output; an
  * entry that cannot serve its class's sizes makes the call return
  * TRIDIAG_ERR_NOT_SUPPORTED.
- * tridiag_ragged_solve_* / _adjoint_* issue one launch per non-empty class
+ * tridiag_ragged_solve_* / _adjoint_* issue one launch per non-empty bucket
  * on the stream (capturable in one CUDA graph); offsets is the device copy of
- * the offsets used to build the plan.  info (may be NULL) per system. */
+ * the offsets used to build the plan.  info (may be NULL) per system.  A plan
+ * is used by one stream at a time (it holds the bucket tickets and kinds). */
 #define TRIDIAG_RAGGED_CLASSES 18
 typedef struct tridiag_ragged_plan tridiag_ragged_plan;
 int tridiag_ragged_plan_create(tridiag_ragged_plan **plan, int precision, const long long *offsets_host, int n_batch,
@@ -342,20 +343,42 @@ int tridiag_ragged_plan_create(tridiag_ragged_plan **plan, int precision, const 
 int tridiag_ragged_plan_create_ex(tridiag_ragged_plan **plan, int precision, const long long *offsets_host,
                                   int n_batch, const int *variant_by_class, int n_classes,
                                   const unsigned char *no_pivoting_host);
+/* As tridiag_ragged_plan_create, with the library deciding which systems
+ * need no pivoting: every tridiag_ragged_solve_* call starts each system of a
+ * size the unpivoted method serves (64 < n <= 262144 FP32 / 65536 FP64) as a
+ * candidate; the unpivoted kernels check the rows they stage for strict
+ * diagonal dominance by rows (|b_i| > |a_i| + |c_i|) and hand a system that
+ * fails, before any arithmetic, to the pivoted bucket of its size class (its
+ * list grows on the device; resident CTAs drain every bucket through an
+ * atomic ticket, so no count returns to the host).  tridiag_ragged_adjoint_*
+ * reuses the marks of the plan's last solve (the same coefficients, as the
+ * pivot record of tridiag_gtsv_adjoint_*; called before any solve it marks
+ * the systems in a pass of its own).  unpivoted_by_class (may be NULL;
+ * entries < 0 = default 7): the variant of the marked systems of each class
+ * up to 4096 (FP32) / 2048 (FP64) rows -- 7, or a partitioned pivoted variant
+ * 1-6; chunk_rows: 128-byte rows per CTA of variant 8 (64, 128 or 256; 0 =
+ * 128) -- both the autotuner's choices. */
+int tridiag_ragged_plan_create_classify(tridiag_ragged_plan **plan, int precision, const long long *offsets_host,
+                                        int n_batch, const int *variant_by_class, const int *unpivoted_by_class,
+                                        int n_classes, int chunk_rows);
+/* The marks (1: solved without pivoting) of the plan's last solve, one byte
+ * per system, into host memory (synchronous); TRIDIAG_ERR_NOT_SUPPORTED for
+ * a plan without marks. */
+int tridiag_ragged_plan_kinds(const tridiag_ragged_plan *plan, unsigned char *kinds_host);
 void tridiag_ragged_plan_destroy(tridiag_ragged_plan *plan);
 /* Buckets of a plan, longest first: 4 ints each (class, variant, systems,
  * largest n); returns the number of buckets. */
 int tridiag_ragged_plan_buckets(const tridiag_ragged_plan *plan, int *out, int max_buckets);
 /* Largest n a variant serves (0: none). */
 int tridiag_ragged_variant_max_n(int precision, int variant);
-int tridiag_ragged_solve_single(const tridiag_ragged_plan *plan, const float *a, const float *b, const float *c,
+int tridiag_ragged_solve_single(tridiag_ragged_plan *plan, const float *a, const float *b, const float *c,
                                 const float *d, float *x, int *info, const long long *offsets, void *stream);
-int tridiag_ragged_solve_double(const tridiag_ragged_plan *plan, const double *a, const double *b, const double *c,
+int tridiag_ragged_solve_double(tridiag_ragged_plan *plan, const double *a, const double *b, const double *c,
                                 const double *d, double *x, int *info, const long long *offsets, void *stream);
-int tridiag_ragged_adjoint_single(const tridiag_ragged_plan *plan, const float *a, const float *b, const float *c,
+int tridiag_ragged_adjoint_single(tridiag_ragged_plan *plan, const float *a, const float *b, const float *c,
                                   const float *x, const float *xbar, float *ga, float *gb, float *gc, float *gd,
                                   int *info, const long long *offsets, void *stream);
-int tridiag_ragged_adjoint_double(const tridiag_ragged_plan *plan, const double *a, const double *b,
+int tridiag_ragged_adjoint_double(tridiag_ragged_plan *plan, const double *a, const double *b,
                                   const double *c, const double *x, const double *xbar, double *ga, double *gb,
                                   double *gc, double *gd, int *info, const long long *offsets, void *stream);
 

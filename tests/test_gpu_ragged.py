@@ -136,24 +136,28 @@ def test_ragged_plan_table_and_autotune(cuda):
         T.RaggedPlan(np.array([0, 30000]), table={15: 1})
 
 
-@pytest.mark.parametrize("mark_dominant", [False, True])
-def test_ragged_full_workload(cuda, mark_dominant):
+@pytest.mark.parametrize("routing", ["pivoted", "caller_mask", "classify"])
+def test_ragged_full_workload(cuda, routing):
     """100000 systems, n log-uniform in [32, 65536] (~8.6e8 rows), FP32, 20%
-    non-dominant: forward and adjoint; 40 sampled systems checked.  With
-    mark_dominant the dominant systems run the unpivoted partition method."""
+    non-dominant: forward and adjoint; 40 sampled systems checked.  Routing:
+    every system pivoted; the dominant systems marked by the caller; or
+    found by the library itself (its marks must equal the generator's)."""
     import tridiagonalsolver_gb300 as T
     from tridiagonalsolver_gb300 import ragged
 
     torch = cuda
     sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
     a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, seed=2024)
-    plan = T.RaggedPlan(off, no_pivoting=~nondom if mark_dominant else None)
+    plan = T.RaggedPlan(off, no_pivoting=~nondom if routing == "caller_mask" else None,
+                        classify=routing == "classify")
     info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
     x = plan.solve(a, b, c, d, info=info)
     w = torch.rand_like(d) * 2 - 1
     ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
     torch.cuda.synchronize()
     assert int((info != 0).sum()) == 0
+    if routing == "classify":
+        np.testing.assert_array_equal(plan.kinds(), ~nondom & (sizes > 64))
     rng = np.random.default_rng(7)
     pick = list(rng.choice(len(sizes), 36, replace=False)) + list(np.argsort(sizes)[-4:])
     for s in pick:
@@ -193,3 +197,147 @@ def test_ragged_unpivoted_buckets(cuda, dtype_name, max_n):
         hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
         grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
         _check_system(hs, grads, n, not nondom[s], ETA[dtype_name], GTOL[dtype_name])
+
+
+def _capable(sizes, dtype_name):
+    """Sizes the unpivoted method serves (64 < n <= 262144 FP32 / 65536 FP64)."""
+    top = 262144 if dtype_name == "float32" else 65536
+    return (sizes > 64) & (sizes <= top)
+
+
+@pytest.mark.parametrize("chunk_rows", [0, 64, 256])
+@pytest.mark.parametrize("dtype_name,max_n", [("float32", 65536), ("float64", 27648)])
+def test_ragged_classified(cuda, dtype_name, max_n, chunk_rows):
+    """The library finds the systems that need no pivoting itself (the
+    unpivoted kernels check the rows they stage and hand the others to the
+    pivoted buckets): its marks equal the generator's truth (strictly
+    dominant rows vs b ~ U[-1, 1]) on every size the unpivoted method serves;
+    forward and adjoint checked per system; the adjoint reuses the marks."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    dt = getattr(torch, dtype_name)
+    sizes = _sizes(max_n)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=dt, nondominant_fraction=0.3, seed=11)
+    plan = T.RaggedPlan(off, dtype=dt, classify=True, chunk_rows=chunk_rows)
+    info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+    x = plan.solve(a, b, c, d, info=info)
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    assert int((info != 0).sum()) == 0
+    np.testing.assert_array_equal(plan.kinds(), ~nondom & _capable(sizes, dtype_name))
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], ETA[dtype_name], GTOL[dtype_name])
+
+
+def test_ragged_classified_adjoint_first(cuda):
+    """An adjoint before any solve of a classifying plan marks the systems in
+    a pass of its own; gradients checked against a plan given the truth."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = _sizes(20000)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, nondominant_fraction=0.3, seed=15)
+    x = T.RaggedPlan(off, no_pivoting=~nondom).solve(a, b, c, d)
+    w = torch.rand_like(d) * 2 - 1
+    plan = T.RaggedPlan(off, classify=True)
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(plan.kinds(), ~nondom & _capable(sizes, "float32"))
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], ETA["float32"], GTOL["float32"])
+
+
+def test_ragged_classified_marks_follow_coefficients(cuda):
+    """A second solve with other coefficients marks the systems again: rows
+    made non-dominant move their systems to the pivoted buckets."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = np.array([100, 700, 3000, 5000, 9000, 200, 40], dtype=np.int64)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, nondominant_fraction=0.0, seed=12)
+    plan = T.RaggedPlan(off, classify=True)
+    plan.solve(a, b, c, d)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(plan.kinds(), sizes > 64)
+    b2 = b.clone()
+    for s in (1, 4):  # one row of systems 1 and 4 no longer dominant
+        r = int(off[s]) + int(sizes[s]) // 2
+        b2[r] = 0.5 * (a[r].abs() + c[r].abs())
+    x2 = plan.solve(a, b2, c, d)
+    torch.cuda.synchronize()
+    expect = sizes > 64
+    expect[[1, 4]] = False
+    np.testing.assert_array_equal(plan.kinds(), expect)
+    for s in range(len(sizes)):
+        hs = [_host(t, off, s) for t in (a, b2, c, d, x2)]
+        _, eta = O.backward_error(*hs, int(sizes[s]))
+        assert eta <= 1e-6
+
+
+def test_ragged_classified_graph_capture(cuda):
+    """The resets, every bucket and the hand-overs in one CUDA graph: two
+    replays give the eager call's bits, forward and adjoint."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = ragged.log_uniform_sizes(2000, 32, 40000, seed=13)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, seed=13)
+    plan = T.RaggedPlan(off, classify=True)
+    x = torch.empty_like(d)
+    w = torch.rand_like(d) * 2 - 1
+    grads = [torch.empty_like(d) for _ in range(4)]
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.solve(a, b, c, d, out=x, stream=s)
+        plan.adjoint(a, b, c, x, w, grads=grads, stream=s)
+    s.synchronize()
+    ref = [x.clone()] + [g.clone() for g in grads]
+    for t in [x] + grads:
+        t.zero_()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        plan.solve(a, b, c, d, out=x, stream=s)
+        plan.adjoint(a, b, c, x, w, grads=grads, stream=s)
+    with torch.cuda.stream(s):
+        g.replay()
+        g.replay()
+    s.synchronize()
+    for got, want in zip([x] + grads, ref):
+        assert torch.equal(got, want)
+
+
+def test_ragged_autotune_unpivoted(cuda):
+    """The unpivoted autotuner: a variant per one-CTA class (7 or a pivoted
+    one that serves the class), a chunk width for the long classes; the plan
+    built from its output solves correctly."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    table, chunk, timings = ragged.autotune_unpivoted([8, 12, 14], rows_per_class=2 ** 20, reps=1)
+    assert set(table) == {8, 12}
+    assert table[8] in (7, 1, 2, 3) and table[12] in (7, 1, 2, 3, 4, 5, 6)
+    assert chunk in (64, 128, 256) and set(timings["chunk_rows"]) == {64, 128, 256}
+    sizes = np.array([150, 3000, 12000, 70], dtype=np.int64)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, nondominant_fraction=0.0, seed=14)
+    plan = T.RaggedPlan(off, classify=True, unpivoted_table=table, chunk_rows=chunk)
+    x = plan.solve(a, b, c, d)
+    torch.cuda.synchronize()
+    for s in range(len(sizes)):
+        hs = [_host(t, off, s) for t in (a, b, c, d, x)]
+        _, eta = O.backward_error(*hs, int(sizes[s]))
+        assert eta <= 1e-6

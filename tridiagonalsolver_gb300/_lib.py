@@ -81,6 +81,8 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_block2_double": (_I, [_I, _I, _P, _P, _P, _P, _P, _I, _I, _P]),
     "tridiag_ragged_plan_create": (_I, [_P, _I, _P, _I, _P, _I]),
     "tridiag_ragged_plan_create_ex": (_I, [_P, _I, _P, _I, _P, _I, _P]),
+    "tridiag_ragged_plan_create_classify": (_I, [_P, _I, _P, _I, _P, _P, _I, _I]),
+    "tridiag_ragged_plan_kinds": (_I, [_P, _P]),
     "tridiag_ragged_plan_destroy": (None, [_P]),
     "tridiag_ragged_plan_buckets": (_I, [_P, _P, _I]),
     "tridiag_ragged_variant_max_n": (_I, [_I, _I]),

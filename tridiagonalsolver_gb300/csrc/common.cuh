@@ -113,6 +113,39 @@ __device__ __forceinline__ bool abs_ge(float x, float y) {
 __device__ __forceinline__ bool is_zero(double x) { return (bits_of(x) << 1) == 0ull; }
 __device__ __forceinline__ bool is_zero(float x) { return (bits_of(x) << 1) == 0u; }
 
+// FP32 bounds of |x| formed on the integer pipe: mag_below(x) <= |x| <=
+// mag_above(x) (FP64: the mantissa truncated to 23 bits, and the next float
+// up; exponents beyond the FP32 range clamp to 0 / FLT_MIN / FLT_MAX / inf
+// the safe way).
+__device__ __forceinline__ float mag_below(float v) { return fabsf(v); }
+__device__ __forceinline__ float mag_above(float v) { return fabsf(v); }
+__device__ __forceinline__ float mag_below(double v) {
+  const unsigned long long u = bits_of(v) & 0x7fffffffffffffffull;
+  const int e = (int)(u >> 52) - 1023 + 127;
+  if (e <= 0) return 0.0f;
+  if (e >= 255) return 3.4028234663852886e38f;
+  return __uint_as_float(((unsigned)e << 23) | (unsigned)((u >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ float mag_above(double v) {
+  const unsigned long long u = bits_of(v) & 0x7fffffffffffffffull;
+  const int e = (int)(u >> 52) - 1023 + 127;
+  if (u == 0ull) return 0.0f;
+  if (e <= 0) return 1.17549435e-38f;
+  if (e >= 255) return __int_as_float(0x7f800000);
+  return __uint_as_float((((unsigned)e << 23) | (unsigned)((u >> 29) & 0x7fffffu)) + 1u);
+}
+
+// Row i strictly diagonally dominant: |b_i| > |a_i| + |c_i| (the caller
+// passes 0 for a_0 and c_{n-1}).  FP32 compares the values themselves; FP64
+// compares the FP32 bounds above with the sum rounded up, so it never
+// accepts a row that is not dominant (and keeps the test off the FP64 pipe).
+template <typename T>
+__device__ __forceinline__ bool dominant_row(T a, T b, T c) {
+  const float off = mag_above(a) + mag_above(c);
+  const float bound = sizeof(T) == 8 ? __uint_as_float(__float_as_uint(off) + 1u) : off;
+  return mag_below(b) > bound;
+}
+
 // ---------------------------------------------------------------------------
 // Streaming memory access with cache hints.  Inputs that are read once go
 // through the read-only path and are marked evict-first; values re-read soon

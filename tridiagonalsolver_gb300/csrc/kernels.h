@@ -5,6 +5,29 @@
 
 namespace tdg {
 
+// A size bucket served by resident CTAs: each takes the next list entry
+// from *ticket (zeroed before the launch) while it is below *dcount (the
+// entries a device pass wrote; NULL: the launch's count), and skips the
+// systems s with kinds[s] != want (kinds NULL: none skipped).
+struct BucketTicket {
+  int* ticket = nullptr;
+  const int* dcount = nullptr;
+  const unsigned char* kinds = nullptr;
+  int want = 0;
+};
+// Ragged forward solves by the unpivoted method that check the rows they
+// stage: a system with a row that is not strictly diagonally dominant is
+// not solved there but handed to the pivoted bucket of its size class --
+// kinds[s] = 0, and s appended once (claim[s]) to the class's kind-0 list
+// (region reg[2 k], length kcount[2 k] of klists).
+struct RaggedCheck {
+  unsigned char* kinds = nullptr;
+  int* claim = nullptr;
+  const int* reg = nullptr;
+  int* kcount = nullptr;
+  int* klists = nullptr;
+};
+
 // seq.cu: one thread per system
 template <typename T>
 cudaError_t launch_thomas_seq(int layout, T* a, T* b, T* c, T* d, int n, int batch, cudaStream_t s);
@@ -77,6 +100,7 @@ constexpr int WML_CHUNK_R = 128;
 // (cl_li, cl_ch) of 256 128-byte rows.
 struct WmlRagged {
   int L = 0, C = 0, Pmax = 0;
+  int R = WML_CHUNK_R;  // 128-byte rows per chunk CTA (64, 128 or 256)
   long long P = 0;
   const int* l_sys = nullptr;
   const long long* roff = nullptr;
@@ -85,14 +109,22 @@ struct WmlRagged {
 };
 template <typename T>
 size_t wml_ragged_workspace_elems(long long total_partitions);
+// kinds (may be NULL): the long systems s with kinds[s] != 1 are skipped
+// (a pivoted bucket serves them); chk (forward solves, may be NULL): the
+// chunks check the rows they stage (RaggedCheck).
 template <typename T>
 cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
                               T* o2, T* o3, const long long* offsets, const WmlRagged& lr, T* work, int* info,
-                              cudaStream_t s);
+                              cudaStream_t s, const unsigned char* kinds = nullptr,
+                              const RaggedCheck* chk = nullptr);
+// tk (may be NULL): skip systems by kind; with a ticket, resident CTAs drain
+// the bucket.  kind_map: the kinds index of launch system j (NULL: j).
+// chk: as for launch_wml_ragged (mode 0).
 template <typename T>
 cudaError_t launch_wmc_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
                               T* o2, T* o3, const long long* offsets, const int* list, int count, int Rmax, int* info,
-                              cudaStream_t s);
+                              cudaStream_t s, const BucketTicket* tk = nullptr, const int* kind_map = nullptr,
+                              const RaggedCheck* chk = nullptr);
 template <typename T>
 cudaError_t launch_wmc(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                        cudaStream_t s, bool* used);
@@ -168,10 +200,11 @@ int pge_variant_mmax(int v);
 // packed arrays (system s = rows [offsets[s], offsets[s+1])), variant v, shared
 // memory for m_max rows per partition; mode 0 solves, mode 1 is the adjoint
 // (d = xbar, x = lambda, gradients to ga/gb/gc, xf = forward solution).
+// With tk (ticket set): resident CTAs (clusters) drain the bucket.
 template <typename T>
 cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, const T* c, const T* d, T* x,
                               const T* xf, T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
-                              int count, int m_max, cudaStream_t s);
+                              int count, int m_max, cudaStream_t s, const BucketTicket* tk = nullptr);
 
 // periodic.cu: Sherman-Morrison pieces of the periodic solve (contiguous).
 template <typename T>

@@ -30,6 +30,7 @@
 // (Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884, without pivoting there);
 // the pivoting is that of its MKL row (Tridiagonal_AVX512/
 // tridiagonal_basic.cpp:131-143).
+#include <algorithm>
 #include <cooperative_groups.h>
 #include <cstdint>
 
@@ -259,6 +260,16 @@ struct PgeIO {
   T* carry;      // [batch][nchunks][4]: Y, V, W of partition 0's first row, c of the last separator row
   const T* xsep;  // [batch][nchunks NT]: the separators (MODE 3)
   int* flag;     // [batch]: MODE 3 sets 1 where a separator row misses its bound
+  // size buckets of a ragged batch served by resident CTAs (clusters): each
+  // takes the next entry of list[0 .. count) -- count from *dcount where a
+  // device pass wrote the list -- from the ticket counter (zero before the
+  // launch) until none is left, and skips the systems s with kinds[s] !=
+  // want (kinds NULL: serves every entry)
+  int* ticket;
+  int count;
+  const int* dcount;
+  const unsigned char* kinds;
+  int want;
 };
 
 // Tensor maps of the TMA-staged FP64 kernel (pge_kernel with SWZ): a, b, c,
@@ -356,22 +367,22 @@ __host__ __device__ constexpr int pge_array_elems(int ms) {
 }
 
 template <typename T, int NT, int MODE, int LAY>
-__global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
+__device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps, const int bid, uint64_t* s_bar) {
   constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
   int ch = 0;                       // chunk of a long system (MODE 2 / 3)
   bool zero_a0 = true, zero_cl = true;  // this CTA holds the system's first / last row
   if constexpr (MODE >= 2) {
-    sys = blockIdx.x / io.nchunks;
-    ch = blockIdx.x % io.nchunks;
+    sys = bid / io.nchunks;
+    ch = bid % io.nchunks;
     base = (size_t)sys * io.stride + (size_t)ch * io.chunk_rows;
     n = min(io.chunk_rows, io.n - ch * io.chunk_rows);
     m = ms = io.chunk_rows / NT;  // odd (the launch's choice)
     zero_a0 = ch == 0;
     zero_cl = ch == io.nchunks - 1;
   } else {
-    pge_system(io, blockIdx.x, NT, sys, base, n, m, ms);
+    pge_system(io, bid, NT, sys, base, n, m, ms);
   }
   if constexpr (LAY == PGE_SWZ) ms = PGE_SWZ_M;  // (the launch guarantees n = NT * 32)
   if constexpr (LAY == PGE_DENSE) m |= 1;        // odd partitions (ms = m)
@@ -381,7 +392,6 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   const T* gd = io.d;
   int* info = io.info;
   auto off = [&](int p, int i) { return pge_off<NT, LAY>(p, i, m); };
-  __shared__ __align__(8) uint64_t s_bar[2];
   extern __shared__ __align__(16) unsigned char pge_smem[];
   unsigned char* sm = pge_smem;
   if constexpr (LAY == PGE_SWZ) sm += (1024u - (smem_u32(pge_smem) & 1023u)) & 1023u;  // 128-byte swizzle: 1 KB aligned
@@ -483,8 +493,8 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   }
   // One CTA per SM fits: the CTA that runs here next (about one wave later)
   // finds its system in L2 instead of HBM.
-  if (io.pf_ahead > 0 && t == 0 && (int)blockIdx.x + io.pf_ahead < (int)gridDim.x) {
-    const size_t nb = (size_t)(blockIdx.x + io.pf_ahead) * io.stride;
+  if (io.pf_ahead > 0 && t == 0 && bid + io.pf_ahead < (int)gridDim.x) {
+    const size_t nb = (size_t)(bid + io.pf_ahead) * io.stride;
     const unsigned bytes = (unsigned)((size_t)n * sizeof(T)) & ~15u;
     const T* arr[4] = {ga, gb, gc, gd};
 #pragma unroll
@@ -944,6 +954,40 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
   }
 }
 
+// The next entry of a ticket-driven bucket (the same for every thread of the
+// CTA), or -1 when the bucket is exhausted or a device error was recorded.
+template <typename T>
+__device__ __forceinline__ int pge_next_item(const PgeIO<T>& io, int* s_item) {
+  if (threadIdx.x == 0) {
+    const int k = atomicAdd(io.ticket, 1);
+    const int cnt = io.dcount ? *(volatile const int*)io.dcount : io.count;
+    *s_item = k < cnt && (!io.err || *(volatile int*)io.err == 0) ? k : -1;
+  }
+  __syncthreads();
+  const int k = *s_item;
+  __syncthreads();  // (read by all before thread 0 writes the next one)
+  return k;
+}
+
+template <typename T, int NT, int MODE, int LAY>
+__global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
+  __shared__ __align__(8) uint64_t s_bar[2];
+  if constexpr (LAY == PGE_DENSE && MODE <= 1) {
+    if (io.ticket) {
+      // resident CTAs drain one size bucket of a ragged batch
+      __shared__ int s_item;
+      for (int k = pge_next_item(io, &s_item); k >= 0; k = pge_next_item(io, &s_item)) {
+        if (io.kinds && io.kinds[io.list[k]] != io.want) continue;
+        pge_body<T, NT, MODE, LAY>(io, maps, k, s_bar);
+        __syncthreads();
+        if (threadIdx.x == 0) mbar_inval(&s_bar[0]);  // re-armed by the next system
+      }
+      return;
+    }
+  }
+  pge_body<T, NT, MODE, LAY>(io, maps, blockIdx.x, s_bar);
+}
+
 // ---------------------------------------------------------------------------
 // Cluster version for systems longer than one CTA's shared memory: a cluster
 // of CL CTAs holds one system, CTA r the rows [r NT m, (r+1) NT m), so the
@@ -968,7 +1012,7 @@ struct PgcLayout {
 };
 
 template <typename T, int NT, int CL, int MODE>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(const PgeIO<T> io) {
+__device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint64_t* s_barp) {
   namespace cg = cooperative_groups;
   using Lay = PgcLayout<T, NT, CL>;
   constexpr int R = Lay::R;
@@ -977,7 +1021,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
-  pge_system(io, blockIdx.x / CL, R, sys, base, n, m, ms);
+  pge_system(io, bid, R, sys, base, n, m, ms);
   // dense layout (as pge_kernel's PGE_DENSE): odd partitions, this CTA's
   // rows in order, each staged array shifted by its rows' 16-byte phase
   // (the same in every CTA: a CTA's rows span a multiple of 16 bytes)
@@ -1047,7 +1091,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   // row n-1 of c stay out of the bulk ranges (zero, and outside the arrays
   // for the adjoint's shifted pointers)
   const int hi = max(0, min(rows, n - row0));
-  __shared__ __align__(8) uint64_t s_bar;
+  uint64_t& s_bar = *s_barp;
   {
     T* const Sk[4] = {SA, SB, SC, SD};
     const T* const Gk[4] = {ga, gb, gc, gd};
@@ -1393,6 +1437,36 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
   cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
 
+// TICKET: resident clusters drain one size bucket of a ragged batch (CTA 0
+// of the cluster takes the ticket, the others read it through distributed
+// shared memory); a separate instance, so the one-cluster-per-system kernel
+// keeps its register allocation.
+template <typename T, int NT, int CL, int MODE, bool TICKET = false>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(const PgeIO<T> io) {
+  __shared__ __align__(8) uint64_t s_bar;
+  if constexpr (!TICKET) {
+    pgc_body<T, NT, CL, MODE>(io, blockIdx.x / CL, &s_bar);
+  } else {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ int s_item;
+    for (;;) {
+      if (cluster.block_rank() == 0 && threadIdx.x == 0) {
+        const int k = atomicAdd(io.ticket, 1);
+        const int cnt = io.dcount ? *(volatile const int*)io.dcount : io.count;
+        s_item = k < cnt && (!io.err || *(volatile int*)io.err == 0) ? k : -1;
+      }
+      cluster.sync();
+      const int k = *cluster.map_shared_rank(&s_item, 0);
+      cluster.sync();  // (read by all before CTA 0 writes the next one)
+      if (k < 0) break;
+      if (io.kinds && io.kinds[io.list[k]] != io.want) continue;
+      pgc_body<T, NT, CL, MODE>(io, k, &s_bar);  // (ends with a cluster barrier)
+      if (threadIdx.x == 0) mbar_inval(&s_bar);   // re-armed by the next system
+    }
+  }
+}
+
 template <typename T, int NT>
 static size_t pge_smem_bytes(int ms) {
   return ((size_t)5 * pge_array_elems<T, NT>(ms) + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
@@ -1460,6 +1534,15 @@ static cudaError_t pge_launch_k(const PgeIO<T>& io_in, const PgeMaps& maps, int 
         per > 0 && grid > sms * per)
       io.pf_ahead = sms * per;
   }
+  if (io.ticket) {
+    // a ticket-driven bucket: as many CTAs as stay resident at once
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE, LAY>, NT, smem) == cudaSuccess &&
+        per > 0)
+      grid = std::min(grid, sms * per);
+  }
   pge_kernel<T, NT, MODE, LAY><<<grid, NT, smem, s>>>(io, maps);
   return cudaGetLastError();
 }
@@ -1491,6 +1574,22 @@ static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int m_max, cudaSt
 template <typename T, int NT, int CL, int MODE>
 static cudaError_t pgc_launch(const PgeIO<T>& io, int grid, int ms, cudaStream_t s) {
   const size_t smem = pgc_smem_bytes<T, NT, CL>(ms);
+  if (io.ticket) {
+    // a ticket-driven bucket: as many clusters as stay resident at once
+    cudaError_t e = cudaFuncSetAttribute(pgc_kernel<T, NT, CL, MODE, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid * CL);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, pgc_kernel<T, NT, CL, MODE, true>, &cfg) == cudaSuccess && ncl > 0)
+      grid = std::min(grid, ncl);
+    pgc_kernel<T, NT, CL, MODE, true><<<(unsigned)grid * CL, NT, smem, s>>>(io);
+    return cudaGetLastError();
+  }
   cudaError_t e =
       cudaFuncSetAttribute(pgc_kernel<T, NT, CL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1712,9 +1811,17 @@ cudaError_t launch_pge_adjoint(int layout, const T* a, const T* b, const T* c, c
 template <typename T>
 cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, const T* c, const T* d, T* x,
                               const T* xf, T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
-                              int count, int m_max, cudaStream_t s) {
+                              int count, int m_max, cudaStream_t s, const BucketTicket* tk) {
   if (count <= 0) return cudaSuccess;
   PgeIO<T> io{};
+  io.err = error_word();
+  if (tk && tk->ticket) {
+    io.ticket = tk->ticket;
+    io.count = count;
+    io.dcount = tk->dcount;
+    io.kinds = tk->kinds;
+    io.want = tk->want;
+  }
   io.b = b;
   io.d = d;
   io.x = x;
@@ -1770,7 +1877,8 @@ cudaError_t pge_path_counts(unsigned long long* out, bool reset) {
   template cudaError_t launch_pge_adjoint<T>(int, const T*, const T*, const T*, const T*, const T*, T*, T*, T*, T*, \
                                              int*, int, int, cudaStream_t, bool*);                                \
   template cudaError_t launch_pge_ragged<T>(int, int, const T*, const T*, const T*, const T*, T*, const T*, T*, T*, \
-                                            T*, int*, const long long*, const int*, int, int, cudaStream_t);
+                                            T*, int*, const long long*, const int*, int, int, cudaStream_t,       \
+                                            const BucketTicket*);
 INST(float)
 INST(double)
 #undef INST

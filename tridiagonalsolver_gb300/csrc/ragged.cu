@@ -7,13 +7,22 @@
 // solve for n < 65 (variant 0), the partitioned solve with 64/128/256
 // partitions in one CTA (1-3) or in a cluster of 2/4/8 CTAs (4-6).  A
 // variant table (from the autotuner, or the defaults) overrides the choice
-// per class.  Systems the caller marks as needing no pivoting (diagonally
-// dominant ones, say) form buckets of their own that run the unpivoted
-// partition method: one CTA per system up to 128 128-byte rows (variant 7),
-// chunks of that size per CTA with the separators' system in between for
-// longer ones (variant 8), forward and adjoint.  Within a bucket the systems run longest first.  Solving is one
-// launch per non-empty bucket on the caller's stream, so the whole ragged
-// solve can be captured in one CUDA graph and replayed.
+// per class.  Systems that need no pivoting -- marked by the caller, or
+// found by the library itself -- run the unpivoted partition method in
+// buckets of their own: one CTA per system up to 128 128-byte rows (variant
+// 7), chunks per CTA with the separators' system in between for longer ones
+// (variant 8), forward and adjoint.  When the library finds them, each
+// solve starts every system of a size the unpivoted method serves as a
+// candidate; the unpivoted kernels check the rows they stage (strict
+// diagonal dominance) and hand a system that fails to the pivoted bucket of
+// its class -- appended to that bucket's list on the device -- before any
+// arithmetic, so the classification costs no pass of its own.  A bucket
+// whose list a device pass writes, and every bucket of one kind, is served
+// by resident CTAs (clusters) that take entries through an atomic ticket.
+// Within a class the unpivoted bucket runs before the pivoted one.  Solving
+// is a few device-side resets and one launch per non-empty bucket on the
+// caller's stream, so the whole ragged solve can be captured in one CUDA
+// graph and replayed.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -104,12 +113,16 @@ static cudaError_t launch_tiny(int mode, const T* a, const T* b, const T* c, con
 struct tridiag_ragged_plan {
   struct Bucket {
     int cls;      // size class
-    int variant;  // 0 tiny, 1-6 partitioned, 7 unpivoted partition method
-    int count;    // systems
+    int variant;  // 0 tiny, 1-6 partitioned, 7 unpivoted partition method, 8 its chunked form
+    int count;    // systems (list entries; for kind 0 the room, the length being on the device)
     int m_max;    // rows per partition of the longest system
     int max_n;
     long long rows;
     size_t list_off;  // into d_lists
+    int kind;         // -1: every system of the class; 0 / 1: the class's systems of that kind
+    int ticket;       // -1: one CTA (cluster) per list entry; else index of its ticket counter
+    int klist;        // -1: list in d_lists; else 2 k + kind: the kind list in d_klists
+    size_t klist_off;
   };
   int precision = 0;
   int batch = 0;
@@ -117,11 +130,32 @@ struct tridiag_ragged_plan {
   std::vector<Bucket> buckets;
   int* d_lists = nullptr;
   int device = 0;
-  // long systems marked as needing no pivoting (variant 8): chunk lists and
-  // the partition workspace, one device allocation
+  // long systems for the unpivoted chunked method (variant 8): chunk lists
+  // and the partition workspace, one device allocation
   tdg::WmlRagged lr;
   void* d_lr = nullptr;
   void* lr_work = nullptr;
+  // kinds of the systems (1: solved without pivoting): the caller's mask
+  // (mode 1), or found by every solve (mode 2: the unpivoted kernels check
+  // the rows they stage and hand the systems that need pivoting over)
+  int kinds_mode = 0;  // 0 none, 1 caller's mask, 2 found by the solves
+  unsigned char* d_kinds = nullptr;
+  bool classified = false;
+  int* d_tickets = nullptr;
+  int n_tickets = 0;
+  int unp_max = 0, long_max = 0;  // rows served by variants 7 and 8
+  // per class and kind, the list of the class's systems of that kind: its
+  // region in d_klists (d_reg[2 k + kind], -1: none) and its length
+  // d_kcount[2 k + kind]
+  int* d_klists = nullptr;
+  int* d_kcount = nullptr;
+  int* d_reg = nullptr;
+  // mode 2: the state each forward solve starts from -- every candidate of
+  // kind 1 (d_kinds0), the lists' initial lengths (d_kcount0) -- and per
+  // system whether a chunk has handed it over (d_claim)
+  unsigned char* d_kinds0 = nullptr;
+  int* d_kcount0 = nullptr;
+  int* d_claim = nullptr;
 };
 
 namespace {
@@ -142,9 +176,15 @@ int unpivoted_max_n() {
 
 // long unpivoted systems: beyond one CTA, their separators' system within one
 template <typename T>
-bool long_unpivoted_ok(long long n) {
+long long long_unpivoted_max_n() {
   constexpr int M = 128 / (int)sizeof(T);
-  return n > unpivoted_max_n<T>() && (n + M - 1) / M <= (long long)tdg::WMC_GEN_MAX_ROWS * M;
+  return (long long)tdg::WMC_GEN_MAX_ROWS * M * M;
+}
+
+// sizes the unpivoted method serves (variant 7 up to unpivoted_max_n, 8 beyond)
+template <typename T>
+bool unpivoted_capable(long long n) {
+  return n > tdg::RAGGED_TINY_MAX && n <= long_unpivoted_max_n<T>();
 }
 
 template <typename T>
@@ -154,72 +194,179 @@ bool variant_serves(int v, int max_n) {
   return max_n >= 65 && max_n <= tdg::pge_variant_max_n<T>(v);
 }
 
-// no_pivoting (may be NULL): systems marked 1 need no pivoting and run the
-// unpivoted partition method (variant 7) where their class allows it.
+void free_plan(tridiag_ragged_plan* plan) {
+  if (!plan) return;
+  cudaFree(plan->d_kinds0);
+  cudaFree(plan->d_kcount0);
+  cudaFree(plan->d_claim);
+  cudaFree(plan->d_klists);
+  cudaFree(plan->d_kcount);
+  cudaFree(plan->d_reg);
+  cudaFree(plan->d_lists);
+  cudaFree(plan->d_lr);
+  cudaFree(plan->lr_work);
+  cudaFree(plan->d_kinds);
+  cudaFree(plan->d_tickets);
+  delete plan;
+}
+
+// The kinds in a pass of their own (an adjoint called before any solve of a
+// mode-2 plan): one warp per system, grid-stride; a candidate (cand[s]) whose
+// rows are all strictly dominant keeps kind 1, the others get kind 0 and go
+// to their class's kind-0 list.
+template <typename T>
+__global__ void __launch_bounds__(256) ragged_classify_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                              const T* __restrict__ c,
+                                                              const long long* __restrict__ offsets, int batch,
+                                                              unsigned char* kinds,
+                                                              const unsigned char* __restrict__ cand,
+                                                              const int* __restrict__ reg, int* kcount, int* klists) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (int)(gridDim.x * blockDim.x / 32);
+  constexpr int U = 4;
+  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += warps) {
+    const long long base = offsets[s];
+    const long long n = offsets[s + 1] - base;
+    bool ok = cand[s] != 0;
+    if (ok) {
+      for (long long i0 = 0; i0 < n && ok; i0 += 32 * U) {
+        T av[U], bv[U], cv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const long long i = i0 + u * 32 + lane;
+          av[u] = i > 0 && i < n ? __ldcs(a + base + i) : T(0);
+          bv[u] = i < n ? __ldcs(b + base + i) : T(1);
+          cv[u] = i < n - 1 ? __ldcs(c + base + i) : T(0);
+        }
+        bool lane_ok = true;
+#pragma unroll
+        for (int u = 0; u < U; ++u) lane_ok &= tdg::dominant_row(av[u], bv[u], cv[u]);
+        ok = __all_sync(0xffffffffu, lane_ok);
+      }
+    }
+    if (lane == 0) {
+      kinds[s] = ok ? 1 : 0;
+      if (cand[s] && !ok) {
+        int cls = 0;
+        while ((1ll << cls) < n) ++cls;
+        const int r = reg[2 * cls];
+        if (r >= 0) klists[r + atomicAdd(&kcount[2 * cls], 1)] = s;
+      }
+    }
+  }
+}
+
+// mode: 0 every system pivoted; 1 the caller's host mask (1: needs no
+// pivoting); 2 found by each solve.  unp_table (may be NULL, per class, < 0 =
+// default): the variant of the kind-1 systems of a class the one-CTA
+// unpivoted method serves (7, or a pivoted variant 1-6); chunk_r: 128-byte
+// rows per CTA of variant 8 (0 = default).
 template <typename T>
 int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, const int* table, int table_len,
-                const unsigned char* no_pivoting = nullptr) {
-  if (!out || !offsets || batch <= 0) return TRIDIAG_ERR_INVALID_VALUE;
+                int mode, const unsigned char* mask, const int* unp_table, int chunk_r) {
+  if (!out || !offsets || batch <= 0 || mode < 0 || mode > 2 || (mode == 1 && !mask)) return TRIDIAG_ERR_INVALID_VALUE;
+  if (chunk_r == 0) chunk_r = tdg::WML_CHUNK_R;
+  if (chunk_r != 64 && chunk_r != 128 && chunk_r != 256) return TRIDIAG_ERR_INVALID_VALUE;
   *out = nullptr;
-  // classes 0 .. CLASSES-1 pivoted, CLASSES .. 2 CLASSES-1 unpivoted; long
-  // unpivoted systems apart
-  std::vector<std::vector<int>> by_class(2 * TRIDIAG_RAGGED_CLASSES);
-  std::vector<int> longs;
+  std::vector<std::vector<int>> by_class(TRIDIAG_RAGGED_CLASSES);
   for (int s = 0; s < batch; ++s) {
     const long long n = offsets[s + 1] - offsets[s];
     if (n < 1 || n > (1ll << (TRIDIAG_RAGGED_CLASSES - 1))) return TRIDIAG_ERR_INVALID_VALUE;
-    const bool unp = no_pivoting && no_pivoting[s] && n <= unpivoted_max_n<T>();
-    if (no_pivoting && no_pivoting[s] && !unp && long_unpivoted_ok<T>(n)) {
-      longs.push_back(s);
-      continue;
-    }
-    by_class[size_class(n) + (unp ? TRIDIAG_RAGGED_CLASSES : 0)].push_back(s);
+    by_class[size_class(n)].push_back(s);
   }
   auto* plan = new (std::nothrow) tridiag_ragged_plan;
   if (!plan) return TRIDIAG_ERR_WORKSPACE;
   plan->precision = sizeof(T) == 8 ? 1 : 0;
   plan->batch = batch;
   plan->total_rows = offsets[batch] - offsets[0];
+  plan->kinds_mode = mode;
+  plan->unp_max = unpivoted_max_n<T>();
+  plan->long_max = (int)long_unpivoted_max_n<T>();
   cudaGetDevice(&plan->device);
+  constexpr int M = 128 / (int)sizeof(T);
   std::vector<int> lists;
-  for (int kk = 0; kk < 2 * TRIDIAG_RAGGED_CLASSES; ++kk) {
-    auto& sys = by_class[kk];
+  std::vector<int> longs;   // systems for variant 8
+  std::vector<int> klists;  // the kind lists (kind 0 with room for the whole class)
+  std::vector<int> reg(2 * TRIDIAG_RAGGED_CLASSES, -1), kcount(2 * TRIDIAG_RAGGED_CLASSES, 0);
+  auto len = [&](int q) { return offsets[q + 1] - offsets[q]; };
+  auto candidate = [&](int q) { return mode != 0 && unpivoted_capable<T>(len(q)) && (mode != 1 || mask[q]); };
+  for (int k = 0; k < TRIDIAG_RAGGED_CLASSES; ++k) {
+    auto& sys = by_class[k];
     if (sys.empty()) continue;
-    const bool unp = kk >= TRIDIAG_RAGGED_CLASSES;
-    const int k = kk % TRIDIAG_RAGGED_CLASSES;
-    std::sort(sys.begin(), sys.end(), [&](int p, int q) {
-      const long long np = offsets[p + 1] - offsets[p], nq = offsets[q + 1] - offsets[q];
-      return np != nq ? np > nq : p < q;
-    });
-    const int max_n = (int)(offsets[sys[0] + 1] - offsets[sys[0]]);
-    int v = unp ? RAGGED_UNPIVOTED : -1;
-    if (!unp && table && k < table_len && table[k] >= 0) {
+    std::sort(sys.begin(), sys.end(), [&](int p, int q) { return len(p) != len(q) ? len(p) > len(q) : p < q; });
+    const int max_n = (int)len(sys[0]);
+    std::vector<int> cand, rest;
+    for (int q : sys) (candidate(q) ? cand : rest).push_back(q);
+    const bool capable = !cand.empty();
+    int v = -1;
+    if (table && k < table_len && table[k] >= 0) {
       if (!variant_serves<T>(table[k], max_n)) {  // an explicit choice that cannot serve the class
-        delete plan;
+        free_plan(plan);
         return TRIDIAG_ERR_NOT_SUPPORTED;
       }
       v = table[k];
     }
     if (v < 0) v = max_n <= tdg::RAGGED_TINY_MAX ? 0 : tdg::pge_default_variant<T>(max_n);
     if (v < 0 || (v == 0 && max_n > tdg::RAGGED_TINY_MAX) || (v > 0 && !variant_serves<T>(v, max_n))) {
-      delete plan;
+      free_plan(plan);
       return TRIDIAG_ERR_NOT_SUPPORTED;
     }
-    tridiag_ragged_plan::Bucket bk;
-    bk.cls = k;
-    bk.variant = v;
-    bk.count = (int)sys.size();
-    bk.max_n = max_n;
-    constexpr int M = 128 / (int)sizeof(T);
-    bk.m_max = v == 0                  ? 0
-               : v == RAGGED_UNPIVOTED ? (max_n + M - 1) / M  // 128-byte rows of the longest system
-                                       : std::max(2, (max_n + tdg::pge_variant_partitions(v) - 1) /
-                                                         tdg::pge_variant_partitions(v));
-    bk.rows = 0;
-    for (int q : sys) bk.rows += offsets[q + 1] - offsets[q];
-    bk.list_off = lists.size();
+    const bool one_cta_unp = max_n <= unpivoted_max_n<T>();
+    int vu = RAGGED_UNPIVOTED;
+    if (capable && one_cta_unp && unp_table && k < table_len && unp_table[k] >= 0) {
+      if (unp_table[k] != RAGGED_UNPIVOTED &&
+          (unp_table[k] < 1 || unp_table[k] > 6 || !variant_serves<T>(unp_table[k], max_n))) {
+        free_plan(plan);
+        return TRIDIAG_ERR_NOT_SUPPORTED;
+      }
+      vu = unp_table[k];
+    }
+    const size_t list_off = lists.size();
     lists.insert(lists.end(), sys.begin(), sys.end());
-    plan->buckets.push_back(bk);
+    long long rows = 0;
+    for (int q : sys) rows += len(q);
+    if (capable) {
+      // kind 1 (one-CTA classes): the candidates, a fixed list, which each
+      // solve checks (mode 2) -- the ones that need pivoting are handed to
+      // kind 0.  Kind 0: room for the whole class; its initial entries are
+      // the systems without an unpivoted alternative (or the mask's 0s).
+      if (one_cta_unp) {
+        reg[2 * k + 1] = (int)klists.size();
+        klists.insert(klists.end(), cand.begin(), cand.end());
+        kcount[2 * k + 1] = (int)cand.size();
+      } else {
+        longs.insert(longs.end(), cand.begin(), cand.end());
+      }
+      reg[2 * k] = (int)klists.size();
+      klists.insert(klists.end(), rest.begin(), rest.end());
+      kcount[2 * k] = (int)rest.size();
+      klists.resize(reg[2 * k] + sys.size(), -1);
+    }
+    auto add = [&](int variant, int kind, int count) {
+      tridiag_ragged_plan::Bucket bk;
+      bk.cls = k;
+      bk.variant = variant;
+      bk.count = count;
+      bk.max_n = max_n;
+      bk.m_max = variant == 0                  ? 0
+                 : variant == RAGGED_UNPIVOTED ? (max_n + M - 1) / M  // 128-byte rows of the longest system
+                                               : std::max(2, (max_n + tdg::pge_variant_partitions(variant) - 1) /
+                                                                 tdg::pge_variant_partitions(variant));
+      bk.rows = rows;
+      bk.list_off = list_off;
+      bk.kind = kind;
+      bk.ticket = kind >= 0 && variant != 0 ? plan->n_tickets++ : -1;
+      bk.klist = kind >= 0 ? 2 * k + kind : -1;
+      bk.klist_off = kind >= 0 ? (size_t)reg[2 * k + kind] : 0;
+      plan->buckets.push_back(bk);
+    };
+    if (!capable) {
+      add(v, -1, (int)sys.size());
+      continue;
+    }
+    // within a class the unpivoted bucket runs first: its checks fill the pivoted one
+    if (one_cta_unp) add(vu, 1, (int)cand.size());
+    add(v, 0, (int)sys.size());
   }
   // longest buckets first: their few, long launches start before the short ones fill the GPU
   std::stable_sort(plan->buckets.begin(), plan->buckets.end(),
@@ -227,18 +374,14 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
                      return p.cls > q.cls;
                    });
   if (!longs.empty()) {
-    constexpr int M = 128 / (int)sizeof(T);
-    const long long chunk_rows = (long long)tdg::WML_CHUNK_R * M;
-    std::sort(longs.begin(), longs.end(), [&](int p, int q) {
-      const long long np = offsets[p + 1] - offsets[p], nq = offsets[q + 1] - offsets[q];
-      return np != nq ? np > nq : p < q;
-    });
+    const long long chunk_rows = (long long)chunk_r * M;
+    std::sort(longs.begin(), longs.end(), [&](int p, int q) { return len(p) != len(q) ? len(p) > len(q) : p < q; });
     std::vector<long long> roff(longs.size() + 1, 0);
     std::vector<int> cl_li, cl_ch;
     int pmax = 0;
     long long rows = 0;
     for (size_t i = 0; i < longs.size(); ++i) {
-      const long long n = offsets[longs[i] + 1] - offsets[longs[i]];
+      const long long n = len(longs[i]);
       const long long P = (n + M - 1) / M;
       roff[i + 1] = roff[i] + P;
       pmax = std::max(pmax, (int)P);
@@ -252,6 +395,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     plan->lr.C = (int)cl_li.size();
     plan->lr.P = roff.back();
     plan->lr.Pmax = pmax;
+    plan->lr.R = chunk_r;
     const size_t b_lsys = longs.size() * sizeof(int), b_roff = roff.size() * sizeof(long long),
                  b_cl = cl_li.size() * sizeof(int);
     const size_t o_roff = (b_lsys + 255) / 256 * 256, o_li = o_roff + (b_roff + 255) / 256 * 256,
@@ -260,7 +404,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     if (cudaMalloc(&mem, o_end) != cudaSuccess ||
         cudaMalloc(&plan->lr_work, tdg::wml_ragged_workspace_elems<T>(plan->lr.P) * sizeof(T)) != cudaSuccess) {
       cudaFree(mem);
-      delete plan;
+      free_plan(plan);
       return TRIDIAG_ERR_CUDA;
     }
     plan->d_lr = mem;
@@ -273,7 +417,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     plan->lr.cl_li = reinterpret_cast<int*>(mem + o_li);
     plan->lr.cl_ch = reinterpret_cast<int*>(mem + o_ch);
     tridiag_ragged_plan::Bucket bk;
-    const int max_n = (int)(offsets[longs[0] + 1] - offsets[longs[0]]);
+    const int max_n = (int)len(longs[0]);
     bk.cls = size_class(max_n);
     bk.variant = RAGGED_UNPIVOTED_LONG;
     bk.count = (int)longs.size();
@@ -281,47 +425,116 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     bk.m_max = 0;
     bk.rows = rows;
     bk.list_off = 0;
-    plan->buckets.insert(plan->buckets.begin(), bk);  // longest work first
+    bk.kind = 1;
+    bk.ticket = -1;
+    bk.klist = -1;
+    bk.klist_off = 0;
+    plan->buckets.insert(plan->buckets.begin(), bk);  // longest work first (and before the pivoted long buckets)
   }
-  if (cudaMalloc(&plan->d_lists, std::max<size_t>(lists.size(), 1) * sizeof(int)) != cudaSuccess) {
-    cudaFree(plan->d_lr);
-    cudaFree(plan->lr_work);
-    delete plan;
+  if (cudaMalloc(&plan->d_lists, std::max<size_t>(lists.size(), 1) * sizeof(int)) != cudaSuccess ||
+      cudaMemcpy(plan->d_lists, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    free_plan(plan);
     return TRIDIAG_ERR_CUDA;
   }
-  if (cudaMemcpy(plan->d_lists, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
-    cudaFree(plan->d_lists);
-    delete plan;
-    return TRIDIAG_ERR_CUDA;
+  if (mode != 0) {
+    std::vector<unsigned char> kinds(batch, 0);
+    for (int q = 0; q < batch; ++q) kinds[q] = candidate(q) ? 1 : 0;
+    const size_t nk = std::max<size_t>(klists.size(), 1);
+    if (cudaMalloc(&plan->d_kinds, (size_t)batch) != cudaSuccess ||
+        cudaMemcpy(plan->d_kinds, kinds.data(), (size_t)batch, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMalloc(&plan->d_tickets, std::max(plan->n_tickets, 1) * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&plan->d_klists, nk * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(plan->d_klists, klists.data(), klists.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->d_kcount, kcount.size() * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(plan->d_kcount, kcount.data(), kcount.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->d_reg, reg.size() * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(plan->d_reg, reg.data(), reg.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (mode == 2 && (cudaMalloc(&plan->d_kinds0, (size_t)batch) != cudaSuccess ||
+                       cudaMemcpy(plan->d_kinds0, kinds.data(), (size_t)batch, cudaMemcpyHostToDevice) !=
+                           cudaSuccess ||
+                       cudaMalloc(&plan->d_kcount0, kcount.size() * sizeof(int)) != cudaSuccess ||
+                       cudaMemcpy(plan->d_kcount0, kcount.data(), kcount.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice) != cudaSuccess ||
+                       cudaMalloc(&plan->d_claim, (size_t)batch * sizeof(int)) != cudaSuccess))) {
+      free_plan(plan);
+      return TRIDIAG_ERR_CUDA;
+    }
+    plan->classified = mode == 1;
   }
   *out = plan;
   return TRIDIAG_SUCCESS;
 }
 
 template <typename T>
-int plan_run(const tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const T* c, const T* d, T* x,
-             const T* xf, T* ga, T* gb, T* gc, int* info, const long long* offsets, cudaStream_t s) {
+int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const T* c, const T* d, T* x, const T* xf,
+             T* ga, T* gb, T* gc, int* info, const long long* offsets, cudaStream_t s) {
   if (!plan || !a || !b || !c || !d || !x || !offsets) return TRIDIAG_ERR_INVALID_VALUE;
   if (plan->precision != (sizeof(T) == 8 ? 1 : 0)) return TRIDIAG_ERR_INVALID_VALUE;
   if (mode == 1 && (!xf || !ga || !gb || !gc)) return TRIDIAG_ERR_INVALID_VALUE;
+  if (plan->n_tickets > 0 && cudaMemsetAsync(plan->d_tickets, 0, plan->n_tickets * sizeof(int), s) != cudaSuccess)
+    return TRIDIAG_ERR_CUDA;
+  const bool check = plan->kinds_mode == 2 && mode == 0;
+  if (plan->kinds_mode == 2) {
+    // every solve starts from the candidates; its unpivoted kernels hand the
+    // systems that need pivoting over as they stage them.  (An adjoint with
+    // no solve before it sorts the systems in a pass of its own.)
+    if (check || !plan->classified) {
+      const size_t nk = 2 * TRIDIAG_RAGGED_CLASSES * sizeof(int);
+      if (cudaMemcpyAsync(plan->d_kinds, plan->d_kinds0, (size_t)plan->batch, cudaMemcpyDeviceToDevice, s) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(plan->d_kcount, plan->d_kcount0, nk, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+          cudaMemsetAsync(plan->d_claim, 0, (size_t)plan->batch * sizeof(int), s) != cudaSuccess)
+        return TRIDIAG_ERR_CUDA;
+    }
+    if (!check && !plan->classified) {
+      int dev = 0, sms = 152;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int grid = std::min((plan->batch + 7) / 8, sms * 8);
+      ragged_classify_kernel<T><<<grid, 256, 0, s>>>(a, b, c, offsets, plan->batch, plan->d_kinds, plan->d_kinds0,
+                                                     plan->d_reg, plan->d_kcount, plan->d_klists);
+      if (cudaGetLastError() != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    }
+    plan->classified = true;
+  }
+  tdg::RaggedCheck chk;
+  if (check) {
+    chk.kinds = plan->d_kinds;
+    chk.claim = plan->d_claim;
+    chk.reg = plan->d_reg;
+    chk.kcount = plan->d_kcount;
+    chk.klists = plan->d_klists;
+  }
   for (const auto& bk : plan->buckets) {
-    const int* list = plan->d_lists + bk.list_off;
+    // a bucket of one kind runs through that kind's list of its class
+    const int* list = bk.klist >= 0 ? plan->d_klists + bk.klist_off : plan->d_lists + bk.list_off;
+    tdg::BucketTicket tk;
+    tk.ticket = bk.ticket >= 0 ? plan->d_tickets + bk.ticket : nullptr;
+    // kind 0: the list's length on the device (grown by the checks); kind 1:
+    // the fixed candidates, of which the adjoint skips those handed over
+    tk.dcount = bk.kind == 0 ? plan->d_kcount + bk.klist : nullptr;
+    tk.kinds = bk.kind == 1 && !check && plan->kinds_mode == 2 ? plan->d_kinds : nullptr;
+    tk.want = bk.kind;
+    const tdg::BucketTicket* tkp = bk.kind >= 0 ? &tk : nullptr;
     cudaError_t e;
     if (bk.variant == RAGGED_UNPIVOTED_LONG)
       e = mode == 0 ? tdg::launch_wml_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets,
-                                                plan->lr, static_cast<T*>(plan->lr_work), info, s)
+                                                plan->lr, static_cast<T*>(plan->lr_work), info, s, plan->d_kinds,
+                                                check ? &chk : nullptr)
                     : tdg::launch_wml_ragged<T>(1, a, b, c, d, xf, x, ga, gb, gc, offsets, plan->lr,
-                                                static_cast<T*>(plan->lr_work), info, s);
+                                                static_cast<T*>(plan->lr_work), info, s, plan->d_kinds);
     else if (bk.variant == 0)
       e = tdg::launch_tiny<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count, s);
     else if (bk.variant == RAGGED_UNPIVOTED)
       e = mode == 0 ? tdg::launch_wmc_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets, list,
-                                                bk.count, bk.m_max, info, s)
+                                                bk.count, bk.m_max, info, s, tkp, nullptr, check ? &chk : nullptr)
                     : tdg::launch_wmc_ragged<T>(1, a, b, c, d, xf, ga, gb, gc, x, offsets, list, bk.count, bk.m_max,
-                                                info, s);
+                                                info, s, tkp);
     else
       e = tdg::launch_pge_ragged<T>(bk.variant, mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
-                                    bk.m_max, s);
+                                    bk.m_max, s, tkp);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
   }
   return TRIDIAG_SUCCESS;
@@ -333,24 +546,38 @@ extern "C" {
 
 int tridiag_ragged_plan_create(tridiag_ragged_plan** plan, int precision, const long long* offsets_host, int batch,
                                const int* variant_by_class, int n_classes) {
-  return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes)
-                   : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes);
+  return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes, 0, nullptr, nullptr, 0)
+                   : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes, 0, nullptr, nullptr, 0);
 }
 
 int tridiag_ragged_plan_create_ex(tridiag_ragged_plan** plan, int precision, const long long* offsets_host,
                                   int batch, const int* variant_by_class, int n_classes,
                                   const unsigned char* no_pivoting_host) {
-  return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes, no_pivoting_host)
-                   : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes, no_pivoting_host);
+  const int mode = no_pivoting_host ? 1 : 0;
+  return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes, mode,
+                                         no_pivoting_host, nullptr, 0)
+                   : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes, mode,
+                                        no_pivoting_host, nullptr, 0);
 }
 
-void tridiag_ragged_plan_destroy(tridiag_ragged_plan* plan) {
-  if (!plan) return;
-  cudaFree(plan->d_lists);
-  cudaFree(plan->d_lr);
-  cudaFree(plan->lr_work);
-  delete plan;
+int tridiag_ragged_plan_create_classify(tridiag_ragged_plan** plan, int precision, const long long* offsets_host,
+                                        int batch, const int* variant_by_class, const int* unpivoted_by_class,
+                                        int n_classes, int chunk_rows) {
+  return precision ? plan_create<double>(plan, offsets_host, batch, variant_by_class, n_classes, 2, nullptr,
+                                         unpivoted_by_class, chunk_rows)
+                   : plan_create<float>(plan, offsets_host, batch, variant_by_class, n_classes, 2, nullptr,
+                                        unpivoted_by_class, chunk_rows);
 }
+
+int tridiag_ragged_plan_kinds(const tridiag_ragged_plan* plan, unsigned char* kinds_host) {
+  if (!plan || !kinds_host) return TRIDIAG_ERR_INVALID_VALUE;
+  if (!plan->d_kinds || !plan->classified) return TRIDIAG_ERR_NOT_SUPPORTED;
+  return cudaMemcpy(kinds_host, plan->d_kinds, (size_t)plan->batch, cudaMemcpyDeviceToHost) == cudaSuccess
+             ? TRIDIAG_SUCCESS
+             : TRIDIAG_ERR_CUDA;
+}
+
+void tridiag_ragged_plan_destroy(tridiag_ragged_plan* plan) { free_plan(plan); }
 
 int tridiag_ragged_plan_buckets(const tridiag_ragged_plan* plan, int* out, int max_buckets) {
   if (!plan) return -1;
@@ -374,22 +601,22 @@ int tridiag_ragged_variant_max_n(int precision, int variant) {
   return precision ? tdg::pge_variant_max_n<double>(variant) : tdg::pge_variant_max_n<float>(variant);
 }
 
-int tridiag_ragged_solve_single(const tridiag_ragged_plan* plan, const float* a, const float* b, const float* c,
+int tridiag_ragged_solve_single(tridiag_ragged_plan* plan, const float* a, const float* b, const float* c,
                                 const float* d, float* x, int* info, const long long* offsets, void* stream) {
   return plan_run<float>(plan, 0, a, b, c, d, x, nullptr, nullptr, nullptr, nullptr, info, offsets,
                          (cudaStream_t)stream);
 }
-int tridiag_ragged_solve_double(const tridiag_ragged_plan* plan, const double* a, const double* b, const double* c,
+int tridiag_ragged_solve_double(tridiag_ragged_plan* plan, const double* a, const double* b, const double* c,
                                 const double* d, double* x, int* info, const long long* offsets, void* stream) {
   return plan_run<double>(plan, 0, a, b, c, d, x, nullptr, nullptr, nullptr, nullptr, info, offsets,
                           (cudaStream_t)stream);
 }
-int tridiag_ragged_adjoint_single(const tridiag_ragged_plan* plan, const float* a, const float* b, const float* c,
+int tridiag_ragged_adjoint_single(tridiag_ragged_plan* plan, const float* a, const float* b, const float* c,
                                   const float* x, const float* xbar, float* ga, float* gb, float* gc, float* gd,
                                   int* info, const long long* offsets, void* stream) {
   return plan_run<float>(plan, 1, a, b, c, xbar, gd, x, ga, gb, gc, info, offsets, (cudaStream_t)stream);
 }
-int tridiag_ragged_adjoint_double(const tridiag_ragged_plan* plan, const double* a, const double* b,
+int tridiag_ragged_adjoint_double(tridiag_ragged_plan* plan, const double* a, const double* b,
                                   const double* c, const double* x, const double* xbar, double* ga, double* gb,
                                   double* gc, double* gd, int* info, const long long* offsets, void* stream) {
   return plan_run<double>(plan, 1, a, b, c, xbar, gd, x, ga, gb, gc, info, offsets, (cudaStream_t)stream);

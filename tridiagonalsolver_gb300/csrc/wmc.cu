@@ -84,6 +84,17 @@ struct WmcGen {
   int* info;  // may be NULL: 0 written per system
   long long stride;
   int n;
+  // ragged size buckets: systems s with kinds[kind_map ? kind_map[s] : s] !=
+  // want are skipped (kinds NULL: none); with a ticket, resident CTAs take
+  // the entries list[0 .. count) in turn (one-CTA solves only; count from
+  // *dcount where a device pass wrote the list)
+  const unsigned char* kinds;
+  const int* kind_map;
+  int want;
+  int* ticket;
+  int count;
+  const int* dcount;
+  RaggedCheck chk;  // (chk.kinds NULL: off) forward solves that check the rows they stage
 };
 
 template <typename T>
@@ -146,10 +157,9 @@ __device__ __forceinline__ T& wmc_elem(unsigned char* S, int t, int k) {
 // GEN: element-wise staging (WmcGen); with TRANS the staged system is A^T
 // (sub-diagonal c_{i-1}, super-diagonal a_{i+1}, read shifted from global
 // memory) and MODE 3 writes lambda and the gradients (x from gen.in[4]).
-template <typename T, int MODE, bool GEN = false, bool TRANS = false>
-__global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
-                                                        int packed, int* err, const WmcChunk<T> ck,
-                                                        const WmcGen<T> gen) {
+template <typename T, int MODE, bool GEN, bool TRANS>
+__device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int packed, int* err, const WmcChunk<T>& ck,
+                                         const WmcGen<T>& gen, const int bid) {
   using W = WmcVec<T>;
   constexpr int NV = W::N;     // values per 16-byte unit
   constexpr int M = 8 * NV;    // rows per thread (128 bytes)
@@ -167,8 +177,8 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
 
   constexpr bool CHUNKED = MODE >= 2;
   static_assert(!TRANS || (GEN && CHUNKED), "transposed staging serves the chunked element-wise path");
-  int j = CHUNKED ? (int)(blockIdx.x / ck.nchunks) : (int)blockIdx.x;
-  int ch = CHUNKED ? (int)(blockIdx.x % ck.nchunks) : 0;
+  int j = CHUNKED ? bid / ck.nchunks : bid;
+  int ch = CHUNKED ? bid % ck.nchunks : 0;
   bool last_chunk = !CHUNKED || ch == ck.nchunks - 1;
   int Rc = CHUNKED && last_chunk ? ck.Rlast : R;  // partitions of this CTA
   int nn = n;                                      // rows of this system
@@ -180,11 +190,11 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   if constexpr (GEN) {
     int li = 0;
     if constexpr (CHUNKED) {
-      li = ck.cl_li[blockIdx.x];
-      ch = ck.cl_ch[blockIdx.x];
+      li = ck.cl_li[bid];
+      ch = ck.cl_ch[bid];
       j = ck.l_sys[li];
     } else {
-      j = gen.list ? gen.list[blockIdx.x] : (int)blockIdx.x;
+      j = gen.list ? gen.list[bid] : bid;
     }
     const long long gsys = gen.offsets ? gen.offsets[j] : (long long)j * gen.stride;
     nn = gen.offsets ? (int)(gen.offsets[j + 1] - gsys) : gen.n;
@@ -219,6 +229,30 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
+    if constexpr ((MODE == 0 || MODE == 2) && !TRANS) {
+      if (gen.chk.kinds) {
+        // a system that needs pivoting is not solved here: it goes to the
+        // pivoted bucket of its size class (the staged rows are checked
+        // before any arithmetic; a chunk checks its own rows)
+        bool bad = false;
+        if (active)
+          for (int q = 0; q < M; ++q)
+            if (t * M + q < rows_here)
+              bad |= !dominant_row(wmc_elem<T>(S[0], t, q), wmc_elem<T>(S[1], t, q), wmc_elem<T>(S[2], t, q));
+        if (__syncthreads_or(bad)) {
+          if (t == 0) {
+            gen.chk.kinds[j] = 0;
+            if (!CHUNKED || atomicExch(&gen.chk.claim[j], 1) == 0) {
+              int cls = 0;
+              while ((1ll << cls) < (long long)nn) ++cls;
+              const int r = gen.chk.reg[2 * cls];
+              if (r >= 0) gen.chk.klists[r + atomicAdd(&gen.chk.kcount[2 * cls], 1)] = j;
+            }
+          }
+          return;
+        }
+      }
+    }
   } else {
     if (t == 0) {
       mbar_init(bar, 1);
@@ -516,6 +550,40 @@ __global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ 
   }
 }
 
+template <typename T, int MODE, bool GEN = false, bool TRANS = false>
+__global__ void __launch_bounds__(WMC_MAX_R) wmc_kernel(const __grid_constant__ WmcMaps maps, int n, int R,
+                                                        int packed, int* err, const WmcChunk<T> ck,
+                                                        const WmcGen<T> gen) {
+  if constexpr (GEN) {
+    auto skipped = [&](int j) { return gen.kinds && gen.kinds[gen.kind_map ? gen.kind_map[j] : j] != gen.want; };
+    if constexpr (MODE <= 1) {
+      if (gen.ticket) {
+        // resident CTAs drain one size bucket of a ragged batch
+        __shared__ int s_item;
+        for (;;) {
+          if (threadIdx.x == 0) {
+            const int k = atomicAdd(gen.ticket, 1);
+            const int cnt = gen.dcount ? *(volatile const int*)gen.dcount : gen.count;
+            s_item = k < cnt && (!err || *(volatile int*)err == 0) ? k : -1;
+          }
+          __syncthreads();
+          const int k = s_item;
+          __syncthreads();
+          if (k < 0) break;
+          if (skipped(gen.list ? gen.list[k] : k)) continue;
+          wmc_body<T, MODE, GEN, TRANS>(maps, n, R, packed, err, ck, gen, k);
+          __syncthreads();
+        }
+        return;
+      }
+      if (skipped(gen.list ? gen.list[blockIdx.x] : (int)blockIdx.x)) return;
+    } else {
+      if (skipped(ck.l_sys[ck.cl_li[blockIdx.x]])) return;
+    }
+  }
+  wmc_body<T, MODE, GEN, TRANS>(maps, n, R, packed, err, ck, gen, blockIdx.x);
+}
+
 template <typename T>
 bool wmc_eligible(int layout, int n) {
   constexpr int M = 128 / (int)sizeof(T);
@@ -539,8 +607,19 @@ static cudaError_t wmc_gen_launch(const WmcGen<T>& gen, int count, int Rmax, cud
   cudaError_t e =
       cudaFuncSetAttribute(wmc_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  int grid = count;
+  if (gen.ticket) {
+    // a ticket-driven bucket: as many CTAs as stay resident at once
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, wmc_kernel<T, MODE, true>, threads, smem) ==
+            cudaSuccess &&
+        per > 0)
+      grid = count < sms * per ? count : sms * per;
+  }
   WmcMaps maps{};
-  wmc_kernel<T, MODE, true><<<count, threads, smem, s>>>(maps, 0, Rmax, 0, error_word(), WmcChunk<T>{}, gen);
+  wmc_kernel<T, MODE, true><<<grid, threads, smem, s>>>(maps, 0, Rmax, 0, error_word(), WmcChunk<T>{}, gen);
   return cudaGetLastError();
 }
 
@@ -760,10 +839,19 @@ template cudaError_t launch_wml<double>(const double*, const double*, const doub
 template <typename T>
 cudaError_t launch_wmc_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
                               T* o2, T* o3, const long long* offsets, const int* list, int count, int Rmax, int* info,
-                              cudaStream_t s) {
+                              cudaStream_t s, const BucketTicket* tk, const int* kind_map, const RaggedCheck* chk) {
   if (count <= 0) return cudaSuccess;
   if (Rmax < 1 || Rmax > WMC_MAX_R) return cudaErrorInvalidValue;
   WmcGen<T> gen{};
+  if (tk) {
+    gen.ticket = tk->ticket;
+    gen.count = count;
+    gen.dcount = tk->dcount;
+    gen.kinds = tk->kinds;
+    gen.want = tk->want;
+    gen.kind_map = kind_map;
+  }
+  if (chk && mode == 0) gen.chk = *chk;
   gen.in[0] = a;
   gen.in[1] = b;
   gen.in[2] = c;
@@ -815,10 +903,10 @@ size_t wml_ragged_workspace_elems(long long total_partitions) {
 template <typename T>
 cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, const T* d, const T* xf, T* o0, T* o1,
                               T* o2, T* o3, const long long* offsets, const WmlRagged& lr, T* work, int* info,
-                              cudaStream_t s) {
+                              cudaStream_t s, const unsigned char* kinds, const RaggedCheck* chk) {
   if (lr.L <= 0) return cudaSuccess;
   constexpr int M = 128 / (int)sizeof(T);
-  const int R = WML_CHUNK_R;
+  const int R = lr.R;
   T* rel = work;
   T* ra = rel + (size_t)WMC_REL * lr.P;
   T* rb = ra + lr.P;
@@ -844,6 +932,10 @@ cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, cons
   gen.out[1] = o1;
   gen.out[2] = o2;
   gen.out[3] = o3;
+  gen.kinds = kinds;  // (systems marked for pivoting are skipped)
+  gen.want = 1;
+  WmcGen<T> gen2 = gen;  // MODE 2 of a forward solve checks the rows it stages
+  if (chk && mode == 0) gen2.chk = *chk;
   const size_t smem = wmc_smem_bytes<T>(R, R, 4);
   WmcMaps maps{};
   cudaError_t e;
@@ -858,7 +950,7 @@ cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, cons
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wmc_kernel<T, 3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    wmc_kernel<T, 2, true, false><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen);
+    wmc_kernel<T, 2, true, false><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen2);
   }
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
@@ -866,8 +958,11 @@ cudaError_t launch_wml_ragged(int mode, const T* a, const T* b, const T* c, cons
   const long long blocks = (lr.P + 255) / 256;
   const unsigned ag = (unsigned)(blocks < (long long)sms * 8 ? blocks : (long long)sms * 8);
   wml_assemble_ragged<T><<<ag, 256, 0, s>>>(rel, ra, rb, rc, rd, lr.roff, lr.L, lr.P);
+  BucketTicket sk;
+  sk.kinds = kinds;
+  sk.want = 1;
   e = launch_wmc_ragged<T>(0, ra, rb, rc, rd, nullptr, rd, nullptr, nullptr, nullptr, lr.roff, nullptr, lr.L,
-                           (lr.Pmax + M - 1) / M, nullptr, s);
+                           (lr.Pmax + M - 1) / M, nullptr, s, kinds ? &sk : nullptr, lr.l_sys);
   if (e != cudaSuccess) return e;
   if (mode == 1)
     wmc_kernel<T, 3, true, true><<<lr.C, R, smem, s>>>(maps, 0, R, 0, error_word(), ck, gen);
@@ -880,17 +975,21 @@ template size_t wml_ragged_workspace_elems<float>(long long);
 template size_t wml_ragged_workspace_elems<double>(long long);
 template cudaError_t launch_wml_ragged<float>(int, const float*, const float*, const float*, const float*,
                                               const float*, float*, float*, float*, float*, const long long*,
-                                              const WmlRagged&, float*, int*, cudaStream_t);
+                                              const WmlRagged&, float*, int*, cudaStream_t,
+                                              const unsigned char*, const RaggedCheck*);
 template cudaError_t launch_wml_ragged<double>(int, const double*, const double*, const double*, const double*,
                                                const double*, double*, double*, double*, double*, const long long*,
-                                               const WmlRagged&, double*, int*, cudaStream_t);
+                                               const WmlRagged&, double*, int*, cudaStream_t,
+                                               const unsigned char*, const RaggedCheck*);
 
 template cudaError_t launch_wmc_ragged<float>(int, const float*, const float*, const float*, const float*,
                                               const float*, float*, float*, float*, float*, const long long*,
-                                              const int*, int, int, int*, cudaStream_t);
+                                              const int*, int, int, int*, cudaStream_t, const BucketTicket*,
+                                              const int*, const RaggedCheck*);
 template cudaError_t launch_wmc_ragged<double>(int, const double*, const double*, const double*, const double*,
                                                const double*, double*, double*, double*, double*, const long long*,
-                                               const int*, int, int, int*, cudaStream_t);
+                                               const int*, int, int, int*, cudaStream_t, const BucketTicket*,
+                                               const int*, const RaggedCheck*);
 template bool wmc_gen_eligible<float>(int, int);
 template bool wmc_gen_eligible<double>(int, int);
 template bool wmc_eligible<float>(int, int);

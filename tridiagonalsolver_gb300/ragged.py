@@ -5,9 +5,14 @@ rows ``offsets[s] .. offsets[s+1]-1`` of the 1-D tensors a, b, c, d.  A
 :class:`RaggedPlan` (built once on the host from the offsets) groups the
 systems into size classes and picks a kernel variant per class; its
 :meth:`~RaggedPlan.solve` and :meth:`~RaggedPlan.adjoint` issue one launch
-per class on the current stream, so the whole call can be captured in one
-CUDA graph.  :func:`autotune` measures the variants on synthetic batches of
-each class and returns the fastest per class (the table a plan takes).
+per bucket on the current stream, so the whole call can be captured in one
+CUDA graph.  With ``classify=True`` the library itself finds, in each solve,
+the systems that need no pivoting (strictly diagonally dominant) and runs
+them by the unpivoted partition method, the others by the pivoted variants.
+:func:`autotune` measures the pivoted variants on synthetic batches of each
+class and returns the fastest per class (the table a plan takes);
+:func:`autotune_unpivoted` does the same for the unpivoted systems' variant
+and the chunk width of long ones.
 """
 from __future__ import annotations
 
@@ -47,9 +52,13 @@ class RaggedPlan:
     host or device; ``table`` maps size class -> variant (None: defaults);
     ``no_pivoting`` (bool per system, optional) marks systems that need no
     pivoting (diagonally dominant, say), which then run the unpivoted
-    partition method where their size allows."""
+    partition method where their size allows; ``classify=True`` lets each
+    solve find those systems itself (``unpivoted_table``: class -> variant of
+    the unpivoted systems, ``chunk_rows``: 128-byte rows per CTA of long
+    ones; the adjoint reuses the marks of the last solve)."""
 
-    def __init__(self, offsets, dtype=torch.float32, table: dict | None = None, device=None, no_pivoting=None):
+    def __init__(self, offsets, dtype=torch.float32, table: dict | None = None, device=None, no_pivoting=None,
+                 classify: bool = False, unpivoted_table: dict | None = None, chunk_rows: int = 0):
         L = _sig()
         off = offsets.detach().cpu().numpy() if isinstance(offsets, torch.Tensor) else np.asarray(offsets)
         off = np.ascontiguousarray(off, dtype=np.int64)
@@ -61,7 +70,16 @@ class RaggedPlan:
             tab[int(k)] = int(v)
         self._tab = tab
         h = _P()
-        if no_pivoting is None:
+        if classify:
+            if no_pivoting is not None:
+                raise ValueError("classify and no_pivoting exclude each other")
+            utab = np.full(CLASSES, -1, dtype=np.int32)
+            for k, v in (unpivoted_table or {}).items():
+                utab[int(k)] = int(v)
+            st = L.tridiag_ragged_plan_create_classify(ctypes.addressof(h), self.precision, off.ctypes.data,
+                                                       self.batch, tab.ctypes.data, utab.ctypes.data, CLASSES,
+                                                       int(chunk_rows))
+        elif no_pivoting is None:
             st = L.tridiag_ragged_plan_create(ctypes.addressof(h), self.precision, off.ctypes.data, self.batch,
                                               tab.ctypes.data, CLASSES)
         else:
@@ -76,11 +94,19 @@ class RaggedPlan:
         self.offsets = torch.from_numpy(off).to(dev)
         self.rows = int(off[-1] - off[0])
 
+    def kinds(self):
+        """Per system: True where the last solve ran it without pivoting
+        (synchronous)."""
+        out = np.zeros(self.batch, dtype=np.uint8)
+        check(_sig().tridiag_ragged_plan_kinds(self._h, out.ctypes.data), "tridiag_ragged_plan_kinds")
+        return out.astype(bool)
+
     def buckets(self):
-        """[(class, variant, systems, largest n)], longest class first."""
+        """[(class, variant, systems, largest n)], longest class first (for a
+        bucket of one kind, systems = the room of its list)."""
         L = _sig()
-        out = np.zeros(4 * 2 * CLASSES, dtype=np.int32)  # pivoted and unpivoted buckets per class
-        nb = min(L.tridiag_ragged_plan_buckets(self._h, out.ctypes.data, 2 * CLASSES), 2 * CLASSES)
+        out = np.zeros(4 * 3 * CLASSES, dtype=np.int32)  # pivoted and unpivoted buckets per class
+        nb = min(L.tridiag_ragged_plan_buckets(self._h, out.ctypes.data, 3 * CLASSES), 3 * CLASSES)
         return [tuple(int(v) for v in out[4 * i:4 * i + 4]) for i in range(nb)]
 
     def solve(self, a, b, c, d, out=None, info=None, stream=None):
@@ -204,17 +230,103 @@ def autotune(classes, dtype=torch.float32, systems_per_class=None, rows_per_clas
     return table, timings
 
 
-def save_table(path, table, dtype=torch.float32, timings=None):
+def autotune_unpivoted(classes, dtype=torch.float32, rows_per_class=2 ** 24, seed=0, reps=3, verbose=False):
+    """For the systems that need no pivoting: per size class up to the
+    one-CTA limit, time variant 7 against the partitioned pivoted variants
+    that serve the class; for the longer classes, time the chunk widths 64 /
+    128 / 256 (128-byte rows per CTA) of variant 8.  Synthetic batches of
+    dominant systems, sizes log-uniform inside each class, through classified
+    plans.  Returns ({class: variant}, chunk_rows, timings)."""
+    precision = 1 if dtype == torch.float64 else 0
+    unp_max = variant_max_n(precision, 7)
+    table, timings = {}, {}
+    long_classes = []
+    for k in classes:
+        lo, hi = max(2 ** (k - 1) + 1, 2), 2 ** k
+        if hi <= 64:
+            continue
+        if hi > unp_max:
+            long_classes.append(k)
+            continue
+        count = max(64, min(20000, rows_per_class // hi))
+        sizes = log_uniform_sizes(count, lo, hi, seed=seed + k)
+        a, b, c, d, off, _ = synthetic_batch(sizes, dtype=dtype, nondominant_fraction=0.0, seed=seed + k)
+        x = torch.empty_like(d)
+        res = {}
+        for v in [7] + [v for v in range(1, 7) if variant_max_n(precision, v) >= hi]:
+            plan = RaggedPlan(off, dtype=dtype, classify=True, unpivoted_table={k: v})
+            res[v] = _time(lambda: plan.solve(a, b, c, d, out=x), reps)
+            del plan
+        table[k] = min(res, key=res.get)
+        timings[k] = res
+        if verbose:
+            print(f"class {k:2d} (n <= {hi:6d}, unpivoted): " +
+                  ", ".join(f"v{v} {t:.3f} ms" for v, t in sorted(res.items())) + f" -> v{table[k]}")
+        del a, b, c, d, x
+    chunk = 0
+    if long_classes:
+        sizes = np.concatenate([log_uniform_sizes(max(16, min(4000, rows_per_class // 2 ** k)), 2 ** (k - 1) + 1,
+                                                  2 ** k, seed=seed + k) for k in long_classes])
+        a, b, c, d, off, _ = synthetic_batch(sizes, dtype=dtype, nondominant_fraction=0.0, seed=seed + 99)
+        x = torch.empty_like(d)
+        res = {}
+        for r in (64, 128, 256):
+            plan = RaggedPlan(off, dtype=dtype, classify=True, chunk_rows=r)
+            res[r] = _time(lambda: plan.solve(a, b, c, d, out=x), reps)
+            del plan
+        chunk = min(res, key=res.get)
+        timings["chunk_rows"] = res
+        if verbose:
+            print("long unpivoted classes " + str(long_classes) + ": " +
+                  ", ".join(f"{r} rows {t:.3f} ms" for r, t in sorted(res.items())) + f" -> {chunk}")
+        del a, b, c, d, x
+    return table, chunk, timings
+
+
+def save_table(path, table, dtype=torch.float32, timings=None, unpivoted=None, chunk_rows=0):
+    """Persist the autotuner's choices (and timings) as JSON."""
     doc = {"device": torch.cuda.get_device_name(), "dtype": str(dtype).replace("torch.", ""),
            "table": {str(k): int(v) for k, v in table.items()},
-           "timings_ms": {str(k): {str(v): t for v, t in r.items()} for k, r in (timings or {}).items()}}
+           "unpivoted": {str(k): int(v) for k, v in (unpivoted or {}).items()}, "chunk_rows": int(chunk_rows),
+           "timings_ms": {str(k): ({str(v): t for v, t in r.items()} if isinstance(r, dict) else r)
+                          for k, r in (timings or {}).items()}}
     Path(path).write_text(json.dumps(doc, indent=1))
 
 
-def load_table(path):
+def load_table(path, full: bool = False):
+    """The table saved by :func:`save_table` ({class: variant}); with
+    full=True also the unpivoted table and chunk width."""
     doc = json.loads(Path(path).read_text())
-    return {int(k): int(v) for k, v in doc["table"].items()}
+    table = {int(k): int(v) for k, v in doc["table"].items()}
+    if not full:
+        return table
+    return table, {int(k): int(v) for k, v in doc.get("unpivoted", {}).items()}, int(doc.get("chunk_rows", 0))
 
 
-__all__ = ["RaggedPlan", "autotune", "candidates", "load_table", "log_uniform_sizes", "save_table",
+__all__ = ["RaggedPlan", "autotune", "autotune_unpivoted", "candidates", "load_table", "log_uniform_sizes", "save_table",
            "synthetic_batch", "size_class", "variant_max_n", "TridiagError", "CLASSES", "VARIANTS"]
+
+
+def _main() -> None:
+    """python -m tridiagonalsolver_gb300.ragged --tune PATH: autotune the
+    pivoted variants, the unpivoted variants and the chunk width over the
+    size classes of the log-uniform [32, 65536] workload on this GPU and save
+    the table (load it with load_table(PATH, full=True))."""
+    import argparse
+
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--tune", required=True, help="output JSON path")
+    ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--reps", type=int, default=3)
+    args = ap.parse_args()
+    dt = getattr(torch, args.dtype)
+    classes = sorted({size_class(int(v)) for v in log_uniform_sizes(100000, 32, 65536, seed=2024)})
+    table, timings = autotune(classes, dtype=dt, reps=args.reps, verbose=True)
+    utab, chunk, ut = autotune_unpivoted(classes, dtype=dt, reps=args.reps, verbose=True)
+    timings.update({f"unpivoted_{k}": v for k, v in ut.items()})
+    save_table(args.tune, table, dtype=dt, timings=timings, unpivoted=utab, chunk_rows=chunk)
+    print("saved", args.tune)
+
+
+if __name__ == "__main__":
+    _main()

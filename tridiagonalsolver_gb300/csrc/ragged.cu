@@ -290,13 +290,27 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   std::vector<int> reg(2 * TRIDIAG_RAGGED_CLASSES, -1), kcount(2 * TRIDIAG_RAGGED_CLASSES, 0);
   auto len = [&](int q) { return offsets[q + 1] - offsets[q]; };
   auto candidate = [&](int q) { return mode != 0 && unpivoted_capable<T>(len(q)) && (mode != 1 || mask[q]); };
+  std::vector<unsigned char> kinds(batch, 0);  // (1: a candidate of kind 1)
   for (int k = 0; k < TRIDIAG_RAGGED_CLASSES; ++k) {
     auto& sys = by_class[k];
     if (sys.empty()) continue;
     std::sort(sys.begin(), sys.end(), [&](int p, int q) { return len(p) != len(q) ? len(p) > len(q) : p < q; });
     const int max_n = (int)len(sys[0]);
+    const bool one_cta_unp = max_n <= unpivoted_max_n<T>();
+    int vu = RAGGED_UNPIVOTED;
+    if (mode != 0 && one_cta_unp && unp_table && k < table_len && unp_table[k] >= 0) {
+      if (unp_table[k] != RAGGED_UNPIVOTED &&
+          (unp_table[k] < 1 || unp_table[k] > 6 || !variant_serves<T>(unp_table[k], max_n))) {
+        free_plan(plan);
+        return TRIDIAG_ERR_NOT_SUPPORTED;
+      }
+      vu = unp_table[k];
+    }
+    // a class whose systems that need no pivoting are better served by a
+    // pivoted variant (the autotuner's choice) is one pivoted bucket
     std::vector<int> cand, rest;
-    for (int q : sys) (candidate(q) ? cand : rest).push_back(q);
+    for (int q : sys) (candidate(q) && vu == RAGGED_UNPIVOTED ? cand : rest).push_back(q);
+    for (int q : cand) kinds[q] = 1;
     const bool capable = !cand.empty();
     int v = -1;
     if (table && k < table_len && table[k] >= 0) {
@@ -310,16 +324,6 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     if (v < 0 || (v == 0 && max_n > tdg::RAGGED_TINY_MAX) || (v > 0 && !variant_serves<T>(v, max_n))) {
       free_plan(plan);
       return TRIDIAG_ERR_NOT_SUPPORTED;
-    }
-    const bool one_cta_unp = max_n <= unpivoted_max_n<T>();
-    int vu = RAGGED_UNPIVOTED;
-    if (capable && one_cta_unp && unp_table && k < table_len && unp_table[k] >= 0) {
-      if (unp_table[k] != RAGGED_UNPIVOTED &&
-          (unp_table[k] < 1 || unp_table[k] > 6 || !variant_serves<T>(unp_table[k], max_n))) {
-        free_plan(plan);
-        return TRIDIAG_ERR_NOT_SUPPORTED;
-      }
-      vu = unp_table[k];
     }
     const size_t list_off = lists.size();
     lists.insert(lists.end(), sys.begin(), sys.end());
@@ -355,7 +359,8 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       bk.rows = rows;
       bk.list_off = list_off;
       bk.kind = kind;
-      bk.ticket = kind >= 0 && variant != 0 ? plan->n_tickets++ : -1;
+      // resident CTAs with tickets only where the list grows on the device
+      bk.ticket = kind == 0 && mode == 2 && variant != 0 ? plan->n_tickets++ : -1;
       bk.klist = kind >= 0 ? 2 * k + kind : -1;
       bk.klist_off = kind >= 0 ? (size_t)reg[2 * k + kind] : 0;
       plan->buckets.push_back(bk);
@@ -366,7 +371,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     }
     // within a class the unpivoted bucket runs first: its checks fill the pivoted one
     if (one_cta_unp) add(vu, 1, (int)cand.size());
-    add(v, 0, (int)sys.size());
+    add(v, 0, mode == 2 ? (int)sys.size() : (int)rest.size());
   }
   // longest buckets first: their few, long launches start before the short ones fill the GPU
   std::stable_sort(plan->buckets.begin(), plan->buckets.end(),
@@ -437,8 +442,6 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     return TRIDIAG_ERR_CUDA;
   }
   if (mode != 0) {
-    std::vector<unsigned char> kinds(batch, 0);
-    for (int q = 0; q < batch; ++q) kinds[q] = candidate(q) ? 1 : 0;
     const size_t nk = std::max<size_t>(klists.size(), 1);
     if (cudaMalloc(&plan->d_kinds, (size_t)batch) != cudaSuccess ||
         cudaMemcpy(plan->d_kinds, kinds.data(), (size_t)batch, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -514,7 +517,7 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
     tk.ticket = bk.ticket >= 0 ? plan->d_tickets + bk.ticket : nullptr;
     // kind 0: the list's length on the device (grown by the checks); kind 1:
     // the fixed candidates, of which the adjoint skips those handed over
-    tk.dcount = bk.kind == 0 ? plan->d_kcount + bk.klist : nullptr;
+    tk.dcount = bk.ticket >= 0 ? plan->d_kcount + bk.klist : nullptr;
     tk.kinds = bk.kind == 1 && !check && plan->kinds_mode == 2 ? plan->d_kinds : nullptr;
     tk.want = bk.kind;
     const tdg::BucketTicket* tkp = bk.kind >= 0 ? &tk : nullptr;

@@ -1292,6 +1292,175 @@ def profile_case(name: str) -> None:
     print("ok", name)
 
 
+# ---------------------------------------------------------------------------
+# GPU comparators on the benchmark's shapes: cuSPARSE gtsv2StridedBatch (the
+# reference's vendor row, through its cuSparse_* entry points) and the
+# reference's own CUDA kernels, built from its sources for sm_103a into
+# oracle/_ref (device code only) and launched through the CUDA driver API
+# with the reference's launch configurations (Tridiagonal_CUDA/
+# tridiagonal_wm_pcr.cu:1433-1455, tridiagonal_basic.cu:166-190).
+
+REF_CUBINS = [ROOT / "oracle" / "_ref" / "ref_cuda_wm_pcr.cubin", ROOT / "oracle" / "_ref" / "ref_cuda_basic.cubin"]
+
+
+class RefCudaKernels:
+    """The reference's kernels from the cubins in oracle/_ref: the functions
+    of each module are listed through the driver (cuModuleEnumerateFunctions,
+    cuFuncGetName) and found by their exported names."""
+
+    def __init__(self):
+        import ctypes
+        import re
+
+        self.ct = ctypes
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        P, U = ctypes.c_void_p, ctypes.c_uint
+        self.cu.cuModuleLoad.argtypes = [ctypes.POINTER(P), ctypes.c_char_p]
+        self.cu.cuModuleGetFunctionCount.argtypes = [ctypes.POINTER(U), P]
+        self.cu.cuModuleEnumerateFunctions.argtypes = [ctypes.POINTER(P), U, P]
+        self.cu.cuFuncGetName.argtypes = [ctypes.POINTER(ctypes.c_char_p), P]
+        self.cu.cuLaunchKernel.argtypes = [P, U, U, U, U, U, U, U, P, ctypes.POINTER(P), ctypes.POINTER(P)]
+        self.funcs = {}
+        for path in REF_CUBINS:
+            mod = P()
+            if self.cu.cuModuleLoad(ctypes.byref(mod), str(path).encode()) != 0:
+                raise RuntimeError(f"cuModuleLoad failed for {path.name}")
+            cnt = U()
+            if self.cu.cuModuleGetFunctionCount(ctypes.byref(cnt), mod) != 0:
+                raise RuntimeError("cuModuleGetFunctionCount failed")
+            arr = (P * cnt.value)()
+            if self.cu.cuModuleEnumerateFunctions(arr, cnt, mod) != 0:
+                raise RuntimeError("cuModuleEnumerateFunctions failed")
+            for f in arr:
+                nm = ctypes.c_char_p()
+                if self.cu.cuFuncGetName(ctypes.byref(nm), f) == 0:
+                    m = re.match(r"_Z\d+(\w+?_kernel)I([fd])", nm.value.decode())
+                    if m:  # e.g. WM5_reg_kernel<float, 2> -> ("WM5_reg_kernel", "f")
+                        self.funcs[(m.group(1), m.group(2))] = P(f)
+
+    def launch(self, name, dt, grid, block, ptrs, ints, stream):
+        """One launch: device pointers, then int arguments (the kernels'
+        (T*, ..., int n_eqt, int n_batch) signatures)."""
+        ct = self.ct
+        vals = [ct.c_void_p(v) for v in ptrs] + [ct.c_int(v) for v in ints]
+        params = (ct.c_void_p * len(vals))(*[ct.cast(ct.pointer(v), ct.c_void_p) for v in vals])
+        f = self.funcs[(name, dt)]
+        rc = self.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, 0, ct.c_void_p(stream), params, None)
+        if rc != 0:
+            raise RuntimeError(f"cuLaunchKernel({name}) returned {rc}")
+
+
+def _time_inplace(torch, stream, src, work, fn, reps):
+    """Mean CUDA-event time of fn() over reps calls, the in-place inputs
+    restored from src before each call (outside the timed interval)."""
+    ms = []
+    with torch.cuda.stream(stream):
+        for it in range(reps + 2):
+            for w, s_ in zip(work, src):
+                w.copy_(s_)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            stream.synchronize()
+            if it >= 2:
+                ms.append(e0.elapsed_time(e1))
+    return sum(ms) / len(ms)
+
+
+def comparators(args):
+    """GPU comparators on the benchmark's shapes, each with its time,
+    systems/s (counting the systems it solves), HBM fraction over 5 n s bytes
+    per solved system and the backward error of a sample of its results."""
+    import torch
+
+    import tridiagonalsolver_gb300 as T
+    from oracle import oracle as O
+
+    L = T.lib()
+    dev = torch.device("cuda", 0)
+    peak, _ = _measured_peaks()
+    reps = max(3, min(args.steps, 10))
+    default = torch.cuda.default_stream(dev)
+    shapes = [("float32", 512, 32768, "dominant", "config 2, PCR / CR-PCR shape"),
+              ("float64", 4096, 4096, "dominant", "config 1 shape (contiguous)"),
+              ("float64", 4096, 4096, "nondominant", "config 2, pivoted WM-pGE shape")]
+    try:
+        ref = RefCudaKernels() if all(p.exists() for p in REF_CUBINS) else None
+        ref_note = None if ref else "unavailable: the cubins built from the reference's sources are not present"
+    except Exception as exc:
+        ref, ref_note = None, f"unavailable: {type(exc).__name__}: {exc}"[:200]
+    out = {"cusparse_gtsv2StridedBatch": [], "reference_cuda": [] if ref else ref_note}
+
+    def record(kind, label, dts, n, batch, dist, ms, solved, x_rows, src_host, note=None):
+        es = 4 if dts == "float32" else 8
+        bytes_ = 5 * n * solved * es
+        idx = np.linspace(0, solved - 1, 16).astype(np.int64)
+        a, b, c, d = (v[idx].astype(np.float64) for v in src_host)
+        _, eta = O.backward_error(a, b, c, d, x_rows[idx].astype(np.float64), n)
+        rec = {"algorithm": label, "dtype": dts, "n": n, "batch": batch, "systems_solved": solved,
+               "distribution": dist, "ms_per_call": round(ms, 4), "systems_per_s": solved / (ms * 1e-3),
+               "hbm_gbs": round(bytes_ / (ms * 1e-3) / 1e9, 1),
+               "hbm_frac": round(bytes_ / (ms * 1e-3) / 1e9 / peak, 4), "backward_error_max": eta}
+        if note:
+            rec["note"] = note
+        out[kind].append(rec)
+
+    for dts, n, batch, dist, what in shapes:
+        dt = getattr(torch, dts)
+        g = torch.Generator(device=dev)
+        g.manual_seed(31)
+        u = lambda lo, hi: torch.rand((batch, n), dtype=dt, device=dev, generator=g) * (hi - lo) + lo
+        a, c, d = u(-1, 1), u(-1, 1), u(-1, 1)
+        a[:, 0] = 0
+        c[:, -1] = 0
+        b = a.abs() + c.abs() + u(1, 2) if dist == "dominant" else u(-1, 1)
+        src = [a, b, c, d]
+        host = [t.double().cpu().numpy() for t in src]
+        work = [t.clone() for t in src]
+        P_ = [t.data_ptr() for t in work]
+        sfx = "single" if dts == "float32" else "double"
+        torch.cuda.synchronize()
+        # cuSPARSE (the reference's cuSparse_* protocol: init, synchronous solves on the default stream, final)
+        if getattr(L, f"cuSparse_init_{sfx}")(*P_, n, batch) == 0:
+            ms = _time_inplace(torch, default, src, work, lambda: getattr(L, f"cuSparse_{sfx}")(*P_, n, batch), reps)
+            record("cusparse_gtsv2StridedBatch", "gtsv2StridedBatch (CR + PCR, no pivoting)", dts, n, batch, dist,
+                   ms, batch, work[3].cpu().numpy(), host, note=what)
+            L.cuSparse_final()
+        if ref is None:
+            continue
+        ks = "f" if dts == "float32" else "d"
+        stream = torch.cuda.Stream(device=dev)
+        cands = []
+        if n <= 1024:
+            # warp-per-system kernels, 2 systems per 64-thread block, grid div_ceil(batch, 2) = (batch+1)/2 - 1
+            grid = (batch + 1) // 2 - 1
+            cands += [("PCR5_reg_kernel", "reg PCR-pThomas (PCR5_reg)", grid, 64, grid * 2),
+                      ("WM5_reg_kernel", "reg WM-pGE (WM5_reg)", grid, 64, grid * 2)]
+        else:
+            grid = (batch + 1) // 2 - 1
+            cands += [("WM5_reg_kernel", "reg WM-pGE (WM5_reg)", grid, 64, grid * 2)]
+        cands += [("Thomas_kernel", "Thomas (thread per system)", (batch - 1) // 64 + 1, 64, batch)]
+        for kname, label, grid, block, solved in cands:
+            if (kname, ks) not in ref.funcs:
+                continue
+            ms = _time_inplace(torch, stream, src, work,
+                               lambda: ref.launch(kname, ks, grid, block, P_, [n, batch], stream.cuda_stream), reps)
+            record("reference_cuda", label, dts, n, batch, dist, ms, solved, work[3].cpu().numpy(), host, note=what)
+        if ("CR_kernel", ks) in ref.funcs and n <= 1024:
+            buf = torch.empty(4 * n * batch, dtype=dt, device=dev)
+            ptrs = P_[:4] + [buf.data_ptr()]
+            ms = _time_inplace(torch, stream, src, work,
+                               lambda: ref.launch("CR_kernel", ks, batch, 64, ptrs, [n, batch], stream.cuda_stream),
+                               reps)
+            record("reference_cuda", "CR (global-memory scratch)", dts, n, batch, dist, ms, batch,
+                   work[3].cpu().numpy(), host, note=what)
+            del buf
+        del src, work, host
+        torch.cuda.empty_cache()
+    return out
+
+
 # The other benchmark configurations, measured after the headline in the
 # default run (one GPU) and reported under "configs" of its line.
 OTHER_CONFIGS = [
@@ -1345,6 +1514,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--headline-only", action="store_true",
                     help="default workload: measure configuration 2 only (no 'configs' entry)")
+    ap.add_argument("--comparators", action="store_true",
+                    help="time only the GPU comparators (cuSPARSE, the reference's CUDA kernels) and print them")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2",
                     help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
                          "remaining benchmark configurations, one JSON line each")
@@ -1353,6 +1524,9 @@ def main():
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args.profile_case)
+        return
+    if args.comparators:
+        print(json.dumps({"comparators": comparators(args)}), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3
@@ -1363,6 +1537,10 @@ def main():
         if line is not None:
             if line["n_gpus"] == 1 and not args.headline_only:
                 line["configs"] = other_configs(args)
+                try:
+                    line["comparators"] = comparators(args)
+                except Exception as exc:  # report, keep the headline
+                    line["comparators"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
             print(json.dumps(line), flush=True)
     else:
         print(json.dumps(WORKLOADS[args.workload](args)), flush=True)

@@ -72,6 +72,18 @@ def _measured_peaks():
     return 6800.0, "fallback"
 
 
+def _fp64_counts():
+    """FP64 instructions per row of the FP64 kernels and the measured DFMA rate
+    (key = value lines of the committed ncu summary)."""
+    out = {}
+    for line in (ROOT / "profiles" / "fp64_instructions.txt").read_text().splitlines():
+        line = line.split("#")[0].strip()
+        if "=" in line:
+            k, v = line.split("=")
+            out[k.strip()] = float(v)
+    return out
+
+
 def _traffic_table():
     """DRAM bytes per launch from the committed ncu summary (key value lines)."""
     out = {}
@@ -303,13 +315,8 @@ def run_ours(args):
                     else "fallback 6.8 TB/s"}
         if dom["dtype"] == "float64":
             # the FP64 solve is bound by the FP64 pipe on GB300, not by HBM: report that roofline too
-            # (FP64 operations per row from ncu's instruction counts, profiles/pge_fp64_n4096.md;
-            # peak = measured DFMA rate, profiles/fp64_rates_microbench.txt)
-            ops_per_row, fp64_peak = 20.8, 503.0
-            gops = dom["n"] * dom["batch"] * ops_per_row / (dom["ms_per_launch"] * 1e-3) / 1e9
-            roofline["compute"] = {"bound": "fp64", "achieved": round(gops, 1), "peak": fp64_peak,
-                                   "unit": "Gop/s", "frac": round(gops / fp64_peak, 4),
-                                   "ops_per_row": ops_per_row, "peak_source": "measured DFMA microbenchmark"}
+            # (FP64 instructions per row and the measured DFMA rate: profiles/fp64_instructions.txt)
+            roofline["compute"] = _fp64_roofline(dom["n"] * dom["batch"], dom["ms_per_launch"], "pge_fp64_ops_per_row")
             roofline["note"] = ("the pivoted FP64 solve is bound by GB300's FP64 issue rate (one FP64 warp "
                                 "instruction per 80 cycles per SM sub-partition), not by HBM; see roofline.compute")
         cpu = _cpu_baseline() if (world == 1 and not args.no_cpu) else None
@@ -598,8 +605,18 @@ def _e2e_generic(torch, stream, dev_inputs, dev_outputs, fn, steps, unit_count):
             "steps": steps}
 
 
+def _fp64_roofline(rows, ms, key):
+    """FP64 compute roofline of a kernel that does `rows` rows in `ms`, its
+    instructions per row read under `key` from the committed ncu counts."""
+    f64 = _fp64_counts()
+    ops, peak = f64[key], f64["dfma_gops"]
+    gops = rows * ops / (ms * 1e-3) / 1e9
+    return {"bound": "fp64", "achieved": round(gops, 1), "peak": peak, "unit": "Gop/s", "frac": round(gops / peak, 4),
+            "ops_per_row": ops, "peak_source": "measured DFMA microbenchmark (profiles/fp64_instructions.txt)"}
+
+
 def _line(args, workload, value, ms_step, dtype, config, parts, roof_bytes, roof_ms, cpu, e2e, clocks, launches,
-          note=None):
+          note=None, compute=None):
     peak, peak_kind = _measured_peaks()
     achieved = roof_bytes / (roof_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -608,6 +625,8 @@ def _line(args, workload, value, ms_step, dtype, config, parts, roof_bytes, roof
                 else "fallback 6.8 TB/s"}
     if note:
         roofline["note"] = note
+    if compute:
+        roofline["compute"] = compute
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded, distributions of the workload)", "config": dict(config, workload=workload),
@@ -681,8 +700,9 @@ def run_thomas_fp64(args):
           [{"name": "thomas_fp64", "ms_per_launch": ms, "systems_per_s": batch / (ms * 1e-3),
             "algorithmic_bytes": bytes_, "hbm_gbs": round(bytes_ / (ms * 1e-3) / 1e9, 1),
             "backward_error_max": eta}], bytes_, ms, cpu_b, e2e, clocks,
-          3 * args.steps, note="FP64 issue bound: partitioned Thomas, about 13.4 FP64 instructions per row "
-                               "(7 + 1 in the end partitions, 12 + 2 in the others)")
+          3 * args.steps, note="FP64 issue bound: partitioned Thomas (7 + 1 FP64 instructions per row in the end "
+                               "partitions, 12 + 2 in the others); see roofline.compute",
+          compute=_fp64_roofline(n * batch, ms, "ipt_fp64_ops_per_row"))
 
 
 def run_plain(args):
@@ -877,6 +897,58 @@ def _ragged_cpu_rate(O, sizes, nondom, target_s=8.0):
     return k / t, k, t, cores
 
 
+def _ragged_fp64_parts(torch, T, O, ragged, plan32, sizes, off, nondom, stream):
+    """The same ragged batch in FP64, forward + adjoint: the plain FP64
+    solve (a classifying FP64 plan) and the refined form (FP32 solves through
+    the FP32 plan, FP64 residuals, 1 and 2 refinement steps); worst normwise
+    backward error of x and of lambda (A^T lambda = xbar) over a sample,
+    dominant and non-dominant systems apart."""
+    a, b, c, d, _, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, seed=2024)
+    w = torch.rand_like(d) * 2 - 1
+    x = torch.empty_like(d)
+    grads = [torch.empty_like(d) for _ in range(4)]
+    plan64 = T.RaggedPlan(off, dtype=torch.float64, classify=True)
+    work = plan32.refine_workspace()
+    rng = np.random.default_rng(6)
+    sample = list(rng.choice(len(sizes), 24, replace=False)) + list(np.argsort(sizes)[-2:])
+
+    def accuracy():
+        worst = {True: [0.0, 0.0], False: [0.0, 0.0]}
+        for s_ in sample:
+            lo, hi = int(off[s_]), int(off[s_ + 1])
+            ha, hb, hc, hd, hx, hw, hl = (t[lo:hi].cpu().numpy()[None] for t in (a, b, c, d, x, w, grads[3]))
+            at, ct = np.zeros_like(ha), np.zeros_like(hc)
+            at[:, 1:], ct[:, :-1] = hc[:, :-1], ha[:, 1:]
+            ek = not nondom[s_]
+            worst[ek][0] = max(worst[ek][0], O.backward_error(ha, hb, hc, hd, hx, hi - lo)[1])
+            worst[ek][1] = max(worst[ek][1], O.backward_error(at, hb, ct, hw, hl, hi - lo)[1])
+        return {"backward_error_max_dominant": worst[True][0], "adjoint_backward_error_max_dominant": worst[True][1],
+                "backward_error_max_nondominant": worst[False][0],
+                "adjoint_backward_error_max_nondominant": worst[False][1]}
+
+    def plain():
+        plan64.solve(a, b, c, d, out=x, stream=stream)
+        plan64.adjoint(a, b, c, x, w, grads=grads, stream=stream)
+
+    out = []
+    ms, _ = _graph_time(torch, stream, plain, 3, 3)
+    out.append(dict({"name": "FP64 forward+adjoint, plain (classifying FP64 plan)", "ms_per_step": ms,
+                     "systems_per_s": len(sizes) / (ms * 1e-3),
+                     "buckets": [f"class {k} v{v} x{cnt}" for k, v, cnt, _ in plan64.buckets()]}, **accuracy()))
+    for iters in (1, 2):
+        def refined(iters=iters):
+            plan32.refine(a, b, c, d, iters=iters, out=x, work=work, stream=stream)
+            plan32.refine_adjoint(a, b, c, x, w, iters=iters, grads=grads, work=work, stream=stream)
+
+        ms, _ = _graph_time(torch, stream, refined, 3, 3)
+        out.append(dict({"name": f"FP64 forward+adjoint, refined ({iters} step{'s' if iters > 1 else ''}: FP32 "
+                                 f"solves, FP64 residuals)", "ms_per_step": ms,
+                         "systems_per_s": len(sizes) / (ms * 1e-3)}, **accuracy()))
+    del a, b, c, d, w, x, grads, work, plan64
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ragged(args):
     """100000 systems, n log-uniform in [32, 65536], FP32, 20% non-dominant:
     forward + adjoint through the size-class plan, the library finding per
@@ -947,6 +1019,7 @@ def run_ragged(args):
         worst = max(worst, O.backward_error(*hs, hi - lo)[1])
     rows = int(off[-1])
     e2e = _e2e_generic(torch, stream, [a, b, c, d, w], [x] + grads, step, 3, len(sizes))
+    fp64 = _ragged_fp64_parts(torch, T, O, ragged, plan, sizes, off, nondom, stream)
     rate, k, t, cores = (None, 0, 0, 0) if args.no_cpu else _ragged_cpu_rate(O, sizes, nondom)
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                       "sample": f"{k} random systems of the batch, forward + adjoint (FP64 port), "
@@ -968,7 +1041,7 @@ def run_ragged(args):
                   {"name": "forward+adjoint, every system pivoted", "ms_per_step": ms_piv},
                   {"name": "forward+adjoint, the generator's dominance passed as a mask", "ms_per_step": ms_mask},
                   {"name": "library marks", "systems_marked_unpivoted": int(marks.sum()),
-                   "equal_to_generator_dominance": marks_match}],
+                   "equal_to_generator_dominance": marks_match}] + fp64,
                  14 * rows * 4 + 16 * len(sizes), ms, cpu_b, e2e, clocks, 2 * steps * len(bk))
 
 
@@ -1161,17 +1234,14 @@ def run_block2(args):
     cpu_b = None if args.no_cpu else {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                       "sample": f"{k} of {batch} systems in {t:.2f} s (oracle ?gbsv restatement, FP64)"}
     ms = kernel_ms["pivoted_fp64"]
-    # FP64 instructions per block row from ncu's counts (DFMA 43, DMUL 7, DADD 7;
-    # profiles/block2_fp64_n256.md)
-    ops_per_row, fp64_peak = 57.0, 503.0
-    gops = n * batch * ops_per_row / (ms * 1e-3) / 1e9
+    # FP64 instructions per block row from ncu's counts (profiles/fp64_instructions.txt)
+    compute = _fp64_roofline(n * batch, ms, "block2_fp64_ops_per_row")
     return _line(args, "block tridiagonal (2 x 2 blocks) pivoted FP64, n=512 x 131072, interleaved", batch / (ms * 1e-3), ms,
           "f64", {"n": n, "batch": batch, "layout": "interleaved",
                   "dominant": "block2_pivoted_kernel<double, INTERLEAVED>",
                   "l2": "inputs larger than L2 (3.8 GB FP64)", "timing": "kernel alone, inputs restored between steps"},
           parts, 16 * n * batch * 8, ms, cpu_b, e2e, clocks, 3 * args.steps,
-          note=f"FP64 issue bound: {ops_per_row:.0f} FP64 instructions per block row -> {gops:.0f} Gop/s = "
-               f"{gops / fp64_peak:.0%} of the {fp64_peak:.0f} Gop/s DFMA microbenchmark rate")
+          note="FP64 issue bound; see roofline.compute", compute=compute)
 
 
 # ---------------------------------------------------------------------------
@@ -1223,31 +1293,44 @@ def profile_case(name: str) -> None:
         torch.cuda.synchronize()
         print("ok block2_64")
         return
-    if name == "ragged_step":
-        # the ragged workload: three forward + adjoint steps, then one between
+    if name in ("ragged_step", "ragged64_step", "ragged_refine_step"):
+        # the ragged workload (FP32; FP64 plain; FP64 refined through the FP32
+        # plan, one step): three forward + adjoint steps, then one between
         # torch.cuda.profiler.start() and stop() (ncu --profile-from-start off)
         from tridiagonalsolver_gb300 import ragged
 
+        dt = torch.float64 if name != "ragged_step" else torch.float32
         sizes = ragged.log_uniform_sizes(100000, 32, 65536, seed=2024)
-        a, b, c, d, off, _ = ragged.synthetic_batch(sizes, seed=2024)
+        a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=dt, seed=2024)
         w = torch.rand_like(d) * 2 - 1
         table, utab, chunk = ragged.load_table(RAGGED_TABLE, full=True) if RAGGED_TABLE.exists() else ({}, {}, 0)
-        plan = T.RaggedPlan(off, table=table, classify=True, unpivoted_table=utab, chunk_rows=chunk)
+        if name == "ragged64_step":
+            plan = T.RaggedPlan(off, dtype=dt, classify=True)
+        else:
+            plan = T.RaggedPlan(off, table=table, classify=True, unpivoted_table=utab, chunk_rows=chunk)
         x = torch.empty_like(d)
         grads = [torch.empty_like(d) for _ in range(4)]
+        work = plan.refine_workspace() if name == "ragged_refine_step" else None
+
+        def step():
+            if work is not None:
+                plan.refine(a, b, c, d, iters=1, out=x, work=work, stream=s_)
+                plan.refine_adjoint(a, b, c, x, w, iters=1, grads=grads, work=work, stream=s_)
+            else:
+                plan.solve(a, b, c, d, out=x, stream=s_)
+                plan.adjoint(a, b, c, x, w, grads=grads, stream=s_)
+
         s_ = torch.cuda.Stream()
         s_.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s_):
             for _ in range(3):
-                plan.solve(a, b, c, d, out=x, stream=s_)
-                plan.adjoint(a, b, c, x, w, grads=grads, stream=s_)
+                step()
             s_.synchronize()
             torch.cuda.profiler.start()
-            plan.solve(a, b, c, d, out=x, stream=s_)
-            plan.adjoint(a, b, c, x, w, grads=grads, stream=s_)
+            step()
             s_.synchronize()
             torch.cuda.profiler.stop()
-        print("ok ragged_step", int(off[-1]), "rows")
+        print("ok", name, int(off[-1]), "rows")
         return
     n, batch, dts, dominant, how = PROFILE_CASES[name]
     dt = getattr(torch, dts)
@@ -1519,7 +1602,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2",
                     help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
                          "remaining benchmark configurations, one JSON line each")
-    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step"], default=None,
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step", "ragged64_step",
+                                                                         "ragged_refine_step"], default=None,
                     help="run one small case of one kernel family three times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.profile_case:

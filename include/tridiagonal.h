@@ -320,10 +320,13 @@ int tridiag_partition_adjoint_double(int layout, const double *a, const double *
  * classes (class k: 2^(k-1) < n <= 2^k) and picks a kernel variant per class:
  * 0 = thread-per-system sequential partial pivoting (n <= 64), 1/2/3 = the
  * partitioned solve in one CTA with 64/128/256 partitions, 4/5/6 = in a
- * cluster of 2/4/8 CTAs.  variant_by_class (may be NULL; entries < 0 mean
- * "default") overrides the choice per class -- the autotuner's output; an
- * entry that cannot serve its class's sizes makes the call return
- * TRIDIAG_ERR_NOT_SUPPORTED.
+ * cluster of 2/4/8 CTAs, 9 = thread-per-system sequential partial pivoting
+ * with the eliminated rows in a plan workspace (any n; 2 values + 1 bit per
+ * row of its classes; the default where no partitioned variant serves the
+ * class: FP64 beyond 27648 rows, FP32 beyond 65536).  variant_by_class (may
+ * be NULL; entries < 0 mean "default") overrides the choice per class -- the
+ * autotuner's output; an entry that cannot serve its class's sizes makes the
+ * call return TRIDIAG_ERR_NOT_SUPPORTED.
  * tridiag_ragged_solve_* / _adjoint_* issue one launch per non-empty bucket
  * on the stream (capturable in one CUDA graph); offsets is the device copy of
  * the offsets used to build the plan.  info (may be NULL) per system.  A plan
@@ -361,6 +364,30 @@ int tridiag_ragged_plan_create_ex(tridiag_ragged_plan **plan, int precision, con
 int tridiag_ragged_plan_create_classify(tridiag_ragged_plan **plan, int precision, const long long *offsets_host,
                                         int n_batch, const int *variant_by_class, const int *unpivoted_by_class,
                                         int n_classes, int chunk_rows);
+/* Refined ragged solves (no counterpart in the reference): FP64 systems
+ * solved through an FP32 plan (plan32, precision 0) of the same offsets --
+ * FP32 copies of the coefficients and the right-hand side, an FP32 solve,
+ * then `iters` (0-8) steps of an FP64 residual (one warp per system, the
+ * system boundaries respected) and an FP32 correction solve, the FP64
+ * iterate updated each step.  tridiag_ragged_refine_double writes x;
+ * tridiag_ragged_refine_adjoint_double solves A^T lambda = xbar the same way
+ * (the FP32 copies are of A^T, so a classifying plan checks A^T's rows) and
+ * writes gd = lambda and the FP64 gradients ga_i = -lambda_i x_{i-1}, gb_i =
+ * -lambda_i x_i, gc_i = -lambda_i x_{i+1} from the forward solution x.  a,
+ * b, c, d, xbar are read only.  work: tridiag_ragged_refine_workspace_size()
+ * bytes (28 per row); offsets: the device copy of the plan's offsets.  The
+ * FP32 solves see the narrowed coefficients: the result reaches FP64
+ * accuracy when the FP32 solve converges the iteration (condition number
+ * well below 1 / FP32 epsilon).  A classifying plan32 keeps the marks of its
+ * last FP32 solve (of A^T after an adjoint). */
+size_t tridiag_ragged_refine_workspace_size(long long total_rows);
+int tridiag_ragged_refine_double(tridiag_ragged_plan *plan32, const double *a, const double *b, const double *c,
+                                 const double *d, double *x, int iters, void *work, size_t work_bytes,
+                                 const long long *offsets, void *stream);
+int tridiag_ragged_refine_adjoint_double(tridiag_ragged_plan *plan32, const double *a, const double *b,
+                                         const double *c, const double *x, const double *xbar, double *ga,
+                                         double *gb, double *gc, double *gd, int iters, void *work,
+                                         size_t work_bytes, const long long *offsets, void *stream);
 /* The marks (1: solved without pivoting) of the plan's last solve, one byte
  * per system, into host memory (synchronous); TRIDIAG_ERR_NOT_SUPPORTED for
  * a plan without marks. */

@@ -341,3 +341,98 @@ def test_ragged_autotune_unpivoted(cuda):
         hs = [_host(t, off, s) for t in (a, b, c, d, x)]
         _, eta = O.backward_error(*hs, int(sizes[s]))
         assert eta <= 1e-6
+
+
+@pytest.mark.parametrize("iters", [1, 2])
+def test_ragged_refined_forward_and_adjoint(cuda, iters):
+    """FP64 ragged systems solved through an FP32 classified plan with FP64
+    residual refinement, forward and adjoint: on diagonally dominant systems
+    of every size class up to 20000 rows, normwise backward error <= 1e-12 per
+    system for x and for lambda (A^T lambda = xbar), gradients within 1e-10
+    of the FP64 oracle adjoint (relative to the system's largest entry)."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = _sizes(20000)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=0.0, seed=21)
+    plan32 = T.RaggedPlan(off, dtype=torch.float32, classify=True)
+    x = plan32.refine(a, b, c, d, iters=iters)
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan32.refine_adjoint(a, b, c, x, w, iters=iters)
+    torch.cuda.synchronize()
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, True, 1e-12, 1e-10)
+
+
+def test_ragged_refined_rejects_fp64_plan(cuda):
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    off = np.array([0, 100, 300], dtype=np.int64)
+    t = torch.zeros(300, dtype=torch.float64, device="cuda")
+    plan64 = T.RaggedPlan(off, dtype=torch.float64)
+    with pytest.raises(ValueError):
+        plan64.refine(t, t, t, t)
+
+
+@pytest.mark.parametrize("dtype_name", ["float32", "float64"])
+def test_ragged_sequential_variant(cuda, dtype_name):
+    """Variant 9 (thread-per-system partial pivoting, rows in the plan's
+    workspace) forced for every class above 64 rows: forward and adjoint of
+    dominant and non-dominant systems against the oracle."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    dt = getattr(torch, dtype_name)
+    sizes = _sizes(5000)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=dt, nondominant_fraction=0.3, seed=31)
+    table = {k: 9 for k in range(7, ragged.CLASSES)}
+    plan = T.RaggedPlan(off, dtype=dt, table=table)
+    assert {v for cls, v, _, _ in plan.buckets() if cls >= 7} == {9}
+    info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+    x = plan.solve(a, b, c, d, info=info)
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    assert int((info != 0).sum()) == 0
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], ETA[dtype_name], GTOL[dtype_name])
+
+
+@pytest.mark.parametrize("routing", ["pivoted", "classify"])
+def test_ragged_fp64_beyond_clusters(cuda, routing):
+    """FP64 systems longer than the clusters serve (27648 rows) go to variant
+    9 by default; with the library classifying, the dominant ones run the
+    chunked unpivoted method and the others reach variant 9 through the
+    class's device-grown list.  Every system checked, forward and adjoint."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = np.array([40000, 65536, 27649, 33000, 50000, 30001, 100, 3000, 20000, 64], dtype=np.int64)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=0.5, seed=32)
+    assert nondom[sizes > 27648].any() and (~nondom[sizes > 27648]).any()
+    plan = T.RaggedPlan(off, dtype=torch.float64, classify=routing == "classify")
+    assert 9 in {v for _, v, _, _ in plan.buckets()}
+    info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+    x = plan.solve(a, b, c, d, info=info)
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    assert int((info != 0).sum()) == 0
+    if routing == "classify":
+        big = sizes > 64
+        assert np.array_equal(plan.kinds().astype(bool)[big], ~nondom[big])
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], ETA["float64"], GTOL["float64"])

@@ -20,8 +20,9 @@
 //     x_first = alpha - beta s_{p-1} - gamma x_{i+1}, 12 operations per row;
 //     they leave x_first and x_last as functions of s_{p-1} and s_p.
 // The separators' tridiagonal system (P-1 unknowns per system) is then
-// formed from those relations and solved by one thread per system, and a
-// third launch back-substitutes every partition with its separators known.
+// formed from those relations, row by row in parallel, and solved by one
+// thread per system, and a third launch back-substitutes every partition
+// with its separators known.
 // Factors: d' (d'') in x, c' (a'' of the last partition) and the spike v' in
 // two n x batch workspace arrays, the end relations and the separator system
 // in two small ones.
@@ -50,7 +51,7 @@ struct Ipt {
   T* cp;   // c' (a'' in the last partition)
   T* vp;   // left spike v' of interior partitions
   T* rel;  // [6][P][batch]: end relations of each partition
-  T* sys;  // [2][P][batch]: the separator system's c'', d'' -> s
+  T* sys;  // [2][P][batch]: the separators s in the second half
   int n, batch, P, L;
 };
 
@@ -193,44 +194,70 @@ __global__ void __launch_bounds__(128) ipt_forward_kernel(const Ipt<T> g) {
   relv(g, 5, p, j) = ga;
 }
 
-// ---- the separators' system, one thread per system -------------------------
+// ---- the separators' system ----------------------------------------------
+// A block holds 32 systems (lane = system) and 8 warps: the warps first form
+// the separator rows of the 32 systems in parallel (warp w forms rows w,
+// w + 8, ...; each row reads four inputs and the end relations of the two
+// partitions beside it, independent of the others) into shared memory, then
+// warp 0 runs Thomas over them, one thread per system, and writes the
+// separators.  Dynamic shared memory: 4 (P - 1) 32 values.
+
+constexpr int IPT_SEP_WARPS = 8;
 
 template <typename T>
-__global__ void __launch_bounds__(128) ipt_separator_kernel(const Ipt<T> g) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= g.batch) return;
+__global__ void __launch_bounds__(32 * IPT_SEP_WARPS) ipt_separator_kernel(const Ipt<T> g) {
+  extern __shared__ __align__(16) unsigned char ipt_sep_smem[];
   const int S = g.P - 1;
-  T* sc = g.sys;
+  T* sA = reinterpret_cast<T*>(ipt_sep_smem);
+  T* sB = sA + (size_t)S * 32;
+  T* sC = sB + (size_t)S * 32;
+  T* sD = sC + (size_t)S * 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  const bool live = j < g.batch;
+  for (int q = w; q < S; q += IPT_SEP_WARPS) {
+    T A = T(0), B = T(1), C = T(0), D = T(0);
+    if (live) {
+      const int R = (q + 1) * g.L - 1;
+      const size_t o = at(g, R, j);
+      const T aR = ld_stream(g.a + o), cR = ld_stream(g.c + o);
+      B = ld_stream(g.b + o);
+      D = ld_stream(g.d + o);
+      // x_{R-1}: the last interior row of partition q
+      B = fma(-aR, relv(g, 1, q, j), B);
+      D = fma(-aR, relv(g, 0, q, j), D);
+      if (q > 0) A = -aR * relv(g, 2, q, j);
+      // x_{R+1}: the first interior row of partition q + 1
+      if (q + 1 == g.P - 1) {
+        B = fma(-cR, relv(g, 1, q + 1, j), B);
+        D = fma(-cR, relv(g, 0, q + 1, j), D);
+      } else {
+        B = fma(-cR, relv(g, 4, q + 1, j), B);
+        D = fma(-cR, relv(g, 3, q + 1, j), D);
+        C = -cR * relv(g, 5, q + 1, j);
+      }
+    }
+    sA[q * 32 + lane] = A;
+    sB[q * 32 + lane] = B;
+    sC[q * 32 + lane] = C;
+    sD[q * 32 + lane] = D;
+  }
+  __syncthreads();
+  if (w != 0 || !live) return;
   T* sd = g.sys + (size_t)g.P * g.batch;
   T cprev = T(0), dprev = T(0);
   for (int q = 0; q < S; ++q) {
-    const int R = (q + 1) * g.L - 1;
-    const size_t o = at(g, R, j);
-    const T aR = ld_stream(g.a + o), bR = ld_stream(g.b + o), cR = ld_stream(g.c + o), dR = ld_stream(g.d + o);
-    // x_{R-1}: the last interior row of partition q
-    T A = T(0), B = bR, C = T(0), D = dR;
-    B = fma(-aR, relv(g, 1, q, j), B);
-    D = fma(-aR, relv(g, 0, q, j), D);
-    if (q > 0) A = -aR * relv(g, 2, q, j);
-    // x_{R+1}: the first interior row of partition q + 1
-    if (q + 1 == g.P - 1) {
-      B = fma(-cR, relv(g, 1, q + 1, j), B);
-      D = fma(-cR, relv(g, 0, q + 1, j), D);
-    } else {
-      B = fma(-cR, relv(g, 4, q + 1, j), B);
-      D = fma(-cR, relv(g, 3, q + 1, j), D);
-      C = -cR * relv(g, 5, q + 1, j);
-    }
-    // Thomas forward on the separator rows
-    const T r = rcp(fma(-A, cprev, B));
-    cprev = C * r;
-    dprev = fma(-A, dprev, D) * r;
-    sc[(size_t)q * g.batch + j] = cprev;
-    sd[(size_t)q * g.batch + j] = dprev;
+    const T A = sA[q * 32 + lane];
+    const T r = rcp(fma(-A, cprev, sB[q * 32 + lane]));
+    cprev = sC[q * 32 + lane] * r;
+    dprev = fma(-A, dprev, sD[q * 32 + lane]) * r;
+    sC[q * 32 + lane] = cprev;
+    sD[q * 32 + lane] = dprev;
   }
   T s = dprev;
+  sd[(size_t)(S - 1) * g.batch + j] = s;
   for (int q = S - 2; q >= 0; --q) {
-    s = fma(-sc[(size_t)q * g.batch + j], s, sd[(size_t)q * g.batch + j]);
+    s = fma(-sC[q * 32 + lane], s, sD[q * 32 + lane]);
     sd[(size_t)q * g.batch + j] = s;
   }
 }
@@ -374,7 +401,10 @@ cudaError_t launch_ipt(const T* a, const T* b, const T* c, const T* d, T* x, int
   ipt_forward_kernel<T><<<grid, 128, 0, s>>>(g);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  ipt_separator_kernel<T><<<(batch + 127) / 128, 128, 0, s>>>(g);
+  const size_t sep_smem = (size_t)4 * (P - 1) * 32 * sizeof(T);
+  err = cudaFuncSetAttribute(ipt_separator_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sep_smem);
+  if (err != cudaSuccess) return err;
+  ipt_separator_kernel<T><<<(batch + 31) / 32, 32 * IPT_SEP_WARPS, sep_smem, s>>>(g);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   ipt_back_kernel<T><<<grid, 128, 0, s>>>(g);

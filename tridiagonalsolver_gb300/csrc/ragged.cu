@@ -5,7 +5,9 @@
 // The plan groups the systems by size class (class k: 2^(k-1) < n <= 2^k)
 // and gives each class a kernel variant: the thread-per-system sequential
 // solve for n < 65 (variant 0), the partitioned solve with 64/128/256
-// partitions in one CTA (1-3) or in a cluster of 2/4/8 CTAs (4-6).  A
+// partitions in one CTA (1-3) or in a cluster of 2/4/8 CTAs (4-6), and the
+// thread-per-system sequential solve with its rows in a workspace for sizes
+// beyond every partitioned variant (9: FP64 beyond 27648 rows).  A
 // variant table (from the autotuner, or the defaults) overrides the choice
 // per class.  Systems that need no pivoting -- marked by the caller, or
 // found by the library itself -- run the unpivoted partition method in
@@ -107,13 +109,188 @@ static cudaError_t launch_tiny(int mode, const T* a, const T* b, const T* c, con
   return cudaGetLastError();
 }
 
+// Variant 9: the same elimination for any n, one thread per system, the
+// finished rows kept in global memory -- for the classes no partitioned
+// variant serves (FP64 beyond the clusters' shared memory).  Forward solve
+// (MODE 0): the finished rows' right-hand sides go to x, U1 and 1/U0 to the
+// plan's workspace (w1, w2 at the system's workspace row soff[s]), the
+// interchange bits to piv (word soff[s] / 32 + i / 32); the back
+// substitution reads them back and overwrites x.  MODE 1 (the transposed
+// system: the caller passes c - 1 and a + 1 for a and c): U1 and 1/U0 go to
+// gb and gc, which the back substitution then overwrites with the
+// gradients.  Rows are loaded SEQ_U ahead of the recurrence in both sweeps.
+// A kind-0 list grown on the device has its length at *dcount.
+constexpr int SEQ_U = 8;
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(32) ragged_seq_kernel(const T* a, const T* b, const T* c, const T* d, T* x,
+                                                        const T* xf, T* ga, T* gb, T* gc, int* info,
+                                                        const long long* offsets, const int* list, int count,
+                                                        const int* dcount, const long long* soff, T* w1, T* w2,
+                                                        unsigned* piv) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int live = dcount ? min(*dcount, count) : count;
+  if (k >= live) return;
+  const int sys = list[k];
+  const long long base = offsets[sys];
+  const int n = (int)(offsets[sys + 1] - base);
+  const long long so = soff[sys];
+  T* Rs = x + base;
+  T* Us = MODE == 0 ? w1 + so : gb + base;
+  T* Ws = MODE == 0 ? w2 + so : gc + base;
+  unsigned* pv = piv + so / 32;
+  T u0 = b[base], u1 = n > 1 ? c[base] : T(0), rhs = d[base];
+  int bad = 0;
+  unsigned word = 0;
+  T na[SEQ_U], nb[SEQ_U], nc[SEQ_U], nd[SEQ_U];
+#pragma unroll
+  for (int u = 0; u < SEQ_U; ++u) {
+    const int i = 1 + u;
+    if (i < n) {
+      na[u] = a[base + i];
+      nb[u] = b[base + i];
+      nc[u] = i + 1 < n ? c[base + i] : T(0);
+      nd[u] = d[base + i];
+    }
+  }
+  for (int i0 = 0; i0 + 1 < n; i0 += SEQ_U) {
+    T ra[SEQ_U], rb[SEQ_U], rc[SEQ_U], rd[SEQ_U];
+#pragma unroll
+    for (int u = 0; u < SEQ_U; ++u) { ra[u] = na[u]; rb[u] = nb[u]; rc[u] = nc[u]; rd[u] = nd[u]; }
+#pragma unroll
+    for (int u = 0; u < SEQ_U; ++u) {
+      const int i = i0 + 1 + SEQ_U + u;
+      if (i < n) {
+        na[u] = a[base + i];
+        nb[u] = b[base + i];
+        nc[u] = i + 1 < n ? c[base + i] : T(0);
+        nd[u] = d[base + i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < SEQ_U; ++u) {
+      const int i = i0 + u;  // finishing row i; row i + 1 is (ra, rb, rc, rd)[u]
+      if (i + 1 < n) {
+        const bool sw = !abs_ge(u0, ra[u]);
+        const T p = sw ? ra[u] : u0;
+        const T q = sw ? u0 : ra[u];
+        if (is_zero(p) && bad == 0) bad = i + 1;
+        const T r = Div<T>(p).inv();
+        const T m = q * r;
+        Rs[i] = sw ? rd[u] : rhs;
+        Us[i] = sw ? rb[u] : u1;
+        Ws[i] = r;
+        const T nu0 = fma(-m, sw ? rb[u] : u1, sw ? u1 : rb[u]);
+        const T nu1 = sw ? -m * rc[u] : rc[u];
+        const T nrhs = fma(-m, sw ? rd[u] : rhs, sw ? rhs : rd[u]);
+        word |= (unsigned)sw << (i & 31);
+        if ((i & 31) == 31) {
+          pv[i >> 5] = word;
+          word = 0;
+        }
+        u0 = nu0;
+        u1 = nu1;
+        rhs = nrhs;
+      }
+    }
+  }
+  if (n >= 2 && ((n - 2) & 31) != 31) pv[(n - 2) >> 5] = word;
+  if (is_zero(u0) && bad == 0) bad = n;
+  if (info) info[sys] = bad;
+  if (bad) return;
+  // back substitution: x_i = (R_i - U1_i x_{i+1} - U2_i x_{i+2}) / U0_i, with
+  // U2_i = c_{i+1} where rows i and i+1 were interchanged
+  T x1 = rhs * Div<T>(u0).inv();  // x_{n-1}
+  T x2 = T(0);
+  T fn = T(0), fc = T(0);         // MODE 1: xf of rows i + 1 and i
+  if (MODE == 1) {
+    fc = xf[base + n - 1];
+    const T fp = n > 1 ? xf[base + n - 2] : T(0);
+    ga[base + n - 1] = n > 1 ? -x1 * fp : T(0);
+    gb[base + n - 1] = -x1 * fc;
+    gc[base + n - 1] = T(0);
+    fn = fc;
+    fc = fp;
+  }
+  Rs[n - 1] = x1;
+  T qR[SEQ_U], qU[SEQ_U], qW[SEQ_U], qF[SEQ_U];
+#pragma unroll
+  for (int u = 0; u < SEQ_U; ++u) {
+    const int i = n - 2 - u;
+    if (i >= 0) {
+      qR[u] = Rs[i];
+      qU[u] = Us[i];
+      qW[u] = Ws[i];
+      qF[u] = MODE == 1 && i > 0 ? xf[base + i - 1] : T(0);
+    }
+  }
+  unsigned wcur = 0;
+  int wloaded = -1;
+  for (int i0 = n - 2; i0 >= 0; i0 -= SEQ_U) {
+    T rR[SEQ_U], rU[SEQ_U], rW[SEQ_U], rF[SEQ_U];
+#pragma unroll
+    for (int u = 0; u < SEQ_U; ++u) { rR[u] = qR[u]; rU[u] = qU[u]; rW[u] = qW[u]; rF[u] = qF[u]; }
+#pragma unroll
+    for (int u = 0; u < SEQ_U; ++u) {
+      const int i = i0 - SEQ_U - u;
+      if (i >= 0) {
+        qR[u] = Rs[i];
+        qU[u] = Us[i];
+        qW[u] = Ws[i];
+        qF[u] = MODE == 1 && i > 0 ? xf[base + i - 1] : T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < SEQ_U; ++u) {
+      const int i = i0 - u;
+      if (i >= 0) {
+        if ((i >> 5) != wloaded) {
+          wloaded = i >> 5;
+          wcur = pv[wloaded];
+        }
+        const bool sw = (wcur >> (i & 31)) & 1u;
+        const T u2 = sw && i + 2 < n ? c[base + i + 1] : T(0);
+        T x0 = fma(-rU[u], x1, rR[u]);
+        x0 = fma(-u2, x2, x0) * rW[u];
+        Rs[i] = x0;
+        if (MODE == 1) {  // lambda_i = x0; rows i - 1, i, i + 1 of the forward solution
+          ga[base + i] = -x0 * rF[u];
+          gb[base + i] = -x0 * fc;
+          gc[base + i] = -x0 * fn;
+          fn = fc;
+          fc = rF[u];
+        }
+        x2 = x1;
+        x1 = x0;
+      }
+    }
+  }
+}
+
+template <typename T>
+static cudaError_t launch_ragged_seq(int mode, const T* a, const T* b, const T* c, const T* d, T* x, const T* xf,
+                                     T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
+                                     int count, const int* dcount, const long long* soff, T* w1, T* w2,
+                                     unsigned* piv, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  // one warp per block: the few long systems spread over all SMs
+  const int grid = (count + 31) / 32;
+  if (mode == 0)
+    ragged_seq_kernel<T, 0><<<grid, 32, 0, s>>>(a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, count, dcount,
+                                                soff, w1, w2, piv);
+  else
+    ragged_seq_kernel<T, 1><<<grid, 32, 0, s>>>(c - 1, b, a + 1, d, x, xf, ga, gb, gc, info, offsets, list, count,
+                                                dcount, soff, w1, w2, piv);
+  return cudaGetLastError();
+}
+
 }  // namespace tdg
 
 // The opaque plan of include/tridiagonal.h.
 struct tridiag_ragged_plan {
   struct Bucket {
     int cls;      // size class
-    int variant;  // 0 tiny, 1-6 partitioned, 7 unpivoted partition method, 8 its chunked form
+    int variant;  // 0 tiny, 1-6 partitioned, 7 unpivoted partition method, 8 its chunked form, 9 sequential
     int count;    // systems (list entries; for kind 0 the room, the length being on the device)
     int m_max;    // rows per partition of the longest system
     int max_n;
@@ -144,6 +321,12 @@ struct tridiag_ragged_plan {
   int* d_tickets = nullptr;
   int n_tickets = 0;
   int unp_max = 0, long_max = 0;  // rows served by variants 7 and 8
+  // variant 9: each system's workspace row (d_soff[s], -1 for the systems of
+  // other classes) and the workspace: U1 and 1/U0 (seq_rows values each),
+  // then the interchange bits (seq_rows / 32 words)
+  long long* d_soff = nullptr;
+  void* seq_work = nullptr;
+  long long seq_rows = 0;
   // per class and kind, the list of the class's systems of that kind: its
   // region in d_klists (d_reg[2 k + kind], -1: none) and its length
   // d_kcount[2 k + kind]
@@ -168,6 +351,7 @@ int size_class(long long n) {
 
 constexpr int RAGGED_UNPIVOTED = 7;
 constexpr int RAGGED_UNPIVOTED_LONG = 8;
+constexpr int RAGGED_SEQUENTIAL = 9;
 
 template <typename T>
 int unpivoted_max_n() {
@@ -191,6 +375,7 @@ template <typename T>
 bool variant_serves(int v, int max_n) {
   if (v == 0) return max_n <= tdg::RAGGED_TINY_MAX;
   if (v == RAGGED_UNPIVOTED) return max_n <= unpivoted_max_n<T>();
+  if (v == RAGGED_SEQUENTIAL) return max_n >= 2;
   return max_n >= 65 && max_n <= tdg::pge_variant_max_n<T>(v);
 }
 
@@ -207,6 +392,8 @@ void free_plan(tridiag_ragged_plan* plan) {
   cudaFree(plan->lr_work);
   cudaFree(plan->d_kinds);
   cudaFree(plan->d_tickets);
+  cudaFree(plan->d_soff);
+  cudaFree(plan->seq_work);
   delete plan;
 }
 
@@ -291,6 +478,8 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   auto len = [&](int q) { return offsets[q + 1] - offsets[q]; };
   auto candidate = [&](int q) { return mode != 0 && unpivoted_capable<T>(len(q)) && (mode != 1 || mask[q]); };
   std::vector<unsigned char> kinds(batch, 0);  // (1: a candidate of kind 1)
+  std::vector<long long> soff(batch, -1);      // variant 9 workspace rows
+  long long seq_rows = 0;
   for (int k = 0; k < TRIDIAG_RAGGED_CLASSES; ++k) {
     auto& sys = by_class[k];
     if (sys.empty()) continue;
@@ -321,6 +510,12 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       v = table[k];
     }
     if (v < 0) v = max_n <= tdg::RAGGED_TINY_MAX ? 0 : tdg::pge_default_variant<T>(max_n);
+    if (v == 0 && max_n > tdg::RAGGED_TINY_MAX) v = RAGGED_SEQUENTIAL;  // beyond every partitioned variant
+    if (v == RAGGED_SEQUENTIAL)
+      for (int q : sys) {
+        soff[q] = seq_rows;
+        seq_rows += (len(q) + 31) / 32 * 32;
+      }
     if (v < 0 || (v == 0 && max_n > tdg::RAGGED_TINY_MAX) || (v > 0 && !variant_serves<T>(v, max_n))) {
       free_plan(plan);
       return TRIDIAG_ERR_NOT_SUPPORTED;
@@ -352,7 +547,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       bk.variant = variant;
       bk.count = count;
       bk.max_n = max_n;
-      bk.m_max = variant == 0                  ? 0
+      bk.m_max = variant == 0 || variant == RAGGED_SEQUENTIAL ? 0
                  : variant == RAGGED_UNPIVOTED ? (max_n + M - 1) / M  // 128-byte rows of the longest system
                                                : std::max(2, (max_n + tdg::pge_variant_partitions(variant) - 1) /
                                                                  tdg::pge_variant_partitions(variant));
@@ -360,7 +555,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       bk.list_off = list_off;
       bk.kind = kind;
       // resident CTAs with tickets only where the list grows on the device
-      bk.ticket = kind == 0 && mode == 2 && variant != 0 ? plan->n_tickets++ : -1;
+      bk.ticket = kind == 0 && mode == 2 && variant != 0 && variant != RAGGED_SEQUENTIAL ? plan->n_tickets++ : -1;
       bk.klist = kind >= 0 ? 2 * k + kind : -1;
       bk.klist_off = kind >= 0 ? (size_t)reg[2 * k + kind] : 0;
       plan->buckets.push_back(bk);
@@ -440,6 +635,17 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       cudaMemcpy(plan->d_lists, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
     free_plan(plan);
     return TRIDIAG_ERR_CUDA;
+  }
+  if (seq_rows > 0) {
+    plan->seq_rows = seq_rows;
+    const size_t wbytes = 2 * (size_t)seq_rows * sizeof(T) + (size_t)seq_rows / 32 * sizeof(unsigned);
+    if (cudaMalloc(&plan->d_soff, (size_t)batch * sizeof(long long)) != cudaSuccess ||
+        cudaMemcpy(plan->d_soff, soff.data(), (size_t)batch * sizeof(long long), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->seq_work, wbytes) != cudaSuccess) {
+      free_plan(plan);
+      return TRIDIAG_ERR_CUDA;
+    }
   }
   if (mode != 0) {
     const size_t nk = std::max<size_t>(klists.size(), 1);
@@ -530,6 +736,13 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
                                                 static_cast<T*>(plan->lr_work), info, s, plan->d_kinds);
     else if (bk.variant == 0)
       e = tdg::launch_tiny<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count, s);
+    else if (bk.variant == RAGGED_SEQUENTIAL) {
+      T* w1 = static_cast<T*>(plan->seq_work);
+      e = tdg::launch_ragged_seq<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
+                                    bk.kind == 0 && plan->kinds_mode == 2 ? plan->d_kcount + bk.klist : nullptr,
+                                    plan->d_soff, w1, w1 + plan->seq_rows,
+                                    reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), s);
+    }
     else if (bk.variant == RAGGED_UNPIVOTED)
       e = mode == 0 ? tdg::launch_wmc_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets, list,
                                                 bk.count, bk.m_max, info, s, tkp, nullptr, check ? &chk : nullptr)
@@ -541,6 +754,52 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
   }
   return TRIDIAG_SUCCESS;
+}
+
+// Mixed-precision refined solve of a ragged FP64 batch through an FP32 plan
+// of the same offsets: FP32 copies of A (trans: of A^T) and rhs, an FP32
+// solve, then `iters` steps of FP64 residual -> FP32 correction solve, the
+// FP64 iterate updated each time; out receives x (trans: lambda = A^{-T}
+// rhs).  Workspace: five FP32 rows-long arrays and one FP64 one.
+inline size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+
+size_t ragged_refine_ws(long long rows) {
+  return 5 * up256((size_t)rows * sizeof(float)) + up256((size_t)rows * sizeof(double));
+}
+
+int ragged_refine_impl(tridiag_ragged_plan* plan32, bool trans, const double* a, const double* b, const double* c,
+                       const double* rhs, double* out, int iters, void* work, size_t work_bytes,
+                       const long long* offsets, cudaStream_t s) {
+  if (!plan32 || !a || !b || !c || !rhs || !out || !offsets || iters < 0 || iters > 8)
+    return TRIDIAG_ERR_INVALID_VALUE;
+  if (plan32->precision != 0) return TRIDIAG_ERR_INVALID_VALUE;  // the solves run in FP32
+  const long long rows = plan32->total_rows;
+  if (!work || work_bytes < ragged_refine_ws(rows)) return TRIDIAG_ERR_WORKSPACE;
+  char* w = static_cast<char*>(work);
+  const size_t f = up256((size_t)rows * sizeof(float));
+  float* a32 = reinterpret_cast<float*>(w);
+  float* b32 = reinterpret_cast<float*>(w + f);
+  float* c32 = reinterpret_cast<float*>(w + 2 * f);
+  float* v0 = reinterpret_cast<float*>(w + 3 * f);  // FP32 right-hand side / residual
+  float* v1 = reinterpret_cast<float*>(w + 4 * f);  // FP32 solution / correction
+  double* w64 = reinterpret_cast<double*>(w + 5 * f);
+  const int batch = plan32->batch;
+  if (tdg::launch_ragged_narrow(trans, a, b, c, rhs, a32, b32, c32, v0, offsets, batch, s) != cudaSuccess)
+    return TRIDIAG_ERR_CUDA;
+  int st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s);
+  if (st != TRIDIAG_SUCCESS) return st;
+  // the FP64 iterate alternates between w64 and out so that the last step lands in out
+  double* xs[2] = {(iters % 2) ? out : w64, (iters % 2) ? w64 : out};
+  const double* xcur = nullptr;
+  for (int it = 0; it < iters; ++it) {
+    double* xnew = xs[it % 2];
+    if (tdg::launch_ragged_residual(trans, a, b, c, rhs, xcur, v1, xnew, v0, offsets, batch, s) != cudaSuccess)
+      return TRIDIAG_ERR_CUDA;
+    st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s);
+    if (st != TRIDIAG_SUCCESS) return st;
+    xcur = xnew;
+  }
+  return tdg::launch_update(xcur, v1, out, (size_t)rows, s) == cudaSuccess ? TRIDIAG_SUCCESS : TRIDIAG_ERR_CUDA;
 }
 
 }  // namespace
@@ -582,6 +841,29 @@ int tridiag_ragged_plan_kinds(const tridiag_ragged_plan* plan, unsigned char* ki
 
 void tridiag_ragged_plan_destroy(tridiag_ragged_plan* plan) { free_plan(plan); }
 
+size_t tridiag_ragged_refine_workspace_size(long long total_rows) {
+  return total_rows > 0 ? ragged_refine_ws(total_rows) : 0;
+}
+
+int tridiag_ragged_refine_double(tridiag_ragged_plan* plan32, const double* a, const double* b, const double* c,
+                                 const double* d, double* x, int iters, void* work, size_t work_bytes,
+                                 const long long* offsets, void* stream) {
+  return ragged_refine_impl(plan32, false, a, b, c, d, x, iters, work, work_bytes, offsets, (cudaStream_t)stream);
+}
+
+int tridiag_ragged_refine_adjoint_double(tridiag_ragged_plan* plan32, const double* a, const double* b,
+                                         const double* c, const double* x, const double* xbar, double* ga,
+                                         double* gb, double* gc, double* gd, int iters, void* work,
+                                         size_t work_bytes, const long long* offsets, void* stream) {
+  if (!x || !ga || !gb || !gc || !gd) return TRIDIAG_ERR_INVALID_VALUE;
+  const cudaStream_t s = (cudaStream_t)stream;
+  const int st = ragged_refine_impl(plan32, true, a, b, c, xbar, gd, iters, work, work_bytes, offsets, s);
+  if (st != TRIDIAG_SUCCESS) return st;
+  return tdg::launch_ragged_gradient(gd, x, ga, gb, gc, offsets, plan32->batch, s) == cudaSuccess
+             ? TRIDIAG_SUCCESS
+             : TRIDIAG_ERR_CUDA;
+}
+
 int tridiag_ragged_plan_buckets(const tridiag_ragged_plan* plan, int* out, int max_buckets) {
   if (!plan) return -1;
   const int nb = (int)plan->buckets.size();
@@ -599,6 +881,7 @@ int tridiag_ragged_plan_buckets(const tridiag_ragged_plan* plan, int* out, int m
 int tridiag_ragged_variant_max_n(int precision, int variant) {
   if (variant == 0) return tdg::RAGGED_TINY_MAX;
   if (variant == RAGGED_UNPIVOTED) return precision ? unpivoted_max_n<double>() : unpivoted_max_n<float>();
+  if (variant == RAGGED_SEQUENTIAL) return 0x7fffffff;
   if (variant == RAGGED_UNPIVOTED_LONG)
     return precision ? tdg::WMC_GEN_MAX_ROWS * 16 * 16 : tdg::WMC_GEN_MAX_ROWS * 32 * 32;
   return precision ? tdg::pge_variant_max_n<double>(variant) : tdg::pge_variant_max_n<float>(variant);

@@ -168,6 +168,139 @@ cudaError_t launch_update(const double* xold, const float* dx, double* xout, siz
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Ragged batches (system s = rows [offsets[s], offsets[s+1])): one warp per
+// system, grid-stride over the systems, lane l holding row i0 + l; the
+// neighbouring rows' values travel by shuffles (the row before a 32-row
+// step by the previous step's lane 31, the row after it by one more load),
+// so every row's x is formed once.  a_0 and c_{n-1} of a system are not
+// read.  TRANS: the coefficients of A^T (sub-diagonal c_{i-1},
+// super-diagonal a_{i+1}).
+
+__device__ __forceinline__ int ragged_warps() { return (int)(gridDim.x * blockDim.x / 32); }
+
+// a, b, c, rhs -> FP32 copies of A (TRANS: of A^T) and of the right-hand side
+template <bool TRANS>
+__global__ void __launch_bounds__(256) ragged_narrow_kernel(const double* __restrict__ a,
+                                                            const double* __restrict__ b,
+                                                            const double* __restrict__ c,
+                                                            const double* __restrict__ rhs, float* a32, float* b32,
+                                                            float* c32, float* r32, const long long* offsets,
+                                                            int batch) {
+  const int lane = threadIdx.x & 31;
+  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += ragged_warps()) {
+    const long long base = offsets[s], n = offsets[s + 1] - base;
+    for (long long i = lane; i < n; i += 32) {
+      const long long k = base + i;
+      const double lo = i > 0 ? (TRANS ? __ldg(c + k - 1) : __ldg(a + k)) : 0.0;
+      const double up = i < n - 1 ? (TRANS ? __ldg(a + k + 1) : __ldg(c + k)) : 0.0;
+      a32[k] = narrow_rn(lo);
+      b32[k] = narrow_rn(__ldg(b + k));
+      c32[k] = narrow_rn(up);
+      r32[k] = narrow_rn(__ldg(rhs + k));
+    }
+  }
+}
+
+// x_new = x_old + dx (x_old may be NULL: zero), r = rhs - A x_new (FP64,
+// stored as FP32); TRANS: r = rhs - A^T x_new.
+template <bool TRANS>
+__global__ void __launch_bounds__(256) ragged_residual_kernel(
+    const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+    const double* __restrict__ rhs, const double* __restrict__ xold, const float* __restrict__ dx,
+    double* __restrict__ xnew, float* __restrict__ r32, const long long* __restrict__ offsets, int batch) {
+  const int lane = threadIdx.x & 31;
+  auto xat = [&](long long k) { return xold ? __ldg(xold + k) + widen(__ldg(dx + k)) : widen(__ldg(dx + k)); };
+  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += ragged_warps()) {
+    const long long base = offsets[s], n = offsets[s + 1] - base;
+    double xlast = 0.0;  // x of the row before this step
+    for (long long i0 = 0; i0 < n; i0 += 32) {
+      const long long i = i0 + lane, k = base + i;
+      const bool in = i < n;
+      const double xi = in ? xat(k) : 0.0;
+      double xm = __shfl_up_sync(0xffffffffu, xi, 1);
+      if (lane == 0) xm = xlast;
+      double xp = __shfl_down_sync(0xffffffffu, xi, 1);
+      if (lane == 31 && i + 1 < n) xp = xat(k + 1);
+      if (in) {
+        const double lo = i > 0 ? (TRANS ? __ldg(c + k - 1) : __ldg(a + k)) : 0.0;
+        const double up = i < n - 1 ? (TRANS ? __ldg(a + k + 1) : __ldg(c + k)) : 0.0;
+        double r = fma(-__ldg(b + k), xi, __ldg(rhs + k));
+        r = fma(-lo, xm, r);
+        r = fma(-up, xp, r);
+        xnew[k] = xi;
+        r32[k] = narrow_rn(r);
+      }
+      xlast = __shfl_sync(0xffffffffu, xi, 31);
+    }
+  }
+}
+
+// Gradients of the adjoint from lambda and the forward solution x:
+// ga_i = -lambda_i x_{i-1} (0 at a system's first row), gb_i = -lambda_i
+// x_i, gc_i = -lambda_i x_{i+1} (0 at its last row).
+__global__ void __launch_bounds__(256) ragged_gradient_kernel(const double* __restrict__ lam,
+                                                              const double* __restrict__ x, double* ga, double* gb,
+                                                              double* gc, const long long* __restrict__ offsets,
+                                                              int batch) {
+  const int lane = threadIdx.x & 31;
+  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += ragged_warps()) {
+    const long long base = offsets[s], n = offsets[s + 1] - base;
+    double xlast = 0.0;
+    for (long long i0 = 0; i0 < n; i0 += 32) {
+      const long long i = i0 + lane, k = base + i;
+      const bool in = i < n;
+      const double xi = in ? __ldg(x + k) : 0.0;
+      double xm = __shfl_up_sync(0xffffffffu, xi, 1);
+      if (lane == 0) xm = xlast;
+      double xp = __shfl_down_sync(0xffffffffu, xi, 1);
+      if (lane == 31 && i + 1 < n) xp = __ldg(x + k + 1);
+      if (in) {
+        const double l = -__ldg(lam + k);
+        ga[k] = i > 0 ? l * xm : 0.0;
+        gb[k] = l * xi;
+        gc[k] = i < n - 1 ? l * xp : 0.0;
+      }
+      xlast = __shfl_sync(0xffffffffu, xi, 31);
+    }
+  }
+}
+
+static int ragged_grid(int batch) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int want = (batch + 7) / 8;  // eight warps per 256-thread block
+  return want < sms * 8 ? (want > 0 ? want : 1) : sms * 8;
+}
+
+cudaError_t launch_ragged_narrow(bool trans, const double* a, const double* b, const double* c, const double* rhs,
+                                 float* a32, float* b32, float* c32, float* r32, const long long* offsets, int batch,
+                                 cudaStream_t s) {
+  if (trans)
+    ragged_narrow_kernel<true><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, a32, b32, c32, r32, offsets, batch);
+  else
+    ragged_narrow_kernel<false><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, a32, b32, c32, r32, offsets, batch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ragged_residual(bool trans, const double* a, const double* b, const double* c, const double* rhs,
+                                   const double* xold, const float* dx, double* xnew, float* r32,
+                                   const long long* offsets, int batch, cudaStream_t s) {
+  if (trans)
+    ragged_residual_kernel<true><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, offsets, batch);
+  else
+    ragged_residual_kernel<false><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, offsets,
+                                                                     batch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ragged_gradient(const double* lam, const double* x, double* ga, double* gb, double* gc,
+                                   const long long* offsets, int batch, cudaStream_t s) {
+  ragged_gradient_kernel<<<ragged_grid(batch), 256, 0, s>>>(lam, x, ga, gb, gc, offsets, batch);
+  return cudaGetLastError();
+}
+
 // Conversion check used by the tests: out[k] = narrow_rn(in[k]) and
 // back[k] = widen(out[k]).
 __global__ void convert_probe_kernel(const double* in, float* out, double* back, size_t count) {

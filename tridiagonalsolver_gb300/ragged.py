@@ -31,7 +31,8 @@ CLASSES = 18            # TRIDIAG_RAGGED_CLASSES: class k holds 2^(k-1) < n <= 2
 VARIANTS = {0: "sequential (thread per system)", 1: "partitioned, 1 CTA x 64", 2: "partitioned, 1 CTA x 128",
             3: "partitioned, 1 CTA x 256", 4: "partitioned, cluster of 2", 5: "partitioned, cluster of 4",
             6: "partitioned, cluster of 8", 7: "unpivoted partition method (systems marked no_pivoting)",
-            8: "unpivoted partition method, chunked (long systems marked no_pivoting)"}
+            8: "unpivoted partition method, chunked (long systems marked no_pivoting)",
+            9: "sequential (thread per system), rows in a workspace: any n"}
 _P = ctypes.c_void_p
 
 
@@ -130,6 +131,39 @@ class RaggedPlan:
         check(st, f"tridiag_ragged_adjoint_{p}")
         return ga, gb, gc, gd
 
+    def refine_workspace(self):
+        """Workspace of :meth:`refine` / :meth:`refine_adjoint` (uint8 tensor)."""
+        nbytes = _sig().tridiag_ragged_refine_workspace_size(self.rows)
+        return torch.empty(nbytes, dtype=torch.uint8, device=self.offsets.device)
+
+    def refine(self, a, b, c, d, iters=1, out=None, work=None, stream=None):
+        """FP64 systems (a, b, c, d float64) solved through this FP32 plan
+        with `iters` FP64-residual refinement steps; returns x (float64)."""
+        if self.precision != 0:
+            raise ValueError("refine runs through an FP32 plan")
+        x = out if out is not None else torch.empty_like(d)
+        work = work if work is not None else self.refine_workspace()
+        D = torch.float64
+        st = _sig().tridiag_ragged_refine_double(self._h, _ptr(a, D), _ptr(b, D), _ptr(c, D), _ptr(d, D),
+                                                 _ptr(x, D), int(iters), _ptr(work), work.numel(),
+                                                 _ptr(self.offsets), _stream_ptr(stream))
+        check(st, "tridiag_ragged_refine_double")
+        return x
+
+    def refine_adjoint(self, a, b, c, x, xbar, iters=1, grads=None, work=None, stream=None):
+        """(ga, gb, gc, gd) in FP64 of L with dL/dx = xbar through x = A^-1 d,
+        lambda = A^-T xbar by the refined solve of A^T through this FP32 plan."""
+        if self.precision != 0:
+            raise ValueError("refine_adjoint runs through an FP32 plan")
+        ga, gb, gc, gd = grads if grads is not None else (torch.empty_like(x) for _ in range(4))
+        work = work if work is not None else self.refine_workspace()
+        D = torch.float64
+        st = _sig().tridiag_ragged_refine_adjoint_double(
+            self._h, _ptr(a, D), _ptr(b, D), _ptr(c, D), _ptr(x, D), _ptr(xbar, D), _ptr(ga, D), _ptr(gb, D),
+            _ptr(gc, D), _ptr(gd, D), int(iters), _ptr(work), work.numel(), _ptr(self.offsets), _stream_ptr(stream))
+        check(st, "tridiag_ragged_refine_adjoint_double")
+        return ga, gb, gc, gd
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -192,7 +226,7 @@ def candidates(precision: int, cls: int):
     out = [0] if hi <= 64 else []
     if lo >= 65:
         out += [v for v in range(1, 7) if variant_max_n(precision, v) >= hi]
-    return out
+    return out or [9]
 
 
 def autotune(classes, dtype=torch.float32, systems_per_class=None, rows_per_class=2 ** 24, seed=0, reps=3,

@@ -1293,6 +1293,19 @@ def profile_case(name: str) -> None:
         torch.cuda.synchronize()
         print("ok block2_64")
         return
+    if name == "ragged_seq64":
+        # variant 9 alone: 64 non-dominant FP64 systems of 40000 rows (102 MB), three solves
+        from tridiagonalsolver_gb300 import ragged
+
+        sizes = np.full(64, 40000, dtype=np.int64)
+        a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=1.0, seed=9)
+        plan = T.RaggedPlan(off, dtype=torch.float64, table={16: 9})
+        x = torch.empty_like(d)
+        for _ in range(3):
+            plan.solve(a, b, c, d, out=x)
+        torch.cuda.synchronize()
+        print("ok", name, [bk for bk in plan.buckets()])
+        return
     if name in ("ragged_step", "ragged64_step", "ragged_refine_step"):
         # the ragged workload (FP32; FP64 plain; FP64 refined through the FP32
         # plan, one step): three forward + adjoint steps, then one between
@@ -1603,7 +1616,7 @@ def main():
                     help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
                          "remaining benchmark configurations, one JSON line each")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step", "ragged64_step",
-                                                                         "ragged_refine_step"], default=None,
+                                                                         "ragged_refine_step", "ragged_seq64"], default=None,
                     help="run one small case of one kernel family three times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.profile_case:

@@ -371,15 +371,19 @@ int tridiag_ragged_plan_create_classify(tridiag_ragged_plan **plan, int precisio
  * system boundaries respected) and an FP32 correction solve, the FP64
  * iterate updated each step.  tridiag_ragged_refine_double writes x;
  * tridiag_ragged_refine_adjoint_double solves A^T lambda = xbar the same way
- * (the FP32 copies are of A^T, so a classifying plan checks A^T's rows) and
+ * (FP32 copies of A^T) and
  * writes gd = lambda and the FP64 gradients ga_i = -lambda_i x_{i-1}, gb_i =
  * -lambda_i x_i, gc_i = -lambda_i x_{i+1} from the forward solution x.  a,
  * b, c, d, xbar are read only.  work: tridiag_ragged_refine_workspace_size()
- * bytes (28 per row); offsets: the device copy of the plan's offsets.  The
+ * bytes (28 per row); offsets: the device copy of the plan's offsets, which
+ * must start at 0 (else TRIDIAG_ERR_INVALID_VALUE).  The
  * FP32 solves see the narrowed coefficients: the result reaches FP64
  * accuracy when the FP32 solve converges the iteration (condition number
- * well below 1 / FP32 epsilon).  A classifying plan32 keeps the marks of its
- * last FP32 solve (of A^T after an adjoint). */
+ * well below 1 / FP32 epsilon).  A classifying plan32 marks the systems by
+ * A's rows in the first FP32 solve of tridiag_ragged_refine_double; its other
+ * FP32 solves, and those of the adjoint (A strictly diagonally dominant by
+ * rows needs no pivoting for A^T either), run on the marks as they stand --
+ * an adjoint on a plan with no marks marks by A's rows first. */
 size_t tridiag_ragged_refine_workspace_size(long long total_rows);
 int tridiag_ragged_refine_double(tridiag_ragged_plan *plan32, const double *a, const double *b, const double *c,
                                  const double *d, double *x, int iters, void *work, size_t work_bytes,

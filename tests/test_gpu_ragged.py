@@ -343,8 +343,8 @@ def test_ragged_autotune_unpivoted(cuda):
         assert eta <= 1e-6
 
 
-@pytest.mark.parametrize("iters", [1, 2])
-def test_ragged_refined_forward_and_adjoint(cuda, iters):
+@pytest.mark.parametrize("iters,shape", [(1, "classes"), (2, "classes"), (1, "short")])
+def test_ragged_refined_forward_and_adjoint(cuda, iters, shape):
     """FP64 ragged systems solved through an FP32 classified plan with FP64
     residual refinement, forward and adjoint: on diagonally dominant systems
     of every size class up to 20000 rows, normwise backward error <= 1e-12 per
@@ -354,7 +354,10 @@ def test_ragged_refined_forward_and_adjoint(cuda, iters):
     from tridiagonalsolver_gb300 import ragged
 
     torch = cuda
-    sizes = _sizes(20000)
+    if shape == "classes":
+        sizes = _sizes(20000)
+    else:  # many boundaries in one 32-row step, and systems across the 2048-row chunks of the row passes
+        sizes = np.array([1] * 40 + [2] * 20 + [3, 5000, 1, 1, 31, 33, 2047, 2049, 4096] + [1] * 33, dtype=np.int64)
     a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=0.0, seed=21)
     plan32 = T.RaggedPlan(off, dtype=torch.float32, classify=True)
     x = plan32.refine(a, b, c, d, iters=iters)

@@ -241,18 +241,27 @@ cudaError_t launch_residual(int layout, const double* a, const double* b, const 
                             const double* xold, const float* dx, double* xnew, float* r32, int n, int batch,
                             cudaStream_t s);
 cudaError_t launch_update(const double* xold, const float* dx, double* xout, size_t count, cudaStream_t s);
-// Ragged batches (offsets, batch systems), one warp per system: FP32 copies
-// of A (trans: of A^T) and of rhs; x_new = x_old + dx and r = rhs - A x_new
-// (trans: A^T) in FP64, r stored as FP32; the adjoint's gradients from
-// lambda and x.
+// Ragged batches (system s = rows [offsets[s], offsets[s+1]) of `rows`
+// packed rows): one warp per RAGGED_ROW_CHUNK rows of the packed arrays,
+// chunk_sys[k] = the system holding row k * RAGGED_ROW_CHUNK (built with the
+// plan).  FP32 copies of A (trans: of A^T) and of rhs; x_new = x_old + dx and
+// r = rhs - A x_new (trans: A^T) in FP64, r stored as FP32; the adjoint's
+// gradients from lambda and x.
+constexpr int RAGGED_ROW_CHUNK = 2048;
+struct RaggedRows {
+  const long long* offsets;
+  int batch;
+  const int* chunk_sys;
+  long long rows;
+};
 cudaError_t launch_ragged_narrow(bool trans, const double* a, const double* b, const double* c, const double* rhs,
-                                 float* a32, float* b32, float* c32, float* r32, const long long* offsets, int batch,
+                                 float* a32, float* b32, float* c32, float* r32, const RaggedRows& rr,
                                  cudaStream_t s);
 cudaError_t launch_ragged_residual(bool trans, const double* a, const double* b, const double* c, const double* rhs,
                                    const double* xold, const float* dx, double* xnew, float* r32,
-                                   const long long* offsets, int batch, cudaStream_t s);
+                                   const RaggedRows& rr, cudaStream_t s);
 cudaError_t launch_ragged_gradient(const double* lam, const double* x, double* ga, double* gb, double* gc,
-                                   const long long* offsets, int batch, cudaStream_t s);
+                                   const RaggedRows& rr, cudaStream_t s);
 cudaError_t launch_convert_probe(const double* in, float* out, double* back, size_t count, cudaStream_t s);
 
 // ipt.cu: Thomas for batch-interleaved systems, P partitions per system

@@ -213,7 +213,10 @@ __global__ void __launch_bounds__(32) ragged_seq_kernel(const T* a, const T* b, 
     fc = fp;
   }
   Rs[n - 1] = x1;
-  T qR[SEQ_U], qU[SEQ_U], qW[SEQ_U], qF[SEQ_U];
+  // (every operand of a row, U2's candidate c_{i+1} and the interchange
+  // word included, is loaded SEQ_U rows ahead: a load on the recurrence
+  // would cost a memory latency per row)
+  T qR[SEQ_U], qU[SEQ_U], qW[SEQ_U], qF[SEQ_U], qC[SEQ_U];
 #pragma unroll
   for (int u = 0; u < SEQ_U; ++u) {
     const int i = n - 2 - u;
@@ -222,14 +225,15 @@ __global__ void __launch_bounds__(32) ragged_seq_kernel(const T* a, const T* b, 
       qU[u] = Us[i];
       qW[u] = Ws[i];
       qF[u] = MODE == 1 && i > 0 ? xf[base + i - 1] : T(0);
+      qC[u] = i + 2 < n ? c[base + i + 1] : T(0);
     }
   }
-  unsigned wcur = 0;
-  int wloaded = -1;
+  int wnext = (n - 2) >> 5;  // word of the next row to finish, and the one after it
+  unsigned wcur = n >= 2 ? pv[wnext] : 0u, wpre = wnext > 0 ? pv[wnext - 1] : 0u;
   for (int i0 = n - 2; i0 >= 0; i0 -= SEQ_U) {
-    T rR[SEQ_U], rU[SEQ_U], rW[SEQ_U], rF[SEQ_U];
+    T rR[SEQ_U], rU[SEQ_U], rW[SEQ_U], rF[SEQ_U], rC[SEQ_U];
 #pragma unroll
-    for (int u = 0; u < SEQ_U; ++u) { rR[u] = qR[u]; rU[u] = qU[u]; rW[u] = qW[u]; rF[u] = qF[u]; }
+    for (int u = 0; u < SEQ_U; ++u) { rR[u] = qR[u]; rU[u] = qU[u]; rW[u] = qW[u]; rF[u] = qF[u]; rC[u] = qC[u]; }
 #pragma unroll
     for (int u = 0; u < SEQ_U; ++u) {
       const int i = i0 - SEQ_U - u;
@@ -238,18 +242,20 @@ __global__ void __launch_bounds__(32) ragged_seq_kernel(const T* a, const T* b, 
         qU[u] = Us[i];
         qW[u] = Ws[i];
         qF[u] = MODE == 1 && i > 0 ? xf[base + i - 1] : T(0);
+        qC[u] = i + 2 < n ? c[base + i + 1] : T(0);
       }
     }
 #pragma unroll
     for (int u = 0; u < SEQ_U; ++u) {
       const int i = i0 - u;
       if (i >= 0) {
-        if ((i >> 5) != wloaded) {
-          wloaded = i >> 5;
-          wcur = pv[wloaded];
+        if ((i >> 5) != wnext) {  // rows of the next word: it was loaded a word ahead
+          wnext = i >> 5;
+          wcur = wpre;
+          wpre = wnext > 0 ? pv[wnext - 1] : 0u;
         }
         const bool sw = (wcur >> (i & 31)) & 1u;
-        const T u2 = sw && i + 2 < n ? c[base + i + 1] : T(0);
+        const T u2 = sw ? rC[u] : T(0);
         T x0 = fma(-rU[u], x1, rR[u]);
         x0 = fma(-u2, x2, x0) * rW[u];
         Rs[i] = x0;
@@ -304,6 +310,7 @@ struct tridiag_ragged_plan {
   int precision = 0;
   int batch = 0;
   long long total_rows = 0;
+  long long row0 = 0;  // offsets[0]
   std::vector<Bucket> buckets;
   int* d_lists = nullptr;
   int device = 0;
@@ -327,6 +334,9 @@ struct tridiag_ragged_plan {
   long long* d_soff = nullptr;
   void* seq_work = nullptr;
   long long seq_rows = 0;
+  // the system holding row k * RAGGED_ROW_CHUNK (the row-parallel passes of
+  // the refined solves)
+  int* d_chunk_sys = nullptr;
   // per class and kind, the list of the class's systems of that kind: its
   // region in d_klists (d_reg[2 k + kind], -1: none) and its length
   // d_kcount[2 k + kind]
@@ -394,6 +404,7 @@ void free_plan(tridiag_ragged_plan* plan) {
   cudaFree(plan->d_tickets);
   cudaFree(plan->d_soff);
   cudaFree(plan->seq_work);
+  cudaFree(plan->d_chunk_sys);
   delete plan;
 }
 
@@ -466,6 +477,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   plan->precision = sizeof(T) == 8 ? 1 : 0;
   plan->batch = batch;
   plan->total_rows = offsets[batch] - offsets[0];
+  plan->row0 = offsets[0];
   plan->kinds_mode = mode;
   plan->unp_max = unpivoted_max_n<T>();
   plan->long_max = (int)long_unpivoted_max_n<T>();
@@ -636,6 +648,20 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     free_plan(plan);
     return TRIDIAG_ERR_CUDA;
   }
+  {
+    std::vector<int> cs((size_t)((plan->total_rows + tdg::RAGGED_ROW_CHUNK - 1) / tdg::RAGGED_ROW_CHUNK));
+    int q = 0;
+    for (size_t k = 0; k < cs.size(); ++k) {
+      const long long r = (long long)k * tdg::RAGGED_ROW_CHUNK;
+      while (offsets[q + 1] <= r) ++q;
+      cs[k] = q;
+    }
+    if (cudaMalloc(&plan->d_chunk_sys, std::max<size_t>(cs.size(), 1) * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(plan->d_chunk_sys, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+      free_plan(plan);
+      return TRIDIAG_ERR_CUDA;
+    }
+  }
   if (seq_rows > 0) {
     plan->seq_rows = seq_rows;
     const size_t wbytes = 2 * (size_t)seq_rows * sizeof(T) + (size_t)seq_rows / 32 * sizeof(unsigned);
@@ -676,15 +702,20 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   return TRIDIAG_SUCCESS;
 }
 
+// recheck (forward solves of a mode-2 plan): the unpivoted kernels check
+// the rows they stage and the marks follow; false: the solve runs on the
+// plan's marks as they stand (marked first, where it has none, by the
+// classify pass on ka, kb, kc -- a, b, c when NULL).
 template <typename T>
 int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const T* c, const T* d, T* x, const T* xf,
-             T* ga, T* gb, T* gc, int* info, const long long* offsets, cudaStream_t s) {
+             T* ga, T* gb, T* gc, int* info, const long long* offsets, cudaStream_t s, bool recheck = true,
+             const T* ka = nullptr, const T* kb = nullptr, const T* kc = nullptr) {
   if (!plan || !a || !b || !c || !d || !x || !offsets) return TRIDIAG_ERR_INVALID_VALUE;
   if (plan->precision != (sizeof(T) == 8 ? 1 : 0)) return TRIDIAG_ERR_INVALID_VALUE;
   if (mode == 1 && (!xf || !ga || !gb || !gc)) return TRIDIAG_ERR_INVALID_VALUE;
   if (plan->n_tickets > 0 && cudaMemsetAsync(plan->d_tickets, 0, plan->n_tickets * sizeof(int), s) != cudaSuccess)
     return TRIDIAG_ERR_CUDA;
-  const bool check = plan->kinds_mode == 2 && mode == 0;
+  const bool check = plan->kinds_mode == 2 && mode == 0 && recheck;
   if (plan->kinds_mode == 2) {
     // every solve starts from the candidates; its unpivoted kernels hand the
     // systems that need pivoting over as they stage them.  (An adjoint with
@@ -702,8 +733,9 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       const int grid = std::min((plan->batch + 7) / 8, sms * 8);
-      ragged_classify_kernel<T><<<grid, 256, 0, s>>>(a, b, c, offsets, plan->batch, plan->d_kinds, plan->d_kinds0,
-                                                     plan->d_reg, plan->d_kcount, plan->d_klists);
+      ragged_classify_kernel<T><<<grid, 256, 0, s>>>(ka ? ka : a, kb ? kb : b, kc ? kc : c, offsets, plan->batch,
+                                                     plan->d_kinds, plan->d_kinds0, plan->d_reg, plan->d_kcount,
+                                                     plan->d_klists);
       if (cudaGetLastError() != cudaSuccess) return TRIDIAG_ERR_CUDA;
     }
     plan->classified = true;
@@ -773,6 +805,7 @@ int ragged_refine_impl(tridiag_ragged_plan* plan32, bool trans, const double* a,
   if (!plan32 || !a || !b || !c || !rhs || !out || !offsets || iters < 0 || iters > 8)
     return TRIDIAG_ERR_INVALID_VALUE;
   if (plan32->precision != 0) return TRIDIAG_ERR_INVALID_VALUE;  // the solves run in FP32
+  if (plan32->row0 != 0) return TRIDIAG_ERR_INVALID_VALUE;       // rows counted from offsets[0] = 0
   const long long rows = plan32->total_rows;
   if (!work || work_bytes < ragged_refine_ws(rows)) return TRIDIAG_ERR_WORKSPACE;
   char* w = static_cast<char*>(work);
@@ -783,19 +816,30 @@ int ragged_refine_impl(tridiag_ragged_plan* plan32, bool trans, const double* a,
   float* v0 = reinterpret_cast<float*>(w + 3 * f);  // FP32 right-hand side / residual
   float* v1 = reinterpret_cast<float*>(w + 4 * f);  // FP32 solution / correction
   double* w64 = reinterpret_cast<double*>(w + 5 * f);
-  const int batch = plan32->batch;
-  if (tdg::launch_ragged_narrow(trans, a, b, c, rhs, a32, b32, c32, v0, offsets, batch, s) != cudaSuccess)
+  const tdg::RaggedRows rr{offsets, plan32->batch, plan32->d_chunk_sys, rows};
+  if (tdg::launch_ragged_narrow(trans, a, b, c, rhs, a32, b32, c32, v0, rr, s) != cudaSuccess)
     return TRIDIAG_ERR_CUDA;
-  int st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s);
+  // The FP32 solves of a classifying plan: the first forward solve marks the
+  // systems by A's rows and the later ones reuse the marks; the solves of A^T
+  // reuse the marks of A as they stand -- A strictly diagonally dominant by
+  // rows needs no pivoting for A^T either (a check of A^T's rows would send
+  // most long systems to the pivoted kernels) -- marking by A's rows first
+  // where the plan has no marks (A's row i = (c32[i-1], b32[i], a32[i+1]) of
+  // the transposed copies).
+  const float* ka = trans ? c32 - 1 : nullptr;
+  const float* kc = trans ? a32 + 1 : nullptr;
+  int st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s,
+                           !trans, ka, b32, kc);
   if (st != TRIDIAG_SUCCESS) return st;
   // the FP64 iterate alternates between w64 and out so that the last step lands in out
   double* xs[2] = {(iters % 2) ? out : w64, (iters % 2) ? w64 : out};
   const double* xcur = nullptr;
   for (int it = 0; it < iters; ++it) {
     double* xnew = xs[it % 2];
-    if (tdg::launch_ragged_residual(trans, a, b, c, rhs, xcur, v1, xnew, v0, offsets, batch, s) != cudaSuccess)
+    if (tdg::launch_ragged_residual(trans, a, b, c, rhs, xcur, v1, xnew, v0, rr, s) != cudaSuccess)
       return TRIDIAG_ERR_CUDA;
-    st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s);
+    st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s,
+                         false, ka, b32, kc);
     if (st != TRIDIAG_SUCCESS) return st;
     xcur = xnew;
   }
@@ -859,7 +903,8 @@ int tridiag_ragged_refine_adjoint_double(tridiag_ragged_plan* plan32, const doub
   const cudaStream_t s = (cudaStream_t)stream;
   const int st = ragged_refine_impl(plan32, true, a, b, c, xbar, gd, iters, work, work_bytes, offsets, s);
   if (st != TRIDIAG_SUCCESS) return st;
-  return tdg::launch_ragged_gradient(gd, x, ga, gb, gc, offsets, plan32->batch, s) == cudaSuccess
+  const tdg::RaggedRows rr{offsets, plan32->batch, plan32->d_chunk_sys, plan32->total_rows};
+  return tdg::launch_ragged_gradient(gd, x, ga, gb, gc, rr, s) == cudaSuccess
              ? TRIDIAG_SUCCESS
              : TRIDIAG_ERR_CUDA;
 }

@@ -169,35 +169,68 @@ cudaError_t launch_update(const double* xold, const float* dx, double* xout, siz
 }
 
 // ---------------------------------------------------------------------------
-// Ragged batches (system s = rows [offsets[s], offsets[s+1])): one warp per
-// system, grid-stride over the systems, lane l holding row i0 + l; the
-// neighbouring rows' values travel by shuffles (the row before a 32-row
-// step by the previous step's lane 31, the row after it by one more load),
-// so every row's x is formed once.  a_0 and c_{n-1} of a system are not
-// read.  TRANS: the coefficients of A^T (sub-diagonal c_{i-1},
-// super-diagonal a_{i+1}).
+// Ragged batches: one warp per RAGGED_ROW_CHUNK rows of the packed arrays,
+// whatever systems they belong to (a warp per system would leave the longest
+// systems' warps running long after the rest), 32 rows per step, lane l on
+// row r0 + l.  The system boundaries inside a step come from the offsets
+// themselves: lane l reads offsets[s + 1 + l] (s = the system holding r0)
+// and a reduction over the warp gives the masks of the step's first and
+// last rows, so a_0, c_{n-1} (TRANS: c_{-1}, a_n) of a system are never
+// read.  x of the neighbouring rows travels by shuffles (lane 0 takes the
+// previous step's lane 31, lane 31 loads row r0 + 32).  TRANS: the
+// coefficients of A^T (sub-diagonal c_{i-1}, super-diagonal a_{i+1}).
 
-__device__ __forceinline__ int ragged_warps() { return (int)(gridDim.x * blockDim.x / 32); }
+// Masks of the first / last rows of their systems among rows [r0, r0 + 32)
+// (bit l: row r0 + l), s the system holding r0; s moves on to the system
+// holding r0 + 32.  Sizes are >= 1, so the boundaries increase strictly and
+// at most 32 of them lie in (r0, r0 + 32].
+__device__ __forceinline__ void ragged_step_masks(const RaggedRows& rr, long long r0, int& s, unsigned& first,
+                                                  unsigned& last) {
+  const int lane = threadIdx.x & 31;
+  const int q = s + 1 + lane;
+  const long long v = q <= rr.batch ? __ldg(rr.offsets + q) : 0x7fffffffffffffffll;
+  const bool f_in = v < r0 + 32, l_in = v <= r0 + 32;  // (v > r0: s holds r0)
+  const unsigned f = __reduce_or_sync(0xffffffffu, f_in ? 1u << (int)(v - r0) : 0u);
+  last = __reduce_or_sync(0xffffffffu, l_in ? 1u << (int)(v - 1 - r0) : 0u);
+  first = f | (__ldg(rr.offsets + s) == r0 ? 1u : 0u);
+  s += __popc(__ballot_sync(0xffffffffu, l_in));
+}
+
+// The warp's chunk: rows [*begin, *end), its first system in *s; false for a
+// warp past the last row.
+__device__ __forceinline__ bool ragged_chunk(const RaggedRows& rr, long long* begin, long long* end, int* s) {
+  const long long k = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  *begin = k * RAGGED_ROW_CHUNK;
+  if (*begin >= rr.rows) return false;
+  *end = min(rr.rows, *begin + RAGGED_ROW_CHUNK);
+  *s = __ldg(rr.chunk_sys + k);
+  return true;
+}
 
 // a, b, c, rhs -> FP32 copies of A (TRANS: of A^T) and of the right-hand side
 template <bool TRANS>
 __global__ void __launch_bounds__(256) ragged_narrow_kernel(const double* __restrict__ a,
                                                             const double* __restrict__ b,
                                                             const double* __restrict__ c,
-                                                            const double* __restrict__ rhs, float* a32, float* b32,
-                                                            float* c32, float* r32, const long long* offsets,
-                                                            int batch) {
+                                                            const double* __restrict__ rhs, float* __restrict__ a32,
+                                                            float* __restrict__ b32, float* __restrict__ c32,
+                                                            float* __restrict__ r32, const RaggedRows rr) {
+  long long begin, end;
+  int s;
+  if (!ragged_chunk(rr, &begin, &end, &s)) return;
   const int lane = threadIdx.x & 31;
-  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += ragged_warps()) {
-    const long long base = offsets[s], n = offsets[s + 1] - base;
-    for (long long i = lane; i < n; i += 32) {
-      const long long k = base + i;
-      const double lo = i > 0 ? (TRANS ? __ldg(c + k - 1) : __ldg(a + k)) : 0.0;
-      const double up = i < n - 1 ? (TRANS ? __ldg(a + k + 1) : __ldg(c + k)) : 0.0;
-      a32[k] = narrow_rn(lo);
-      b32[k] = narrow_rn(__ldg(b + k));
-      c32[k] = narrow_rn(up);
-      r32[k] = narrow_rn(__ldg(rhs + k));
+  for (long long r0 = begin; r0 < end; r0 += 32) {
+    unsigned fm, lm;
+    ragged_step_masks(rr, r0, s, fm, lm);
+    const long long r = r0 + lane;
+    if (r < end) {
+      const bool first = (fm >> lane) & 1u, last = (lm >> lane) & 1u;
+      const double lo = first ? 0.0 : (TRANS ? __ldg(c + r - 1) : __ldg(a + r));
+      const double up = last ? 0.0 : (TRANS ? __ldg(a + r + 1) : __ldg(c + r));
+      a32[r] = narrow_rn(lo);
+      b32[r] = narrow_rn(__ldg(b + r));
+      c32[r] = narrow_rn(up);
+      r32[r] = narrow_rn(__ldg(rhs + r));
     }
   }
 }
@@ -208,31 +241,34 @@ template <bool TRANS>
 __global__ void __launch_bounds__(256) ragged_residual_kernel(
     const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
     const double* __restrict__ rhs, const double* __restrict__ xold, const float* __restrict__ dx,
-    double* __restrict__ xnew, float* __restrict__ r32, const long long* __restrict__ offsets, int batch) {
+    double* __restrict__ xnew, float* __restrict__ r32, const RaggedRows rr) {
+  long long begin, end;
+  int s;
+  if (!ragged_chunk(rr, &begin, &end, &s)) return;
   const int lane = threadIdx.x & 31;
   auto xat = [&](long long k) { return xold ? __ldg(xold + k) + widen(__ldg(dx + k)) : widen(__ldg(dx + k)); };
-  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += ragged_warps()) {
-    const long long base = offsets[s], n = offsets[s + 1] - base;
-    double xlast = 0.0;  // x of the row before this step
-    for (long long i0 = 0; i0 < n; i0 += 32) {
-      const long long i = i0 + lane, k = base + i;
-      const bool in = i < n;
-      const double xi = in ? xat(k) : 0.0;
-      double xm = __shfl_up_sync(0xffffffffu, xi, 1);
-      if (lane == 0) xm = xlast;
-      double xp = __shfl_down_sync(0xffffffffu, xi, 1);
-      if (lane == 31 && i + 1 < n) xp = xat(k + 1);
-      if (in) {
-        const double lo = i > 0 ? (TRANS ? __ldg(c + k - 1) : __ldg(a + k)) : 0.0;
-        const double up = i < n - 1 ? (TRANS ? __ldg(a + k + 1) : __ldg(c + k)) : 0.0;
-        double r = fma(-__ldg(b + k), xi, __ldg(rhs + k));
-        r = fma(-lo, xm, r);
-        r = fma(-up, xp, r);
-        xnew[k] = xi;
-        r32[k] = narrow_rn(r);
-      }
-      xlast = __shfl_sync(0xffffffffu, xi, 31);
+  // x of the row before the chunk (read only where that row is in the same system)
+  double xlast = begin > 0 && __ldg(rr.offsets + s) < begin ? xat(begin - 1) : 0.0;
+  for (long long r0 = begin; r0 < end; r0 += 32) {
+    unsigned fm, lm;
+    ragged_step_masks(rr, r0, s, fm, lm);
+    const long long r = r0 + lane;
+    const bool in = r < end, first = (fm >> lane) & 1u, last = (lm >> lane) & 1u;
+    const double xi = in ? xat(r) : 0.0;
+    double xm = __shfl_up_sync(0xffffffffu, xi, 1);
+    if (lane == 0) xm = xlast;
+    double xp = __shfl_down_sync(0xffffffffu, xi, 1);
+    if (lane == 31 && in && !last) xp = xat(r + 1);
+    if (in) {
+      const double lo = first ? 0.0 : (TRANS ? __ldg(c + r - 1) : __ldg(a + r));
+      const double up = last ? 0.0 : (TRANS ? __ldg(a + r + 1) : __ldg(c + r));
+      double res = fma(-__ldg(b + r), xi, __ldg(rhs + r));
+      res = fma(-lo, xm, res);
+      res = fma(-up, xp, res);
+      xnew[r] = xi;
+      r32[r] = narrow_rn(res);
     }
+    xlast = __shfl_sync(0xffffffffu, xi, 31);
   }
 }
 
@@ -240,64 +276,65 @@ __global__ void __launch_bounds__(256) ragged_residual_kernel(
 // ga_i = -lambda_i x_{i-1} (0 at a system's first row), gb_i = -lambda_i
 // x_i, gc_i = -lambda_i x_{i+1} (0 at its last row).
 __global__ void __launch_bounds__(256) ragged_gradient_kernel(const double* __restrict__ lam,
-                                                              const double* __restrict__ x, double* ga, double* gb,
-                                                              double* gc, const long long* __restrict__ offsets,
-                                                              int batch) {
+                                                              const double* __restrict__ x, double* __restrict__ ga,
+                                                              double* __restrict__ gb, double* __restrict__ gc,
+                                                              const RaggedRows rr) {
+  long long begin, end;
+  int s;
+  if (!ragged_chunk(rr, &begin, &end, &s)) return;
   const int lane = threadIdx.x & 31;
-  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); s < batch; s += ragged_warps()) {
-    const long long base = offsets[s], n = offsets[s + 1] - base;
-    double xlast = 0.0;
-    for (long long i0 = 0; i0 < n; i0 += 32) {
-      const long long i = i0 + lane, k = base + i;
-      const bool in = i < n;
-      const double xi = in ? __ldg(x + k) : 0.0;
-      double xm = __shfl_up_sync(0xffffffffu, xi, 1);
-      if (lane == 0) xm = xlast;
-      double xp = __shfl_down_sync(0xffffffffu, xi, 1);
-      if (lane == 31 && i + 1 < n) xp = __ldg(x + k + 1);
-      if (in) {
-        const double l = -__ldg(lam + k);
-        ga[k] = i > 0 ? l * xm : 0.0;
-        gb[k] = l * xi;
-        gc[k] = i < n - 1 ? l * xp : 0.0;
-      }
-      xlast = __shfl_sync(0xffffffffu, xi, 31);
+  double xlast = begin > 0 && __ldg(rr.offsets + s) < begin ? __ldg(x + begin - 1) : 0.0;
+  for (long long r0 = begin; r0 < end; r0 += 32) {
+    unsigned fm, lm;
+    ragged_step_masks(rr, r0, s, fm, lm);
+    const long long r = r0 + lane;
+    const bool in = r < end, first = (fm >> lane) & 1u, last = (lm >> lane) & 1u;
+    const double xi = in ? __ldg(x + r) : 0.0;
+    double xm = __shfl_up_sync(0xffffffffu, xi, 1);
+    if (lane == 0) xm = xlast;
+    double xp = __shfl_down_sync(0xffffffffu, xi, 1);
+    if (lane == 31 && in && !last) xp = __ldg(x + r + 1);
+    if (in) {
+      const double l = -__ldg(lam + r);
+      ga[r] = first ? 0.0 : l * xm;
+      gb[r] = l * xi;
+      gc[r] = last ? 0.0 : l * xp;
     }
+    xlast = __shfl_sync(0xffffffffu, xi, 31);
   }
 }
 
-static int ragged_grid(int batch) {
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int want = (batch + 7) / 8;  // eight warps per 256-thread block
-  return want < sms * 8 ? (want > 0 ? want : 1) : sms * 8;
+static int ragged_grid(const RaggedRows& rr) {
+  const long long chunks = (rr.rows + RAGGED_ROW_CHUNK - 1) / RAGGED_ROW_CHUNK;
+  return (int)((chunks + 7) / 8);  // eight warps (chunks) per 256-thread block
 }
 
 cudaError_t launch_ragged_narrow(bool trans, const double* a, const double* b, const double* c, const double* rhs,
-                                 float* a32, float* b32, float* c32, float* r32, const long long* offsets, int batch,
+                                 float* a32, float* b32, float* c32, float* r32, const RaggedRows& rr,
                                  cudaStream_t s) {
+  if (rr.rows <= 0) return cudaSuccess;
   if (trans)
-    ragged_narrow_kernel<true><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, a32, b32, c32, r32, offsets, batch);
+    ragged_narrow_kernel<true><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, a32, b32, c32, r32, rr);
   else
-    ragged_narrow_kernel<false><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, a32, b32, c32, r32, offsets, batch);
+    ragged_narrow_kernel<false><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, a32, b32, c32, r32, rr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ragged_residual(bool trans, const double* a, const double* b, const double* c, const double* rhs,
                                    const double* xold, const float* dx, double* xnew, float* r32,
-                                   const long long* offsets, int batch, cudaStream_t s) {
+                                   const RaggedRows& rr, cudaStream_t s) {
+  if (rr.rows <= 0) return cudaSuccess;
   if (trans)
-    ragged_residual_kernel<true><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, offsets, batch);
+    ragged_residual_kernel<true><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, rr);
   else
-    ragged_residual_kernel<false><<<ragged_grid(batch), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, offsets,
-                                                                     batch);
+    ragged_residual_kernel<false><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, rr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ragged_gradient(const double* lam, const double* x, double* ga, double* gb, double* gc,
-                                   const long long* offsets, int batch, cudaStream_t s) {
-  ragged_gradient_kernel<<<ragged_grid(batch), 256, 0, s>>>(lam, x, ga, gb, gc, offsets, batch);
+                                   const RaggedRows& rr, cudaStream_t s) {
+  if (rr.rows <= 0) return cudaSuccess;
+  ragged_gradient_kernel<<<ragged_grid(rr), 256, 0, s>>>(lam, x, ga, gb, gc, rr);
   return cudaGetLastError();
 }
 

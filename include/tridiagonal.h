@@ -322,8 +322,11 @@ int tridiag_partition_adjoint_double(int layout, const double *a, const double *
  * partitioned solve in one CTA with 64/128/256 partitions, 4/5/6 = in a
  * cluster of 2/4/8 CTAs, 9 = thread-per-system sequential partial pivoting
  * with the eliminated rows in a plan workspace (any n; 2 values + 1 bit per
- * row of its classes; the default where no partitioned variant serves the
- * class: FP64 beyond 27648 rows, FP32 beyond 65536).  variant_by_class (may
+ * row of its classes), 10 = the partitioned solve in chunks of 4224 rows (one
+ * CTA each) with the separators' systems solved in between, each chunk's
+ * result checked and a failing system re-solved by 9 (the default where no
+ * one-CTA or cluster variant serves the class: FP64 beyond 27648 rows, FP32
+ * beyond 65536; ~0.15 values of workspace per row besides 9's).  variant_by_class (may
  * be NULL; entries < 0 mean "default") overrides the choice per class -- the
  * autotuner's output; an entry that cannot serve its class's sizes makes the
  * call return TRIDIAG_ERR_NOT_SUPPORTED.

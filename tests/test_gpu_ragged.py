@@ -410,12 +410,14 @@ def test_ragged_sequential_variant(cuda, dtype_name):
         _check_system(hs, grads, n, not nondom[s], ETA[dtype_name], GTOL[dtype_name])
 
 
+@pytest.mark.parametrize("variant", [10, 9])
 @pytest.mark.parametrize("routing", ["pivoted", "classify"])
-def test_ragged_fp64_beyond_clusters(cuda, routing):
+def test_ragged_fp64_beyond_clusters(cuda, routing, variant):
     """FP64 systems longer than the clusters serve (27648 rows) go to variant
-    9 by default; with the library classifying, the dominant ones run the
-    chunked unpivoted method and the others reach variant 9 through the
-    class's device-grown list.  Every system checked, forward and adjoint."""
+    10 (chunks of 4224 rows) by default, or to variant 9 by the table; with
+    the library classifying, the dominant ones run the chunked unpivoted
+    method and the others reach the pivoted bucket through the class's
+    device-grown list.  Every system checked, forward and adjoint."""
     import tridiagonalsolver_gb300 as T
     from tridiagonalsolver_gb300 import ragged
 
@@ -423,8 +425,9 @@ def test_ragged_fp64_beyond_clusters(cuda, routing):
     sizes = np.array([40000, 65536, 27649, 33000, 50000, 30001, 100, 3000, 20000, 64], dtype=np.int64)
     a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=0.5, seed=32)
     assert nondom[sizes > 27648].any() and (~nondom[sizes > 27648]).any()
-    plan = T.RaggedPlan(off, dtype=torch.float64, classify=routing == "classify")
-    assert 9 in {v for _, v, _, _ in plan.buckets()}
+    table = None if variant == 10 else {15: 9, 16: 9}
+    plan = T.RaggedPlan(off, dtype=torch.float64, table=table, classify=routing == "classify")
+    assert variant in {v for _, v, _, _ in plan.buckets()}
     info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
     x = plan.solve(a, b, c, d, info=info)
     w = torch.rand_like(d) * 2 - 1
@@ -439,3 +442,65 @@ def test_ragged_fp64_beyond_clusters(cuda, routing):
         hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
         grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
         _check_system(hs, grads, n, not nondom[s], ETA["float64"], GTOL["float64"])
+
+
+@pytest.mark.parametrize("dtype_name", ["float32", "float64"])
+def test_ragged_chunked_variant(cuda, dtype_name):
+    """Variant 10 (the partitioned solve in chunks of 4224 rows, the
+    separators' systems in between) forced on every class above 2048 rows,
+    sizes around the chunk boundaries: forward and adjoint of dominant and
+    non-dominant systems against the oracle (FP32 systems whose chunk misses
+    its bound are re-solved by variant 9)."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    dt = getattr(torch, dtype_name)
+    top = 65536 if dtype_name == "float32" else 27648
+    sizes = np.array([s for s in _sizes(top) if s > 2048] + [4224, 4225, 8448, 8449, 12000, 300], dtype=np.int64)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=dt, nondominant_fraction=0.4, seed=33)
+    table = {k: 10 for k in range(12, ragged.CLASSES)}
+    plan = T.RaggedPlan(off, dtype=dt, table=table)
+    assert {v for cls, v, _, _ in plan.buckets() if cls >= 12} == {10}
+    info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+    x = plan.solve(a, b, c, d, info=info)
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    assert int((info != 0).sum()) == 0
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], ETA[dtype_name], GTOL[dtype_name])
+
+
+def test_ragged_chunked_flagged_system_resolved(cuda):
+    """A singular interior block in chunk 2 of one system (a partition's first
+    row with zero diagonal and superdiagonal; the matrix is regular): that
+    chunk misses its bound, the system is re-solved by variant 9, the others
+    keep the chunks' result; forward and adjoint against the oracle."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = np.array([40000, 30000, 50000, 100], dtype=np.int64)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=1.0, seed=34)
+    r = int(off[1]) + 2 * 128 * 33 + 5 * 33
+    b[r], c[r], a[r] = 0.0, 0.0, 1.0
+    plan = T.RaggedPlan(off, dtype=torch.float64)
+    assert 10 in {v for _, v, _, _ in plan.buckets()}
+    T.lib().tridiag_partition_fallbacks(1)
+    info = torch.full((len(sizes),), -7, dtype=torch.int32, device="cuda")
+    x = plan.solve(a, b, c, d, info=info)
+    torch.cuda.synchronize()
+    assert T.lib().tridiag_partition_fallbacks(1) >= 1
+    assert int((info != 0).sum()) == 0
+    w = torch.rand_like(d) * 2 - 1
+    ga, gb, gc, gd = plan.adjoint(a, b, c, x, w)
+    torch.cuda.synchronize()
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, False, ETA["float64"], GTOL["float64"])

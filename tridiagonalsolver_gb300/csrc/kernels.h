@@ -227,6 +227,19 @@ cudaError_t launch_relayout(int from, int to, const T* const src[4], T* const ds
 // flag: batch ints.  *used = false when n is not covered.
 template <typename T>
 bool pge_long_eligible(int n);
+// Ragged long systems in chunks of pge_long_chunk_rows() rows (see pge.cu):
+// the largest n the separators' systems allow, and the passes of one size
+// bucket (chunk entries cl_sys / cl_ch over the bucket's class; separator
+// rows of system s at sep_off[s]; flag[s] set where a chunk fails).
+int pge_long_chunk_rows();
+template <typename T>
+int pge_long_ragged_max_n();
+template <typename T>
+cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* d, T* x, const long long* offsets,
+                                   const int* cl_sys, const int* cl_ch, int C, const long long* sep_off,
+                                   size_t sep_total, T* sep, T* xsep, T* carry, int* flag, int sep_variant,
+                                   int sep_m_max, const int* list, int count, const BucketTicket* tk,
+                                   cudaStream_t s);
 template <typename T>
 cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info, int n, int batch, T* w1, T* w2,
                             unsigned* piv, int* flag, cudaStream_t s, bool* used);

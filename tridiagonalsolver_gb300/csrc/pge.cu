@@ -260,6 +260,15 @@ struct PgeIO {
   T* carry;      // [batch][nchunks][4]: Y, V, W of partition 0's first row, c of the last separator row
   const T* xsep;  // [batch][nchunks NT]: the separators (MODE 3)
   int* flag;     // [batch]: MODE 3 sets 1 where a separator row misses its bound
+  // ragged chunked systems (cl_sys non-NULL): CTA b is chunk cl_ch[b] of
+  // system cl_sys[b] (rows [offsets[s], offsets[s+1])), whose separator rows
+  // start at row sep_off[s] of the separator arrays (sep_total rows each) and
+  // its chunks' carries at sep_off[s] / NT; systems with kinds[s] != want
+  // are skipped
+  const int* cl_sys;
+  const int* cl_ch;
+  const long long* sep_off;
+  size_t sep_total;
   // size buckets of a ragged batch served by resident CTAs (clusters): each
   // takes the next entry of list[0 .. count) -- count from *dcount where a
   // device pass wrote the list -- from the ticket counter (zero before the
@@ -372,15 +381,31 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   int sys, n, m, ms;
   size_t base;
   int ch = 0;                       // chunk of a long system (MODE 2 / 3)
+  size_t sq = 0;                    // its first separator row in io.sep / io.xsep
   bool zero_a0 = true, zero_cl = true;  // this CTA holds the system's first / last row
   if constexpr (MODE >= 2) {
-    sys = bid / io.nchunks;
-    ch = bid % io.nchunks;
-    base = (size_t)sys * io.stride + (size_t)ch * io.chunk_rows;
-    n = min(io.chunk_rows, io.n - ch * io.chunk_rows);
+    int nch;
+    if (io.cl_sys) {
+      sys = io.cl_sys[bid];
+      ch = io.cl_ch[bid];
+      if (io.kinds && io.kinds[sys] != io.want) return;  // (the whole CTA)
+      const long long s0 = io.offsets[sys];
+      const int nsys = (int)(io.offsets[sys + 1] - s0);
+      nch = (nsys + io.chunk_rows - 1) / io.chunk_rows;
+      base = (size_t)s0 + (size_t)ch * io.chunk_rows;
+      n = min(io.chunk_rows, nsys - ch * io.chunk_rows);
+      sq = (size_t)io.sep_off[sys];
+    } else {
+      sys = bid / io.nchunks;
+      ch = bid % io.nchunks;
+      nch = io.nchunks;
+      base = (size_t)sys * io.stride + (size_t)ch * io.chunk_rows;
+      n = min(io.chunk_rows, io.n - ch * io.chunk_rows);
+      sq = (size_t)sys * io.nchunks * NT;
+    }
     m = ms = io.chunk_rows / NT;  // odd (the launch's choice)
     zero_a0 = ch == 0;
-    zero_cl = ch == io.nchunks - 1;
+    zero_cl = ch == nch - 1;
   } else {
     pge_system(io, bid, NT, sys, base, n, m, ms);
   }
@@ -649,13 +674,13 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
       // a long system's chunk: its separator rows go to the system-wide
       // separator system; the last one still lacks the next chunk's first
       // row (added by pge_long_link from `carry`)
-      const size_t ptot = (size_t)io.nchunks * NT, bsz = ptot * gridDim.x / io.nchunks;
-      const size_t q = (size_t)sys * ptot + (size_t)ch * NT + t;
+      const size_t bsz = io.sep_total;
+      const size_t q = sq + (size_t)ch * NT + t;
       io.sep[q] = SEP[t];
       io.sep[bsz + q] = SEP[NT + t];
       io.sep[2 * bsz + q] = SEP[2 * NT + t];
       io.sep[3 * bsz + q] = SEP[3 * NT + t];
-      T* cy_ = io.carry + ((size_t)sys * io.nchunks + ch) * 4;
+      T* cy_ = io.carry + (sq / NT + ch) * 4;
       if (t == 0) {
         cy_[0] = FST[0];
         cy_[1] = FST[NT];
@@ -668,7 +693,7 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   __syncthreads();
   if constexpr (MODE == 3) {
     // the separators from the system-wide solve
-    FST[t] = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT + t];
+    FST[t] = io.xsep[sq + (size_t)ch * NT + t];
   } else {
   // Parallel cyclic reduction of the separator system (SEP[0..4NT) keeps the
   // original rows, SEP[4NT..12NT) is the ping-pong pair) ...  Thread t owns
@@ -749,7 +774,7 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   T sp = t > 0 ? FST[t - 1] : T(0);
   if constexpr (MODE == 3)
     if (t == 0 && ch > 0) {
-      sp = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)ch * NT - 1];
+      sp = io.xsep[sq + (size_t)ch * NT - 1];
       s_xprev = sp;  // (the previous chunk's last row is its last separator)
     }
   const T st = FST[t];
@@ -792,8 +817,8 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     if constexpr (MODE == 3) {
       if (t + 1 == NT && !zero_cl) {
         // the next chunk's first row: x = Y - V s_t - W s_{t+1}
-        const T* cy_ = io.carry + ((size_t)sys * io.nchunks + ch + 1) * 4;
-        const T s_next = io.xsep[(size_t)sys * io.nchunks * NT + (size_t)(ch + 1) * NT];
+        const T* cy_ = io.carry + (sq / NT + ch + 1) * 4;
+        const T s_next = io.xsep[sq + (size_t)(ch + 1) * NT];
         x_next = fma(-cy_[2], s_next, fma(-cy_[1], st, cy_[0]));
         s_xnext = x_next;
       }
@@ -1745,6 +1770,7 @@ cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info,
   io.carry = carry;
   io.xsep = xsep;
   io.flag = flag;
+  io.sep_total = bsz;
   const size_t smem = pge_smem_bytes<T, PGE_LONG_NT>(PGE_LONG_M);
   const PgeMaps maps{};
   const int grid = batch * nchunks;
@@ -1775,6 +1801,92 @@ cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info,
   // the flagged systems: sequential partial pivoting in place on d (their
   // right-hand side is still there), w1/w2 now free for its factors
   return launch_gtsv_seq_masked<T>(a, b, c, d, w1, w2, piv, info, n, batch, flag, s);
+}
+
+// Ragged long systems in chunks (the passes above, per system of a size
+// bucket of a ragged batch): C chunk entries (cl_sys, cl_ch) cover every
+// system of the bucket's size class, the passes skip the systems with
+// kinds[s] != want; separator rows of system s at sep_off[s] (sep_total rows
+// per array), the separators' systems solved by the partitioned solve of
+// variant sep_variant on their ragged offsets (sep_off, the bucket's list,
+// count / *dcount entries, ticket); x is written to x, and flag[s] set where
+// a chunk misses its bound (the caller re-solves those).
+constexpr int PGE_LONG_ROWS = PGE_LONG_NT * PGE_LONG_M;
+
+template <typename T>
+__global__ void __launch_bounds__(256) pge_long_link_ragged(T* sep, const T* carry, const int* cl_sys,
+                                                            const int* cl_ch, int C, const long long* offsets,
+                                                            const long long* sep_off, size_t sep_total,
+                                                            const unsigned char* kinds, int want) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= C) return;
+  const int sys = cl_sys[k], ch = cl_ch[k];
+  if (kinds && kinds[sys] != want) return;
+  const int nch = (int)((offsets[sys + 1] - offsets[sys] + PGE_LONG_ROWS - 1) / PGE_LONG_ROWS);
+  if (ch + 1 >= nch) return;
+  const size_t sq = (size_t)sep_off[sys];
+  const T cs = carry[(sq / PGE_LONG_NT + ch) * 4 + 3];  // c of chunk ch's last separator row
+  const T* f = carry + (sq / PGE_LONG_NT + ch + 1) * 4;  // Y, V, W of chunk ch+1's first row
+  const size_t q = sq + (size_t)(ch + 1) * PGE_LONG_NT - 1;
+  sep[sep_total + q] = fma(-cs, f[1], sep[sep_total + q]);
+  sep[2 * sep_total + q] = -cs * f[2];
+  sep[3 * sep_total + q] = fma(-cs, f[0], sep[3 * sep_total + q]);
+}
+
+int pge_long_chunk_rows() { return PGE_LONG_ROWS; }
+
+template <typename T>
+int pge_long_ragged_max_n() {
+  // the separators' system (PGE_LONG_NT rows per chunk) within one partitioned variant
+  int best = 0;
+  for (int v = 1; v <= 6; ++v) best = std::max(best, pge_variant_max_n<T>(v));
+  const long long n = (long long)(best / PGE_LONG_NT) * PGE_LONG_ROWS;
+  return pge_smem_bytes<T, PGE_LONG_NT>(PGE_LONG_M) <= PGE_SMEM_MAX ? (int)std::min<long long>(n, 1 << 30) : 0;
+}
+
+template <typename T>
+cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* d, T* x, const long long* offsets,
+                                   const int* cl_sys, const int* cl_ch, int C, const long long* sep_off,
+                                   size_t sep_total, T* sep, T* xsep, T* carry, int* flag, int sep_variant,
+                                   int sep_m_max, const int* list, int count, const BucketTicket* tk,
+                                   cudaStream_t s) {
+  if (C <= 0 || count <= 0) return cudaSuccess;
+  PgeIO<T> io{};
+  io.a = a;
+  io.b = b;
+  io.c = c;
+  io.d = d;
+  io.offsets = offsets;
+  io.err = error_word();
+  io.chunk_rows = PGE_LONG_ROWS;
+  io.sep = sep;
+  io.carry = carry;
+  io.xsep = xsep;
+  io.flag = flag;
+  io.cl_sys = cl_sys;
+  io.cl_ch = cl_ch;
+  io.sep_off = sep_off;
+  io.sep_total = sep_total;
+  io.kinds = tk ? tk->kinds : nullptr;
+  io.want = tk ? tk->want : 0;
+  const size_t smem = pge_smem_bytes<T, PGE_LONG_NT>(PGE_LONG_M);
+  const PgeMaps maps{};
+  cudaError_t e = cudaFuncSetAttribute(pge_kernel<T, PGE_LONG_NT, 2, PGE_DENSE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(pge_kernel<T, PGE_LONG_NT, 3, PGE_DENSE>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  pge_kernel<T, PGE_LONG_NT, 2, PGE_DENSE><<<C, PGE_LONG_NT, smem, s>>>(io, maps);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  pge_long_link_ragged<T><<<(C + 255) / 256, 256, 0, s>>>(sep, carry, cl_sys, cl_ch, C, offsets, sep_off, sep_total,
+                                                         io.kinds, io.want);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  e = launch_pge_ragged<T>(sep_variant, 0, sep, sep + sep_total, sep + 2 * sep_total, sep + 3 * sep_total, xsep,
+                           nullptr, nullptr, nullptr, nullptr, nullptr, sep_off, list, count, sep_m_max, s, tk);
+  if (e != cudaSuccess) return e;
+  io.x = x;
+  pge_kernel<T, PGE_LONG_NT, 3, PGE_DENSE><<<C, PGE_LONG_NT, smem, s>>>(io, maps);
+  return cudaGetLastError();
 }
 
 template <typename T>
@@ -1870,6 +1982,10 @@ cudaError_t pge_path_counts(unsigned long long* out, bool reset) {
   template cudaError_t launch_pge<T>(int, const T*, const T*, const T*, const T*, T*, int*, int, int, cudaStream_t, \
                                      bool*);                                                                      \
   template bool pge_long_eligible<T>(int);                                                                        \
+  template int pge_long_ragged_max_n<T>();                                                                        \
+  template cudaError_t launch_pge_long_ragged<T>(const T*, const T*, const T*, const T*, T*, const long long*,      \
+                                                 const int*, const int*, int, const long long*, size_t, T*, T*, T*, \
+                                                 int*, int, int, const int*, int, const BucketTicket*, cudaStream_t);   \
   template cudaError_t launch_pge_long<T>(const T*, const T*, const T*, T*, int*, int, int, T*, T*, unsigned*, int*, \
                                           cudaStream_t, bool*);                                                   \
   template cudaError_t launch_pge_strided<T>(const T*, const T*, const T*, const T*, T*, int*, int, int, size_t,  \

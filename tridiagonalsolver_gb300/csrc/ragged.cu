@@ -7,7 +7,10 @@
 // solve for n < 65 (variant 0), the partitioned solve with 64/128/256
 // partitions in one CTA (1-3) or in a cluster of 2/4/8 CTAs (4-6), and the
 // thread-per-system sequential solve with its rows in a workspace for sizes
-// beyond every partitioned variant (9: FP64 beyond 27648 rows).  A
+// beyond every partitioned variant (9), or -- the default there -- the
+// partitioned solve in chunks of 4224 rows with the separators' systems in
+// between (10: FP64 beyond 27648 rows), which re-solves a system by 9 when
+// a chunk misses its accuracy bound.  A
 // variant table (from the autotuner, or the defaults) overrides the choice
 // per class.  Systems that need no pivoting -- marked by the caller, or
 // found by the library itself -- run the unpivoted partition method in
@@ -127,11 +130,15 @@ __global__ void __launch_bounds__(32) ragged_seq_kernel(const T* a, const T* b, 
                                                         const T* xf, T* ga, T* gb, T* gc, int* info,
                                                         const long long* offsets, const int* list, int count,
                                                         const int* dcount, const long long* soff, T* w1, T* w2,
-                                                        unsigned* piv) {
+                                                        unsigned* piv, const int* flag) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int live = dcount ? min(*dcount, count) : count;
   if (k >= live) return;
   const int sys = list[k];
+  if (flag && !flag[sys]) {  // (variant 10's re-solve: only the systems a chunk failed)
+    if (info) info[sys] = 0;
+    return;
+  }
   const long long base = offsets[sys];
   const int n = (int)(offsets[sys + 1] - base);
   const long long so = soff[sys];
@@ -277,17 +284,46 @@ template <typename T>
 static cudaError_t launch_ragged_seq(int mode, const T* a, const T* b, const T* c, const T* d, T* x, const T* xf,
                                      T* ga, T* gb, T* gc, int* info, const long long* offsets, const int* list,
                                      int count, const int* dcount, const long long* soff, T* w1, T* w2,
-                                     unsigned* piv, cudaStream_t s) {
+                                     unsigned* piv, const int* flag, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   // one warp per block: the few long systems spread over all SMs
   const int grid = (count + 31) / 32;
   if (mode == 0)
     ragged_seq_kernel<T, 0><<<grid, 32, 0, s>>>(a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, count, dcount,
-                                                soff, w1, w2, piv);
+                                                soff, w1, w2, piv, flag);
   else
     ragged_seq_kernel<T, 1><<<grid, 32, 0, s>>>(c - 1, b, a + 1, d, x, xf, ga, gb, gc, info, offsets, list, count,
-                                                dcount, soff, w1, w2, piv);
+                                                dcount, soff, w1, w2, piv, flag);
   return cudaGetLastError();
+}
+
+// Gradients of variant 10's adjoint from lambda and the forward solution
+// xf, one warp per chunk entry (system cl_sys[k], rows [cl_ch[k] CR,
+// (cl_ch[k] + 1) CR)), skipping the systems of the other kind and those a
+// chunk failed (re-solved with their gradients by variant 9).
+template <typename T>
+__global__ void __launch_bounds__(256) ragged_chunk_gradient_kernel(const T* __restrict__ lam,
+                                                                    const T* __restrict__ xf, T* __restrict__ ga,
+                                                                    T* __restrict__ gb, T* __restrict__ gc,
+                                                                    const long long* __restrict__ offsets,
+                                                                    const int* __restrict__ cl_sys,
+                                                                    const int* __restrict__ cl_ch, int C, int CR,
+                                                                    const unsigned char* kinds, int want,
+                                                                    const int* flag) {
+  const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / 32);
+  const int lane = threadIdx.x & 31;
+  if (k >= C) return;
+  const int sys = cl_sys[k];
+  if ((kinds && kinds[sys] != want) || flag[sys]) return;
+  const long long s0 = offsets[sys];
+  const long long n = offsets[sys + 1] - s0;
+  const long long lo = (long long)cl_ch[k] * CR, hi = min(n, lo + CR);
+  for (long long i = lo + lane; i < hi; i += 32) {
+    const T l = -lam[s0 + i];
+    ga[s0 + i] = i > 0 ? l * xf[s0 + i - 1] : T(0);
+    gb[s0 + i] = l * xf[s0 + i];
+    gc[s0 + i] = i + 1 < n ? l * xf[s0 + i + 1] : T(0);
+  }
 }
 
 }  // namespace tdg
@@ -306,6 +342,11 @@ struct tridiag_ragged_plan {
     int ticket;       // -1: one CTA (cluster) per list entry; else index of its ticket counter
     int klist;        // -1: list in d_lists; else 2 k + kind: the kind list in d_klists
     size_t klist_off;
+    // variant 10: the bucket's chunk entries (cl_off .. cl_off + cl_count in
+    // d_cl), the separators' systems' variant and rows per partition
+    size_t cl_off = 0;
+    int cl_count = 0;
+    int sep_variant = 0, sep_m_max = 0;
   };
   int precision = 0;
   int batch = 0;
@@ -334,6 +375,18 @@ struct tridiag_ragged_plan {
   long long* d_soff = nullptr;
   void* seq_work = nullptr;
   long long seq_rows = 0;
+  // variant 10: chunk entries (system, chunk) of its buckets ([2][n_cl]),
+  // each system's first separator row (batch + 1 entries: its separators'
+  // system is rows [d_sep_off[s], d_sep_off[s+1])), the separator arrays
+  // (4 x sep_total, then x of the separators, then 4 carries per chunk) and
+  // per system whether a chunk missed its bound (its systems also have
+  // variant 9's workspace, for the re-solve)
+  int* d_cl = nullptr;
+  size_t n_cl = 0;
+  long long* d_sep_off = nullptr;
+  long long sep_total = 0;
+  void* sep_work = nullptr;
+  int* d_flag = nullptr;
   // the system holding row k * RAGGED_ROW_CHUNK (the row-parallel passes of
   // the refined solves)
   int* d_chunk_sys = nullptr;
@@ -362,6 +415,7 @@ int size_class(long long n) {
 constexpr int RAGGED_UNPIVOTED = 7;
 constexpr int RAGGED_UNPIVOTED_LONG = 8;
 constexpr int RAGGED_SEQUENTIAL = 9;
+constexpr int RAGGED_CHUNKED = 10;
 
 template <typename T>
 int unpivoted_max_n() {
@@ -386,6 +440,7 @@ bool variant_serves(int v, int max_n) {
   if (v == 0) return max_n <= tdg::RAGGED_TINY_MAX;
   if (v == RAGGED_UNPIVOTED) return max_n <= unpivoted_max_n<T>();
   if (v == RAGGED_SEQUENTIAL) return max_n >= 2;
+  if (v == RAGGED_CHUNKED) return max_n > 64 && max_n <= tdg::pge_long_ragged_max_n<T>();
   return max_n >= 65 && max_n <= tdg::pge_variant_max_n<T>(v);
 }
 
@@ -403,6 +458,10 @@ void free_plan(tridiag_ragged_plan* plan) {
   cudaFree(plan->d_kinds);
   cudaFree(plan->d_tickets);
   cudaFree(plan->d_soff);
+  cudaFree(plan->d_cl);
+  cudaFree(plan->d_sep_off);
+  cudaFree(plan->sep_work);
+  cudaFree(plan->d_flag);
   cudaFree(plan->seq_work);
   cudaFree(plan->d_chunk_sys);
   delete plan;
@@ -492,6 +551,9 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   std::vector<unsigned char> kinds(batch, 0);  // (1: a candidate of kind 1)
   std::vector<long long> soff(batch, -1);      // variant 9 workspace rows
   long long seq_rows = 0;
+  std::vector<int> cl_sys, cl_ch;                 // variant 10 chunk entries
+  std::vector<long long> sep_rows(batch, 0);      // variant 10 separator rows per system
+  const int CR = tdg::pge_long_chunk_rows();
   for (int k = 0; k < TRIDIAG_RAGGED_CLASSES; ++k) {
     auto& sys = by_class[k];
     if (sys.empty()) continue;
@@ -522,12 +584,34 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       v = table[k];
     }
     if (v < 0) v = max_n <= tdg::RAGGED_TINY_MAX ? 0 : tdg::pge_default_variant<T>(max_n);
-    if (v == 0 && max_n > tdg::RAGGED_TINY_MAX) v = RAGGED_SEQUENTIAL;  // beyond every partitioned variant
-    if (v == RAGGED_SEQUENTIAL)
+    if (v == 0 && max_n > tdg::RAGGED_TINY_MAX)  // beyond every partitioned variant
+      v = variant_serves<T>(RAGGED_CHUNKED, max_n) ? RAGGED_CHUNKED : RAGGED_SEQUENTIAL;
+    if (v == RAGGED_SEQUENTIAL || v == RAGGED_CHUNKED)  // (variant 10 re-solves a failing system by 9)
       for (int q : sys) {
         soff[q] = seq_rows;
         seq_rows += (len(q) + 31) / 32 * 32;
       }
+    size_t cl_off = cl_sys.size();
+    int sep_variant = 0, sep_m_max = 0;
+    if (v == RAGGED_CHUNKED) {
+      for (int q : sys) {
+        const int nch = (int)((len(q) + CR - 1) / CR);
+        sep_rows[q] = (long long)nch * 128;
+        for (int c = 0; c < nch; ++c) {
+          cl_sys.push_back(q);
+          cl_ch.push_back(c);
+        }
+      }
+      const int max_sep = (int)((max_n + CR - 1) / CR) * 128;
+      sep_variant = tdg::pge_default_variant<T>(max_sep);
+      if (sep_variant <= 0) {
+        free_plan(plan);
+        return TRIDIAG_ERR_NOT_SUPPORTED;
+      }
+      sep_m_max = std::max(2, (max_sep + tdg::pge_variant_partitions(sep_variant) - 1) /
+                                  tdg::pge_variant_partitions(sep_variant));
+    }
+    const size_t cl_count = cl_sys.size() - cl_off;
     if (v < 0 || (v == 0 && max_n > tdg::RAGGED_TINY_MAX) || (v > 0 && !variant_serves<T>(v, max_n))) {
       free_plan(plan);
       return TRIDIAG_ERR_NOT_SUPPORTED;
@@ -559,7 +643,7 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       bk.variant = variant;
       bk.count = count;
       bk.max_n = max_n;
-      bk.m_max = variant == 0 || variant == RAGGED_SEQUENTIAL ? 0
+      bk.m_max = variant == 0 || variant >= RAGGED_SEQUENTIAL ? 0
                  : variant == RAGGED_UNPIVOTED ? (max_n + M - 1) / M  // 128-byte rows of the longest system
                                                : std::max(2, (max_n + tdg::pge_variant_partitions(variant) - 1) /
                                                                  tdg::pge_variant_partitions(variant));
@@ -570,6 +654,12 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       bk.ticket = kind == 0 && mode == 2 && variant != 0 && variant != RAGGED_SEQUENTIAL ? plan->n_tickets++ : -1;
       bk.klist = kind >= 0 ? 2 * k + kind : -1;
       bk.klist_off = kind >= 0 ? (size_t)reg[2 * k + kind] : 0;
+      if (variant == RAGGED_CHUNKED) {
+        bk.cl_off = cl_off;
+        bk.cl_count = (int)cl_count;
+        bk.sep_variant = sep_variant;
+        bk.sep_m_max = sep_m_max;
+      }
       plan->buckets.push_back(bk);
     };
     if (!capable) {
@@ -658,6 +748,26 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     }
     if (cudaMalloc(&plan->d_chunk_sys, std::max<size_t>(cs.size(), 1) * sizeof(int)) != cudaSuccess ||
         cudaMemcpy(plan->d_chunk_sys, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+      free_plan(plan);
+      return TRIDIAG_ERR_CUDA;
+    }
+  }
+  if (!cl_sys.empty()) {
+    plan->n_cl = cl_sys.size();
+    std::vector<long long> so(batch + 1, 0);
+    for (int q = 0; q < batch; ++q) so[q + 1] = so[q] + sep_rows[q];
+    plan->sep_total = so[batch];
+    const size_t st = (size_t)plan->sep_total;
+    const size_t wbytes = (5 * st + 4 * (st / 128)) * sizeof(T);
+    if (cudaMalloc(&plan->d_cl, 2 * plan->n_cl * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(plan->d_cl, cl_sys.data(), plan->n_cl * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(plan->d_cl + plan->n_cl, cl_ch.data(), plan->n_cl * sizeof(int), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->d_sep_off, (size_t)(batch + 1) * sizeof(long long)) != cudaSuccess ||
+        cudaMemcpy(plan->d_sep_off, so.data(), (size_t)(batch + 1) * sizeof(long long), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->sep_work, wbytes) != cudaSuccess ||
+        cudaMalloc(&plan->d_flag, (size_t)batch * sizeof(int)) != cudaSuccess) {
       free_plan(plan);
       return TRIDIAG_ERR_CUDA;
     }
@@ -773,7 +883,35 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
       e = tdg::launch_ragged_seq<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
                                     bk.kind == 0 && plan->kinds_mode == 2 ? plan->d_kcount + bk.klist : nullptr,
                                     plan->d_soff, w1, w1 + plan->seq_rows,
-                                    reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), s);
+                                    reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), nullptr, s);
+    } else if (bk.variant == RAGGED_CHUNKED) {
+      // the chunked partitioned solve (of A^T for the adjoint), then the
+      // adjoint's gradients, then variant 9 for the systems a chunk failed
+      tdg::BucketTicket tc = tk;
+      tc.kinds = bk.kind >= 0 ? plan->d_kinds : nullptr;
+      tc.want = bk.kind >= 0 ? bk.kind : 0;
+      const int* cls = plan->d_cl + bk.cl_off;
+      const int* clc = plan->d_cl + plan->n_cl + bk.cl_off;
+      const size_t st = (size_t)plan->sep_total;
+      T* sep = static_cast<T*>(plan->sep_work);
+      e = cudaMemsetAsync(plan->d_flag, 0, (size_t)plan->batch * sizeof(int), s);
+      if (e == cudaSuccess)
+        e = tdg::launch_pge_long_ragged<T>(mode == 0 ? a : c - 1, b, mode == 0 ? c : a + 1, d, x, offsets, cls, clc,
+                                           bk.cl_count, plan->d_sep_off, st, sep, sep + 4 * st, sep + 5 * st,
+                                           plan->d_flag, bk.sep_variant, bk.sep_m_max, list, bk.count, &tc, s);
+      if (e == cudaSuccess && mode == 1) {
+        tdg::ragged_chunk_gradient_kernel<T><<<(unsigned)(((long long)bk.cl_count * 32 + 255) / 256), 256, 0, s>>>(
+            x, xf, ga, gb, gc, offsets, cls, clc, bk.cl_count, tdg::pge_long_chunk_rows(), tc.kinds, tc.want,
+            plan->d_flag);
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) {
+        T* w1 = static_cast<T*>(plan->seq_work);
+        e = tdg::launch_ragged_seq<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
+                                      bk.kind == 0 && plan->kinds_mode == 2 ? plan->d_kcount + bk.klist : nullptr,
+                                      plan->d_soff, w1, w1 + plan->seq_rows,
+                                      reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), plan->d_flag, s);
+      }
     }
     else if (bk.variant == RAGGED_UNPIVOTED)
       e = mode == 0 ? tdg::launch_wmc_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets, list,
@@ -927,6 +1065,8 @@ int tridiag_ragged_variant_max_n(int precision, int variant) {
   if (variant == 0) return tdg::RAGGED_TINY_MAX;
   if (variant == RAGGED_UNPIVOTED) return precision ? unpivoted_max_n<double>() : unpivoted_max_n<float>();
   if (variant == RAGGED_SEQUENTIAL) return 0x7fffffff;
+  if (variant == RAGGED_CHUNKED)
+    return precision ? tdg::pge_long_ragged_max_n<double>() : tdg::pge_long_ragged_max_n<float>();
   if (variant == RAGGED_UNPIVOTED_LONG)
     return precision ? tdg::WMC_GEN_MAX_ROWS * 16 * 16 : tdg::WMC_GEN_MAX_ROWS * 32 * 32;
   return precision ? tdg::pge_variant_max_n<double>(variant) : tdg::pge_variant_max_n<float>(variant);

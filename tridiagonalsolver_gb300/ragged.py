@@ -32,7 +32,8 @@ VARIANTS = {0: "sequential (thread per system)", 1: "partitioned, 1 CTA x 64", 2
             3: "partitioned, 1 CTA x 256", 4: "partitioned, cluster of 2", 5: "partitioned, cluster of 4",
             6: "partitioned, cluster of 8", 7: "unpivoted partition method (systems marked no_pivoting)",
             8: "unpivoted partition method, chunked (long systems marked no_pivoting)",
-            9: "sequential (thread per system), rows in a workspace: any n"}
+            9: "sequential (thread per system), rows in a workspace: any n",
+            10: "partitioned, chunks of 4224 rows per CTA, separators' system in between"}
 _P = ctypes.c_void_p
 
 
@@ -226,6 +227,8 @@ def candidates(precision: int, cls: int):
     out = [0] if hi <= 64 else []
     if lo >= 65:
         out += [v for v in range(1, 7) if variant_max_n(precision, v) >= hi]
+    if not out and lo >= 65:
+        out = ([10] if variant_max_n(precision, 10) >= hi else []) + [9]
     return out or [9]
 
 

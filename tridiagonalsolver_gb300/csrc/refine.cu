@@ -88,7 +88,11 @@ __global__ void __launch_bounds__(256) narrow4_kernel(const double* __restrict__
 // Row i of system j lives at j*n + i (CONTIG) or i*batch + j (INTERLEAVED);
 // the neighbours of a row are one element (CONTIG) or one row of the batch
 // (INTERLEAVED) away.  The grid walks (outer, inner) tiles: outer = system
-// for CONTIG, row for INTERLEAVED; inner is the unit-stride index.
+// for CONTIG, row for INTERLEAVED; inner is the unit-stride index.  CONTIG:
+// a warp holds 32 consecutive rows of one system and x_new of the rows
+// beside a lane's comes by shuffles (lanes 0 and 31 form their outer
+// neighbour), so each row's x_old + dx is formed once: 4 FP64 instructions
+// per row.  INTERLEAVED forms the neighbours' x again (3 more).
 template <int L>
 __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict__ a, const double* __restrict__ b,
                                                        const double* __restrict__ c, const double* __restrict__ d,
@@ -98,17 +102,33 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   const int inner_len = L == INTERLEAVED ? batch : n;
   const int outer_len = L == INTERLEAVED ? n : batch;
   const size_t nb = (size_t)(L == INTERLEAVED ? batch : 1);  // distance to the neighbouring row
+  auto xat = [&](size_t q) { return (xold ? xold[q] : 0.0) + widen(dx[q]); };
+  const int lane = threadIdx.x & 31;
   for (int o = blockIdx.y; o < outer_len; o += gridDim.y) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < inner_len; t += gridDim.x * blockDim.x) {
+    // (warp-uniform trip count: the shuffles need every lane)
+    for (int t0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); t0 < inner_len; t0 += gridDim.x * blockDim.x) {
+      const int t = t0 + lane;
+      const bool in = t < inner_len;
       const size_t k = (size_t)o * inner_len + t;
       const int i = L == INTERLEAVED ? o : t;  // row index within the system
-      auto xat = [&](size_t q) { return (xold ? xold[q] : 0.0) + widen(dx[q]); };
-      const double xi = xat(k);
-      double r = fma(-__ldg(b + k), xi, __ldg(d + k));
-      if (i > 0) r = fma(-__ldg(a + k), xat(k - nb), r);
-      if (i < n - 1) r = fma(-__ldg(c + k), xat(k + nb), r);
-      xnew[k] = xi;
-      r32[k] = narrow_rn(r);
+      const double xi = in ? xat(k) : 0.0;
+      double xm, xp;
+      if (L == INTERLEAVED) {
+        xm = in && i > 0 ? xat(k - nb) : 0.0;
+        xp = in && i < n - 1 ? xat(k + nb) : 0.0;
+      } else {
+        xm = __shfl_up_sync(0xffffffffu, xi, 1);
+        xp = __shfl_down_sync(0xffffffffu, xi, 1);
+        if (lane == 0 && in && i > 0) xm = xat(k - 1);
+        if ((lane == 31 || t + 1 == inner_len) && in && i < n - 1) xp = xat(k + 1);
+      }
+      if (in) {
+        double r = fma(-__ldg(b + k), xi, __ldg(d + k));
+        if (i > 0) r = fma(-__ldg(a + k), xm, r);
+        if (i < n - 1) r = fma(-__ldg(c + k), xp, r);
+        xnew[k] = xi;
+        r32[k] = narrow_rn(r);
+      }
     }
   }
 }

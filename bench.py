@@ -1295,6 +1295,21 @@ def profile_case(name: str) -> None:
         torch.cuda.synchronize()
         print("ok block2_64")
         return
+    if name == "ragged_long32":
+        # long unpivoted FP32 systems of a ragged batch (the chunked partition
+        # method with element-wise staging): 256 dominant systems, n in
+        # [32769, 65536] (~200 MB), three solves
+        from tridiagonalsolver_gb300 import ragged
+
+        sizes = ragged.log_uniform_sizes(256, 32769, 65536, seed=11)
+        a, b, c, d, off, _ = ragged.synthetic_batch(sizes, nondominant_fraction=0.0, seed=11)
+        plan = T.RaggedPlan(off, no_pivoting=np.ones(len(sizes), dtype=bool))
+        x = torch.empty_like(d)
+        for _ in range(3):
+            plan.solve(a, b, c, d, out=x)
+        torch.cuda.synchronize()
+        print("ok", name, plan.buckets())
+        return
     if name == "ragged_seq64":
         # variant 9 alone: 64 non-dominant FP64 systems of 40000 rows (102 MB), three solves
         from tridiagonalsolver_gb300 import ragged
@@ -1618,7 +1633,8 @@ def main():
                     help="config2 (default): PCR + CR-PCR FP32 and pivoted WM-pGE FP64; the others are the "
                          "remaining benchmark configurations, one JSON line each")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step", "ragged64_step",
-                                                                         "ragged_refine_step", "ragged_seq64"], default=None,
+                                                                         "ragged_refine_step", "ragged_seq64",
+                                                                         "ragged_long32"], default=None,
                     help="run one small case of one kernel family three times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.profile_case:

@@ -330,7 +330,8 @@ def test_ragged_autotune_unpivoted(cuda):
     torch = cuda
     table, chunk, timings = ragged.autotune_unpivoted([8, 12, 14], rows_per_class=2 ** 20, reps=1)
     assert set(table) == {8, 12}
-    assert table[8] in (7, 1, 2, 3) and table[12] in (7, 1, 2, 3, 4, 5, 6)
+    # (timing decides: any variant that serves the class)
+    assert table[8] in (7, 1, 2, 3, 4, 5, 6) and table[12] in (7, 1, 2, 3, 4, 5, 6)
     assert chunk in (64, 128, 256) and set(timings["chunk_rows"]) == {64, 128, 256}
     sizes = np.array([150, 3000, 12000, 70], dtype=np.int64)
     a, b, c, d, off, _ = ragged.synthetic_batch(sizes, nondominant_fraction=0.0, seed=14)

@@ -20,6 +20,12 @@
 
 namespace tdg {
 
+// The hardware conversions of the rare cases sit in functions of their own:
+// inlined, the compiler may turn the branch around them into predicated
+// instructions that every row then issues on the FP64 pipe.
+__device__ __noinline__ float narrow_rare(double v) { return __double2float_rn(v); }
+__device__ __noinline__ double widen_rare(float f) { return (double)f; }
+
 __device__ __forceinline__ float narrow_rn(double v) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(v);
   const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
@@ -35,14 +41,14 @@ __device__ __forceinline__ float narrow_rn(double v) {
     r += half & ((rest != 0u) | (m & 1u));  // ties to even; a carry rolls into the exponent (up to inf)
     return __uint_as_float(r);
   }
-  return __double2float_rn(v);  // inf, NaN, overflow, FP32 subnormal range
+  return narrow_rare(v);  // inf, NaN, overflow, FP32 subnormal range
 }
 
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xffu;
   if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-  if (e == 0u || e == 255u) return (double)f;  // FP32 subnormal, inf, NaN
+  if (e == 0u || e == 255u) return widen_rare(f);  // FP32 subnormal, inf, NaN
   const unsigned hi = (u & 0x80000000u) | ((e + 1023u - 127u) << 20) | ((u & 0x7fffffu) >> 3);
   return __hiloint2double((int)hi, (int)(u << 29));
 }
@@ -133,6 +139,64 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   }
 }
 
+// CONTIG with n a multiple of 4 and 16-byte aligned arrays: a warp holds
+// 128 consecutive rows of one system, lane l rows 4l .. 4l+3 (16-byte
+// loads), so the rows' x_old + dx are formed once by full-warp instructions
+// and only the two rows beyond the warp's tile are formed again by one lane.
+__global__ void __launch_bounds__(256) residual4_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                        const double* __restrict__ c, const double* __restrict__ d,
+                                                        const double* __restrict__ xold, const float* __restrict__ dx,
+                                                        double* __restrict__ xnew, float* __restrict__ r32, int n,
+                                                        int batch) {
+  const int lane = threadIdx.x & 31;
+  auto xat = [&](size_t q) { return (xold ? xold[q] : 0.0) + widen(dx[q]); };
+  for (int o = blockIdx.y; o < batch; o += gridDim.y) {
+    for (int t0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) * 4; t0 < n; t0 += gridDim.x * blockDim.x * 4) {
+      const int i0 = t0 + 4 * lane;  // (warp-uniform trip count: the shuffles need every lane)
+      const bool in = i0 < n;       // (n % 4 == 0: a lane's four rows are all in or all out)
+      const size_t k = (size_t)o * n + i0;
+      double x[4] = {0.0, 0.0, 0.0, 0.0};
+      if (in) {
+        const float4 v = *reinterpret_cast<const float4*>(dx + k);
+        const float dv[4] = {v.x, v.y, v.z, v.w};
+        double xo[4] = {0.0, 0.0, 0.0, 0.0};
+        if (xold) {
+          const double2 p0 = *reinterpret_cast<const double2*>(xold + k);
+          const double2 p1 = *reinterpret_cast<const double2*>(xold + k + 2);
+          xo[0] = p0.x; xo[1] = p0.y; xo[2] = p1.x; xo[3] = p1.y;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = xo[u] + widen(dv[u]);
+      }
+      double xm = __shfl_up_sync(0xffffffffu, x[3], 1);
+      double xp = __shfl_down_sync(0xffffffffu, x[0], 1);
+      if (lane == 0 && in && i0 > 0) xm = xat(k - 1);
+      if (lane == 31 && in && i0 + 4 < n) xp = xat(k + 4);
+      if (in) {
+        const double2 a0 = __ldg(reinterpret_cast<const double2*>(a + k)), a1 = __ldg(reinterpret_cast<const double2*>(a + k + 2));
+        const double2 b0 = __ldg(reinterpret_cast<const double2*>(b + k)), b1 = __ldg(reinterpret_cast<const double2*>(b + k + 2));
+        const double2 c0 = __ldg(reinterpret_cast<const double2*>(c + k)), c1 = __ldg(reinterpret_cast<const double2*>(c + k + 2));
+        const double2 d0 = __ldg(reinterpret_cast<const double2*>(d + k)), d1 = __ldg(reinterpret_cast<const double2*>(d + k + 2));
+        const double av[4] = {a0.x, a0.y, a1.x, a1.y}, bv[4] = {b0.x, b0.y, b1.x, b1.y};
+        const double cv[4] = {c0.x, c0.y, c1.x, c1.y}, dvv[4] = {d0.x, d0.y, d1.x, d1.y};
+        float rr[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u;
+          const double left = u > 0 ? x[u - 1] : xm, right = u < 3 ? x[u + 1] : xp;
+          double r = fma(-bv[u], x[u], dvv[u]);
+          if (i > 0) r = fma(-av[u], left, r);
+          if (i < n - 1) r = fma(-cv[u], right, r);
+          rr[u] = narrow_rn(r);
+        }
+        *reinterpret_cast<double2*>(xnew + k) = make_double2(x[0], x[1]);
+        *reinterpret_cast<double2*>(xnew + k + 2) = make_double2(x[2], x[3]);
+        *reinterpret_cast<float4*>(r32 + k) = make_float4(rr[0], rr[1], rr[2], rr[3]);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) update_kernel(const double* __restrict__ xold, const float* __restrict__ dx,
                                                      double* xout, size_t count) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -176,10 +240,21 @@ cudaError_t launch_residual(int layout, const double* a, const double* b, const 
   const int gy_cap = (sms * 8 + gx - 1) / gx;
   const int gy = outer < gy_cap ? outer : (gy_cap < 65535 ? gy_cap : 65535);
   dim3 grid(gx, gy > 0 ? gy : 1);
-  if (layout == INTERLEAVED)
+  const bool vec4 = layout == CONTIG && n % 4 == 0 &&
+                    ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(c) |
+                      reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(xold) |
+                      reinterpret_cast<uintptr_t>(dx) | reinterpret_cast<uintptr_t>(xnew) |
+                      reinterpret_cast<uintptr_t>(r32)) & 15u) == 0;
+  if (vec4) {
+    const int gx4 = (n / 4 + threads - 1) / threads;
+    const int gy4_cap = (sms * 8 + gx4 - 1) / gx4;
+    const int gy4 = outer < gy4_cap ? outer : (gy4_cap < 65535 ? gy4_cap : 65535);
+    residual4_kernel<<<dim3(gx4, gy4 > 0 ? gy4 : 1), threads, 0, s>>>(a, b, c, d, xold, dx, xnew, r32, n, batch);
+  } else if (layout == INTERLEAVED) {
     residual_kernel<INTERLEAVED><<<grid, threads, 0, s>>>(a, b, c, d, xold, dx, xnew, r32, n, batch);
-  else
+  } else {
     residual_kernel<CONTIG><<<grid, threads, 0, s>>>(a, b, c, d, xold, dx, xnew, r32, n, batch);
+  }
   return cudaGetLastError();
 }
 

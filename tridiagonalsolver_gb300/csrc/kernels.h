@@ -14,6 +14,7 @@ struct BucketTicket {
   const int* dcount = nullptr;
   const unsigned char* kinds = nullptr;
   int want = 0;
+  const int* only = nullptr;  // (partitioned variants) serve only the systems s with only[s] != 0
 };
 // Ragged forward solves by the unpivoted method that check the rows they
 // stage: a system with a row that is not strictly diagonally dominant is
@@ -232,6 +233,7 @@ bool pge_long_eligible(int n);
 // bucket (chunk entries cl_sys / cl_ch over the bucket's class; separator
 // rows of system s at sep_off[s]; flag[s] set where a chunk fails).
 int pge_long_chunk_rows();
+int pge_long_retry_rows();
 template <typename T>
 int pge_long_ragged_max_n();
 template <typename T>
@@ -239,7 +241,7 @@ cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* 
                                    const int* cl_sys, const int* cl_ch, int C, const long long* sep_off,
                                    size_t sep_total, T* sep, T* xsep, T* carry, int* flag, int sep_variant,
                                    int sep_m_max, const int* list, int count, const BucketTicket* tk,
-                                   cudaStream_t s);
+                                   cudaStream_t s, int chunk_rows);
 template <typename T>
 cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info, int n, int batch, T* w1, T* w2,
                             unsigned* piv, int* flag, cudaStream_t s, bool* used);

@@ -269,6 +269,9 @@ struct PgeIO {
   const int* cl_ch;
   const long long* sep_off;
   size_t sep_total;
+  // (non-NULL) only the systems s with only[s] != 0 are served: the chunked
+  // passes, and the entries the resident CTAs take by ticket
+  const int* only;
   // size buckets of a ragged batch served by resident CTAs (clusters): each
   // takes the next entry of list[0 .. count) -- count from *dcount where a
   // device pass wrote the list -- from the ticket counter (zero before the
@@ -388,7 +391,7 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     if (io.cl_sys) {
       sys = io.cl_sys[bid];
       ch = io.cl_ch[bid];
-      if (io.kinds && io.kinds[sys] != io.want) return;  // (the whole CTA)
+      if ((io.kinds && io.kinds[sys] != io.want) || (io.only && !io.only[sys])) return;  // (the whole CTA)
       const long long s0 = io.offsets[sys];
       const int nsys = (int)(io.offsets[sys + 1] - s0);
       nch = (nsys + io.chunk_rows - 1) / io.chunk_rows;
@@ -1003,6 +1006,7 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
       __shared__ int s_item;
       for (int k = pge_next_item(io, &s_item); k >= 0; k = pge_next_item(io, &s_item)) {
         if (io.kinds && io.kinds[io.list[k]] != io.want) continue;
+        if (io.only && !io.only[io.list[k]]) continue;
         pge_body<T, NT, MODE, LAY>(io, maps, k, s_bar);
         __syncthreads();
         if (threadIdx.x == 0) mbar_inval(&s_bar[0]);  // re-armed by the next system
@@ -1486,6 +1490,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       cluster.sync();  // (read by all before CTA 0 writes the next one)
       if (k < 0) break;
       if (io.kinds && io.kinds[io.list[k]] != io.want) continue;
+      if (io.only && !io.only[io.list[k]]) continue;
       pgc_body<T, NT, CL, MODE>(io, k, &s_bar);  // (ends with a cluster barrier)
       if (threadIdx.x == 0) mbar_inval(&s_bar);   // re-armed by the next system
     }
@@ -1817,12 +1822,13 @@ template <typename T>
 __global__ void __launch_bounds__(256) pge_long_link_ragged(T* sep, const T* carry, const int* cl_sys,
                                                             const int* cl_ch, int C, const long long* offsets,
                                                             const long long* sep_off, size_t sep_total,
-                                                            const unsigned char* kinds, int want) {
+                                                            const unsigned char* kinds, int want, const int* only,
+                                                            int chunk_rows) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= C) return;
   const int sys = cl_sys[k], ch = cl_ch[k];
-  if (kinds && kinds[sys] != want) return;
-  const int nch = (int)((offsets[sys + 1] - offsets[sys] + PGE_LONG_ROWS - 1) / PGE_LONG_ROWS);
+  if ((kinds && kinds[sys] != want) || (only && !only[sys])) return;
+  const int nch = (int)((offsets[sys + 1] - offsets[sys] + chunk_rows - 1) / chunk_rows);
   if (ch + 1 >= nch) return;
   const size_t sq = (size_t)sep_off[sys];
   const T cs = carry[(sq / PGE_LONG_NT + ch) * 4 + 3];  // c of chunk ch's last separator row
@@ -1834,13 +1840,16 @@ __global__ void __launch_bounds__(256) pge_long_link_ragged(T* sep, const T* car
 }
 
 int pge_long_chunk_rows() { return PGE_LONG_ROWS; }
+// the chunks of a re-solve: partitions of 31 rows, so that their boundaries
+// fall elsewhere than the first pass's
+int pge_long_retry_rows() { return PGE_LONG_NT * 31; }
 
 template <typename T>
 int pge_long_ragged_max_n() {
   // the separators' system (PGE_LONG_NT rows per chunk) within one partitioned variant
   int best = 0;
   for (int v = 1; v <= 6; ++v) best = std::max(best, pge_variant_max_n<T>(v));
-  const long long n = (long long)(best / PGE_LONG_NT) * PGE_LONG_ROWS;
+  const long long n = (long long)(best / PGE_LONG_NT) * (PGE_LONG_NT * 31);  // (the re-solve's chunks are the shorter)
   return pge_smem_bytes<T, PGE_LONG_NT>(PGE_LONG_M) <= PGE_SMEM_MAX ? (int)std::min<long long>(n, 1 << 30) : 0;
 }
 
@@ -1849,8 +1858,11 @@ cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* 
                                    const int* cl_sys, const int* cl_ch, int C, const long long* sep_off,
                                    size_t sep_total, T* sep, T* xsep, T* carry, int* flag, int sep_variant,
                                    int sep_m_max, const int* list, int count, const BucketTicket* tk,
-                                   cudaStream_t s) {
+                                   cudaStream_t s, int chunk_rows) {
   if (C <= 0 || count <= 0) return cudaSuccess;
+  if (chunk_rows <= 0 || chunk_rows % PGE_LONG_NT || (chunk_rows / PGE_LONG_NT) % 2 == 0 ||
+      chunk_rows > PGE_LONG_ROWS)
+    return cudaErrorInvalidValue;
   PgeIO<T> io{};
   io.a = a;
   io.b = b;
@@ -1858,11 +1870,12 @@ cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* 
   io.d = d;
   io.offsets = offsets;
   io.err = error_word();
-  io.chunk_rows = PGE_LONG_ROWS;
+  io.chunk_rows = chunk_rows;
   io.sep = sep;
   io.carry = carry;
   io.xsep = xsep;
   io.flag = flag;
+  io.only = tk ? tk->only : nullptr;
   io.cl_sys = cl_sys;
   io.cl_ch = cl_ch;
   io.sep_off = sep_off;
@@ -1879,7 +1892,7 @@ cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* 
   pge_kernel<T, PGE_LONG_NT, 2, PGE_DENSE><<<C, PGE_LONG_NT, smem, s>>>(io, maps);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   pge_long_link_ragged<T><<<(C + 255) / 256, 256, 0, s>>>(sep, carry, cl_sys, cl_ch, C, offsets, sep_off, sep_total,
-                                                         io.kinds, io.want);
+                                                         io.kinds, io.want, io.only, chunk_rows);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   e = launch_pge_ragged<T>(sep_variant, 0, sep, sep + sep_total, sep + 2 * sep_total, sep + 3 * sep_total, xsep,
                            nullptr, nullptr, nullptr, nullptr, nullptr, sep_off, list, count, sep_m_max, s, tk);
@@ -1933,6 +1946,7 @@ cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, con
     io.dcount = tk->dcount;
     io.kinds = tk->kinds;
     io.want = tk->want;
+    io.only = tk->only;
   }
   io.b = b;
   io.d = d;
@@ -1985,7 +1999,8 @@ cudaError_t pge_path_counts(unsigned long long* out, bool reset) {
   template int pge_long_ragged_max_n<T>();                                                                        \
   template cudaError_t launch_pge_long_ragged<T>(const T*, const T*, const T*, const T*, T*, const long long*,      \
                                                  const int*, const int*, int, const long long*, size_t, T*, T*, T*, \
-                                                 int*, int, int, const int*, int, const BucketTicket*, cudaStream_t);   \
+                                                 int*, int, int, const int*, int, const BucketTicket*, cudaStream_t, \
+                                                 int);                                                            \
   template cudaError_t launch_pge_long<T>(const T*, const T*, const T*, T*, int*, int, int, T*, T*, unsigned*, int*, \
                                           cudaStream_t, bool*);                                                   \
   template cudaError_t launch_pge_strided<T>(const T*, const T*, const T*, const T*, T*, int*, int, int, size_t,  \

@@ -347,6 +347,12 @@ struct tridiag_ragged_plan {
     size_t cl_off = 0;
     int cl_count = 0;
     int sep_variant = 0, sep_m_max = 0;
+    // its re-solve of the systems a chunk failed (chunks of 31-row
+    // partitions: entries cl2_off .. in d_cl2, separators at d_sep_off2)
+    size_t cl2_off = 0;
+    int cl2_count = 0;
+    int sep2_variant = 0, sep2_m_max = 0;
+    int ticket2 = -1;  // its separators' solve's ticket counter
   };
   int precision = 0;
   int batch = 0;
@@ -387,6 +393,13 @@ struct tridiag_ragged_plan {
   long long sep_total = 0;
   void* sep_work = nullptr;
   int* d_flag = nullptr;
+  // the re-solve's chunk entries, separator offsets (sep_total2 rows in the
+  // same separator arrays) and the systems its chunks fail in turn
+  int* d_cl2 = nullptr;
+  size_t n_cl2 = 0;
+  long long* d_sep_off2 = nullptr;
+  long long sep_total2 = 0;
+  int* d_flag2 = nullptr;
   // the system holding row k * RAGGED_ROW_CHUNK (the row-parallel passes of
   // the refined solves)
   int* d_chunk_sys = nullptr;
@@ -462,6 +475,9 @@ void free_plan(tridiag_ragged_plan* plan) {
   cudaFree(plan->d_sep_off);
   cudaFree(plan->sep_work);
   cudaFree(plan->d_flag);
+  cudaFree(plan->d_cl2);
+  cudaFree(plan->d_sep_off2);
+  cudaFree(plan->d_flag2);
   cudaFree(plan->seq_work);
   cudaFree(plan->d_chunk_sys);
   delete plan;
@@ -554,6 +570,9 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   std::vector<int> cl_sys, cl_ch;                 // variant 10 chunk entries
   std::vector<long long> sep_rows(batch, 0);      // variant 10 separator rows per system
   const int CR = tdg::pge_long_chunk_rows();
+  std::vector<int> cl2_sys, cl2_ch;               // ... of its re-solve
+  std::vector<long long> sep2_rows(batch, 0);
+  const int CR2 = tdg::pge_long_retry_rows();
   for (int k = 0; k < TRIDIAG_RAGGED_CLASSES; ++k) {
     auto& sys = by_class[k];
     if (sys.empty()) continue;
@@ -591,27 +610,35 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
         soff[q] = seq_rows;
         seq_rows += (len(q) + 31) / 32 * 32;
       }
-    size_t cl_off = cl_sys.size();
-    int sep_variant = 0, sep_m_max = 0;
+    size_t cl_off = cl_sys.size(), cl2_off = cl2_sys.size();
+    int sep_variant = 0, sep_m_max = 0, sep2_variant = 0, sep2_m_max = 0;
     if (v == RAGGED_CHUNKED) {
       for (int q : sys) {
-        const int nch = (int)((len(q) + CR - 1) / CR);
+        const int nch = (int)((len(q) + CR - 1) / CR), nch2 = (int)((len(q) + CR2 - 1) / CR2);
         sep_rows[q] = (long long)nch * 128;
+        sep2_rows[q] = (long long)nch2 * 128;
         for (int c = 0; c < nch; ++c) {
           cl_sys.push_back(q);
           cl_ch.push_back(c);
         }
+        for (int c = 0; c < nch2; ++c) {
+          cl2_sys.push_back(q);
+          cl2_ch.push_back(c);
+        }
       }
-      const int max_sep = (int)((max_n + CR - 1) / CR) * 128;
+      const int max_sep = (int)((max_n + CR - 1) / CR) * 128, max_sep2 = (int)((max_n + CR2 - 1) / CR2) * 128;
       sep_variant = tdg::pge_default_variant<T>(max_sep);
-      if (sep_variant <= 0) {
+      sep2_variant = tdg::pge_default_variant<T>(max_sep2);
+      if (sep_variant <= 0 || sep2_variant <= 0) {
         free_plan(plan);
         return TRIDIAG_ERR_NOT_SUPPORTED;
       }
       sep_m_max = std::max(2, (max_sep + tdg::pge_variant_partitions(sep_variant) - 1) /
                                   tdg::pge_variant_partitions(sep_variant));
+      sep2_m_max = std::max(2, (max_sep2 + tdg::pge_variant_partitions(sep2_variant) - 1) /
+                                   tdg::pge_variant_partitions(sep2_variant));
     }
-    const size_t cl_count = cl_sys.size() - cl_off;
+    const size_t cl_count = cl_sys.size() - cl_off, cl2_count = cl2_sys.size() - cl2_off;
     if (v < 0 || (v == 0 && max_n > tdg::RAGGED_TINY_MAX) || (v > 0 && !variant_serves<T>(v, max_n))) {
       free_plan(plan);
       return TRIDIAG_ERR_NOT_SUPPORTED;
@@ -659,6 +686,11 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
         bk.cl_count = (int)cl_count;
         bk.sep_variant = sep_variant;
         bk.sep_m_max = sep_m_max;
+        bk.cl2_off = cl2_off;
+        bk.cl2_count = (int)cl2_count;
+        bk.sep2_variant = sep2_variant;
+        bk.sep2_m_max = sep2_m_max;
+        bk.ticket2 = plan->n_tickets++;
       }
       plan->buckets.push_back(bk);
     };
@@ -754,11 +786,27 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
   }
   if (!cl_sys.empty()) {
     plan->n_cl = cl_sys.size();
-    std::vector<long long> so(batch + 1, 0);
-    for (int q = 0; q < batch; ++q) so[q + 1] = so[q] + sep_rows[q];
+    plan->n_cl2 = cl2_sys.size();
+    std::vector<long long> so(batch + 1, 0), so2(batch + 1, 0);
+    for (int q = 0; q < batch; ++q) {
+      so[q + 1] = so[q] + sep_rows[q];
+      so2[q + 1] = so2[q] + sep2_rows[q];
+    }
     plan->sep_total = so[batch];
-    const size_t st = (size_t)plan->sep_total;
+    plan->sep_total2 = so2[batch];
+    const size_t st = (size_t)std::max(plan->sep_total, plan->sep_total2);  // (the two passes share the arrays)
     const size_t wbytes = (5 * st + 4 * (st / 128)) * sizeof(T);
+    if (cudaMalloc(&plan->d_cl2, 2 * plan->n_cl2 * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(plan->d_cl2, cl2_sys.data(), plan->n_cl2 * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(plan->d_cl2 + plan->n_cl2, cl2_ch.data(), plan->n_cl2 * sizeof(int), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->d_sep_off2, (size_t)(batch + 1) * sizeof(long long)) != cudaSuccess ||
+        cudaMemcpy(plan->d_sep_off2, so2.data(), (size_t)(batch + 1) * sizeof(long long), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMalloc(&plan->d_flag2, (size_t)batch * sizeof(int)) != cudaSuccess) {
+      free_plan(plan);
+      return TRIDIAG_ERR_CUDA;
+    }
     if (cudaMalloc(&plan->d_cl, 2 * plan->n_cl * sizeof(int)) != cudaSuccess ||
         cudaMemcpy(plan->d_cl, cl_sys.data(), plan->n_cl * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(plan->d_cl + plan->n_cl, cl_ch.data(), plan->n_cl * sizeof(int), cudaMemcpyHostToDevice) !=
@@ -783,11 +831,14 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
       return TRIDIAG_ERR_CUDA;
     }
   }
+  if (plan->n_tickets > 0 && cudaMalloc(&plan->d_tickets, plan->n_tickets * sizeof(int)) != cudaSuccess) {
+    free_plan(plan);
+    return TRIDIAG_ERR_CUDA;
+  }
   if (mode != 0) {
     const size_t nk = std::max<size_t>(klists.size(), 1);
     if (cudaMalloc(&plan->d_kinds, (size_t)batch) != cudaSuccess ||
         cudaMemcpy(plan->d_kinds, kinds.data(), (size_t)batch, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMalloc(&plan->d_tickets, std::max(plan->n_tickets, 1) * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&plan->d_klists, nk * sizeof(int)) != cudaSuccess ||
         cudaMemcpy(plan->d_klists, klists.data(), klists.size() * sizeof(int), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
@@ -869,7 +920,7 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
     tk.kinds = bk.kind == 1 && !check && plan->kinds_mode == 2 ? plan->d_kinds : nullptr;
     tk.want = bk.kind;
     const tdg::BucketTicket* tkp = bk.kind >= 0 ? &tk : nullptr;
-    cudaError_t e;
+    cudaError_t e = cudaErrorInvalidValue;  // (a variant no branch serves is an error)
     if (bk.variant == RAGGED_UNPIVOTED_LONG)
       e = mode == 0 ? tdg::launch_wml_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets,
                                                 plan->lr, static_cast<T*>(plan->lr_work), info, s, plan->d_kinds,
@@ -885,24 +936,41 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
                                     plan->d_soff, w1, w1 + plan->seq_rows,
                                     reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), nullptr, s);
     } else if (bk.variant == RAGGED_CHUNKED) {
-      // the chunked partitioned solve (of A^T for the adjoint), then the
-      // adjoint's gradients, then variant 9 for the systems a chunk failed
+      // the chunked partitioned solve (of A^T for the adjoint); the systems a
+      // chunk fails solved again in chunks of 31-row partitions; the
+      // adjoint's gradients; variant 9 for the systems that fail twice
       tdg::BucketTicket tc = tk;
       tc.kinds = bk.kind >= 0 ? plan->d_kinds : nullptr;
       tc.want = bk.kind >= 0 ? bk.kind : 0;
       const int* cls = plan->d_cl + bk.cl_off;
       const int* clc = plan->d_cl + plan->n_cl + bk.cl_off;
-      const size_t st = (size_t)plan->sep_total;
+      const int* cls2 = plan->d_cl2 + bk.cl2_off;
+      const int* clc2 = plan->d_cl2 + plan->n_cl2 + bk.cl2_off;
+      const size_t st = (size_t)std::max(plan->sep_total, plan->sep_total2);
       T* sep = static_cast<T*>(plan->sep_work);
+      const T* pa = mode == 0 ? a : c - 1;
+      const T* pc = mode == 0 ? c : a + 1;
       e = cudaMemsetAsync(plan->d_flag, 0, (size_t)plan->batch * sizeof(int), s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(plan->d_flag2, 0, (size_t)plan->batch * sizeof(int), s);
       if (e == cudaSuccess)
-        e = tdg::launch_pge_long_ragged<T>(mode == 0 ? a : c - 1, b, mode == 0 ? c : a + 1, d, x, offsets, cls, clc,
-                                           bk.cl_count, plan->d_sep_off, st, sep, sep + 4 * st, sep + 5 * st,
-                                           plan->d_flag, bk.sep_variant, bk.sep_m_max, list, bk.count, &tc, s);
+        e = tdg::launch_pge_long_ragged<T>(pa, b, pc, d, x, offsets, cls, clc, bk.cl_count, plan->d_sep_off,
+                                           (size_t)plan->sep_total, sep, sep + 4 * st, sep + 5 * st, plan->d_flag,
+                                           bk.sep_variant, bk.sep_m_max, list, bk.count, &tc, s,
+                                           tdg::pge_long_chunk_rows());
+      if (e == cudaSuccess) {
+        tdg::BucketTicket t2 = tc;  // the re-solve: the systems flagged above, through their own ticket
+        t2.ticket = plan->d_tickets + bk.ticket2;
+        t2.dcount = bk.kind == 0 && plan->kinds_mode == 2 ? plan->d_kcount + bk.klist : nullptr;
+        t2.only = plan->d_flag;
+        e = tdg::launch_pge_long_ragged<T>(pa, b, pc, d, x, offsets, cls2, clc2, bk.cl2_count, plan->d_sep_off2,
+                                           (size_t)plan->sep_total2, sep, sep + 4 * st, sep + 5 * st,
+                                           plan->d_flag2, bk.sep2_variant, bk.sep2_m_max, list, bk.count, &t2, s,
+                                           tdg::pge_long_retry_rows());
+      }
       if (e == cudaSuccess && mode == 1) {
         tdg::ragged_chunk_gradient_kernel<T><<<(unsigned)(((long long)bk.cl_count * 32 + 255) / 256), 256, 0, s>>>(
             x, xf, ga, gb, gc, offsets, cls, clc, bk.cl_count, tdg::pge_long_chunk_rows(), tc.kinds, tc.want,
-            plan->d_flag);
+            plan->d_flag2);
         e = cudaGetLastError();
       }
       if (e == cudaSuccess) {
@@ -910,15 +978,14 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
         e = tdg::launch_ragged_seq<T>(mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
                                       bk.kind == 0 && plan->kinds_mode == 2 ? plan->d_kcount + bk.klist : nullptr,
                                       plan->d_soff, w1, w1 + plan->seq_rows,
-                                      reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), plan->d_flag, s);
+                                      reinterpret_cast<unsigned*>(w1 + 2 * plan->seq_rows), plan->d_flag2, s);
       }
-    }
-    else if (bk.variant == RAGGED_UNPIVOTED)
+    } else if (bk.variant == RAGGED_UNPIVOTED)
       e = mode == 0 ? tdg::launch_wmc_ragged<T>(0, a, b, c, d, nullptr, x, nullptr, nullptr, nullptr, offsets, list,
                                                 bk.count, bk.m_max, info, s, tkp, nullptr, check ? &chk : nullptr)
                     : tdg::launch_wmc_ragged<T>(1, a, b, c, d, xf, ga, gb, gc, x, offsets, list, bk.count, bk.m_max,
                                                 info, s, tkp);
-    else
+    else if (bk.variant >= 1 && bk.variant <= 6)
       e = tdg::launch_pge_ragged<T>(bk.variant, mode, a, b, c, d, x, xf, ga, gb, gc, info, offsets, list, bk.count,
                                     bk.m_max, s, tkp);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;

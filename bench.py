@@ -1085,13 +1085,14 @@ def run_refined(args):
                 time.sleep(0.6)
                 sampler.mark("begin")
             ms, _ = _graph_time(torch, stream, fn, max(3, min(args.steps, 20)), args.warmup)
+            hs = [t.index_select(0, idx).cpu().numpy() for t in (a, b, c, d, x)]
+            _, eta = O.backward_error(*hs, n)
             if sampler:
                 sampler.mark("end")
                 clocks = sampler.stop()
                 ms_main = ms
                 bmain = b
-            hs = [t.index_select(0, idx).cpu().numpy() for t in (a, b, c, d, x)]
-            _, eta = O.backward_error(*hs, n)
+                eta_main = eta
             parts.append({"name": f"refined delta={delta:g}, {iters} step{'s' if iters > 1 else ''}",
                           "ms_per_launch": ms, "systems_per_s": batch / (ms * 1e-3), "backward_error_max": eta})
     # the same refinement with pivoted FP32 solves (hardest delta)
@@ -1135,13 +1136,15 @@ def run_refined(args):
         rate, k, t, cores = _cpu_sample(cpu, batch, start=16)
         cpu_b = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                  "sample": f"{k} of {batch} systems, plain FP64 partial pivoting, {t:.2f} s"}
-    return _line(args, "refined: FP32 WM-pGE + FP64-residual refinement, n=65536 x 1024, delta sweep",
+    line = _line(args, "refined: FP32 WM-pGE + FP64-residual refinement, n=65536 x 1024, delta sweep",
           batch / (ms_main * 1e-3), ms_main, "f32+f64 residual",
           {"n": n, "batch": batch, "iters": 2, "fp32_solver": "partition method (unpivoted), chunked",
            "l2": "inputs larger than L2 (2.1 GB)", "headline_case": "delta=1e-6"},
           parts, 5 * n * batch * 8, ms_main, cpu_b, e2e, clocks, 7 * max(3, min(args.steps, 20)),
           note="algorithmic bytes counted as 5*n*8 (FP64 in/out), as for the plain FP64 solve; value: 2 steps "
                "at delta=1e-6")
+    line["backward_error_max"] = eta_main  # of the line's own case (2 steps, delta=1e-6); each part has its own
+    return line
 
 
 def run_block2(args):
@@ -1264,6 +1267,7 @@ PROFILE_CASES = {
     "crpcr32": (512, 32768, "float32", True, "cr"),        # CR-PCR at the config-2 shape
     "wm32": (1024, 16384, "float32", True, "wm"),          # on-chip WM-pGE, one warp per system
     "thomas64i": (4096, 2048, "float64", True, "thomas_i"),  # Thomas FP64, interleaved (config 1 kernel)
+    "thomas64c": (4096, 2048, "float64", True, "thomas_c"),  # Thomas FP64, contiguous (the Thomas_* entry points)
     "refine64": (65536, 128, "float64", True, "refine"),   # refinement pieces + chunked FP32 solves
     "factor64": (1024, 8192, "float64", False, "factor"),  # factor once / solve many
     "relayout64": (1024, 16384, "float64", True, "relayout"),  # contiguous -> interleaved transposes
@@ -1309,6 +1313,24 @@ def profile_case(name: str) -> None:
             plan.solve(a, b, c, d, out=x)
         torch.cuda.synchronize()
         print("ok", name, plan.buckets())
+        return
+    if name == "ragged_refine_small":
+        # the ragged refinement passes on 3000 FP64 systems, n log-uniform in [32, 65536] (~25 M rows, 1 GB):
+        # one refined solve and its adjoint (1 step) through the FP32 plan, three times
+        from tridiagonalsolver_gb300 import ragged
+
+        sizes = ragged.log_uniform_sizes(3000, 32, 65536, seed=12)
+        a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, seed=12)
+        w = torch.rand_like(d) * 2 - 1
+        plan = T.RaggedPlan(off, classify=True)
+        work = plan.refine_workspace()
+        x = torch.empty_like(d)
+        grads = [torch.empty_like(d) for _ in range(4)]
+        for _ in range(3):
+            plan.refine(a, b, c, d, iters=1, out=x, work=work)
+            plan.refine_adjoint(a, b, c, x, w, iters=1, grads=grads, work=work)
+        torch.cuda.synchronize()
+        print("ok", name, int(off[-1]), "rows")
         return
     if name == "ragged_seq64":
         # variant 9 alone: 64 non-dominant FP64 systems of 40000 rows (102 MB), three solves
@@ -1390,6 +1412,8 @@ def profile_case(name: str) -> None:
             T.solve_out(a, b, c, d, n, algo=how, out=x)
         elif how == "thomas_i":
             T.solve_out(a, b, c, d, n, algo="thomas", layout="interleaved", out=x)
+        elif how == "thomas_c":
+            T.solve_out(a, b, c, d, n, algo="thomas", out=x)
         elif how == "refine":
             T.refine(a, b, c, d, n, iters=2, out=x, algo="partition")
         elif how == "factor":
@@ -1605,6 +1629,8 @@ def other_configs(args):
             out[key] = {"workload": wl, "error": f"{type(exc).__name__}: {exc}"[:300]}
             continue
         etas = [p.get("backward_error_max") for p in ln.get("parts", []) if p.get("backward_error_max") is not None]
+        if ln.get("backward_error_max") is not None:  # a line that names its own case's error
+            etas = [ln["backward_error_max"]]
         out[key] = {"workload": ln["config"]["workload"], "systems_per_s": ln["value"],
                     "ms_per_step": ln["ms_per_step"], "dtype": ln["dtype"],
                     "hbm_frac": ln["roofline"]["frac"], "achieved_gbs": ln["roofline"]["achieved"],
@@ -1634,7 +1660,7 @@ def main():
                          "remaining benchmark configurations, one JSON line each")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step", "ragged64_step",
                                                                          "ragged_refine_step", "ragged_seq64",
-                                                                         "ragged_long32"], default=None,
+                                                                         "ragged_long32", "ragged_refine_small"], default=None,
                     help="run one small case of one kernel family three times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.profile_case:

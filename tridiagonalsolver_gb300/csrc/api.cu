@@ -141,6 +141,16 @@ int adjoint_impl(int layout, const T* a, const T* b, const T* c, const T* x, con
       tdg::launch_gtsv_adjoint<T>(layout, a, b, c, x, piv, g, ga, gb, gc, gd, w.w1, w.w2, n, batch, s));
 }
 
+// Thomas on long contiguous / packed systems in batches too small for one
+// thread (two, two-ended) per system to fill the GPU -- every batch in FP32,
+// up to 4096 systems in FP64 -- runs as the partition method: one CTA per
+// system, the same elimination without pivoting, partition by partition
+// (FP64 4096 x 4096: 0.71 ms against 1.07 ms for the two-ended sweep).
+template <typename T>
+bool thomas_by_partition(int layout, int n, int batch) {
+  return layout != TRIDIAG_LAYOUT_INTERLEAVED && n > 1024 && (sizeof(T) == 4 || batch <= 4096);
+}
+
 template <typename T>
 int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, cudaStream_t s) {
   if (!valid_dims(n, batch) || !valid_layout(layout) || !a) return TRIDIAG_ERR_INVALID_VALUE;
@@ -173,7 +183,9 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
     }
     case TRIDIAG_ALGO_THOMAS: {
       bool used = false;
-      cudaError_t e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
+      cudaError_t e = cudaSuccess;
+      if (thomas_by_partition<T>(layout, n, batch)) e = tdg::launch_wmc<T>(layout, a, b, c, d, d, n, batch, s, &used);
+      if (e == cudaSuccess && !used) e = tdg::launch_thomas_tw<T>(layout, a, b, c, d, n, batch, s, &used);
       if (e == cudaSuccess && !used) e = tdg::launch_thomas_seq<T>(layout, a, b, c, d, n, batch, s);
       return cuda_status(e);
     }
@@ -270,6 +282,12 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
     }
       // fall through: shapes beyond the on-chip kernel use the Thomas sweep
     case TRIDIAG_ALGO_THOMAS: {
+      if (thomas_by_partition<T>(layout, n, batch)) {
+        bool used = false;
+        const cudaError_t e = tdg::launch_wmc<T>(layout, a, b, c, d, x, n, batch, s, &used);
+        if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+        if (used) return TRIDIAG_SUCCESS;
+      }
       if (layout == TRIDIAG_LAYOUT_INTERLEAVED) {
         // partitioned sweep: every SM sub-partition busy for a few thousand systems
         bool used = false;

@@ -1299,13 +1299,16 @@ def profile_case(name: str) -> None:
         torch.cuda.synchronize()
         print("ok block2_64")
         return
-    if name == "ragged_long32":
+    if name in ("ragged_long32", "ragged_long32a"):
         # long unpivoted FP32 systems of a ragged batch (the chunked partition
         # method with element-wise staging): 256 dominant systems, n in
-        # [32769, 65536] (~200 MB), three solves
+        # [32769, 65536] (~200 MB), three solves; ragged_long32a: sizes
+        # rounded up to multiples of 4, every system 16-byte aligned
         from tridiagonalsolver_gb300 import ragged
 
         sizes = ragged.log_uniform_sizes(256, 32769, 65536, seed=11)
+        if name == "ragged_long32a":
+            sizes = (sizes + 3) // 4 * 4
         a, b, c, d, off, _ = ragged.synthetic_batch(sizes, nondominant_fraction=0.0, seed=11)
         plan = T.RaggedPlan(off, no_pivoting=np.ones(len(sizes), dtype=bool))
         x = torch.empty_like(d)
@@ -1660,7 +1663,8 @@ def main():
                          "remaining benchmark configurations, one JSON line each")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES) + ["block2_64", "ragged_step", "ragged64_step",
                                                                          "ragged_refine_step", "ragged_seq64",
-                                                                         "ragged_long32", "ragged_refine_small"], default=None,
+                                                                         "ragged_long32", "ragged_long32a",
+                                                                         "ragged_refine_small"], default=None,
                     help="run one small case of one kernel family three times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.profile_case:

@@ -716,11 +716,15 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
     long long rows = 0;
     for (size_t i = 0; i < longs.size(); ++i) {
       const long long n = len(longs[i]);
-      const long long P = (n + M - 1) / M;
+      // the chunk kernels put the system's first row after its 16-byte phase
+      // in identity rows, so that every chunk starts on a 16-byte boundary
+      long long phase = offsets[longs[i]] % (16 / (long long)sizeof(T));
+      if ((n + phase + M - 1) / M > (long long)tdg::WMC_GEN_MAX_ROWS * M) phase = 0;  // (as the kernels decide)
+      const long long P = (n + phase + M - 1) / M;
       roff[i + 1] = roff[i] + P;
       pmax = std::max(pmax, (int)P);
       rows += n;
-      for (long long c = 0; c * chunk_rows < n; ++c) {
+      for (long long c = 0; c * chunk_rows < n + phase; ++c) {
         cl_li.push_back((int)i);
         cl_ch.push_back((int)c);
       }

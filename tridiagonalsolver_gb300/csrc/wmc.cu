@@ -106,6 +106,12 @@ __device__ __forceinline__ void wmc_cp_async(T* smem, const T* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
+// 16 bytes (both addresses 16-byte aligned).
+__device__ __forceinline__ void wmc_cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
 template <typename T>
 struct WmcVec;
 template <>
@@ -185,6 +191,7 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
   long long goff = 0;                              // first row of this CTA (GEN)
   int row_start = 0;                               // ... within its system
   int rows_here = n;                               // rows this CTA holds
+  int lead = 0;                                    // identity rows before them (GEN)
   size_t rel_base = CHUNKED ? (size_t)j * ck.Rt + (size_t)ch * R : 0;     // partition index of t = 0
   size_t y_base = CHUNKED ? (size_t)j * ck.Ppad + (size_t)ch * R : 0;
   if constexpr (GEN) {
@@ -198,10 +205,17 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
     }
     const long long gsys = gen.offsets ? gen.offsets[j] : (long long)j * gen.stride;
     nn = gen.offsets ? (int)(gen.offsets[j + 1] - gsys) : gen.n;
-    row_start = CHUNKED ? ch * R * M : 0;
-    rows_here = min(nn - row_start, R * M);
-    Rc = (rows_here + M - 1) / M;
-    last_chunk = row_start + R * M >= nn;
+    // a long ragged system's chunks start on 16-byte boundaries (of arrays
+    // that start on one): chunk 0 holds the system's first rows after
+    // `phase` identity rows, the others start `phase` rows early (the plan
+    // counts the system's partitions and chunks with the phase)
+    int phase = CHUNKED && gen.offsets ? (int)(gsys % NV) : 0;
+    if ((nn + phase + M - 1) / M > WMC_GEN_MAX_ROWS * M) phase = 0;  // (its separators must stay within one CTA)
+    lead = CHUNKED && ch == 0 ? phase : 0;
+    row_start = CHUNKED ? (ch == 0 ? 0 : ch * R * M - phase) : 0;
+    rows_here = min(nn - row_start, R * M - lead);
+    Rc = (lead + rows_here + M - 1) / M;
+    last_chunk = row_start + rows_here >= nn;
     goff = gsys + row_start;
     if constexpr (CHUNKED) rel_base = y_base = (size_t)ck.roff[li] + (size_t)ch * R;
   }
@@ -210,20 +224,37 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
   const int t = threadIdx.x;
   const bool active = t < Rc;
   if constexpr (GEN) {
-    const int rows = Rc * M;
+    const int units = Rc * M / NV;
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
-      // TRANS: slot 0 <- c_{r-1}, slot 2 <- a_{r+1}; a_0 and c_{n-1} are not read
+      // TRANS: slot 0 <- c_{r-1}, slot 2 <- a_{r+1}; a_0 and c_{n-1} are not read.
+      // Shared row i holds the CTA's row i - lead; a 16-byte unit whose rows
+      // are all real (none of them a_0 or c_{n-1}) and whose global address
+      // is 16-byte aligned moves as one copy, the others element by element
+      // (identity rows: b = 1, the rest 0).
       const T* src = TRANS && k == 0 ? gen.in[2] + goff - 1 : TRANS && k == 2 ? gen.in[0] + goff + 1 : gen.in[k] + goff;
       const T pad = k == 1 ? T(1) : T(0);
-      for (int i = t; i < rows; i += nt) {
-        T* dst = &wmc_elem<T>(S[k], i / M, i % M);
-        const int r = row_start + i;  // row within the system
-        const bool skip = (k == 0 && r == 0) || (k == 2 && r == nn - 1);
-        if (i < rows_here && !skip)
-          wmc_cp_async(dst, src + i);
-        else
-          *dst = i < rows_here ? T(0) : pad;
+      const bool aligned = ((reinterpret_cast<uintptr_t>(src) / sizeof(T) + (uintptr_t)(NV - lead)) % NV) == 0;
+      for (int v = t; v < units; v += nt) {
+        const int i = v * NV, j0 = i - lead;  // first shared row of the unit, its row in the CTA
+        unsigned char* dst = S[k] + wmc_swz(i / M, (i % M) / NV);
+        const int r = row_start + j0;  // row within the system
+        const bool whole = aligned && j0 >= 0 && j0 + NV <= rows_here && !(k == 0 && r == 0) && !(k == 2 && r + NV >= nn);
+        if (whole) {
+          wmc_cp_async16(dst, src + j0);
+        } else {
+#pragma unroll
+          for (int e = 0; e < NV; ++e) {
+            T* de = reinterpret_cast<T*>(dst) + e;
+            const int jj = j0 + e;
+            const bool real = jj >= 0 && jj < rows_here;
+            const bool skip = (k == 0 && r + e == 0) || (k == 2 && r + e == nn - 1);
+            if (real && !skip)
+              wmc_cp_async(de, src + jj);
+            else
+              *de = real ? T(0) : pad;
+          }
+        }
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -237,7 +268,7 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
         bool bad = false;
         if (active)
           for (int q = 0; q < M; ++q)
-            if (t * M + q < rows_here)
+            if (t * M + q < lead + rows_here)  // (identity rows pass)
               bad |= !dominant_row(wmc_elem<T>(S[0], t, q), wmc_elem<T>(S[1], t, q), wmc_elem<T>(S[2], t, q));
         if (__syncthreads_or(bad)) {
           if (t == 0) {
@@ -510,7 +541,7 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
             if (r > 0) xl_[u] = __ldg(xf + i - 1);
             xc_[u] = __ldg(xf + i);
             if (r + 1 < nn) xr_[u] = __ldg(xf + i + 1);
-            lam[u] = wmc_elem<T>(S[3], i / M, i % M);
+            lam[u] = wmc_elem<T>(S[3], (i + lead) / M, (i + lead) % M);
           }
         }
 #pragma unroll
@@ -530,7 +561,24 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
       for (int k = 0; k < NO; ++k) {
         unsigned char* src = S[MODE == 1 ? k : 3];
         T* dst = gen.out[k] + goff;
-        for (int i = t; i < rows_here; i += nt) dst[i] = wmc_elem<T>(src, i / M, i % M);
+        // whole 16-byte units where the rows' global addresses allow (shared
+        // row i is the CTA's row i - lead)
+        if (((reinterpret_cast<uintptr_t>(dst) / sizeof(T) + (uintptr_t)(NV - lead)) % NV) == 0 &&
+            (reinterpret_cast<uintptr_t>(dst) % sizeof(T)) == 0) {
+          const int units = (lead + rows_here + NV - 1) / NV;
+          for (int v = t; v < units; v += nt) {
+            const int i = v * NV, j0 = i - lead;
+            const unsigned char* su = src + wmc_swz(i / M, (i % M) / NV);
+            if (j0 >= 0 && j0 + NV <= rows_here) {
+              *reinterpret_cast<uint4*>(dst + j0) = *reinterpret_cast<const uint4*>(su);
+            } else {
+              for (int e = 0; e < NV; ++e)
+                if (j0 + e >= 0 && j0 + e < rows_here) dst[j0 + e] = reinterpret_cast<const T*>(su)[e];
+            }
+          }
+        } else {
+          for (int i = t; i < rows_here; i += nt) dst[i] = wmc_elem<T>(src, (i + lead) / M, (i + lead) % M);
+        }
       }
     }
     return;

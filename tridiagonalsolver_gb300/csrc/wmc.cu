@@ -227,12 +227,12 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
     const int units = Rc * M / NV;
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
-      // TRANS: slot 0 <- c_{r-1}, slot 2 <- a_{r+1}; a_0 and c_{n-1} are not read.
-      // Shared row i holds the CTA's row i - lead; a 16-byte unit whose rows
-      // are all real (none of them a_0 or c_{n-1}) and whose global address
-      // is 16-byte aligned moves as one copy, the others element by element
-      // (identity rows: b = 1, the rest 0).
-      const T* src = TRANS && k == 0 ? gen.in[2] + goff - 1 : TRANS && k == 2 ? gen.in[0] + goff + 1 : gen.in[k] + goff;
+      // A as it is (TRANS too: A^T is formed below); a_0 and c_{n-1} are
+      // not read.  Shared row i holds the CTA's row i - lead; a 16-byte unit
+      // whose rows are all real (none of them a_0 or c_{n-1}) and whose
+      // global address is 16-byte aligned moves as one copy, the others
+      // element by element (identity rows: b = 1, the rest 0).
+      const T* src = gen.in[k] + goff;
       const T pad = k == 1 ? T(1) : T(0);
       const bool aligned = ((reinterpret_cast<uintptr_t>(src) / sizeof(T) + (uintptr_t)(NV - lead)) % NV) == 0;
       for (int v = t; v < units; v += nt) {
@@ -266,10 +266,20 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
         // pivoted bucket of its size class (the staged rows are checked
         // before any arithmetic; a chunk checks its own rows)
         bool bad = false;
-        if (active)
-          for (int q = 0; q < M; ++q)
-            if (t * M + q < lead + rows_here)  // (identity rows pass)
-              bad |= !dominant_row(wmc_elem<T>(S[0], t, q), wmc_elem<T>(S[1], t, q), wmc_elem<T>(S[2], t, q));
+        if (active) {
+          // 16-byte units of the partition's row; rows past the system are
+          // identity rows, which pass
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            T av[NV], bv[NV], cv[NV];
+            const int off = wmc_swz(t, u);
+            W::split(*reinterpret_cast<const typename W::V*>(S[0] + off), av);
+            W::split(*reinterpret_cast<const typename W::V*>(S[1] + off), bv);
+            W::split(*reinterpret_cast<const typename W::V*>(S[2] + off), cv);
+#pragma unroll
+            for (int e = 0; e < NV; ++e) bad |= !dominant_row(av[e], bv[e], cv[e]);
+          }
+        }
         if (__syncthreads_or(bad)) {
           if (t == 0) {
             gen.chk.kinds[j] = 0;
@@ -283,6 +293,43 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
           return;
         }
       }
+    }
+    if constexpr (TRANS) {
+      // A^T of the staged A, as MODE 1 forms it below: sub-diagonal c_{i-1}
+      // into the a slot, super-diagonal a_{i+1} into the c slot; across the
+      // chunk's edges from global memory (c of the row before its first row,
+      // a of the row after its last one where that row is in the system)
+      T cprev = T(0), anext = T(0);
+      if (active) {
+        if (t > 0) cprev = wmc_elem<T>(S[2], t - 1, M - 1);
+        else if (row_start > 0) cprev = gen.in[2][goff - 1];
+        if (t + 1 < Rc) anext = wmc_elem<T>(S[0], t + 1, 0);
+        else if (lead + rows_here == Rc * M && row_start + rows_here < nn) anext = gen.in[0][goff + rows_here];
+      }
+      __syncthreads();
+      if (active) {
+        T carry = cprev;
+        T av[NV], an[NV];
+        W::split(*reinterpret_cast<const typename W::V*>(S[0] + wmc_swz(t, 0)), av);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int off = wmc_swz(t, q);
+          if (q < 7) W::split(*reinterpret_cast<const typename W::V*>(S[0] + wmc_swz(t, q + 1)), an);
+          T cv[NV], sub[NV], sup[NV];
+          W::split(*reinterpret_cast<const typename W::V*>(S[2] + off), cv);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            sub[v] = v == 0 ? carry : cv[v - 1];
+            sup[v] = v + 1 < NV ? av[v + 1] : (q < 7 ? an[0] : anext);
+          }
+          carry = cv[NV - 1];
+          *reinterpret_cast<typename W::V*>(S[0] + off) = W::join(sub);
+          *reinterpret_cast<typename W::V*>(S[2] + off) = W::join(sup);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) av[v] = an[v];
+        }
+      }
+      __syncthreads();
     }
   } else {
     if (t == 0) {
@@ -530,6 +577,46 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
       T* __restrict__ o1 = gen.out[1] + goff;
       T* __restrict__ o2 = gen.out[2] + goff;
       T* __restrict__ o3 = gen.out[3] + goff;
+      auto al16 = [&](const T* q) {  // shared row 0's global address 16-byte aligned
+        return ((reinterpret_cast<uintptr_t>(q) / sizeof(T) + (uintptr_t)(NV - lead)) % NV) == 0 &&
+               reinterpret_cast<uintptr_t>(q) % sizeof(T) == 0;
+      };
+      if (al16(xf) && al16(o0) && al16(o1) && al16(o2) && al16(o3)) {
+        // whole 16-byte units of rows: lambda from shared memory, x of the
+        // unit and of the rows either side from global memory
+        const int units = (lead + rows_here + NV - 1) / NV;
+        for (int v = t; v < units; v += nt) {
+          const int i = v * NV, j0 = i - lead, r0 = row_start + j0;
+          if (j0 >= 0 && j0 + NV <= rows_here) {
+            T lam[NV], xc[NV], g1[NV], g2[NV], g3[NV];
+            W::split(*reinterpret_cast<const typename W::V*>(S[3] + wmc_swz(i / M, (i % M) / NV)), lam);
+            W::split(__ldg(reinterpret_cast<const typename W::V*>(xf + j0)), xc);
+            const T xl = r0 > 0 ? __ldg(xf + j0 - 1) : T(0);
+            const T xr = r0 + NV < nn ? __ldg(xf + j0 + NV) : T(0);
+#pragma unroll
+            for (int e = 0; e < NV; ++e) {
+              g1[e] = r0 + e > 0 ? -lam[e] * (e > 0 ? xc[e - 1] : xl) : T(0);
+              g2[e] = -lam[e] * xc[e];
+              g3[e] = r0 + e + 1 < nn ? -lam[e] * (e + 1 < NV ? xc[e + 1] : xr) : T(0);
+            }
+            *reinterpret_cast<typename W::V*>(o0 + j0) = W::join(lam);
+            *reinterpret_cast<typename W::V*>(o1 + j0) = W::join(g1);
+            *reinterpret_cast<typename W::V*>(o2 + j0) = W::join(g2);
+            *reinterpret_cast<typename W::V*>(o3 + j0) = W::join(g3);
+          } else {
+            for (int e = 0; e < NV; ++e) {
+              const int jj = j0 + e, r = row_start + jj;
+              if (jj < 0 || jj >= rows_here) continue;
+              const T l = wmc_elem<T>(S[3], (jj + lead) / M, (jj + lead) % M);
+              o0[jj] = l;
+              o1[jj] = r > 0 ? -l * __ldg(xf + jj - 1) : T(0);
+              o2[jj] = -l * __ldg(xf + jj);
+              o3[jj] = r + 1 < nn ? -l * __ldg(xf + jj + 1) : T(0);
+            }
+          }
+        }
+        return;
+      }
       constexpr int U = 8;
       for (int i0 = t; i0 < rows_here; i0 += U * nt) {
         T xl_[U], xc_[U], xr_[U], lam[U];

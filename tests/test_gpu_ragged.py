@@ -344,7 +344,7 @@ def test_ragged_autotune_unpivoted(cuda):
         assert eta <= 1e-6
 
 
-@pytest.mark.parametrize("iters,shape", [(1, "classes"), (2, "classes"), (1, "short")])
+@pytest.mark.parametrize("iters,shape", [(1, "classes"), (2, "classes"), (1, "short"), (3, "classes")])
 def test_ragged_refined_forward_and_adjoint(cuda, iters, shape):
     """FP64 ragged systems solved through an FP32 classified plan with FP64
     residual refinement, forward and adjoint: on diagonally dominant systems

@@ -90,3 +90,35 @@ def test_reference_names_vs_golden(cuda, golden, algo, dt, case):
         assert np.max(_rel(x, xr)) <= FWD[dt], name
         np.testing.assert_array_equal(a.cpu().numpy(), z[f"{case}/a"])
         np.testing.assert_array_equal(b.cpu().numpy(), z[f"{case}/b"])
+
+
+@pytest.mark.parametrize("dt,n", [(np.float32, 512), (np.float64, 256)])
+def test_pcr_tma_and_direct_paths(cuda, dt, n):
+    """PCR at n = 32 x 16 (FP32) / 32 x 8 (FP64): the persistent TMA-fed
+    kernel (contiguous layout; four PCR steps, the stride-16 chains solved by
+    lane pairs from both ends) and the direct-load kernel (packed layout;
+    five steps, one chain per lane) both meet the tolerances against the
+    oracle.  a[0] and c[n-1] are not part of a system: nonzero values there
+    leave each path's x exactly unchanged."""
+    import tridiagonalsolver_gb300 as T
+
+    batch = 1000
+    a, b, c, d = (v.astype(dt) for v in inputs.dominant(n, batch, seed=77))
+    a2, c2 = a.copy(), c.copy()
+    a2[:, 0], c2[:, n - 1] = 5.0, -7.0  # outside the system
+    tma, direct = [], []
+    for aa, cc in ((a, c), (a2, c2)):
+        ts = [cuda.from_numpy(v.copy()).cuda() for v in (aa, b, cc, d)]
+        tma.append(T.solve_out(*ts, n, algo="pcr").cpu().numpy().reshape(batch, n))
+        p = cuda.from_numpy(inputs.to_packed(aa, b, cc, d)).cuda()
+        T.solve(p, None, None, None, n, algo="pcr", layout="packed")
+        direct.append(p.cpu().numpy().reshape(batch, 4, n)[:, 3, :])
+    np.testing.assert_array_equal(tma[1], tma[0])
+    np.testing.assert_array_equal(direct[1], direct[0])
+    a64, b64, c64, d64 = (v.astype(np.float64) for v in (a, b, c, d))
+    xo = O.gtsv(a64, b64, c64, d64, n).reshape(batch, n)
+    for x in (tma[0], direct[0]):
+        x = x.astype(np.float64)
+        _, eta = O.backward_error(a64, b64, c64, d64, x, n)
+        assert eta <= ETA[dt]
+        assert np.max(_rel(x, xo)) <= FWD[dt]

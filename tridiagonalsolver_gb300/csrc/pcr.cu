@@ -16,14 +16,16 @@
 // index, conflict-free for the chunk-wise writes and the chain-wise reads)
 // and lane c runs Thomas on chain c (rows c, c+32, ...), whose solution it
 // stores with coalesced 32-row writes.  The step and chain code is in
-// pcr.cuh, shared with the persistent TMA-fed kernel of wm.cu that serves
-// n = 512 (FP32) / 256 (FP64) in the contiguous layout.
+// pcr.cuh; the steps are shared with the persistent TMA-fed kernel of wm.cu,
+// which serves n = 512 (FP32) / 256 (FP64) in the contiguous layout with the
+// half variant (four steps, each stride-16 chain solved by two lanes).
 //
 // Reference: PCR5_{reg,shmem}_kernel, Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:
 // 886-1282 (5 PCR steps over streamed 32-row chunks, then a per-lane Thomas
 // on the stride-32 chains), and the CPU versions
 // Tridiagonal_AVX512/tridiagonal_d_avx512.cpp:419-646.  The "half" variants
-// (4 steps, chains shared by two lanes) are served by the same 5-step kernel.
+// (4 steps, chains shared by two lanes, PCR4_reg_kernel at :1020-1158) are
+// served by the same kernels.
 #include "common.cuh"
 #include "kernels.h"
 #include "pcr.cuh"

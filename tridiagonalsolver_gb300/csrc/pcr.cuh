@@ -1,5 +1,6 @@
-// PCR-pThomas pieces shared by the direct-load kernel (pcr.cu) and the
-// persistent TMA-fed chunk kernel (wm.cu).
+// PCR-pThomas pieces: the PCR steps (shared by the direct-load kernel,
+// pcr.cu, and the persistent TMA-fed chunk kernel, wm.cu) and the
+// one-chain-per-lane Thomas of the direct-load kernel.
 //
 // A warp holds one system of 32*Q rows, lane l the Q consecutive rows
 // l*Q .. l*Q+Q-1 (identity rows past n).  Five PCR steps with strides 1, 2,
@@ -22,11 +23,37 @@ namespace tdg {
 
 __device__ __forceinline__ int pcr_swz(int r) { return (r & ~31) | ((r & 31) ^ ((r >> 5) & 31)); }
 
-// The five PCR steps on the lane's chunk (A, B, C, D updated in place).
-template <typename T, int Q>
-__device__ __forceinline__ void pcr_chunk_steps(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (&D)[Q], int lane) {
+// Whole-lane neighbour exchange for the PCR strides s >= Q: lo receives v of
+// lane - ls, hi v of lane + ls.  Lanes whose partner lies outside the warp
+// receive a finite value of their own warp, which reaches only rows whose
+// coupling coefficient is an exact zero (see pcr_chunk_steps).
+struct PcrShfl {
+  template <typename T, int Q>
+  __device__ __forceinline__ void lanes(const T (&v)[Q], T (&lo)[Q], T (&hi)[Q], int, int ls) const {
 #pragma unroll
-  for (int s = 1; s < 32; s <<= 1) {
+    for (int q = 0; q < Q; ++q) {
+      lo[q] = shfl_up(v[q], ls);
+      hi[q] = shfl_down(v[q], ls);
+    }
+  }
+};
+
+// STEPS PCR steps (strides 1 .. 2^(STEPS-1)) on the lane's chunk (A, B, C,
+// D updated in place): five for PCR-pThomas (32 chains of stride 32), four
+// for the half variant (16 chains of stride 16).
+//
+// Ends of the system.  A of row 0 and C of row 32 Q - 1 must be zero (the
+// callers load them so; rows past n are identity rows, A = C = 0).  Step s
+// then keeps A = 0 on rows < 2 s and C = 0 on rows >= 32 Q - 2 s (each new
+// coefficient is a product with the old one or with the neighbour's), so a
+// neighbour that lies outside the system is always multiplied by an exact
+// zero: the exchanges take whatever finite value the shuffle returns there
+// instead of selecting an identity row (one select per exchanged value).
+template <typename T, int Q, int STEPS = 5, typename X = PcrShfl>
+__device__ __forceinline__ void pcr_chunk_steps(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (&D)[Q], int lane,
+                                                const X& xch = X()) {
+#pragma unroll
+  for (int s = 1; s < (1 << STEPS); s <<= 1) {
     T al[Q], ga[Q], de[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -35,7 +62,7 @@ __device__ __forceinline__ void pcr_chunk_steps(T (&A)[Q], T (&B)[Q], T (&C)[Q],
       ga[q] = k.div(C[q]);
       de[q] = k.div(D[q]);
     }
-    // neighbours s rows above (L) and below (R), identity outside the system
+    // neighbours s rows above (L) and below (R)
     T aL[Q], gL[Q], dL[Q], aR[Q], gR[Q], dR[Q];
     if (s < Q) {
 #pragma unroll
@@ -45,36 +72,25 @@ __device__ __forceinline__ void pcr_chunk_steps(T (&A)[Q], T (&B)[Q], T (&C)[Q],
           gL[q] = ga[q - s];
           dL[q] = de[q - s];
         } else {  // row q - s + Q of lane - 1
-          const T u0 = shfl_up(al[q - s + Q], 1), u1 = shfl_up(ga[q - s + Q], 1), u2 = shfl_up(de[q - s + Q], 1);
-          aL[q] = lane >= 1 ? u0 : T(0);
-          gL[q] = lane >= 1 ? u1 : T(0);
-          dL[q] = lane >= 1 ? u2 : T(0);
+          aL[q] = shfl_up(al[q - s + Q], 1);
+          gL[q] = shfl_up(ga[q - s + Q], 1);
+          dL[q] = shfl_up(de[q - s + Q], 1);
         }
         if (q + s < Q) {
           aR[q] = al[q + s];
           gR[q] = ga[q + s];
           dR[q] = de[q + s];
         } else {  // row q + s - Q of lane + 1
-          const T u0 = shfl_down(al[q + s - Q], 1), u1 = shfl_down(ga[q + s - Q], 1),
-                  u2 = shfl_down(de[q + s - Q], 1);
-          aR[q] = lane <= 30 ? u0 : T(0);
-          gR[q] = lane <= 30 ? u1 : T(0);
-          dR[q] = lane <= 30 ? u2 : T(0);
+          aR[q] = shfl_down(al[q + s - Q], 1);
+          gR[q] = shfl_down(ga[q + s - Q], 1);
+          dR[q] = shfl_down(de[q + s - Q], 1);
         }
       }
     } else {
       const int ls = s / Q;  // whole lanes
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const T u0 = shfl_up(al[q], ls), u1 = shfl_up(ga[q], ls), u2 = shfl_up(de[q], ls);
-        aL[q] = lane >= ls ? u0 : T(0);
-        gL[q] = lane >= ls ? u1 : T(0);
-        dL[q] = lane >= ls ? u2 : T(0);
-        const T v0 = shfl_down(al[q], ls), v1 = shfl_down(ga[q], ls), v2 = shfl_down(de[q], ls);
-        aR[q] = lane + ls <= 31 ? v0 : T(0);
-        gR[q] = lane + ls <= 31 ? v1 : T(0);
-        dR[q] = lane + ls <= 31 ? v2 : T(0);
-      }
+      xch.lanes(al, aL, aR, lane, ls);
+      xch.lanes(ga, gL, gR, lane, ls);
+      xch.lanes(de, dL, dR, lane, ls);
     }
 #pragma unroll
     for (int q = 0; q < Q; ++q) {

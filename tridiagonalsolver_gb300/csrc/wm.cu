@@ -335,10 +335,27 @@ struct WmOut {
   alignas(1024) T buf[32 * M];
 };
 
-// warps per CTA: as many as fit their buffers in 210 KB, at most 8
-template <typename T, int M>
+// FP32 PCR-pThomas instead runs 12 warps per SM with a two-slot ring: its
+// warps are latency bound (one system after another), so more of them beat
+// a deeper ring; the launch bound caps its registers at 168, which it fits
+// without spilling (FP64 would spill: it keeps 8 warps).
+constexpr int WM_PCR_WARPS = 12;
+template <int ALG, typename T>
+constexpr bool wm_wide() {
+  return ALG == CHUNK_PCR && sizeof(T) == 4;
+}
+template <int ALG, typename T>
+constexpr int wm_slots() {
+  return wm_wide<ALG, T>() ? 2 : WM_SLOTS;
+}
+
+// warps per CTA: as many as fit their buffers in 210 KB, at most 8 (FP32
+// PCR: 12 in 216 KB)
+template <int ALG, typename T, int M>
 constexpr int wm_warps() {
-  return (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 8 <= 215040 ? 8
+  return wm_wide<ALG, T>() && (sizeof(WmSlot<T, M>) * 2 + sizeof(WmOut<T, M>)) * WM_PCR_WARPS <= 221184
+             ? WM_PCR_WARPS
+         : (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 8 <= 215040 ? 8
          : (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 4 <= 215040 ? 4 : 2;
 }
 
@@ -351,10 +368,139 @@ __device__ __forceinline__ int wm_swz(int t, int q) {
   return logical ^ (((logical >> 7) & mask) << 4);
 }
 
+// PCR whole-lane exchange through the warp's output buffer (free while the
+// PCR steps run): each lane writes its chunk of one array as 16-byte units at
+// the buffer's swizzled offsets, then reads the chunks of lanes lane -/+ ls
+// (mod 32).  Any 8 consecutive chunk rows hit 8 distinct bank groups under
+// the 64-byte swizzle, so writes and reads are conflict free; 3 Q/NV shared
+// accesses per array replace 2 Q shuffles.
+template <typename T, int ROWB>
+struct WmXch {
+  unsigned char* buf;
+  template <int Q>
+  __device__ __forceinline__ void lanes(const T (&v)[Q], T (&lo)[Q], T (&hi)[Q], int lane, int ls) const {
+    using W = Vec16<T>;
+    constexpr int NV = W::N;
+    static_assert(Q * (int)sizeof(T) == ROWB, "one chunk per buffer row");
+#pragma unroll
+    for (int u = 0; u < Q / NV; ++u)
+      *reinterpret_cast<typename W::V*>(buf + wm_swz<ROWB>(lane, u)) = W::make(v, u * NV);
+    __syncwarp();
+    const int tl = (lane - ls) & 31, th = (lane + ls) & 31;
+#pragma unroll
+    for (int u = 0; u < Q / NV; ++u) {
+      const typename W::V x = *reinterpret_cast<const typename W::V*>(buf + wm_swz<ROWB>(tl, u));
+      const typename W::V y = *reinterpret_cast<const typename W::V*>(buf + wm_swz<ROWB>(th, u));
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        lo[u * NV + k] = W::get(x, k);
+        hi[u * NV + k] = W::get(y, k);
+      }
+    }
+    __syncwarp();
+  }
+};
+
+// PCR-half-pThomas chain phase for 64-byte lane rows (Q = 16 FP32, Q = 8
+// FP64), after four PCR steps: row r couples only to r -/+ 16, so chain
+// c = r mod 16 (positions p = r div 16, 2Q rows) is a tridiagonal system of
+// its own.  Lanes 2c and 2c+1 solve it from both ends: lane 2c eliminates
+// positions 0 .. Q-1 top-down, lane 2c+1 positions 2Q-1 .. Q bottom-up (its
+// sub- and super-diagonal exchange roles), each leaving one row
+//     x_own + e x_partner = f
+// of the two middle unknowns; one shuffle and a 2 x 2 solve give both, and
+// each lane back-substitutes its half.  Both lanes run the same instructions
+// on slots k = 0 .. Q-1 (position k, resp. 2Q-1-k).
+//
+// The rows reach their lanes through `buf` (32 x 64 bytes, the TMA
+// swizzle): row L of the buffer holds lane L's Q slots, which it reads as
+// 16-byte units (conflict free); lane l's row Q l + q goes to lane
+// L = 2 (r & 15) + h, slot k, where h = [p >= Q], k = h ? 2Q-1-p : p.  p is
+// the same for all q of a lane and L = L0 + 2q with (L >> 1) & 3 = q & 3, so
+// the byte offset is q * 128 + base[q & 3].  The lane's sub-/super-diagonal
+// roles are chosen by the writer (h is the writer's too).  The a of row 0
+// and the c of row 32 Q - 1, and after four steps A of rows < 16 and C of
+// rows >= 32 Q - 16, are zero, so the chains start and end clean.
+//
+// x leaves in buf in the TMA store layout (row r at chunk r / Q, element
+// r % Q).  The caller's buf must be free; it is left holding x.
+template <typename T, int Q>
+__device__ __forceinline__ void wm_pcr_half(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (&D)[Q], int lane,
+                                            unsigned char* buf) {
+  using W = Vec16<T>;
+  constexpr int NV = W::N;
+  constexpr int ES = (int)sizeof(T);
+  static_assert(Q * ES == 64 && Q / NV == 4, "64-byte lane rows");
+  const int r0 = Q * lane;
+  const int p = r0 >> 4;
+  const int h = p >= Q ? 1 : 0;
+  const int k = h ? 2 * Q - 1 - p : p;
+  const int L0 = 2 * (r0 & 15) + h;
+  int base[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) base[j] = L0 * 64 + (((k / NV) ^ j) << 4) + (k % NV) * ES;
+  const int rb = lane * 64, rx = (lane >> 1) & 3;
+  T LO[Q], MI[Q], HI[Q], RH[Q];
+  auto pass = [&](int round, T (&dst)[Q]) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const T v = round == 0 ? (h ? C[q] : A[q]) : round == 1 ? (h ? A[q] : C[q]) : round == 2 ? B[q] : D[q];
+      *reinterpret_cast<T*>(buf + q * 128 + base[q & 3]) = v;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < Q / NV; ++u) {
+      const typename W::V w = *reinterpret_cast<const typename W::V*>(buf + rb + ((u ^ rx) << 4));
+#pragma unroll
+      for (int i = 0; i < NV; ++i) dst[u * NV + i] = W::get(w, i);
+    }
+    __syncwarp();
+  };
+  pass(0, LO);
+  pass(1, HI);
+  pass(2, MI);
+  pass(3, RH);
+  // elimination towards the middle
+  T e = T(0), f = T(0);
+#pragma unroll
+  for (int s = 0; s < Q; ++s) {
+    const Div<T> piv(fma(-LO[s], e, MI[s]));
+    e = piv.div(HI[s]);
+    f = piv.div(fma(-LO[s], f, RH[s]));
+    HI[s] = e;
+    RH[s] = f;
+  }
+  const T pe = __shfl_xor_sync(FULL, e, 1), pf = __shfl_xor_sync(FULL, f, 1);
+  T xv = Div<T>(fma(-e, pe, T(1))).div(fma(-e, pf, f));
+  RH[Q - 1] = xv;
+#pragma unroll
+  for (int ss = 1; ss < Q; ++ss) {
+    const int s = Q - 1 - ss;
+    xv = fma(-HI[s], xv, RH[s]);
+    RH[s] = xv;
+  }
+  // x of slot s: row c + 16 p(s), p(s) = h ? 2Q-1-s : s; chunk t = p (16 / Q) + c / Q, element c % Q
+  const int c = lane >> 1, hh = lane & 1;
+  const int e0 = c % Q;
+  const int t0 = hh * (2 * Q - 1) * (16 / Q) + c / Q;  // chunk of slot 0
+  const int ts = hh ? -(16 / Q) : (16 / Q);            // chunk step per slot
+  // (t >> 1) & 3 of slot s is g(s) ^ 3 hh with g(s) known at compile time
+  const int ex = (e0 / NV) ^ (3 * hh);
+  const int eo = (e0 % NV) * ES;
+#pragma unroll
+  for (int s = 0; s < Q; ++s) {
+    constexpr int SPC = 16 / Q;
+    const int g = ((s * SPC) >> 1) & 3;  // (t >> 1) & 3 for hh = 0
+    const int t = t0 + s * ts;
+    *reinterpret_cast<T*>(buf + t * 64 + (((ex ^ g) & 3) << 4) + eo) = RH[s];
+  }
+}
+
 template <int ALG, typename T, int M, int G>
-__global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
+__global__ void __launch_bounds__(32 * wm_warps<ALG, T, M>(), 1)
     wm_tma_kernel(const __grid_constant__ TwMaps maps, int n, int nboxes, int* err) {
-  constexpr int WARPS = wm_warps<T, M>();
+  constexpr int WARPS = wm_warps<ALG, T, M>();
+  constexpr int SLOTS = wm_slots<ALG, T>();
   using W = Vec16<T>;
   constexpr int NV = W::N;
   constexpr int ROWB = M * (int)sizeof(T);
@@ -362,13 +508,13 @@ __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WmSlot<T, M>* slots = reinterpret_cast<WmSlot<T, M>*>(base) + warp * WM_SLOTS;
-  WmOut<T, M>* out = reinterpret_cast<WmOut<T, M>*>(base + sizeof(WmSlot<T, M>) * WM_SLOTS * WARPS) + warp;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * WARPS) +
-                   warp * WM_SLOTS;
+  WmSlot<T, M>* slots = reinterpret_cast<WmSlot<T, M>*>(base) + warp * SLOTS;
+  WmOut<T, M>* out = reinterpret_cast<WmOut<T, M>*>(base + sizeof(WmSlot<T, M>) * SLOTS * WARPS) + warp;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (sizeof(WmSlot<T, M>) * SLOTS + sizeof(WmOut<T, M>)) * WARPS) +
+                   warp * SLOTS;
   const int gw = blockIdx.x * WARPS + warp, nw = gridDim.x * WARPS;
   if (lane == 0) {
-    for (int q = 0; q < WM_SLOTS; ++q) mbar_init(&bars[q], 1);
+    for (int q = 0; q < SLOTS; ++q) mbar_init(&bars[q], 1);
     fence_mbar_init();
   }
   __syncwarp();
@@ -380,11 +526,11 @@ __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
   };
   const int count = gw < nboxes ? (nboxes - gw + nw - 1) / nw : 0;
   if (lane == 0)
-    for (int i = 0; i < count && i < WM_SLOTS; ++i) load(i, i);
+    for (int i = 0; i < count && i < SLOTS; ++i) load(i, i);
   const int tl = lane % G;
   unsigned parity = 0;
   for (int i = 0; i < count; ++i) {
-    const int q = i % WM_SLOTS;
+    const int q = i % SLOTS;
     const bool ok = __all_sync(FULL, mbar_wait(&bars[q], (parity >> q) & 1u, err));
     parity ^= 1u << q;
     if (!ok) break;
@@ -405,23 +551,21 @@ __global__ void __launch_bounds__(32 * wm_warps<T, M>(), 1)
       }
     }
     __syncwarp();
-    // the slot is free again: refill it with the box WM_SLOTS ahead
-    if (lane == 0 && i + WM_SLOTS < count) load(i + WM_SLOTS, q);
+    // the slot is free again: refill it with the box SLOTS ahead
+    if (lane == 0 && i + SLOTS < count) load(i + SLOTS, q);
     if constexpr (ALG == CHUNK_PCR) {
-      // PCR-pThomas (32 lanes per system): the PCR steps on the chunks, then
-      // the chains through the output buffer (free once the previous x
-      // store has read it), then x of rows lane + 32 k into the buffer's
-      // TMA layout
-      pcr_chunk_steps<T, M>(A, B, C, D, lane);
+      // PCR-half-pThomas (32 lanes per system): four PCR steps on the chunks
+      // (a of row 0 and c of the last row are not part of the system), then
+      // the stride-16 chains by lane pairs; both exchange through the output
+      // buffer (free once the previous x store has read it), which is left
+      // holding x in its TMA layout
+      if (lane == 0) A[0] = T(0);
+      if (lane == 31) C[M - 1] = T(0);
       if (lane == 0) bulk_wait_read<0>();
       __syncwarp();
-      pcr_chain_thomas<T, M>(A, B, C, D, X, lane, out->buf);
-#pragma unroll
-      for (int k = 0; k < M; ++k) {
-        const int r = lane + 32 * k;
-        const int off = wm_swz<ROWB>(r / M, (r % M) / NV) + (r % NV) * (int)sizeof(T);
-        *reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(out->buf) + off) = X[k];
-      }
+      unsigned char* ob = reinterpret_cast<unsigned char*>(out->buf);
+      pcr_chunk_steps<T, M, 4>(A, B, C, D, lane, WmXch<T, ROWB>{ob});
+      wm_pcr_half<T, M>(A, B, C, D, lane, ob);
     } else {
       chunk_solve<ALG, T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
       if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer
@@ -446,7 +590,8 @@ template <int ALG, typename T, int M, int G>
 static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch, cudaStream_t st,
                             cudaError_t* e) {
   constexpr int ROWB = M * (int)sizeof(T);
-  constexpr int WARPS = wm_warps<T, M>();
+  constexpr int WARPS = wm_warps<ALG, T, M>();
+  constexpr int SLOTS = wm_slots<ALG, T>();
   const CUtensorMapSwizzle sw = ROWB == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
                                 : ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
                                 : ROWB == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
@@ -460,7 +605,7 @@ static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x
       return false;
   const int nboxes = (int)((rows + 31) / 32);
   const size_t smem =
-      (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * WARPS + 8 * WM_SLOTS * WARPS + 1024;
+      (sizeof(WmSlot<T, M>) * SLOTS + sizeof(WmOut<T, M>)) * WARPS + 8 * SLOTS * WARPS + 1024;
   *e = cudaFuncSetAttribute(wm_tma_kernel<ALG, T, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (*e != cudaSuccess) return true;
   int dev = 0, sms = 0;
@@ -530,8 +675,9 @@ static cudaError_t launch_chunk(int layout, const T* a, const T* b, const T* c, 
   return cudaSuccess;
 }
 
-// PCR-pThomas for n = 32 * 16 (FP32) / 32 * 8 (FP64), contiguous layout,
-// on the persistent TMA-fed kernel; other shapes: pcr.cu.
+// PCR for n = 32 * 16 (FP32) / 32 * 8 (FP64), contiguous layout, on the
+// persistent TMA-fed kernel (the half variant: four PCR steps, lane-pair
+// chains); other shapes: pcr.cu.
 template <typename T>
 cudaError_t launch_pcr_tma(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int n, int batch,
                            cudaStream_t st, bool* used) {

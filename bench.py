@@ -900,7 +900,8 @@ def _ragged_cpu_rate(O, sizes, nondom, target_s=8.0):
 def _ragged_fp64_parts(torch, T, O, ragged, plan32, sizes, off, nondom, stream):
     """The same ragged batch in FP64, forward + adjoint: the plain FP64
     solve (a classifying FP64 plan) and the refined form (FP32 solves through
-    the FP32 plan, FP64 residuals, 1 and 2 refinement steps); worst normwise
+    the FP32 plan, FP64 residuals, 1 and 2 refinement steps, and 1 step plus
+    1 on the systems the plan pivots); worst normwise
     backward error of x and of lambda (A^T lambda = xbar) over a sample,
     dominant and non-dominant systems apart."""
     a, b, c, d, _, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, seed=2024)
@@ -935,15 +936,16 @@ def _ragged_fp64_parts(torch, T, O, ragged, plan32, sizes, off, nondom, stream):
     out.append(dict({"name": "FP64 forward+adjoint, plain (classifying FP64 plan)", "ms_per_step": ms,
                      "systems_per_s": len(sizes) / (ms * 1e-3),
                      "buckets": [f"class {k} v{v} x{cnt}" for k, v, cnt, _ in plan64.buckets()]}, **accuracy()))
-    for iters in (1, 2):
-        def refined(iters=iters):
-            plan32.refine(a, b, c, d, iters=iters, out=x, work=work, stream=stream)
-            plan32.refine_adjoint(a, b, c, x, w, iters=iters, grads=grads, work=work, stream=stream)
+    for iters, piv in ((1, 0), (2, 0), (1, 1)):
+        def refined(iters=iters, piv=piv):
+            plan32.refine(a, b, c, d, iters=iters, out=x, work=work, stream=stream, pivoted_iters=piv)
+            plan32.refine_adjoint(a, b, c, x, w, iters=iters, grads=grads, work=work, stream=stream,
+                                  pivoted_iters=piv)
 
         ms, _ = _graph_time(torch, stream, refined, 3, 3)
-        out.append(dict({"name": f"FP64 forward+adjoint, refined ({iters} step{'s' if iters > 1 else ''}: FP32 "
-                                 f"solves, FP64 residuals)", "ms_per_step": ms,
-                         "systems_per_s": len(sizes) / (ms * 1e-3)}, **accuracy()))
+        steps = f"{iters} step{'s' if iters > 1 else ''}" + (", then 1 step on the pivoted systems" if piv else "")
+        out.append(dict({"name": f"FP64 forward+adjoint, refined ({steps}: FP32 solves, FP64 residuals)",
+                         "ms_per_step": ms, "systems_per_s": len(sizes) / (ms * 1e-3)}, **accuracy()))
     del a, b, c, d, w, x, grads, work, plan64
     torch.cuda.empty_cache()
     return out

@@ -395,6 +395,21 @@ int tridiag_ragged_refine_adjoint_double(tridiag_ragged_plan *plan32, const doub
                                          const double *c, const double *x, const double *xbar, double *ga,
                                          double *gb, double *gc, double *gd, int iters, void *work,
                                          size_t work_bytes, const long long *offsets, void *stream);
+/* As the two above, then `pivoted_iters` (0-8) more steps on the systems
+ * the plan solves with pivoting only (every system for a plan without marks):
+ * the FP64 residual of their rows, an FP32 correction solve of their buckets
+ * alone, their rows of x (lambda) updated in place; the systems marked for
+ * the unpivoted kernels keep the result of the `iters` steps.  Diagonally
+ * dominant systems converge in fewer steps than the ones that need pivoting,
+ * so iters = 1, pivoted_iters = 1 costs little more than one step. */
+int tridiag_ragged_refine_ex_double(tridiag_ragged_plan *plan32, const double *a, const double *b, const double *c,
+                                    const double *d, double *x, int iters, int pivoted_iters, void *work,
+                                    size_t work_bytes, const long long *offsets, void *stream);
+int tridiag_ragged_refine_adjoint_ex_double(tridiag_ragged_plan *plan32, const double *a, const double *b,
+                                            const double *c, const double *x, const double *xbar, double *ga,
+                                            double *gb, double *gc, double *gd, int iters, int pivoted_iters,
+                                            void *work, size_t work_bytes, const long long *offsets,
+                                            void *stream);
 /* The marks (1: solved without pivoting) of the plan's last solve, one byte
  * per system, into host memory (synchronous); TRIDIAG_ERR_NOT_SUPPORTED for
  * a plan without marks. */

@@ -372,6 +372,46 @@ def test_ragged_refined_forward_and_adjoint(cuda, iters, shape):
         _check_system(hs, grads, n, True, 1e-12, 1e-10)
 
 
+@pytest.mark.parametrize("shape", ["classes", "long"])
+def test_ragged_refined_pivoted_steps(cuda, shape):
+    """The refinement steps restricted to the systems the plan solves with
+    pivoting (iters = 1, pivoted_iters = 1) on a batch with 30% non-dominant
+    systems: normwise backward error <= 1e-12 for x and lambda on every
+    system; the systems marked for the unpivoted kernels keep the one-step
+    result exactly and the pivoted ones get the two-step result exactly (the
+    same arithmetic per system), forward and adjoint."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    if shape == "classes":
+        sizes = _sizes(20000)
+    else:  # long systems: the chunked kernels of both kinds, and systems sharing the row passes' chunks
+        sizes = np.array([40000, 3, 70000, 2049, 1, 65536, 33000, 100, 47000, 5], dtype=np.int64)
+    a, b, c, d, off, nondom = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=0.3, seed=31)
+    plan32 = T.RaggedPlan(off, dtype=torch.float32, classify=True)
+    w = torch.rand_like(d) * 2 - 1
+    x1 = plan32.refine(a, b, c, d, iters=1).clone()
+    x2 = plan32.refine(a, b, c, d, iters=2).clone()
+    x = plan32.refine(a, b, c, d, iters=1, pivoted_iters=1)
+    kinds = plan32.kinds()
+    ga, gb, gc, gd = plan32.refine_adjoint(a, b, c, x, w, iters=1, pivoted_iters=1)
+    l1 = plan32.refine_adjoint(a, b, c, x, w, iters=1)[3]
+    l2 = plan32.refine_adjoint(a, b, c, x, w, iters=2)[3]
+    torch.cuda.synchronize()
+    assert nondom.any() and kinds[nondom].max() == 0  # the non-dominant systems are pivoted
+    assert kinds.max() == 1  # and some systems are not
+    for s in range(len(sizes)):
+        n = int(sizes[s])
+        lo, hi = int(off[s]), int(off[s + 1])
+        ref_x, ref_l = (x1, l1) if kinds[s] == 1 else (x2, l2)
+        assert torch.equal(x[lo:hi], ref_x[lo:hi]), ("x", s, n, int(kinds[s]))
+        assert torch.equal(gd[lo:hi], ref_l[lo:hi]), ("lambda", s, n, int(kinds[s]))
+        hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
+        grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
+        _check_system(hs, grads, n, not nondom[s], 1e-12, 1e-10)
+
+
 def test_ragged_refined_rejects_fp64_plan(cuda):
     import tridiagonalsolver_gb300 as T
 

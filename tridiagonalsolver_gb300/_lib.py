@@ -86,6 +86,8 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_ragged_refine_workspace_size": (_SZ, [ctypes.c_longlong]),
     "tridiag_ragged_refine_double": (_I, [_P] * 6 + [_I, _P, _SZ, _P, _P]),
     "tridiag_ragged_refine_adjoint_double": (_I, [_P] * 10 + [_I, _P, _SZ, _P, _P]),
+    "tridiag_ragged_refine_ex_double": (_I, [_P] * 6 + [_I, _I, _P, _SZ, _P, _P]),
+    "tridiag_ragged_refine_adjoint_ex_double": (_I, [_P] * 10 + [_I, _I, _P, _SZ, _P, _P]),
     "tridiag_ragged_plan_destroy": (None, [_P]),
     "tridiag_ragged_plan_buckets": (_I, [_P, _P, _I]),
     "tridiag_ragged_variant_max_n": (_I, [_I, _I]),

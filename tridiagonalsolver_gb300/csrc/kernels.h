@@ -277,6 +277,12 @@ cudaError_t launch_ragged_residual(bool trans, const double* a, const double* b,
                                    const RaggedRows& rr, cudaStream_t s);
 cudaError_t launch_ragged_gradient(const double* lam, const double* x, double* ga, double* gb, double* gc,
                                    const RaggedRows& rr, cudaStream_t s);
+// restricted to the systems with kinds[s] == 0 (all when kinds is NULL), x in place
+cudaError_t launch_ragged_residual_sel(bool trans, const double* a, const double* b, const double* c,
+                                       const double* rhs, const double* x, float* r32, const unsigned char* kinds,
+                                       const RaggedRows& rr, cudaStream_t s);
+cudaError_t launch_ragged_update_sel(double* x, const float* dx, const unsigned char* kinds, const RaggedRows& rr,
+                                     cudaStream_t s);
 cudaError_t launch_convert_probe(const double* in, float* out, double* back, size_t count, cudaStream_t s);
 
 // ipt.cu: Thomas for batch-interleaved systems, P partitions per system

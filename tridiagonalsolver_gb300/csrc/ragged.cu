@@ -870,11 +870,13 @@ int plan_create(tridiag_ragged_plan** out, const long long* offsets, int batch, 
 // recheck (forward solves of a mode-2 plan): the unpivoted kernels check
 // the rows they stage and the marks follow; false: the solve runs on the
 // plan's marks as they stand (marked first, where it has none, by the
-// classify pass on ka, kb, kc -- a, b, c when NULL).
+// classify pass on ka, kb, kc -- a, b, c when NULL).  pivoted_only: the
+// buckets of the systems marked for the unpivoted kernels are skipped (their
+// x is left as it is).
 template <typename T>
 int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const T* c, const T* d, T* x, const T* xf,
              T* ga, T* gb, T* gc, int* info, const long long* offsets, cudaStream_t s, bool recheck = true,
-             const T* ka = nullptr, const T* kb = nullptr, const T* kc = nullptr) {
+             const T* ka = nullptr, const T* kb = nullptr, const T* kc = nullptr, bool pivoted_only = false) {
   if (!plan || !a || !b || !c || !d || !x || !offsets) return TRIDIAG_ERR_INVALID_VALUE;
   if (plan->precision != (sizeof(T) == 8 ? 1 : 0)) return TRIDIAG_ERR_INVALID_VALUE;
   if (mode == 1 && (!xf || !ga || !gb || !gc)) return TRIDIAG_ERR_INVALID_VALUE;
@@ -914,6 +916,7 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
     chk.klists = plan->d_klists;
   }
   for (const auto& bk : plan->buckets) {
+    if (pivoted_only && bk.kind == 1) continue;
     // a bucket of one kind runs through that kind's list of its class
     const int* list = bk.klist >= 0 ? plan->d_klists + bk.klist_off : plan->d_lists + bk.list_off;
     tdg::BucketTicket tk;
@@ -1001,7 +1004,11 @@ int plan_run(tridiag_ragged_plan* plan, int mode, const T* a, const T* b, const 
 // of the same offsets: FP32 copies of A (trans: of A^T) and rhs, an FP32
 // solve, then `iters` steps of FP64 residual -> FP32 correction solve, the
 // FP64 iterate updated each time; out receives x (trans: lambda = A^{-T}
-// rhs).  Workspace: five FP32 rows-long arrays and one FP64 one.
+// rhs).  Then `piv_iters` more steps on the systems the plan solves with
+// pivoting only (all of them for a plan without marks): their residual, their
+// correction solves, their rows of out updated -- the systems marked for the
+// unpivoted kernels are diagonally dominant, and their FP32 solves need fewer
+// steps.  Workspace: five FP32 rows-long arrays and one FP64 one.
 inline size_t up256(size_t x) { return (x + 255) / 256 * 256; }
 
 size_t ragged_refine_ws(long long rows) {
@@ -1009,9 +1016,10 @@ size_t ragged_refine_ws(long long rows) {
 }
 
 int ragged_refine_impl(tridiag_ragged_plan* plan32, bool trans, const double* a, const double* b, const double* c,
-                       const double* rhs, double* out, int iters, void* work, size_t work_bytes,
+                       const double* rhs, double* out, int iters, int piv_iters, void* work, size_t work_bytes,
                        const long long* offsets, cudaStream_t s) {
-  if (!plan32 || !a || !b || !c || !rhs || !out || !offsets || iters < 0 || iters > 8)
+  if (!plan32 || !a || !b || !c || !rhs || !out || !offsets || iters < 0 || iters > 8 || piv_iters < 0 ||
+      piv_iters > 8)
     return TRIDIAG_ERR_INVALID_VALUE;
   if (plan32->precision != 0) return TRIDIAG_ERR_INVALID_VALUE;  // the solves run in FP32
   if (plan32->row0 != 0) return TRIDIAG_ERR_INVALID_VALUE;       // rows counted from offsets[0] = 0
@@ -1052,7 +1060,17 @@ int ragged_refine_impl(tridiag_ragged_plan* plan32, bool trans, const double* a,
     if (st != TRIDIAG_SUCCESS) return st;
     xcur = xnew;
   }
-  return tdg::launch_update(xcur, v1, out, (size_t)rows, s) == cudaSuccess ? TRIDIAG_SUCCESS : TRIDIAG_ERR_CUDA;
+  if (tdg::launch_update(xcur, v1, out, (size_t)rows, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  const unsigned char* sel = plan32->kinds_mode != 0 ? plan32->d_kinds : nullptr;
+  for (int it = 0; it < piv_iters; ++it) {
+    if (tdg::launch_ragged_residual_sel(trans, a, b, c, rhs, out, v0, sel, rr, s) != cudaSuccess)
+      return TRIDIAG_ERR_CUDA;
+    st = plan_run<float>(plan32, 0, a32, b32, c32, v0, v1, nullptr, nullptr, nullptr, nullptr, nullptr, offsets, s,
+                         false, ka, b32, kc, true);
+    if (st != TRIDIAG_SUCCESS) return st;
+    if (tdg::launch_ragged_update_sel(out, v1, sel, rr, s) != cudaSuccess) return TRIDIAG_ERR_CUDA;
+  }
+  return TRIDIAG_SUCCESS;
 }
 
 }  // namespace
@@ -1098,24 +1116,40 @@ size_t tridiag_ragged_refine_workspace_size(long long total_rows) {
   return total_rows > 0 ? ragged_refine_ws(total_rows) : 0;
 }
 
+int tridiag_ragged_refine_ex_double(tridiag_ragged_plan* plan32, const double* a, const double* b, const double* c,
+                                    const double* d, double* x, int iters, int pivoted_iters, void* work,
+                                    size_t work_bytes, const long long* offsets, void* stream) {
+  return ragged_refine_impl(plan32, false, a, b, c, d, x, iters, pivoted_iters, work, work_bytes, offsets,
+                            (cudaStream_t)stream);
+}
+
 int tridiag_ragged_refine_double(tridiag_ragged_plan* plan32, const double* a, const double* b, const double* c,
                                  const double* d, double* x, int iters, void* work, size_t work_bytes,
                                  const long long* offsets, void* stream) {
-  return ragged_refine_impl(plan32, false, a, b, c, d, x, iters, work, work_bytes, offsets, (cudaStream_t)stream);
+  return tridiag_ragged_refine_ex_double(plan32, a, b, c, d, x, iters, 0, work, work_bytes, offsets, stream);
+}
+
+int tridiag_ragged_refine_adjoint_ex_double(tridiag_ragged_plan* plan32, const double* a, const double* b,
+                                            const double* c, const double* x, const double* xbar, double* ga,
+                                            double* gb, double* gc, double* gd, int iters, int pivoted_iters,
+                                            void* work, size_t work_bytes, const long long* offsets, void* stream) {
+  if (!x || !ga || !gb || !gc || !gd) return TRIDIAG_ERR_INVALID_VALUE;
+  const cudaStream_t s = (cudaStream_t)stream;
+  const int st =
+      ragged_refine_impl(plan32, true, a, b, c, xbar, gd, iters, pivoted_iters, work, work_bytes, offsets, s);
+  if (st != TRIDIAG_SUCCESS) return st;
+  const tdg::RaggedRows rr{offsets, plan32->batch, plan32->d_chunk_sys, plan32->total_rows};
+  return tdg::launch_ragged_gradient(gd, x, ga, gb, gc, rr, s) == cudaSuccess
+             ? TRIDIAG_SUCCESS
+             : TRIDIAG_ERR_CUDA;
 }
 
 int tridiag_ragged_refine_adjoint_double(tridiag_ragged_plan* plan32, const double* a, const double* b,
                                          const double* c, const double* x, const double* xbar, double* ga,
                                          double* gb, double* gc, double* gd, int iters, void* work,
                                          size_t work_bytes, const long long* offsets, void* stream) {
-  if (!x || !ga || !gb || !gc || !gd) return TRIDIAG_ERR_INVALID_VALUE;
-  const cudaStream_t s = (cudaStream_t)stream;
-  const int st = ragged_refine_impl(plan32, true, a, b, c, xbar, gd, iters, work, work_bytes, offsets, s);
-  if (st != TRIDIAG_SUCCESS) return st;
-  const tdg::RaggedRows rr{offsets, plan32->batch, plan32->d_chunk_sys, plan32->total_rows};
-  return tdg::launch_ragged_gradient(gd, x, ga, gb, gc, rr, s) == cudaSuccess
-             ? TRIDIAG_SUCCESS
-             : TRIDIAG_ERR_CUDA;
+  return tridiag_ragged_refine_adjoint_ex_double(plan32, a, b, c, x, xbar, ga, gb, gc, gd, iters, 0, work,
+                                                 work_bytes, offsets, stream);
 }
 
 int tridiag_ragged_plan_buckets(const tridiag_ragged_plan* plan, int* out, int max_buckets) {

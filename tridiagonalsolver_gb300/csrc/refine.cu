@@ -399,6 +399,80 @@ __global__ void __launch_bounds__(256) ragged_gradient_kernel(const double* __re
   }
 }
 
+// The refinement steps restricted to the systems solved with pivoting
+// (kinds[s] == 0; every system when kinds is NULL), on x in place.
+//
+// ragged_sel: the system of row r0 + lane is s0 (the one holding r0) plus
+// the system starts in (r0, r0 + lane]; a warp whose chunk lies inside one
+// unselected system returns at once.
+__device__ __forceinline__ bool ragged_sel_skip(const RaggedRows& rr, const unsigned char* kinds, int s,
+                                                long long end) {
+  return kinds && __ldg(kinds + s) != 0 && __ldg(rr.offsets + s + 1) >= end;
+}
+__device__ __forceinline__ int ragged_lane_sys(int s0, unsigned first) {
+  const int lane = threadIdx.x & 31;
+  const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+  return s0 + __popc(first & upto & ~1u);
+}
+
+// r = rhs - A x (TRANS: A^T) as FP32, on the rows of the selected systems.
+// A step with no selected row is skipped: the x of its last row is then
+// needed by no later row (a selected row that is not its system's first has
+// its predecessor in the same, selected system).
+template <bool TRANS>
+__global__ void __launch_bounds__(256) ragged_residual_sel_kernel(
+    const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+    const double* __restrict__ rhs, const double* __restrict__ x, float* __restrict__ r32,
+    const unsigned char* __restrict__ kinds, const RaggedRows rr) {
+  long long begin, end;
+  int s;
+  if (!ragged_chunk(rr, &begin, &end, &s)) return;
+  if (ragged_sel_skip(rr, kinds, s, end)) return;
+  const int lane = threadIdx.x & 31;
+  double xlast = begin > 0 && __ldg(rr.offsets + s) < begin ? __ldg(x + begin - 1) : 0.0;
+  for (long long r0 = begin; r0 < end; r0 += 32) {
+    const int s0 = s;
+    unsigned fm, lm;
+    ragged_step_masks(rr, r0, s, fm, lm);
+    const long long r = r0 + lane;
+    const bool in = r < end, first = (fm >> lane) & 1u, last = (lm >> lane) & 1u;
+    const bool sel = in && (!kinds || __ldg(kinds + ragged_lane_sys(s0, fm)) == 0);
+    if (!__any_sync(0xffffffffu, sel)) continue;
+    const double xi = in ? __ldg(x + r) : 0.0;
+    double xm = __shfl_up_sync(0xffffffffu, xi, 1);
+    if (lane == 0) xm = xlast;
+    double xp = __shfl_down_sync(0xffffffffu, xi, 1);
+    if (lane == 31 && in && !last) xp = __ldg(x + r + 1);
+    if (sel) {
+      const double lo = first ? 0.0 : (TRANS ? __ldg(c + r - 1) : __ldg(a + r));
+      const double up = last ? 0.0 : (TRANS ? __ldg(a + r + 1) : __ldg(c + r));
+      double res = fma(-__ldg(b + r), xi, __ldg(rhs + r));
+      res = fma(-lo, xm, res);
+      res = fma(-up, xp, res);
+      r32[r] = narrow_rn(res);
+    }
+    xlast = __shfl_sync(0xffffffffu, xi, 31);
+  }
+}
+
+// x += dx on the rows of the selected systems
+__global__ void __launch_bounds__(256) ragged_update_sel_kernel(double* __restrict__ x, const float* __restrict__ dx,
+                                                                const unsigned char* __restrict__ kinds,
+                                                                const RaggedRows rr) {
+  long long begin, end;
+  int s;
+  if (!ragged_chunk(rr, &begin, &end, &s)) return;
+  if (ragged_sel_skip(rr, kinds, s, end)) return;
+  const int lane = threadIdx.x & 31;
+  for (long long r0 = begin; r0 < end; r0 += 32) {
+    const int s0 = s;
+    unsigned fm, lm;
+    ragged_step_masks(rr, r0, s, fm, lm);
+    const long long r = r0 + lane;
+    if (r < end && (!kinds || __ldg(kinds + ragged_lane_sys(s0, fm)) == 0)) x[r] += widen(__ldg(dx + r));
+  }
+}
+
 static int ragged_grid(const RaggedRows& rr) {
   const long long chunks = (rr.rows + RAGGED_ROW_CHUNK - 1) / RAGGED_ROW_CHUNK;
   return (int)((chunks + 7) / 8);  // eight warps (chunks) per 256-thread block
@@ -423,6 +497,24 @@ cudaError_t launch_ragged_residual(bool trans, const double* a, const double* b,
     ragged_residual_kernel<true><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, rr);
   else
     ragged_residual_kernel<false><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, xold, dx, xnew, r32, rr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ragged_residual_sel(bool trans, const double* a, const double* b, const double* c,
+                                       const double* rhs, const double* x, float* r32, const unsigned char* kinds,
+                                       const RaggedRows& rr, cudaStream_t s) {
+  if (rr.rows <= 0) return cudaSuccess;
+  if (trans)
+    ragged_residual_sel_kernel<true><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, x, r32, kinds, rr);
+  else
+    ragged_residual_sel_kernel<false><<<ragged_grid(rr), 256, 0, s>>>(a, b, c, rhs, x, r32, kinds, rr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ragged_update_sel(double* x, const float* dx, const unsigned char* kinds, const RaggedRows& rr,
+                                     cudaStream_t s) {
+  if (rr.rows <= 0) return cudaSuccess;
+  ragged_update_sel_kernel<<<ragged_grid(rr), 256, 0, s>>>(x, dx, kinds, rr);
   return cudaGetLastError();
 }
 

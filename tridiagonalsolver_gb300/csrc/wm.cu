@@ -335,26 +335,26 @@ struct WmOut {
   alignas(1024) T buf[32 * M];
 };
 
-// FP32 PCR-pThomas instead runs 12 warps per SM with a two-slot ring: its
-// warps are latency bound (one system after another), so more of them beat
-// a deeper ring; the launch bound caps its registers at 168, which it fits
-// without spilling (FP64 would spill: it keeps 8 warps).
-constexpr int WM_PCR_WARPS = 12;
-template <int ALG, typename T>
+// FP32 PCR and CR-PCR with 64-byte lane rows instead run 12 warps per SM
+// with a two-slot ring: their warps are latency bound (one system after
+// another), so more of them beat a deeper ring; the launch bound caps their
+// registers at 168, which they fit without spilling (FP64 PCR would spill).
+constexpr int WM_WIDE_WARPS = 12;
+template <int ALG, typename T, int M>
 constexpr bool wm_wide() {
-  return ALG == CHUNK_PCR && sizeof(T) == 4;
+  return (ALG == CHUNK_PCR || ALG == CHUNK_CRPCR) && sizeof(T) == 4 &&
+         (sizeof(WmSlot<T, M>) * 2 + sizeof(WmOut<T, M>)) * WM_WIDE_WARPS <= 221184;
 }
-template <int ALG, typename T>
+template <int ALG, typename T, int M>
 constexpr int wm_slots() {
-  return wm_wide<ALG, T>() ? 2 : WM_SLOTS;
+  return wm_wide<ALG, T, M>() ? 2 : WM_SLOTS;
 }
 
-// warps per CTA: as many as fit their buffers in 210 KB, at most 8 (FP32
-// PCR: 12 in 216 KB)
+// warps per CTA: as many as fit their buffers in 210 KB, at most 8 (the
+// wide kernels: 12 in 216 KB)
 template <int ALG, typename T, int M>
 constexpr int wm_warps() {
-  return wm_wide<ALG, T>() && (sizeof(WmSlot<T, M>) * 2 + sizeof(WmOut<T, M>)) * WM_PCR_WARPS <= 221184
-             ? WM_PCR_WARPS
+  return wm_wide<ALG, T, M>() ? WM_WIDE_WARPS
          : (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 8 <= 215040 ? 8
          : (sizeof(WmSlot<T, M>) * WM_SLOTS + sizeof(WmOut<T, M>)) * 4 <= 215040 ? 4 : 2;
 }
@@ -500,7 +500,7 @@ template <int ALG, typename T, int M, int G>
 __global__ void __launch_bounds__(32 * wm_warps<ALG, T, M>(), 1)
     wm_tma_kernel(const __grid_constant__ TwMaps maps, int n, int nboxes, int* err) {
   constexpr int WARPS = wm_warps<ALG, T, M>();
-  constexpr int SLOTS = wm_slots<ALG, T>();
+  constexpr int SLOTS = wm_slots<ALG, T, M>();
   using W = Vec16<T>;
   constexpr int NV = W::N;
   constexpr int ROWB = M * (int)sizeof(T);
@@ -591,7 +591,7 @@ static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x
                             cudaError_t* e) {
   constexpr int ROWB = M * (int)sizeof(T);
   constexpr int WARPS = wm_warps<ALG, T, M>();
-  constexpr int SLOTS = wm_slots<ALG, T>();
+  constexpr int SLOTS = wm_slots<ALG, T, M>();
   const CUtensorMapSwizzle sw = ROWB == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
                                 : ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
                                 : ROWB == 32 ? CU_TENSOR_MAP_SWIZZLE_32B

@@ -235,7 +235,7 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
       const T* src = gen.in[k] + goff;
       const T pad = k == 1 ? T(1) : T(0);
       const bool aligned = ((reinterpret_cast<uintptr_t>(src) / sizeof(T) + (uintptr_t)(NV - lead)) % NV) == 0;
-      for (int v = t; v < units; v += nt) {
+      auto unit = [&](int v) {
         const int i = v * NV, j0 = i - lead;  // first shared row of the unit, its row in the CTA
         unsigned char* dst = S[k] + wmc_swz(i / M, (i % M) / NV);
         const int r = row_start + j0;  // row within the system
@@ -255,7 +255,24 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
               *de = real ? T(0) : pad;
           }
         }
+      };
+      // The units [vlo, vhi) are whole by construction -- past the lead rows
+      // and a_0, before the chunk's last real row and c_{n-1} -- and move
+      // with no per-unit tests; only the few units at the chunk's ends take
+      // the tests above.
+      int vlo = 0, vhi = 0;
+      if (aligned) {
+        vlo = (lead > 0 ? 1 : 0) + (k == 0 && row_start == 0 && lead == 0 ? 1 : 0);
+        vhi = (rows_here + lead) / NV;
+        if (k == 2) {
+          const int xc = nn - row_start + lead - NV;  // whole c units need r + NV < nn
+          vhi = min(vhi, xc > 0 ? (xc + NV - 1) / NV : 0);
+        }
       }
+      int v = t;
+      for (; v < units && v < vlo; v += nt) unit(v);
+      for (; v < vhi; v += nt) wmc_cp_async16(S[k] + wmc_swz(v >> 3, v & 7), src + (v * NV - lead));
+      for (; v < units; v += nt) unit(v);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_all;\n" ::: "memory");

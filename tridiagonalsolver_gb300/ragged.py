@@ -137,32 +137,36 @@ class RaggedPlan:
         nbytes = _sig().tridiag_ragged_refine_workspace_size(self.rows)
         return torch.empty(nbytes, dtype=torch.uint8, device=self.offsets.device)
 
-    def refine(self, a, b, c, d, iters=1, out=None, work=None, stream=None):
+    def refine(self, a, b, c, d, iters=1, out=None, work=None, stream=None, pivoted_iters=0):
         """FP64 systems (a, b, c, d float64) solved through this FP32 plan
-        with `iters` FP64-residual refinement steps; returns x (float64)."""
+        with `iters` FP64-residual refinement steps, then `pivoted_iters`
+        more on the systems the plan solves with pivoting only; returns x
+        (float64)."""
         if self.precision != 0:
             raise ValueError("refine runs through an FP32 plan")
         x = out if out is not None else torch.empty_like(d)
         work = work if work is not None else self.refine_workspace()
         D = torch.float64
-        st = _sig().tridiag_ragged_refine_double(self._h, _ptr(a, D), _ptr(b, D), _ptr(c, D), _ptr(d, D),
-                                                 _ptr(x, D), int(iters), _ptr(work), work.numel(),
-                                                 _ptr(self.offsets), _stream_ptr(stream))
-        check(st, "tridiag_ragged_refine_double")
+        st = _sig().tridiag_ragged_refine_ex_double(self._h, _ptr(a, D), _ptr(b, D), _ptr(c, D), _ptr(d, D),
+                                                    _ptr(x, D), int(iters), int(pivoted_iters), _ptr(work),
+                                                    work.numel(), _ptr(self.offsets), _stream_ptr(stream))
+        check(st, "tridiag_ragged_refine_ex_double")
         return x
 
-    def refine_adjoint(self, a, b, c, x, xbar, iters=1, grads=None, work=None, stream=None):
+    def refine_adjoint(self, a, b, c, x, xbar, iters=1, grads=None, work=None, stream=None, pivoted_iters=0):
         """(ga, gb, gc, gd) in FP64 of L with dL/dx = xbar through x = A^-1 d,
-        lambda = A^-T xbar by the refined solve of A^T through this FP32 plan."""
+        lambda = A^-T xbar by the refined solve of A^T through this FP32 plan
+        (`iters` steps, then `pivoted_iters` on the pivoted systems only)."""
         if self.precision != 0:
             raise ValueError("refine_adjoint runs through an FP32 plan")
         ga, gb, gc, gd = grads if grads is not None else (torch.empty_like(x) for _ in range(4))
         work = work if work is not None else self.refine_workspace()
         D = torch.float64
-        st = _sig().tridiag_ragged_refine_adjoint_double(
+        st = _sig().tridiag_ragged_refine_adjoint_ex_double(
             self._h, _ptr(a, D), _ptr(b, D), _ptr(c, D), _ptr(x, D), _ptr(xbar, D), _ptr(ga, D), _ptr(gb, D),
-            _ptr(gc, D), _ptr(gd, D), int(iters), _ptr(work), work.numel(), _ptr(self.offsets), _stream_ptr(stream))
-        check(st, "tridiag_ragged_refine_adjoint_double")
+            _ptr(gc, D), _ptr(gd, D), int(iters), int(pivoted_iters), _ptr(work), work.numel(), _ptr(self.offsets),
+            _stream_ptr(stream))
+        check(st, "tridiag_ragged_refine_adjoint_ex_double")
         return ga, gb, gc, gd
 
     def __del__(self):

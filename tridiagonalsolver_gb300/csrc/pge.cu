@@ -1466,10 +1466,36 @@ __device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint
   cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
 
+// L2 prefetch of CTA `rank`'s rows of bucket entry k (the system a resident
+// cluster solves next): the four arrays' rows [row0 + 1, row0 + rows - 1)
+// within the system -- a row dropped at each end and the range aligned
+// inward to 16 bytes, so that it stays inside the arrays for the adjoint's
+// shifted a and c as well.
+template <typename T, int NT, int CL>
+__device__ __forceinline__ void pgc_prefetch(const PgeIO<T>& io, int k, int rank) {
+  int sys, n, m, ms;
+  size_t base;
+  pge_system(io, k, CL * NT, sys, base, n, m, ms);
+  m |= 1;
+  const int row0 = rank * NT * m;
+  const int lo = row0 + 1, hi = min(n, row0 + NT * m) - 1;
+  if (hi <= lo) return;
+  const T* arr[4] = {io.a, io.b, io.c, io.d};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uintptr_t s = (reinterpret_cast<uintptr_t>(arr[q] + base + lo) + 15) & ~uintptr_t(15);
+    const uintptr_t e = reinterpret_cast<uintptr_t>(arr[q] + base + hi) & ~uintptr_t(15);
+    if (e > s)
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"((unsigned)(e - s)) : "memory");
+  }
+}
+
 // TICKET: resident clusters drain one size bucket of a ragged batch (CTA 0
 // of the cluster takes the ticket, the others read it through distributed
 // shared memory); a separate instance, so the one-cluster-per-system kernel
-// keeps its register allocation.
+// keeps its register allocation.  Each cluster holds its next ticket while
+// it solves the current system, and every CTA prefetches its rows of that
+// next system into L2, so that the next staging reads L2 instead of HBM.
 template <typename T, int NT, int CL, int MODE, bool TICKET = false>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(const PgeIO<T> io) {
   __shared__ __align__(8) uint64_t s_bar;
@@ -1479,8 +1505,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ int s_item;
-    for (;;) {
-      if (cluster.block_rank() == 0 && threadIdx.x == 0) {
+    const int rank = (int)cluster.block_rank();
+    auto take = [&]() {  // the next ticket, -1 past the bucket's end
+      if (rank == 0 && threadIdx.x == 0) {
         const int k = atomicAdd(io.ticket, 1);
         const int cnt = io.dcount ? *(volatile const int*)io.dcount : io.count;
         s_item = k < cnt && (!io.err || *(volatile int*)io.err == 0) ? k : -1;
@@ -1488,11 +1515,20 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) pgc_kernel(c
       cluster.sync();
       const int k = *cluster.map_shared_rank(&s_item, 0);
       cluster.sync();  // (read by all before CTA 0 writes the next one)
-      if (k < 0) break;
-      if (io.kinds && io.kinds[io.list[k]] != io.want) continue;
-      if (io.only && !io.only[io.list[k]]) continue;
-      pgc_body<T, NT, CL, MODE>(io, k, &s_bar);  // (ends with a cluster barrier)
-      if (threadIdx.x == 0) mbar_inval(&s_bar);   // re-armed by the next system
+      return k;
+    };
+    auto wanted = [&](int k) {
+      return !(io.kinds && io.kinds[io.list[k]] != io.want) && !(io.only && !io.only[io.list[k]]);
+    };
+    int k = take();
+    while (k >= 0) {
+      const int kn = take();
+      if (kn >= 0 && threadIdx.x == 0 && wanted(kn)) pgc_prefetch<T, NT, CL>(io, kn, rank);
+      if (wanted(k)) {
+        pgc_body<T, NT, CL, MODE>(io, k, &s_bar);  // (ends with a cluster barrier)
+        if (threadIdx.x == 0) mbar_inval(&s_bar);   // re-armed by the next system
+      }
+      k = kn;
     }
   }
 }

@@ -4,10 +4,12 @@
 //
 // A warp holds one system of 32*Q rows, lane l the Q consecutive rows
 // l*Q .. l*Q+Q-1 (identity rows past n).  Five PCR steps with strides 1, 2,
-// 4, 8, 16 leave every row coupled only to the rows 32 above and below; a
-// step of stride s < Q finds most neighbours in the lane's own registers and
+// 4, 8, 16 leave every row coupled only to the rows 32 above and below (four
+// steps, for the half variant of wm.cu: 16 above and below); a step of
+// stride s < Q finds most neighbours in the lane's own registers and
 // exchanges only the s rows at each end of the chunk with the adjacent lane
-// (6 s shuffles), strides s >= Q shift whole lanes (6 Q shuffles).
+// (6 s shuffles), strides s >= Q shift whole lanes (6 Q shuffles, or an
+// exchange through shared memory).
 //
 // Chain transpose.  Afterwards chain c (rows c, c+32, ...) is solved by lane
 // c.  The rows pass through shared memory at index

@@ -95,3 +95,17 @@ def test_host_solve_and_path_count_checks_need_no_device(lib):
     n, batch = 100000, 5
     need = 2 * n * batch * 8 + 4 * ((n + 31) // 32) * batch + 4 * batch
     assert lib.tridiag_gtsv_workspace_size(1, 0, n, batch) >= need
+
+
+def test_ragged_refine_ex_checks_need_no_device(lib):
+    """The refined ragged entry points with pivoted_iters reject a missing
+    plan or arrays before any CUDA call."""
+    from tridiagonalsolver_gb300 import _lib
+
+    p = ctypes.c_void_p(256)
+    assert lib.tridiag_ragged_refine_ex_double(None, p, p, p, p, p, 1, 1, p, 1 << 20, p, None) == _lib.ERR_INVALID_VALUE
+    assert lib.tridiag_ragged_refine_adjoint_ex_double(None, p, p, p, p, p, p, p, p, p, 1, 1, p, 1 << 20, p,
+                                                       None) == _lib.ERR_INVALID_VALUE
+    # the adjoint's gradient outputs are checked first
+    assert lib.tridiag_ragged_refine_adjoint_ex_double(p, p, p, p, p, p, None, p, p, p, 1, 1, p, 1 << 20, p,
+                                                       None) == _lib.ERR_INVALID_VALUE

@@ -97,19 +97,21 @@ __device__ __forceinline__ void store_chunk(const T (&r)[M], T* p, int s, int m,
 
 // PCR over segments of G lanes of a warp (G = 4..32, one system per
 // segment): equation alpha x_{t-1} + beta x_t + gamma x_{t+1} = delta per
-// lane, t = lane % G; returns x_t.
+// lane, t = lane % G; returns x_t.  Each lane shuffles its own 1/beta (formed
+// once, by its owner, instead of by each of its two readers: the same value).
 template <typename T, int G>
 __device__ __forceinline__ T warp_pcr(T al, T be, T ga, T de, int tl) {
 #pragma unroll
   for (int s = 1; s < G; s <<= 1) {
-    T aL = __shfl_up_sync(FULL, al, s, G), bL = __shfl_up_sync(FULL, be, s, G);
+    const T ib = Div<T>(be).inv();
+    T aL = __shfl_up_sync(FULL, al, s, G), iL = __shfl_up_sync(FULL, ib, s, G);
     T gL = __shfl_up_sync(FULL, ga, s, G), dL = __shfl_up_sync(FULL, de, s, G);
-    T aR = __shfl_down_sync(FULL, al, s, G), bR = __shfl_down_sync(FULL, be, s, G);
+    T aR = __shfl_down_sync(FULL, al, s, G), iR = __shfl_down_sync(FULL, ib, s, G);
     T gR = __shfl_down_sync(FULL, ga, s, G), dR = __shfl_down_sync(FULL, de, s, G);
-    if (tl < s) { aL = T(0); bL = T(1); gL = T(0); dL = T(0); }
-    if (tl + s >= G) { aR = T(0); bR = T(1); gR = T(0); dR = T(0); }
-    const T k1 = al * Div<T>(bL).inv();
-    const T k2 = ga * Div<T>(bR).inv();
+    if (tl < s) { aL = T(0); iL = T(1); gL = T(0); dL = T(0); }
+    if (tl + s >= G) { aR = T(0); iR = T(1); gR = T(0); dR = T(0); }
+    const T k1 = al * iL;
+    const T k2 = ga * iR;
     const T nb = fma(-k2, aR, fma(-k1, gL, be));
     const T nd = fma(-k2, dR, fma(-k1, dL, de));
     al = -k1 * aL;

@@ -481,39 +481,45 @@ __device__ __forceinline__ void wmc_body(const WmcMaps& maps, int n, int R, int 
     ga = sc * Pn;
     de = fma(-sc, Gn, fma(-sa, dp, sd));
   }
-  // parallel cyclic reduction: row t combines rows t - s and t + s
+  // parallel cyclic reduction: row t combines rows t - s and t + s.  Each
+  // row publishes (a, 1/b, c, d): its reciprocal is formed once, by its
+  // owner, instead of once by each of its two readers (the same value: x
+  // is unchanged), which for FP64 saves three FP64 instructions per row and
+  // step.
+  T ib = active ? Div<T>(be).inv() : T(1);
   for (int s = 1; s < Rc; s <<= 1) {
     if (active) {
       ra[t] = al;
-      rb[t] = be;
+      rb[t] = ib;
       rc[t] = ga;
       rd[t] = de;
     }
     __syncthreads();
     if (active) {
-      T a1 = T(0), b1 = T(1), c1 = T(0), d1 = T(0), a2 = T(0), b2 = T(1), c2 = T(0), d2 = T(0);
+      T a1 = T(0), i1 = T(1), c1 = T(0), d1 = T(0), a2 = T(0), i2 = T(1), c2 = T(0), d2 = T(0);
       if (t - s >= 0) {
         a1 = ra[t - s];
-        b1 = rb[t - s];
+        i1 = rb[t - s];
         c1 = rc[t - s];
         d1 = rd[t - s];
       }
       if (t + s < Rc) {
         a2 = ra[t + s];
-        b2 = rb[t + s];
+        i2 = rb[t + s];
         c2 = rc[t + s];
         d2 = rd[t + s];
       }
-      const T k1 = al * Div<T>(b1).inv();
-      const T k2 = ga * Div<T>(b2).inv();
+      const T k1 = al * i1;
+      const T k2 = ga * i2;
       be = fma(-k2, a2, fma(-k1, c1, be));
       de = fma(-k2, d2, fma(-k1, d1, de));
       al = -k1 * a1;
       ga = -k2 * c2;
+      ib = Div<T>(be).inv();
     }
     __syncthreads();
   }
-  if (active) ys[t] = de * Div<T>(be).inv();
+  if (active) ys[t] = de * ib;
   }
   if constexpr (MODE == 3) {
     if (active) {

@@ -545,3 +545,29 @@ def test_ragged_chunked_flagged_system_resolved(cuda):
         hs = [_host(t, off, s) for t in (a, b, c, d, x, w)]
         grads = [_host(g, off, s) for g in (ga, gb, gc, gd)]
         _check_system(hs, grads, n, False, ETA["float64"], GTOL["float64"])
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_ragged_results_are_reproducible(cuda, dtype):
+    """Forward and adjoint of a classifying plan on a mixed batch (long
+    chunked systems, pivoted clusters and tickets, device-grown lists): the
+    same inputs give bit-identical x and gradients run after run, whatever
+    order the resident CTAs take the systems in."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    dt = getattr(torch, dtype)
+    sizes = ragged.log_uniform_sizes(600, 32, 65536, seed=17)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=dt, nondominant_fraction=0.3, seed=17)
+    w = torch.rand_like(d) * 2 - 1
+    plan = T.RaggedPlan(off, dtype=dt, classify=True)
+    runs = []
+    for _ in range(3):
+        x = plan.solve(a, b, c, d)
+        g = plan.adjoint(a, b, c, x, w)
+        torch.cuda.synchronize()
+        runs.append([x.clone()] + [t.clone() for t in g])
+    for r in runs[1:]:
+        for p, q in zip(runs[0], r):
+            assert torch.equal(p, q)

@@ -414,21 +414,24 @@ struct WmXch {
 // each lane back-substitutes its half.  Both lanes run the same instructions
 // on slots k = 0 .. Q-1 (position k, resp. 2Q-1-k).
 //
-// The rows reach their lanes through `buf` (32 x 64 bytes, the TMA
-// swizzle): row L of the buffer holds lane L's Q slots, which it reads as
-// 16-byte units (conflict free); lane l's row Q l + q goes to lane
+// The rows reach their lanes through `xch`, four arrays of 32 x 64 bytes
+// (the ring slot the system came in, free once its rows are in registers;
+// the TMA swizzle): row L of each array holds lane L's Q slots, which it
+// reads as 16-byte units (conflict free); lane l's row Q l + q goes to lane
 // L = 2 (r & 15) + h, slot k, where h = [p >= Q], k = h ? 2Q-1-p : p.  p is
 // the same for all q of a lane and L = L0 + 2q with (L >> 1) & 3 = q & 3, so
-// the byte offset is q * 128 + base[q & 3].  The lane's sub-/super-diagonal
-// roles are chosen by the writer (h is the writer's too).  The a of row 0
-// and the c of row 32 Q - 1, and after four steps A of rows < 16 and C of
-// rows >= 32 Q - 16, are zero, so the chains start and end clean.
+// the byte offset is q * 128 + base[q & 3].  a, b, c, d go to arrays 0-3 in
+// one round, and each lane reads its sub-/super-diagonal from array 0 or 2
+// by its parity.  Then `refill` runs (the slot is free again: the caller
+// loads the next box into it).  The a of row 0 and the c of row 32 Q - 1,
+// and after four steps A of rows < 16 and C of rows >= 32 Q - 16, are zero,
+// so the chains start and end clean.
 //
 // x leaves in buf in the TMA store layout (row r at chunk r / Q, element
 // r % Q).  The caller's buf must be free; it is left holding x.
-template <typename T, int Q>
+template <typename T, int Q, typename Refill>
 __device__ __forceinline__ void wm_pcr_half(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (&D)[Q], int lane,
-                                            unsigned char* buf) {
+                                            unsigned char* xch, unsigned char* buf, const Refill& refill) {
   using W = Vec16<T>;
   constexpr int NV = W::N;
   constexpr int ES = (int)sizeof(T);
@@ -441,27 +444,36 @@ __device__ __forceinline__ void wm_pcr_half(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (
   int base[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) base[j] = L0 * 64 + (((k / NV) ^ j) << 4) + (k % NV) * ES;
+  constexpr int AB = 32 * Q * ES;  // bytes per exchanged array
   const int rb = lane * 64, rx = (lane >> 1) & 3;
-  T LO[Q], MI[Q], HI[Q], RH[Q];
-  auto pass = [&](int round, T (&dst)[Q]) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const T v = round == 0 ? (h ? C[q] : A[q]) : round == 1 ? (h ? A[q] : C[q]) : round == 2 ? B[q] : D[q];
-      *reinterpret_cast<T*>(buf + q * 128 + base[q & 3]) = v;
-    }
-    __syncwarp();
+  for (int q = 0; q < Q; ++q) {
+    const int o = q * 128 + base[q & 3];
+    *reinterpret_cast<T*>(xch + o) = A[q];
+    *reinterpret_cast<T*>(xch + AB + o) = B[q];
+    *reinterpret_cast<T*>(xch + 2 * AB + o) = C[q];
+    *reinterpret_cast<T*>(xch + 3 * AB + o) = D[q];
+  }
+  __syncwarp();
+  T LO[Q], MI[Q], HI[Q], RH[Q];
+  const int odd = lane & 1;  // bottom-up lane: c below, a above
+  auto read = [&](const unsigned char* src, T (&dst)[Q]) {
 #pragma unroll
     for (int u = 0; u < Q / NV; ++u) {
-      const typename W::V w = *reinterpret_cast<const typename W::V*>(buf + rb + ((u ^ rx) << 4));
+      const typename W::V w = *reinterpret_cast<const typename W::V*>(src + rb + ((u ^ rx) << 4));
 #pragma unroll
       for (int i = 0; i < NV; ++i) dst[u * NV + i] = W::get(w, i);
     }
-    __syncwarp();
   };
-  pass(0, LO);
-  pass(1, HI);
-  pass(2, MI);
-  pass(3, RH);
+  read(xch + (odd ? 2 : 0) * AB, LO);
+  read(xch + (odd ? 0 : 2) * AB, HI);
+  read(xch + AB, MI);
+  read(xch + 3 * AB, RH);
+  // the exchange arrays are free: order these accesses before the async
+  // proxy's refill of them
+  fence_async_smem();
+  __syncwarp();
+  refill();
   // elimination towards the middle
   T e = T(0), f = T(0);
 #pragma unroll
@@ -553,21 +565,26 @@ __global__ void __launch_bounds__(32 * wm_warps<ALG, T, M>(), 1)
       }
     }
     __syncwarp();
-    // the slot is free again: refill it with the box SLOTS ahead
-    if (lane == 0 && i + SLOTS < count) load(i + SLOTS, q);
+    // the slot is free again: refill it with the box SLOTS ahead (PCR first
+    // uses it for its chain transpose)
+    auto refill = [&]() {
+      if (lane == 0 && i + SLOTS < count) load(i + SLOTS, q);
+    };
+    if constexpr (ALG != CHUNK_PCR) refill();
     if constexpr (ALG == CHUNK_PCR) {
       // PCR-half-pThomas (32 lanes per system): four PCR steps on the chunks
-      // (a of row 0 and c of the last row are not part of the system), then
-      // the stride-16 chains by lane pairs; both exchange through the output
-      // buffer (free once the previous x store has read it), which is left
-      // holding x in its TMA layout
+      // (a of row 0 and c of the last row are not part of the system), their
+      // whole-lane exchanges through the output buffer (free once the
+      // previous x store has read it); then the stride-16 chains by lane
+      // pairs, transposed through the slot, which is refilled after; x in
+      // the output buffer's TMA layout
       if (lane == 0) A[0] = T(0);
       if (lane == 31) C[M - 1] = T(0);
       if (lane == 0) bulk_wait_read<0>();
       __syncwarp();
       unsigned char* ob = reinterpret_cast<unsigned char*>(out->buf);
       pcr_chunk_steps<T, M, 4>(A, B, C, D, lane, WmXch<T, ROWB>{ob});
-      wm_pcr_half<T, M>(A, B, C, D, lane, ob);
+      wm_pcr_half<T, M>(A, B, C, D, lane, reinterpret_cast<unsigned char*>(slots[q].buf), ob, refill);
     } else {
       chunk_solve<ALG, T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
       if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer

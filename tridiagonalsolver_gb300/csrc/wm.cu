@@ -427,11 +427,11 @@ struct WmXch {
 // and after four steps A of rows < 16 and C of rows >= 32 Q - 16, are zero,
 // so the chains start and end clean.
 //
-// x leaves in buf in the TMA store layout (row r at chunk r / Q, element
-// r % Q).  The caller's buf must be free; it is left holding x.
+// x goes straight to the system's rows in global memory (xs): for each slot
+// the warp writes two runs of 16 consecutive rows.
 template <typename T, int Q, typename Refill>
 __device__ __forceinline__ void wm_pcr_half(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (&D)[Q], int lane,
-                                            unsigned char* xch, unsigned char* buf, const Refill& refill) {
+                                            unsigned char* xch, T* xs, const Refill& refill) {
   using W = Vec16<T>;
   constexpr int NV = W::N;
   constexpr int ES = (int)sizeof(T);
@@ -493,26 +493,17 @@ __device__ __forceinline__ void wm_pcr_half(T (&A)[Q], T (&B)[Q], T (&C)[Q], T (
     xv = fma(-HI[s], xv, RH[s]);
     RH[s] = xv;
   }
-  // x of slot s: row c + 16 p(s), p(s) = h ? 2Q-1-s : s; chunk t = p (16 / Q) + c / Q, element c % Q
+  // x of slot s: row c + 16 p(s), p(s) = h ? 2Q-1-s : s
   const int c = lane >> 1, hh = lane & 1;
-  const int e0 = c % Q;
-  const int t0 = hh * (2 * Q - 1) * (16 / Q) + c / Q;  // chunk of slot 0
-  const int ts = hh ? -(16 / Q) : (16 / Q);            // chunk step per slot
-  // (t >> 1) & 3 of slot s is g(s) ^ 3 hh with g(s) known at compile time
-  const int ex = (e0 / NV) ^ (3 * hh);
-  const int eo = (e0 % NV) * ES;
+  T* xr = xs + c + hh * 16 * (2 * Q - 1);  // the row of slot 0
+  const int step = hh ? -16 : 16;          // rows per slot
 #pragma unroll
-  for (int s = 0; s < Q; ++s) {
-    constexpr int SPC = 16 / Q;
-    const int g = ((s * SPC) >> 1) & 3;  // (t >> 1) & 3 for hh = 0
-    const int t = t0 + s * ts;
-    *reinterpret_cast<T*>(buf + t * 64 + (((ex ^ g) & 3) << 4) + eo) = RH[s];
-  }
+  for (int s = 0; s < Q; ++s) xr[s * step] = RH[s];
 }
 
 template <int ALG, typename T, int M, int G>
 __global__ void __launch_bounds__(32 * wm_warps<ALG, T, M>(), 1)
-    wm_tma_kernel(const __grid_constant__ TwMaps maps, int n, int nboxes, int* err) {
+    wm_tma_kernel(const __grid_constant__ TwMaps maps, int n, int nboxes, int* err, T* xout) {
   constexpr int WARPS = wm_warps<ALG, T, M>();
   constexpr int SLOTS = wm_slots<ALG, T, M>();
   using W = Vec16<T>;
@@ -574,17 +565,16 @@ __global__ void __launch_bounds__(32 * wm_warps<ALG, T, M>(), 1)
     if constexpr (ALG == CHUNK_PCR) {
       // PCR-half-pThomas (32 lanes per system): four PCR steps on the chunks
       // (a of row 0 and c of the last row are not part of the system), their
-      // whole-lane exchanges through the output buffer (free once the
-      // previous x store has read it); then the stride-16 chains by lane
-      // pairs, transposed through the slot, which is refilled after; x in
-      // the output buffer's TMA layout
+      // whole-lane exchanges (FP64) through the warp's second buffer; then
+      // the stride-16 chains by lane pairs, transposed through the slot,
+      // which is refilled after; x straight to global memory (each warp
+      // store two runs of 16 consecutive rows)
       if (lane == 0) A[0] = T(0);
       if (lane == 31) C[M - 1] = T(0);
-      if (lane == 0) bulk_wait_read<0>();
-      __syncwarp();
       unsigned char* ob = reinterpret_cast<unsigned char*>(out->buf);
       pcr_chunk_steps<T, M, 4>(A, B, C, D, lane, WmXch<T, ROWB>{ob});
-      wm_pcr_half<T, M>(A, B, C, D, lane, reinterpret_cast<unsigned char*>(slots[q].buf), ob, refill);
+      wm_pcr_half<T, M>(A, B, C, D, lane, reinterpret_cast<unsigned char*>(slots[q].buf),
+                        xout + (size_t)(gw + i * nw) * 32 * M, refill);
     } else {
       chunk_solve<ALG, T, M, G>(A, B, C, D, X, n, tl * M, M, M, tl);
       if (lane == 0) bulk_wait_read<0>();  // previous x store has left the buffer
@@ -594,12 +584,12 @@ __global__ void __launch_bounds__(32 * wm_warps<ALG, T, M>(), 1)
         const int off = wm_swz<ROWB>(lane, u);
         *reinterpret_cast<typename W::V*>(reinterpret_cast<unsigned char*>(out->buf) + off) = W::make(X, u * NV);
       }
-    }
-    fence_async_smem();
-    __syncwarp();
-    if (lane == 0) {
-      tma_store_2d(&maps.m[4], 0, (gw + i * nw) * 32, out->buf);
-      bulk_commit();
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        tma_store_2d(&maps.m[4], 0, (gw + i * nw) * 32, out->buf);
+        bulk_commit();
+      }
     }
   }
   if (lane == 0) bulk_wait_all();
@@ -632,7 +622,7 @@ static bool launch_wm_tma_m(const T* a, const T* b, const T* c, const T* d, T* x
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int need = (nboxes + WARPS - 1) / WARPS;
   const int grid = need < sms ? need : sms;
-  wm_tma_kernel<ALG, T, M, G><<<grid, 32 * WARPS, smem, st>>>(maps, n, nboxes, error_word());
+  wm_tma_kernel<ALG, T, M, G><<<grid, 32 * WARPS, smem, st>>>(maps, n, nboxes, error_word(), x);
   *e = cudaGetLastError();
   return true;
 }

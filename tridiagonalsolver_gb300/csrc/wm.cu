@@ -323,9 +323,10 @@ __global__ void __launch_bounds__(128) wm_warp_kernel(const T* __restrict__ a, c
 // the 32/G systems of one warp.  The chunk width picks the shared-memory
 // swizzle (none / 32B / 64B / 128B) that makes each lane's 16-byte reads of
 // its own chunk conflict free.  Every warp runs a ring of WM_SLOTS input
-// buffers; a buffer is refilled as soon as its lanes have read it, so
+// buffers; a buffer is refilled as soon as its lanes have read it (PCR: once
+// its chain transpose, which passes through the buffer, is done), so
 // WM_SLOTS-1 loads stay in flight while the warp solves, and x leaves
-// through a separate buffer by TMA store.
+// through a separate buffer by TMA store (PCR: straight to global memory).
 constexpr int WM_SLOTS = 3;
 
 template <typename T, int M>

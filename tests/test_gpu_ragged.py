@@ -571,3 +571,24 @@ def test_ragged_results_are_reproducible(cuda, dtype):
     for r in runs[1:]:
         for p, q in zip(runs[0], r):
             assert torch.equal(p, q)
+
+
+def test_ragged_refined_pivoted_steps_without_marks(cuda):
+    """A plan without marks (no classification, no mask) pivots every
+    system, so the restricted steps cover all of them: iters = 1,
+    pivoted_iters = 1 gives exactly the two-step result, forward and adjoint."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300 import ragged
+
+    torch = cuda
+    sizes = np.array([3, 700, 5000, 1, 20000, 64, 65], dtype=np.int64)
+    a, b, c, d, off, _ = ragged.synthetic_batch(sizes, dtype=torch.float64, nondominant_fraction=0.3, seed=41)
+    plan32 = T.RaggedPlan(off, dtype=torch.float32)
+    w = torch.rand_like(d) * 2 - 1
+    x2 = plan32.refine(a, b, c, d, iters=2).clone()
+    x = plan32.refine(a, b, c, d, iters=1, pivoted_iters=1)
+    l2 = plan32.refine_adjoint(a, b, c, x, w, iters=2)[3].clone()
+    l = plan32.refine_adjoint(a, b, c, x, w, iters=1, pivoted_iters=1)[3]
+    torch.cuda.synchronize()
+    assert torch.equal(x, x2)
+    assert torch.equal(l, l2)

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cooperative_groups.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -570,11 +571,14 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     amax = max(amax, max(magh(a0), max(magh(b0), magh(c0))));  // magnitudes for the acceptance test
     dmax = max(dmax, magh(d0));
   };
-  // row i+1 (a, b, c, y) against the candidate row: U row i
-  auto eliminate = [&](int i, T na, T nb, T cn, T ny) {
+  // row i+1 (a, b, c, y) against the candidate row: U row i.  LAST (row
+  // i+1 is the last interior row, i = mi-2) is a compile-time tag: as a
+  // run-time test the right spike's product below was formed on every row
+  // and discarded on all but one.
+  auto eliminate = [&](int i, T na, T nb, T cn, T ny, auto last_tag) {
+    constexpr bool last = decltype(last_tag)::value;
     amax = max(amax, max(magh(na), max(magh(nb), magh(cn))));
     dmax = max(dmax, magh(ny));
-    const bool last = i + 2 == mi;  // row i+1 is the last interior row
     const T nc = last ? T(0) : cn;
     const bool sw = !abs_ge(cb, na);
     const T piv = sw ? na : cb;
@@ -607,7 +611,7 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     cc = sw ? tq : nc;
     cy = fma(-l, uy, sw ? cy : ny);
     cv = sw ? cv : tq;
-    if (last) {  // the right spike enters with row mi-1
+    if constexpr (last) {  // the right spike enters with row mi-1
       w_prev = sw ? cn : cw;
       cw = fma(-l, w_prev, sw ? cw : cn);
     }
@@ -623,19 +627,21 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     // software-pipelined: row i+2 (at most the separator row, which always
     // exists) is loaded while row i+1 is eliminated
     T pa = A(1), pb = B(1), pc = C(1), py = D(1);
-    for (int i = 0; i + 1 < mi; ++i) {
+    for (int i = 0; i + 2 < mi; ++i) {
       const T na = pa, nb = pb, cn = pc, ny = py;
       if (LAY == PGE_SWZ && pass == 0 && i + 2 == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
       pa = A(i + 2);
       pb = B(i + 2);
       pc = C(i + 2);
       py = D(i + 2);
-      eliminate(i, na, nb, cn, ny);
+      eliminate(i, na, nb, cn, ny, std::false_type{});
     }
+    if (LAY == PGE_SWZ && pass == 0 && mi == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
     as = A(mi);
     bs = B(mi);
     cs = t * m + mi == n - 1 && zero_cl ? T(0) : C(mi);
     ds = D(mi);
+    if (mi >= 2) eliminate(mi - 2, pa, pb, pc, py, std::true_type{});
   }
   // U row mi-1 is the remaining candidate row (u1 = u2 = 0)
   bad |= is_zero(cb);
@@ -793,7 +799,10 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     // software-pipelined: row i-1's factors are loaded while row i is solved
     int j = mi - 2 >= 0 ? mi - 2 : 0;
     T qz = C(j), qd = D(j), qb = B(j), qa = A(j);
-    for (int i = mi - 2; i >= 0; --i) {
+    // (row mi-2, the one row with a right-spike term, is peeled off the loop
+    // by the compile-time tag: as a run-time test its product was formed on
+    // every row)
+    auto back_row = [&](int i, auto spike_tag) {
       const T zi = qz, di = qd, bi = qb, ai = qa;
       j = i > 0 ? i - 1 : 0;
       qz = C(j);
@@ -803,14 +812,16 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
       // z_i multiplies x_{i+2} (swap) or the previous separator (no swap)
       const T zx = (swm >> i) & 1ull ? x2 : sp;
       T r = fma(-zi, zx, di);
-      if (i == mi - 2) r = fma(-w_prev, st, r);
+      if constexpr (decltype(spike_tag)::value) r = fma(-w_prev, st, r);
       const T xi = fma(-bi, x1, r) * ai;  // one op on x_{i+1}, then the reciprocal
       D(i) = xi;
       xmax = max(xmax, magh(xi));
       bad |= !finite_val(xi);
       x2 = x1;
       x1 = xi;
-    }
+    };
+    if (mi >= 2) back_row(mi - 2, std::true_type{});
+    for (int i = mi - 3; i >= 0; --i) back_row(i, std::false_type{});
     bad |= !finite_val(st);
     D(mi) = st;
     FST[NT + t] = D(0);  // first x of the partition, for the separator residual of t-1
@@ -1186,8 +1197,12 @@ __device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint
     T Y0 = T(0), V0 = T(0);
     // software-pipelined: row i+2 (at most the separator row, which always
     // exists) is loaded while row i+1 is eliminated
+    // (the last interior row, i = mi-2, is peeled off the loop by the
+    // compile-time tag: as a run-time test the right spike's product was
+    // formed on every row)
     T pa = A[1], pb = B[1], pc = C[1], py = D[1];
-    for (int i = 0; i + 1 < mi; ++i) {
+    auto elim_row = [&](int i, auto last_tag) {
+      constexpr bool last = decltype(last_tag)::value;
       const T na = pa, nb = pb, cn = pc, ny = py;
       amax = max(amax, max(magh(na), max(magh(nb), magh(cn))));
       dmax = max(dmax, magh(ny));
@@ -1195,7 +1210,6 @@ __device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint
       pb = B[i + 2];
       pc = C[i + 2];
       py = D[i + 2];
-      const bool last = i + 2 == mi;
       const T nc = last ? T(0) : cn;
       const bool sw = !abs_ge(cb, na);
       const T piv = sw ? na : cb;
@@ -1227,11 +1241,13 @@ __device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint
       cc = sw ? tq : nc;
       cy = fma(-l, uy, sw ? cy : ny);
       cv = sw ? cv : tq;
-      if (last) {
+      if constexpr (last) {
         w_prev = sw ? cn : cw;
         cw = fma(-l, w_prev, sw ? cw : cn);
       }
-    }
+    };
+    for (int i = 0; i + 2 < mi; ++i) elim_row(i, std::false_type{});
+    if (mi >= 2) elim_row(mi - 2, std::true_type{});
     bad |= is_zero(cb);
     const T inv_last = Div<T>(cb).inv();
     {
@@ -1323,7 +1339,8 @@ __device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint
       // software-pipelined: row i-1's factors are loaded while row i is solved
       int j = mi - 2 >= 0 ? mi - 2 : 0;
       T qv = V[j], qd = D[j], qb = B[j], qa = A[j], qc = C[j + 1];
-      for (int i = mi - 2; i >= 0; --i) {
+      // (row mi-2, the one row with a right-spike term, peeled off the loop)
+      auto back_row = [&](int i, auto spike_tag) {
         const T vi = qv, di = qd, bi = qb, ai = qa, ci1 = qc;
         j = i > 0 ? i - 1 : 0;
         qv = V[j];
@@ -1333,14 +1350,16 @@ __device__ __forceinline__ void pgc_body(const PgeIO<T>& io, const int bid, uint
         qc = C[j + 1];
         const T u2 = keep_if(((swaps >> i) & 1ull) && i + 2 < mi, ci1);
         T r = fma(-vi, sp, di);
-        if (i == mi - 2) r = fma(-w_prev, st, r);
+        if constexpr (decltype(spike_tag)::value) r = fma(-w_prev, st, r);
         const T xi = fma(-bi, x1, fma(-u2, x2, r)) * ai;  // x_{i+2} term first: two ops depend on x_{i+1}
         D[i] = xi;
         xmax = max(xmax, magh(xi));
         bad |= !finite_val(xi);
         x2 = x1;
         x1 = xi;
-      }
+      };
+      if (mi >= 2) back_row(mi - 2, std::true_type{});
+      for (int i = mi - 3; i >= 0; --i) back_row(i, std::false_type{});
       bad |= !finite_val(st);
       D[mi] = st;
       XF[t] = D[0];

@@ -126,6 +126,38 @@ def test_pge_bench_shape_fp64(cuda):
     assert worst <= 1e-12
 
 
+def test_pge_persistent_ring_rare_paths(cuda):
+    """FP64 n = 4096 (the TMA-staged persistent kernel) with three systems
+    per CTA.  Singular interior blocks are planted in systems that a CTA
+    solves first, second (right after another planted one) and last: those
+    take the refinement passes, whose copy of x borrows the buffer holding the
+    next system's first half, then the sequential solve.  Every system must
+    still match the oracle, i.e. no system sees another's rows."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    n = 4096
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    batch = 3 * sms
+    a, b, c, d = inputs.nondominant(n, batch, seed=21)
+    planted = (3, 3 + sms, 7 + sms, 9 + 2 * sms, 2 * sms + sms - 1)
+    for j in planted:
+        b[j, 32] = 0.0
+        c[j, 32] = 0.0
+        a[j, 32] = 1.0
+    T.lib().tridiag_partition_fallbacks(1)
+    x, info = _solve(cuda, (a, b, c, d), np.float64, n)
+    assert T.lib().tridiag_partition_fallbacks(1) >= len(planted)
+    assert (info == 0).all()
+    _, worst = O.backward_error(a, b, c, d, x, n)
+    assert worst <= 1e-12
+    xo = O.gtsv(a, b, c, d, n).reshape(batch, n)
+    assert np.median(_rel(x, xo)) <= 1e-11
+    # the same batch again: the kernel's results do not depend on the run
+    x2, _ = _solve(cuda, (a, b, c, d), np.float64, n)
+    assert np.array_equal(x, x2)
+
+
 @pytest.mark.parametrize("name,dt,n", [("WM5_reg_double", np.float64, 4096), ("WM4_shmem_single", np.float32, 3000)])
 def test_reference_wm_names_long_systems(cuda, name, dt, n):
     """The reference's WM entry points on systems beyond one warp use the

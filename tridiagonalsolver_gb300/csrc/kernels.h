@@ -72,6 +72,12 @@ inline bool tw_eligible(int layout, int n, int batch, int elem) {
 // The library's device error word on the current device (allocated on first
 // use, 4 bytes per device), and a synchronous read (optionally clearing it).
 int* error_word();
+// Ticket counters for persistent kernels that hand out work dynamically: a
+// (next, done) pair of ints, zero, one of RING_TICKET_SLOTS per device taken
+// in turn per launch; the launch's last CTA sets it to zero again.  (Two
+// launches share a pair only when RING_TICKET_SLOTS launches are in flight.)
+constexpr unsigned RING_TICKET_SLOTS = 256;
+int* ring_tickets();
 cudaError_t read_device_error(int* code, bool reset);
 
 // wm.cu: WM-pGE, one warp per system (CONTIG / PACKED, n <= 1024 FP32,

@@ -283,6 +283,9 @@ struct PgeIO {
   const int* dcount;
   const unsigned char* kinds;
   int want;
+  // the persistent TMA-staged kernel: its (next, done) ticket pair
+  // (ring_tickets())
+  int* ring;
 };
 
 // Tensor maps of the TMA-staged FP64 kernel (pge_kernel with SWZ): a, b, c,
@@ -294,6 +297,29 @@ struct PgeMaps {
 
 // Rows per partition of the TMA-staged kernel.
 constexpr int PGE_SWZ_M = 32;
+
+// Sweep row of the TMA-staged kernel after which the ring reloads buffers
+// (the previous system's x stores have had these rows' time to leave them;
+// the second half still has ten rows' time to land).
+constexpr int PGE_RING_REFILL = 4;
+
+// The TMA-staged kernel is persistent: each CTA takes systems by ticket (one
+// ahead of the one it solves, so that it can load it early; a CTA held up by
+// a system that needs the slow paths takes fewer) and solves them out of
+// three half buffers of shared memory (a half buffer = rows 0-15 or 16-31 of
+// every partition, for the four arrays).  The j-th
+// system of a CTA has its first half in buffer 0 (j even) or 2 (j odd) and
+// its second half in buffer 1.  The next system's first half is loaded into
+// the other of buffers 0 / 2 while this one is solved; its second half
+// follows into buffer 1 once this system's x (stored from buffers F and 1)
+// has left shared memory, early in the next sweep.  Every thread keeps the
+// same copy of this state (the control flow that changes it is uniform).
+struct PgeRing {
+  int j;              // systems this CTA has begun
+  unsigned fills[3];  // loads issued into each buffer (one mbarrier phase each)
+  unsigned pend;      // bit b: a load into buffer b not yet waited for
+  int next;           // the CTA's next system (io.count or more: none)
+};
 
 // Write rows r = lo + t, lo + t + nt, ... < hi of the result, value(r) from
 // shared memory.  MODE 1 also writes the gradients; the forward solution's
@@ -360,15 +386,16 @@ __device__ __forceinline__ void pge_system(const PgeIO<T>& io, int bid, int R, i
 //    shared 16-byte boundaries coincide), moved by one bulk copy per array;
 //    the partition size m is odd, so the sweeps' column accesses -- lane t,
 //    row i of partition t -- are conflict-free;
-//  * PGE_SWZ (FP64, m = 32): each array as [2][NT][16] elements, half h of
-//    partition p one 128-byte row whose 16-byte pairs are XOR-swizzled by
-//    p mod 8 (the 128-byte swizzle of the tensor maps); column accesses meet
-//    at most four-way bank conflicts.
+//  * PGE_SWZ (FP64, m = 32): each half of each array as [NT][16] elements
+//    (the halves in two of the ring's half buffers, hs elements apart), half
+//    h of partition p one 128-byte row whose 16-byte pairs are XOR-swizzled
+//    by p mod 8 (the 128-byte swizzle of the tensor maps); column accesses
+//    meet at most four-way bank conflicts.
 constexpr int PGE_DENSE = 1, PGE_SWZ = 2;
 
 template <int NT, int LAY>
-__device__ __forceinline__ int pge_off(int p, int i, int m) {
-  if constexpr (LAY == PGE_SWZ) return (i >> 4) * (NT * 16) + p * 16 + ((((i >> 1) & 7) ^ (p & 7)) << 1) + (i & 1);
+__device__ __forceinline__ int pge_off(int p, int i, int m, int hs) {
+  if constexpr (LAY == PGE_SWZ) return (i >> 4) * hs + p * 16 + ((((i >> 1) & 7) ^ (p & 7)) << 1) + (i & 1);
   else return p * m + i;  // (each staged array's base shifted by its delta)
 }
 
@@ -380,7 +407,8 @@ __host__ __device__ constexpr int pge_array_elems(int ms) {
 }
 
 template <typename T, int NT, int MODE, int LAY>
-__device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps, const int bid, uint64_t* s_bar) {
+__device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps, const int bid, uint64_t* s_bar,
+                                         PgeRing* rg = nullptr) {
   constexpr int VE = 16 / (int)sizeof(T);  // elements per 16 bytes
   int sys, n, m, ms;
   size_t base;
@@ -420,11 +448,10 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   const T* __restrict__ gc = io.c;
   const T* gd = io.d;
   int* info = io.info;
-  auto off = [&](int p, int i) { return pge_off<NT, LAY>(p, i, m); };
   extern __shared__ __align__(16) unsigned char pge_smem[];
   unsigned char* sm = pge_smem;
   if constexpr (LAY == PGE_SWZ) sm += (1024u - (smem_u32(pge_smem) & 1023u)) & 1023u;  // 128-byte swizzle: 1 KB aligned
-  const int astride = LAY == PGE_SWZ ? NT * PGE_SWZ_M : pge_array_elems<T, NT>(ms);
+  const int astride = pge_array_elems<T, NT>(ms);
   T* S0 = reinterpret_cast<T*>(sm);
   // dense layout: each staged array shifted by its rows' 16-byte phase
   auto phase = [&](const T* g) {
@@ -437,6 +464,20 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   T* SD = S0 + 3 * astride + dl[3];
   T* SX = S0 + 4 * astride;  // x kept across refinement passes
   T* SEP = SX + astride;     // [3][4][NT] separator rows: original + ping-pong
+  // TMA-staged ring: this system's halves in buffers F and 1 (hs elements
+  // apart), the refinement copy of x (rare) in the third buffer
+  constexpr int HB = 4 * NT * 16;  // elements per half buffer
+  const int F = LAY == PGE_SWZ && (rg->j & 1) ? 2 : 0;
+  const int hs = (1 - F) * HB;
+  if constexpr (LAY == PGE_SWZ) {
+    SA = S0 + F * HB;
+    SB = SA + NT * 16;
+    SC = SA + 2 * NT * 16;
+    SD = SA + 3 * NT * 16;
+    SX = S0 + (2 - F) * HB;
+    SEP = S0 + 3 * HB;
+  }
+  auto off = [&](int p, int i) { return pge_off<NT, LAY>(p, i, m, hs); };
   T* FST = SEP + 12 * NT;  // [3][NT]: Y, V, W of each partition's first row
   T* TMP = FST + 3 * NT;  // [PGE_TMP]: the FP32 separator solve's top level
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -474,16 +515,34 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   // and the identity rows past n by plain copies.  (An SM issues about one
   // bulk or element copy per 15 cycles: element copies of 4 or 8 bytes, or
   // one bulk copy per partition, ran at 7-17 bytes per clock.)
-  if constexpr (LAY == PGE_SWZ) {
+  // (TMA-staged ring) half h of system s into half buffer b: issued by
+  // thread 0, counted by every thread; wait_fill(b) waits for the latest one
+  auto fill = [&](int b, int h, int s) {
     if (t == 0) {
-      mbar_init(&s_bar[0], 1);
-      mbar_init(&s_bar[1], 1);
-      fence_mbar_init();
-      for (int h = 0; h < 2; ++h) {
-        mbar_arrive_expect_tx(&s_bar[h], (unsigned)(4 * NT * 16 * sizeof(T)));
-        T* dst[4] = {SA, SB, SC, SD};
-        for (int k = 0; k < 4; ++k) tma_load_3d(dst[k] + h * NT * 16, &maps.m[k], 0, h, sys * NT, &s_bar[h]);
+      mbar_arrive_expect_tx(&s_bar[b], (unsigned)(HB * sizeof(T)));
+      for (int k = 0; k < 4; ++k) tma_load_3d(S0 + b * HB + k * NT * 16, &maps.m[k], 0, h, s * NT, &s_bar[b]);
+    }
+    ++rg->fills[b];
+    rg->pend |= 1u << b;
+  };
+  auto wait_fill = [&](int b) {
+    rg->pend &= ~(1u << b);
+    return mbar_wait(&s_bar[b], (rg->fills[b] - 1u) & 1u, io.err);
+  };
+  const int nxt = LAY == PGE_SWZ ? rg->next : 0;  // (ring) this CTA's next system
+  const bool has_next = LAY == PGE_SWZ && nxt < io.count;
+  bool clobbered = false;  // (ring) the refinement copy of x overwrote the next system's first half
+  if constexpr (LAY == PGE_SWZ) {
+    if (rg->j == 0) {
+      if (t == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        mbar_init(&s_bar[2], 1);
+        fence_mbar_init();
       }
+      fill(0, 0, sys);
+      fill(1, 1, sys);
+      if (has_next) fill(2, 0, nxt);
     }
   } else if constexpr (LAY == PGE_DENSE) {
     T* const Sk[4] = {SA, SB, SC, SD};
@@ -620,23 +679,41 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     // first pass of a TMA-staged system: wait for each half as the sweep
     // reaches it (a timeout marks the pass bad: the system is then restaged
     // and solved by the refinement passes)
-    if (LAY == PGE_SWZ && pass == 0) bad |= !mbar_wait(&s_bar[0], 0, io.err);
+    if constexpr (LAY == PGE_SWZ)
+      if (pass == 0) bad |= !wait_fill(F);
     // a_0 and c_{n-1} are zero by definition (TMA staging copies whatever
     // the arrays hold there)
     first_row(t == 0 && zero_a0 ? T(0) : A(0), B(0), C(0), D(0));
     // software-pipelined: row i+2 (at most the separator row, which always
     // exists) is loaded while row i+1 is eliminated
     T pa = A(1), pb = B(1), pc = C(1), py = D(1);
-    for (int i = 0; i + 2 < mi; ++i) {
+    auto step = [&](int i) {
       const T na = pa, nb = pb, cn = pc, ny = py;
-      if (LAY == PGE_SWZ && pass == 0 && i + 2 == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
       pa = A(i + 2);
       pb = B(i + 2);
       pc = C(i + 2);
       py = D(i + 2);
       eliminate(i, na, nb, cn, ny, std::false_type{});
+    };
+    if constexpr (LAY == PGE_SWZ) {
+      // (m = 32: rows 0-15 in buffer F, rows 16-31 in buffer 1; the ring's
+      // work sits between the loops, out of their bodies)
+      int i = 0;
+      for (; i < PGE_RING_REFILL; ++i) step(i);
+      if (pass == 0 && rg->j > 0) {
+        // the previous system's x stores have left buffers 1 and 2-F by
+        // now: this system's second half and the next system's first half
+        // go there
+        if (t == 0) bulk_wait_read<0>();
+        fill(1, 1, sys);
+        if (has_next) fill(2 - F, 0, nxt);
+      }
+      for (; i < 14; ++i) step(i);
+      if (pass == 0) bad |= !wait_fill(1);  // (step 14 loads row 16)
+      for (; i + 2 < mi; ++i) step(i);
+    } else {
+      for (int i = 0; i + 2 < mi; ++i) step(i);
     }
-    if (LAY == PGE_SWZ && pass == 0 && mi == 16) bad |= !mbar_wait(&s_bar[1], 0, io.err);
     as = A(mi);
     bs = B(mi);
     cs = t * m + mi == n - 1 && zero_cl ? T(0) : C(mi);
@@ -861,7 +938,7 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
   auto sidx = [&](int r) { return off(r / m, r % m); };
   if (pass > 0 && !pass_bad) {
     // x = x_prev (held in SX) + correction
-    for (int r = t; r < n; r += NT) SD[sidx(r)] += SX[sidx(r)];
+    for (int r = t; r < n; r += NT) SD[sidx(r)] += SX[r];
     __syncthreads();
   }
   if (!pass_bad || pass == 0) {
@@ -910,8 +987,15 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
       break;
     }
     if (pass == PGE_REFINE) break;
-    // keep x in SX and stage the FP64 residual as the next right-hand side
-    for (int r = t; r < n; r += NT) SX[sidx(r)] = SD[sidx(r)];
+    if constexpr (LAY == PGE_SWZ) {
+      // SX is the next system's first-half buffer: let that load land, take
+      // the buffer, and load it again when this system is done
+      if (rg->pend & (1u << (2 - F))) wait_fill(2 - F);
+      clobbered = has_next;
+    }
+    // keep x in SX (row r at r) and stage the FP64 residual as the next
+    // right-hand side
+    for (int r = t; r < n; r += NT) SX[r] = SD[sidx(r)];
     __syncthreads();
   } else {
     break;  // a correction pass broke down
@@ -920,9 +1004,9 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     const int q = sidx(r);
     if (r < n) {
       const T ar = r > 0 ? ga[base + r] : T(0), br = gb[base + r], cr = r < n - 1 ? gc[base + r] : T(0);
-      double res = fma(-(double)br, (double)SX[q], (double)gd[base + r]);
-      if (r > 0) res = fma(-(double)ar, (double)SX[sidx(r - 1)], res);
-      if (r < n - 1) res = fma(-(double)cr, (double)SX[sidx(r + 1)], res);
+      double res = fma(-(double)br, (double)SX[r], (double)gd[base + r]);
+      if (r > 0) res = fma(-(double)ar, (double)SX[r - 1], res);
+      if (r < n - 1) res = fma(-(double)cr, (double)SX[r + 1], res);
       SA[q] = ar;
       SB[q] = br;
       SC[q] = cr;
@@ -939,8 +1023,9 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
 
   if (!accepted) {
     // restage the system densely (4 arrays of n rows fit in the 5 NT ms
-    // staging elements) and solve it in place by one thread
-    T* FA = SA;
+    // staging elements; the ring: in buffers F and 1, contiguous) and solve
+    // it in place by one thread
+    T* FA = LAY == PGE_SWZ ? S0 + (F == 0 ? 0 : HB) : SA;
     T* FB = FA + n;
     T* FC = FB + n;
     T* FD = FC + n;
@@ -961,6 +1046,11 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     __syncthreads();
     if (s_info == 0)
       pge_store_rows<T, MODE>(io, base, n, 0, n, t, NT, [&](int r) { return FD[r]; });
+    if constexpr (LAY == PGE_SWZ) {
+      fence_async_smem();  // (the buffers are reloaded by the TMA)
+      __syncthreads();
+      if (clobbered) fill(2 - F, 0, nxt);
+    }
     return;
   }
   if (MODE < 2 && info && t == 0) info[sys] = 0;
@@ -971,10 +1061,12 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     __syncthreads();
     if (t == 0) {
       tma_store_3d(&maps.m[4], 0, 0, sys * NT, SD);
-      tma_store_3d(&maps.m[4], 0, 1, sys * NT, SD + NT * 16);
+      tma_store_3d(&maps.m[4], 0, 1, sys * NT, SD + hs);
       bulk_commit();
-      bulk_wait_read<0>();  // shared memory stays valid until the stores have read it
+      // (not waited for here: the next system's sweep, or the kernel's end,
+      // waits until the stores have read buffers F and 1)
     }
+    if (clobbered) fill(2 - F, 0, nxt);
   } else if (LAY == PGE_DENSE && (MODE == 0 || MODE == 3) && phase(io.x) == dl[3]) {
     // rows [q0, q1) of x by one bulk store (x in the same 16-byte phase as
     // d), the rest element-wise
@@ -1010,7 +1102,47 @@ __device__ __forceinline__ int pge_next_item(const PgeIO<T>& io, int* s_item) {
 
 template <typename T, int NT, int MODE, int LAY>
 __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __grid_constant__ PgeMaps maps) {
-  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ __align__(8) uint64_t s_bar[3];
+  if constexpr (LAY == PGE_SWZ) {
+    // persistent: systems blockIdx.x, + gridDim.x, ... < io.count through
+    // the ring of half buffers; a device error (a load that never landed)
+    // ends the loop
+    __shared__ int s_stop, s_tk[2];
+    PgeRing rg{0, {0u, 0u, 0u}, 0u, 0};
+    if (threadIdx.x == 0) {
+      s_tk[0] = atomicAdd(io.ring, 1);
+      s_tk[1] = atomicAdd(io.ring, 1);
+    }
+    __syncthreads();
+    int k = s_tk[0];
+    rg.next = s_tk[1];
+    while (k < io.count) {
+      if (threadIdx.x == 0) s_stop = *(volatile int*)io.err != 0;
+      __syncthreads();
+      if (s_stop) break;
+      pge_body<T, NT, MODE, LAY>(io, maps, k, s_bar, &rg);
+      ++rg.j;
+      // the system after the next one (whose load the next sweep issues)
+      if (threadIdx.x == 0) s_tk[0] = rg.next < io.count ? atomicAdd(io.ring, 1) : io.count;
+      __syncthreads();
+      k = rg.next;
+      rg.next = s_tk[0];
+    }
+    // loads and stores still in flight end before the shared memory is released
+    for (int b = 0; b < 3; ++b)
+      if (rg.pend & (1u << b)) mbar_wait(&s_bar[b], (rg.fills[b] - 1u) & 1u, io.err);
+    if (threadIdx.x == 0) {
+      bulk_wait_read<0>();
+      // every CTA counts itself out once it takes no more tickets; the last
+      // one zeroes the pair for the launch that uses it next
+      __threadfence();
+      if (atomicAdd(io.ring + 1, 1) == (int)gridDim.x - 1) {
+        atomicExch(io.ring, 0);
+        atomicExch(io.ring + 1, 0);
+      }
+    }
+    return;
+  }
   if constexpr (LAY == PGE_DENSE && MODE <= 1) {
     if (io.ticket) {
       // resident CTAs drain one size bucket of a ragged batch
@@ -1608,6 +1740,21 @@ static cudaError_t pge_launch_k(const PgeIO<T>& io_in, const PgeMaps& maps, int 
   cudaError_t e =
       cudaFuncSetAttribute(pge_kernel<T, NT, MODE, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  if constexpr (LAY == PGE_SWZ) {
+    // persistent: io.count systems over as many CTAs as stay resident
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pge_kernel<T, NT, MODE, LAY>, NT, smem);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    io.count = grid;
+    io.ring = ring_tickets();
+    if (!io.ring || !io.err) return cudaErrorMemoryAllocation;
+    grid = std::min(grid, sms * per);
+    pge_kernel<T, NT, MODE, LAY><<<grid, NT, smem, s>>>(io, maps);
+    return cudaGetLastError();
+  }
   // L2 prefetch one wave ahead for uniform batches with 16-byte aligned systems
   const uintptr_t al = reinterpret_cast<uintptr_t>(io.a) | reinterpret_cast<uintptr_t>(io.b) |
                        reinterpret_cast<uintptr_t>(io.c) | reinterpret_cast<uintptr_t>(io.d);
@@ -1641,7 +1788,8 @@ static cudaError_t pge_launch(const PgeIO<T>& io_in, int grid, int m_max, cudaSt
   // TMA staging: FP64 solve of a uniform contiguous batch with 32 rows per
   // partition (n = 32 NT), arrays 16-byte aligned
   if constexpr (MODE == 0 && sizeof(T) == 8) {
-    const size_t smem_swz = 1024 + pge_smem_bytes<T, NT>(PGE_SWZ_M);
+    // three half buffers (the ring), the separator rows, first-row values and scratch
+    const size_t smem_swz = 1024 + ((size_t)3 * 4 * NT * 16 + 15 * (size_t)NT + PGE_TMP) * sizeof(T);
     if (!io.offsets && !io.list && io.n == PGE_SWZ_M * NT && io.stride == (size_t)io.n && smem_swz <= PGE_SMEM_MAX &&
         (uint64_t)NT * grid < (1ull << 31)) {
       const T* arr[5] = {io.a, io.b, io.c, io.d, io.x};

@@ -3,6 +3,7 @@
 #include <cudaTypedefs.h>
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
 #include <mutex>
 
 #include "kernels.h"
@@ -94,6 +95,27 @@ int* error_word() {
     g_err_words[dev] = p;
   }
   return g_err_words[dev];
+}
+
+static int* g_ring_words[64] = {};
+static std::atomic<unsigned> g_ring_seq{0};
+
+int* ring_tickets() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  int* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    if (!g_ring_words[dev]) {
+      int* p = nullptr;
+      const size_t bytes = 2 * RING_TICKET_SLOTS * sizeof(int);
+      if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+      if (cudaMemset(p, 0, bytes) != cudaSuccess) return nullptr;
+      g_ring_words[dev] = p;
+    }
+    base = g_ring_words[dev];
+  }
+  return base + 2 * (g_ring_seq.fetch_add(1u) % RING_TICKET_SLOTS);
 }
 
 cudaError_t read_device_error(int* code, bool reset) {

@@ -298,11 +298,6 @@ struct PgeMaps {
 // Rows per partition of the TMA-staged kernel.
 constexpr int PGE_SWZ_M = 32;
 
-// Sweep row of the TMA-staged kernel after which the ring reloads buffers
-// (the previous system's x stores have had these rows' time to leave them;
-// the second half still has ten rows' time to land).
-constexpr int PGE_RING_REFILL = 4;
-
 // The TMA-staged kernel is persistent: each CTA takes systems by ticket (one
 // ahead of the one it solves, so that it can load it early; a CTA held up by
 // a system that needs the slow paths takes fewer) and solves them out of
@@ -312,7 +307,8 @@ constexpr int PGE_RING_REFILL = 4;
 // its second half in buffer 1.  The next system's first half is loaded into
 // the other of buffers 0 / 2 while this one is solved; its second half
 // follows into buffer 1 once this system's x (stored from buffers F and 1)
-// has left shared memory, early in the next sweep.  Every thread keeps the
+// has left shared memory, as the next system begins (of the refill points
+// measured -- sweep rows 0, 1, 2, 4, 8 -- the earliest was fastest).  Every thread keeps the
 // same copy of this state (the control flow that changes it is uniform).
 struct PgeRing {
   int j;              // systems this CTA has begun
@@ -680,7 +676,16 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
     // reaches it (a timeout marks the pass bad: the system is then restaged
     // and solved by the refinement passes)
     if constexpr (LAY == PGE_SWZ)
-      if (pass == 0) bad |= !wait_fill(F);
+      if (pass == 0) {
+        if (rg->j > 0) {
+          // the previous system's x stores leave buffers 1 and 2-F: this
+          // system's second half and the next system's first half go there
+          if (t == 0) bulk_wait_read<0>();
+          fill(1, 1, sys);
+          if (has_next) fill(2 - F, 0, nxt);
+        }
+        bad |= !wait_fill(F);
+      }
     // a_0 and c_{n-1} are zero by definition (TMA staging copies whatever
     // the arrays hold there)
     first_row(t == 0 && zero_a0 ? T(0) : A(0), B(0), C(0), D(0));
@@ -696,18 +701,9 @@ __device__ __forceinline__ void pge_body(const PgeIO<T>& io, const PgeMaps& maps
       eliminate(i, na, nb, cn, ny, std::false_type{});
     };
     if constexpr (LAY == PGE_SWZ) {
-      // (m = 32: rows 0-15 in buffer F, rows 16-31 in buffer 1; the ring's
-      // work sits between the loops, out of their bodies)
+      // (m = 32: rows 0-15 in buffer F, rows 16-31 in buffer 1; the wait
+      // for the second half sits between two loops, out of their bodies)
       int i = 0;
-      for (; i < PGE_RING_REFILL; ++i) step(i);
-      if (pass == 0 && rg->j > 0) {
-        // the previous system's x stores have left buffers 1 and 2-F by
-        // now: this system's second half and the next system's first half
-        // go there
-        if (t == 0) bulk_wait_read<0>();
-        fill(1, 1, sys);
-        if (has_next) fill(2 - F, 0, nxt);
-      }
       for (; i < 14; ++i) step(i);
       if (pass == 0) bad |= !wait_fill(1);  // (step 14 loads row 16)
       for (; i + 2 < mi; ++i) step(i);
@@ -1117,14 +1113,22 @@ __global__ void __launch_bounds__(NT, 1) pge_kernel(const PgeIO<T> io, const __g
     int k = s_tk[0];
     rg.next = s_tk[1];
     while (k < io.count) {
-      if (threadIdx.x == 0) s_stop = *(volatile int*)io.err != 0;
-      __syncthreads();
-      if (s_stop) break;
+      // the ticket after the next one (whose first half the next sweep
+      // loads) and the device error word, asked for now and read after this
+      // system: their latency hides behind its solve
+      int tk = 0, err = 0;
+      if (threadIdx.x == 0) {
+        tk = rg.next < io.count ? atomicAdd(io.ring, 1) : io.count;
+        err = *(volatile int*)io.err;
+      }
       pge_body<T, NT, MODE, LAY>(io, maps, k, s_bar, &rg);
       ++rg.j;
-      // the system after the next one (whose load the next sweep issues)
-      if (threadIdx.x == 0) s_tk[0] = rg.next < io.count ? atomicAdd(io.ring, 1) : io.count;
+      if (threadIdx.x == 0) {
+        s_tk[0] = tk;
+        s_stop = err != 0;
+      }
       __syncthreads();
+      if (s_stop) break;
       k = rg.next;
       rg.next = s_tk[0];
     }

@@ -158,6 +158,136 @@ def test_pge_persistent_ring_rare_paths(cuda):
     assert np.array_equal(x, x2)
 
 
+def _ppt_rows(torch, n, batch):
+    """Partition length of the thread-per-partition solve (ppt.cu: about four
+    warps per SM sub-partition, a multiple of 32 rows, at most 64 partitions)."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    groups = (batch + 31) // 32
+    P = min(max((16 * sms + groups // 2) // groups, 3), 64)
+    return (-(-n // P) + 31) // 32 * 32
+
+
+def _gtsv_many(torch, arrs, n):
+    import tridiagonalsolver_gb300 as T
+
+    batch = arrs[0].shape[0]
+    a, b, c, d = (torch.from_numpy(np.ascontiguousarray(v)).cuda() for v in arrs)
+    info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
+    T.ppt_counts(reset=True)
+    x = T.gtsv(a, b, c, d, n, info=info)  # workspace of tridiag_gtsv_workspace_size() bytes
+    counts = T.ppt_counts(reset=True)
+    return x.cpu().numpy(), info.cpu().numpy(), counts
+
+
+@pytest.mark.parametrize("n,batch", [(6144, 1024), (7001, 1100), (8192, 1024)])
+def test_ppt_matches_oracle(cuda, n, batch):
+    """Many contiguous FP64 systems longer than one CTA's shared memory holds:
+    the thread-per-partition pivoted solve serves them (its counters say so)
+    and every system meets the FP64 bar and agrees with the oracle's
+    partial-pivoting solve."""
+    a, b, c, d = inputs.nondominant(n, batch, seed=7 * n + batch)
+    x, info, counts = _gtsv_many(cuda, (a, b, c, d), n)
+    assert (info == 0).all()
+    assert counts["accepted"] + counts["listed"] == batch
+    assert counts["listed"] <= batch // 16
+    _, worst = O.backward_error(a, b, c, d, x, n)
+    assert worst <= 1e-12
+    xo = O.gtsv(a, b, c, d, n).reshape(batch, n)
+    assert np.median(_rel(x.reshape(batch, n), xo)) <= 1e-11
+
+
+def test_ppt_singular_partition_falls_back(cuda):
+    """A zero diagonal and superdiagonal in the first interior row of
+    partition 1 makes that partition's block singular (the matrix is not):
+    those systems miss the acceptance test and the partitioned solve (here
+    in clusters) takes them."""
+    n, batch = 6144, 1024
+    L = _ppt_rows(cuda, n, batch)
+    a, b, c, d = inputs.nondominant(n, batch, seed=31)
+    planted = (0, 5, 1000, batch - 1)
+    for j in planted:
+        b[j, L] = 0.0
+        c[j, L] = 0.0
+        a[j, L] = 1.0
+    x, info, counts = _gtsv_many(cuda, (a, b, c, d), n)
+    assert counts["listed"] >= len(planted)
+    assert counts["accepted"] + counts["listed"] == batch
+    assert (info == 0).all()
+    _, worst = O.backward_error(a, b, c, d, x, n)
+    assert worst <= 1e-12
+
+
+def test_ppt_not_for_one_cta_sizes(cuda):
+    """At 4096 rows the persistent one-CTA solve keeps the batch (the
+    thread-per-partition solve would be no faster there, in five launches)."""
+    import tridiagonalsolver_gb300 as T
+
+    a, b, c, d = inputs.nondominant(4096, 1024, seed=43)
+    x, info, counts = _gtsv_many(cuda, (a, b, c, d), 4096)
+    assert counts == {"accepted": 0, "listed": 0}
+    assert (info == 0).all()
+
+
+def test_ppt_out_of_place(cuda):
+    """solve_out with TRIDIAG_ALGO_GTSV (the benchmark's call): the same
+    solve out of place -- d untouched, the listed systems solved again from
+    it -- including systems planted to miss the acceptance test."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    n, batch = 6144, 1024
+    L = _ppt_rows(torch, n, batch)
+    a, b, c, d = inputs.nondominant(n, batch, seed=41)
+    for j in (2, 700):
+        b[j, L] = 0.0
+        c[j, L] = 0.0
+        a[j, L] = 1.0
+    ta, tb, tc, td = (torch.from_numpy(np.ascontiguousarray(v)).cuda() for v in (a, b, c, d))
+    x = torch.empty_like(td)
+    work = T.solve_out_workspace(ta, n, "gtsv")
+    T.ppt_counts(reset=True)
+    T.solve_out(ta, tb, tc, td, n, algo="gtsv", out=x, work=work)
+    counts = T.ppt_counts(reset=True)
+    assert counts["accepted"] + counts["listed"] == batch and counts["listed"] >= 2
+    assert np.array_equal(td.cpu().numpy(), d)
+    xh = x.cpu().numpy()
+    _, worst = O.backward_error(a, b, c, d, xh, n)
+    assert worst <= 1e-12
+    # in place (gtsv) gives the same bits
+    x2, _, _ = _gtsv_many(torch, (a, b, c, d), n)
+    assert np.array_equal(x2, xh)
+
+
+def test_ppt_long_systems_fp64(cuda):
+    """FP64 8192 x 4096 non-dominant through gtsv: the thread-per-partition
+    solve serves it, (nearly) every system is accepted there, and 64 sampled
+    systems meet the FP64 bar."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    n, batch = 8192, 4096
+    g = torch.Generator(device="cuda")
+    g.manual_seed(77)
+    a, b, c, d = (torch.rand((batch, n), dtype=torch.float64, device="cuda", generator=g) * 2 - 1 for _ in range(4))
+    d0 = d.clone()
+    info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
+    T.ppt_counts(reset=True)
+    x = T.gtsv(a, b, c, d, n, info=info)
+    counts = T.ppt_counts(reset=True)
+    print(f"thread-per-partition solve of {batch} systems: {counts}")
+    assert counts["accepted"] + counts["listed"] == batch
+    assert counts["listed"] <= batch // 256
+    assert int((info != 0).sum()) == 0
+    idx = torch.arange(0, batch, batch // 64, device="cuda")
+    host = [t.index_select(0, idx).cpu().numpy() for t in (a, b, c, d0, x)]
+    host[0][:, 0] = 0.0
+    host[2][:, -1] = 0.0
+    _, worst = O.backward_error(*host, n)
+    assert worst <= 1e-12
+    xo = O.gtsv(*host[:4], n).reshape(-1, n)
+    assert np.median(_rel(host[4], xo)) <= 1e-11
+
+
 @pytest.mark.parametrize("name,dt,n", [("WM5_reg_double", np.float64, 4096), ("WM4_shmem_single", np.float32, 3000)])
 def test_reference_wm_names_long_systems(cuda, name, dt, n):
     """The reference's WM entry points on systems beyond one warp use the

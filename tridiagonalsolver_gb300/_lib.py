@@ -57,6 +57,7 @@ SIGNATURES: dict[str, tuple] = {
     "tridiag_convert_check": (_I, [_P, _P, _P, _SZ, _P]),
     "tridiag_partition_fallbacks": (ctypes.c_longlong, [_I]),
     "tridiag_partition_path_counts": (_I, [_P, _I]),
+    "tridiag_partition_ppt_counts": (_I, [_P, _I]),
     "tridiag_solve_host_single": (_I, [_I, _I, _P, _P, _P, _P, _P, _I, _I, _I, _P]),
     "tridiag_solve_host_double": (_I, [_I, _I, _P, _P, _P, _P, _P, _I, _I, _I, _P]),
     "tridiag_pge_single": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),

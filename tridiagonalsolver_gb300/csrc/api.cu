@@ -56,6 +56,16 @@ size_t gtsv_ws_bytes(int n, int batch) {
          align_up((size_t)batch * sizeof(int));
 }
 
+// The workspace tridiag_gtsv_* asks for: FP64 contiguous batches that the
+// thread-per-partition solve covers (ppt.cu) get its factor arrays.
+template <typename T>
+size_t gtsv_ws_query(int layout, int n, int batch) {
+  size_t w = gtsv_ws_bytes<T>(n, batch);
+  if (sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch))
+    w = std::max(w, tdg::ppt_workspace_bytes<T>(n, batch));
+  return w;
+}
+
 template <typename T>
 struct GtsvWs {
   T* w1;
@@ -102,6 +112,15 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
       (chunked_first || !tdg::pge_eligible<T>(layout, n))) {
     bool used = false;
     cudaError_t e = tdg::launch_pge_long<T>(a, b, c, d, info, n, batch, w.w1, w.w2, w.piv, w.flag, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    if (used) return TRIDIAG_SUCCESS;
+  }
+  if (!pivots && sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch)) {
+    // many FP64 systems longer than one CTA holds: partitions of a few
+    // hundred rows, a thread each, instead of clusters of CTAs (the systems
+    // that miss its acceptance test take the clusters)
+    bool used = false;
+    cudaError_t e = tdg::launch_ppt<T>(a, b, c, d, d, info, n, batch, work, work_bytes, s, &used);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
     if (used) return TRIDIAG_SUCCESS;
   }
@@ -213,7 +232,7 @@ int solve_impl(int algo, int layout, T* a, T* b, T* c, T* d, int n, int batch, c
       return used ? TRIDIAG_SUCCESS : TRIDIAG_ERR_NOT_SUPPORTED;
     }
     case TRIDIAG_ALGO_GTSV: {
-      size_t bytes = gtsv_ws_bytes<T>(n, batch);
+      size_t bytes = gtsv_ws_query<T>(layout, n, batch);
       void* work = nullptr;
       cudaError_t e = cudaMallocAsync(&work, bytes, s);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
@@ -239,7 +258,7 @@ size_t solve_out_ws(int algo, int n, int batch, int layout = TRIDIAG_LAYOUT_CONT
     const size_t w = align_up((size_t)n * (size_t)batch * sizeof(T));
     return layout == TRIDIAG_LAYOUT_INTERLEAVED ? std::max(w, tdg::ipt_workspace_bytes<T>(n, batch)) : w;
   }
-  if (algo == TRIDIAG_ALGO_GTSV) return gtsv_ws_bytes<T>(n, batch);
+  if (algo == TRIDIAG_ALGO_GTSV) return gtsv_ws_query<T>(layout, n, batch);
   return 0;
 }
 
@@ -313,8 +332,12 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
     }
     case TRIDIAG_ALGO_GTSV: {
       bool used = false;
-      cudaError_t e = n >= PGE_MIN_N ? tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used)
-                                     : cudaSuccess;
+      cudaError_t e = cudaSuccess;
+      if (sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch))
+        e = tdg::launch_ppt<T>(a, b, c, d, x, nullptr, n, batch, work, work_bytes, s, &used);
+      if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+      if (used) return TRIDIAG_SUCCESS;
+      e = n >= PGE_MIN_N ? tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used) : cudaSuccess;
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       size_t bytes = (size_t)n * (size_t)batch * sizeof(T);
@@ -548,9 +571,8 @@ int tridiag_solve_out_double(int algo, int layout, const double* a, const double
 }
 
 size_t tridiag_gtsv_workspace_size(int precision, int layout, int n, int batch) {
-  (void)layout;
   if (!valid_dims(n, batch)) return 0;
-  return precision ? gtsv_ws_bytes<double>(n, batch) : gtsv_ws_bytes<float>(n, batch);
+  return precision ? gtsv_ws_query<double>(layout, n, batch) : gtsv_ws_query<float>(layout, n, batch);
 }
 
 size_t tridiag_pivot_record_size(int n, int batch) {
@@ -630,6 +652,16 @@ extern "C" int tridiag_partition_path_counts(long long* counts, int reset) {
   const cudaError_t e = tdg::pge_path_counts(v, reset != 0);
   if (e != cudaSuccess) return set_status(cuda_status(e));
   for (int k = 0; k < 4; ++k) counts[k] = (long long)v[k];
+  return set_status(TRIDIAG_SUCCESS);
+}
+
+extern "C" int tridiag_partition_ppt_counts(long long* counts, int reset) {
+  if (!counts) return set_status(TRIDIAG_ERR_INVALID_VALUE);
+  unsigned long long v[2] = {0ull, 0ull};
+  const cudaError_t e = tdg::ppt_counts(v, reset != 0);
+  if (e != cudaSuccess) return set_status(cuda_status(e));
+  counts[0] = (long long)v[0];
+  counts[1] = (long long)v[1];
   return set_status(TRIDIAG_SUCCESS);
 }
 

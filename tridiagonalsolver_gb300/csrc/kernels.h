@@ -251,6 +251,25 @@ cudaError_t launch_pge_long_ragged(const T* a, const T* b, const T* c, const T* 
 template <typename T>
 cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info, int n, int batch, T* w1, T* w2,
                             unsigned* piv, int* flag, cudaStream_t s, bool* used);
+// The systems list[0 .. *dcount) (at most batch) of a uniform contiguous
+// batch by the partitioned solve, drained through `ticket` (zero first).
+template <typename T>
+cudaError_t launch_pge_list(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                            const int* list, const int* dcount, int* ticket, cudaStream_t s);
+
+// ppt.cu: the partitioned pivoted solve with a thread per (system,
+// partition) for contiguous batches of many systems (x may alias d); systems
+// that miss its acceptance test are solved again by launch_pge_list.
+// *used = false when (n, batch) is not covered or the workspace is short.
+bool ppt_eligible(int n, int batch);
+template <typename T>
+size_t ppt_workspace_bytes(int n, int batch);
+template <typename T>
+cudaError_t launch_ppt(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                       void* work, size_t work_bytes, cudaStream_t s, bool* used);
+// out[0]: systems it accepted, out[1]: systems it listed (synchronous).
+cudaError_t ppt_counts(unsigned long long* out, bool reset);
+
 cudaError_t pge_fallback_count(unsigned long long* out, bool reset);
 cudaError_t pge_path_counts(unsigned long long* out, bool reset);  // out[4]
 

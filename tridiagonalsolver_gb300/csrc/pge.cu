@@ -2175,6 +2175,32 @@ cudaError_t launch_pge_ragged(int variant, int mode, const T* a, const T* b, con
   return pge_launch_variant<T, 1>(variant, io, count, m_max, s);
 }
 
+// The systems list[0 .. *dcount) of a uniform contiguous batch (at most
+// `batch` of them), drained by resident CTAs through `ticket` (zero before
+// the launch): the fallback of the thread-per-partition solve (ppt.cu).
+template <typename T>
+cudaError_t launch_pge_list(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                            const int* list, const int* dcount, int* ticket, cudaStream_t s) {
+  const int v = pge_default_variant<T>(n);
+  if (v == 0) return cudaErrorInvalidValue;
+  PgeIO<T> io{};
+  io.err = error_word();
+  io.a = a;
+  io.b = b;
+  io.c = c;
+  io.d = d;
+  io.x = x;
+  io.info = info;
+  io.n = n;
+  io.stride = (size_t)n;
+  io.list = list;
+  io.ticket = ticket;
+  io.count = batch;
+  io.dcount = dcount;
+  const int parts = pge_variant_partitions(v);
+  return pge_launch_variant<T, 0>(v, io, batch, (n + parts - 1) / parts, s);
+}
+
 cudaError_t pge_fallback_count(unsigned long long* out, bool reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_pge_fallbacks, sizeof(*out));
   if (e == cudaSuccess && reset) {
@@ -2216,7 +2242,9 @@ cudaError_t pge_path_counts(unsigned long long* out, bool reset) {
                                              int*, int, int, cudaStream_t, bool*);                                \
   template cudaError_t launch_pge_ragged<T>(int, int, const T*, const T*, const T*, const T*, T*, const T*, T*, T*, \
                                             T*, int*, const long long*, const int*, int, int, cudaStream_t,       \
-                                            const BucketTicket*);
+                                            const BucketTicket*);                                                 \
+  template cudaError_t launch_pge_list<T>(const T*, const T*, const T*, const T*, T*, int*, int, int, const int*,  \
+                                          const int*, int*, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

@@ -212,6 +212,15 @@ def partition_path_counts(reset: bool = False) -> dict:
     return dict(zip(("pivoted_separators", "exact_checks", "refinement_passes", "fallbacks"), list(buf)))
 
 
+def ppt_counts(reset: bool = False) -> dict:
+    """Systems the thread-per-partition pivoted solve (many contiguous FP64
+    systems, gtsv without a pivot record) accepted, and those it handed to
+    the one-CTA partitioned solve, on the current device since the last reset."""
+    buf = (ctypes.c_longlong * 2)()
+    check(lib().tridiag_partition_ppt_counts(ctypes.addressof(buf), int(reset)))
+    return dict(zip(("accepted", "listed"), list(buf)))
+
+
 def partition_supported(a, n: int, layout: str = "contiguous") -> bool:
     """Whether TRIDIAG_ALGO_PARTITION's CTA kernel covers (dtype of a, n, layout)."""
     return bool(lib().tridiag_partition_supported(1 if a.dtype == torch.float64 else 0, LAYOUTS[layout], n))

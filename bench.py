@@ -1667,11 +1667,13 @@ def other_configs(args):
 
 def run_gtsv_long(args):
     """Pivoted FP64 solves of systems longer than one CTA's shared memory
-    holds (U[-1,1] coefficients, non-dominant): TRIDIAG_ALGO_GTSV of
-    tridiag_solve_out_double -- the thread-per-partition solve (ppt.cu) --
-    against the partitioned solve in clusters of CTAs (tridiag_pge_double),
-    both graph-replayed and timed with CUDA events; the backward error of 16
-    sampled systems of each, formed in FP64 here."""
+    holds (U[-1,1] coefficients, non-dominant): tridiag_gtsv_double with the
+    workspace tridiag_gtsv_workspace_size() asks for -- the thread-per-
+    partition solve (ppt.cu) -- against the same call with the smaller
+    workspace of the other paths, which takes the path these sizes took
+    before (clusters of CTAs below 12288 rows, the chunked long-system solve
+    from there); both graph-replayed and timed with CUDA events; the backward
+    error of 16 sampled systems of each, formed in FP64 here."""
     import torch
 
     import tridiagonalsolver_gb300 as T
@@ -1695,24 +1697,30 @@ def run_gtsv_long(args):
         scale = (a_.abs() + b_.abs() + c_.abs()).amax(dim=1) * x_.abs().amax(dim=1) + d_.abs().amax(dim=1)
         return float((r.abs().amax(dim=1) / scale).max())
 
+    al = lambda v: (v + 255) // 256 * 256
     parts = []
-    for n, batch in ((6144, 2048), (8192, 2048), (8192, 4096), (11000, 1536)):
+    for n, batch in ((6144, 2048), (8192, 2048), (8192, 4096), (11000, 1536), (16384, 1024), (27648, 1024)):
         g = torch.Generator(device=dev)
         g.manual_seed(5)
         a, b, c, d = (torch.rand((batch, n), dtype=torch.float64, device=dev, generator=g) * 2 - 1 for _ in range(4))
         x, xc = torch.empty_like(d), torch.empty_like(d)
-        work = T.solve_out_workspace(a, n, "gtsv")
-        ms_p, _ = _graph_time(torch, stream, lambda: T.solve_out(a, b, c, d, n, algo="gtsv", out=x, work=work,
-                                                                    stream=stream), args.steps, args.warmup)
+        work = T.gtsv_workspace(a, n)
+        # the other paths' workspace: two n x batch arrays, the pivot words, one int per system
+        small = torch.empty(2 * al(n * batch * 8) + al((n + 31) // 32 * batch * 4) + al(batch * 4),
+                            dtype=torch.uint8, device=dev)
+        ms_p, _ = _graph_time(torch, stream, lambda: T.gtsv(a, b, c, d, n, work=work, out=x, stream=stream),
+                              args.steps, args.warmup)
         T.ppt_counts(reset=True)
         with torch.cuda.stream(stream):
-            T.solve_out(a, b, c, d, n, algo="gtsv", out=x, work=work, stream=stream)
+            T.gtsv(a, b, c, d, n, work=work, out=x, stream=stream)
         stream.synchronize()
         counts = T.ppt_counts(reset=True)
-        ms_c, _ = _graph_time(torch, stream, lambda: T.pge(a, b, c, d, n, out=xc, stream=stream), args.steps,
-                              args.warmup)
+        ms_c, _ = _graph_time(torch, stream, lambda: T.gtsv(a, b, c, d, n, work=small, out=xc, stream=stream),
+                              args.steps, args.warmup)
         parts.append({"n": n, "batch": batch, "ms_thread_per_partition": round(ms_p, 4),
-                      "ms_clusters": round(ms_c, 4), "speedup": round(ms_c / ms_p, 2),
+                      "ms_previous_path": round(ms_c, 4),
+                      "previous_path": "clusters of CTAs" if n < 12288 else "chunked long-system solve",
+                      "speedup": round(ms_c / ms_p, 2),
                       "systems_per_s": batch / (ms_p * 1e-3), "ppt_counts": counts,
                       "backward_error_max": max(eta(a, b, c, d, x, batch), eta(a, b, c, d, xc, batch))})
         del a, b, c, d, x, xc, work

@@ -179,7 +179,7 @@ def _gtsv_many(torch, arrs, n):
     return x.cpu().numpy(), info.cpu().numpy(), counts
 
 
-@pytest.mark.parametrize("n,batch", [(6144, 1024), (7001, 1100), (8192, 1024)])
+@pytest.mark.parametrize("n,batch", [(6144, 1024), (7001, 1100), (8192, 1024), (16384, 1024)])
 def test_ppt_matches_oracle(cuda, n, batch):
     """Many contiguous FP64 systems longer than one CTA's shared memory holds:
     the thread-per-partition pivoted solve serves them (its counters say so)

@@ -101,6 +101,16 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
   }
   if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
   GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
+  if (!pivots && sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch)) {
+    // many FP64 systems longer than one CTA holds, up to the clusters'
+    // 27648 rows: partitions of a few hundred rows, a thread each, instead of
+    // clusters of CTAs or the chunked solve (1.5-2.3x faster, measured on
+    // GB300; the systems that miss its acceptance test take the clusters)
+    bool used = false;
+    cudaError_t e = tdg::launch_ppt<T>(a, b, c, d, d, info, n, batch, work, work_bytes, s, &used);
+    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
+    if (used) return TRIDIAG_SUCCESS;
+  }
   // Long systems without a pivot record, contiguous: the chunked partitioned
   // solve where the one-CTA and cluster solves do not reach, and for FP64
   // from PGE_LONG_MIN_FP64 rows on (measured on GB300: n = 16384 / 27648 FP64
@@ -112,15 +122,6 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
       (chunked_first || !tdg::pge_eligible<T>(layout, n))) {
     bool used = false;
     cudaError_t e = tdg::launch_pge_long<T>(a, b, c, d, info, n, batch, w.w1, w.w2, w.piv, w.flag, s, &used);
-    if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
-    if (used) return TRIDIAG_SUCCESS;
-  }
-  if (!pivots && sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch)) {
-    // many FP64 systems longer than one CTA holds: partitions of a few
-    // hundred rows, a thread each, instead of clusters of CTAs (the systems
-    // that miss its acceptance test take the clusters)
-    bool used = false;
-    cudaError_t e = tdg::launch_ppt<T>(a, b, c, d, d, info, n, batch, work, work_bytes, s, &used);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
     if (used) return TRIDIAG_SUCCESS;
   }

@@ -517,11 +517,12 @@ int ppt_rows(int n, int batch) {
 // partitioned solve would take clusters of CTAs: measured on GB300 at 6144 /
 // 8192 / 11000 rows x 1536-4096 systems, 1.7-2.4x faster than the clusters;
 // at 4096 rows the persistent one-CTA solve is as fast in one launch instead
-// of five), below the chunked long-system solve's 12288 rows, in batches
-// whose partitions fill the GPU with at most PPT_MAX_P of them.
+// of five) up to the clusters' reach, in batches whose partitions fill the
+// GPU with at most PPT_MAX_P of them.
 bool ppt_eligible(int n, int batch) {
   const int one_cta = std::max(pge_variant_max_n<double>(2), pge_variant_max_n<double>(3));
-  return n > one_cta && n < 12288 && batch >= 1024 && ppt_rows(n, batch) > 0;
+  // (the longest system the listed systems' solve reaches: clusters of 8 CTAs, 27648 FP64 rows)
+  return n > one_cta && n <= pge_variant_max_n<double>(6) && batch >= 1024 && ppt_rows(n, batch) > 0;
 }
 
 template <typename T>

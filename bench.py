@@ -1278,7 +1278,7 @@ def run_block2(args):
 PROFILE_CASES = {
     # name: (n, batch, dtype, dominant, how)
     "pge64": (4096, 2048, "float64", False, "pge"),        # partitioned pivoted solve, FP64
-    "ppt64": (4096, 4096, "float64", False, "gtsv"),       # thread-per-partition pivoted solve (gtsv), FP64
+    "ppt64": (8192, 2048, "float64", False, "gtsv"),       # thread-per-partition pivoted solve (gtsv), FP64
     "pge32": (4096, 4096, "float32", True, "pge"),         # the same, FP32
     "pgc32": (65536, 256, "float32", True, "pge"),         # cluster version, FP32
     "pgl64": (65536, 128, "float64", False, "gtsv"),       # long systems in chunks, FP64

@@ -9,7 +9,8 @@ workspace):
 max |x_noalloc - x_gtsv| / max |x_gtsv| <= 1e-12 (FP64) / 1e-5 (FP32) per
 system, and normwise backward error <= 1e-12 / 1e-6.  It also checks that a
 call after the first one leaves the device's free memory unchanged, and
-that a problem larger than the static array is refused.  The file is named to be
+that a problem larger than the static array is refused, and that a call
+captured in a CUDA graph replays to the direct call's bits.  The file is named to be
 collected last; it passes alone and after the other tests.
 """
 import ctypes
@@ -119,4 +120,37 @@ def test_noalloc_leaves_free_memory_unchanged(cuda):
     free1, _ = cuda.cuda.mem_get_info()
     assert free1 == free0
     _, eta = O.backward_error(*(t.cpu().numpy() for t in (a, b, c, d, x)), n)
+    assert eta <= 1e-12
+
+
+def test_noalloc_in_a_cuda_graph(cuda):
+    """After its first call the entry point can be captured: one call captured
+    in a CUDA graph on a side stream, replayed on new right-hand sides copied
+    into the captured buffer, gives the direct call's bits."""
+    import tridiagonalsolver_gb300 as T
+    from tridiagonalsolver_gb300._lib import SUCCESS
+
+    torch = cuda
+    lib = T.lib()
+    n, batch = 700, 128
+    a, b, c, d = (torch.from_numpy(v.copy()).cuda() for v in inputs.nondominant(n, batch, seed=44))
+    d2 = torch.from_numpy(inputs.nondominant(n, batch, seed=45)[3].copy()).cuda()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = torch.cuda.Stream()
+    x = d.clone()
+    with torch.cuda.stream(s):
+        st = ctypes.c_void_p(s.cuda_stream)
+        assert lib.tridiag_gtsv_noalloc_double(0, P(a), P(b), P(c), P(x), None, n, batch, st) == SUCCESS
+        s.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            assert lib.tridiag_gtsv_noalloc_double(0, P(a), P(b), P(c), P(x), None, n, batch, st) == SUCCESS
+        x.copy_(d2)
+        g.replay()
+    s.synchronize()
+    want = d2.clone()
+    assert lib.tridiag_gtsv_noalloc_double(0, P(a), P(b), P(c), P(want), None, n, batch, None) == SUCCESS
+    torch.cuda.synchronize()
+    assert torch.equal(x, want)
+    _, eta = O.backward_error(*(t.cpu().numpy() for t in (a, b, c, d2, x)), n)
     assert eta <= 1e-12

@@ -258,6 +258,36 @@ def test_ppt_out_of_place(cuda):
     assert np.array_equal(x2, xh)
 
 
+@pytest.mark.parametrize("n,batch,planted", [(4096, 1024, ()), (3000, 2048, (1, 777, 2047))])
+def test_ppt_interleaved(cuda, n, batch, planted):
+    """Batch-interleaved FP64 systems (layout 2): the thread-per-partition
+    solve serves them with every access coalesced; planted singular partition
+    blocks take the masked sequential solve.  Every system meets the FP64 bar
+    and agrees with the oracle."""
+    import tridiagonalsolver_gb300 as T
+
+    torch = cuda
+    L = _ppt_rows(torch, n, batch)
+    a, b, c, d = inputs.nondominant(n, batch, seed=n + batch)
+    for j in planted:
+        b[j, L] = 0.0
+        c[j, L] = 0.0
+        a[j, L] = 1.0
+    ti = [torch.from_numpy(np.ascontiguousarray(v)).cuda() for v in inputs.to_interleaved(a, b, c, d)]
+    info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
+    T.ppt_counts(reset=True)
+    x = T.gtsv(*ti, n, layout="interleaved", info=info)
+    counts = T.ppt_counts(reset=True)
+    assert counts["accepted"] + counts["listed"] == batch
+    assert counts["listed"] >= len(planted) and counts["listed"] <= len(planted) + batch // 64
+    assert (info.cpu().numpy() == 0).all()
+    xh = x.cpu().numpy().T.copy()
+    _, worst = O.backward_error(a, b, c, d, xh, n)
+    assert worst <= 1e-12
+    xo = O.gtsv(a, b, c, d, n).reshape(batch, n)
+    assert np.median(_rel(xh, xo)) <= 1e-11
+
+
 def test_ppt_long_systems_fp64(cuda):
     """FP64 8192 x 4096 non-dominant through gtsv: the thread-per-partition
     solve serves it, (nearly) every system is accepted there, and 64 sampled

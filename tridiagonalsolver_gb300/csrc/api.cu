@@ -61,8 +61,7 @@ size_t gtsv_ws_bytes(int n, int batch) {
 template <typename T>
 size_t gtsv_ws_query(int layout, int n, int batch) {
   size_t w = gtsv_ws_bytes<T>(n, batch);
-  if (sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch))
-    w = std::max(w, tdg::ppt_workspace_bytes<T>(n, batch));
+  if (sizeof(T) == 8 && tdg::ppt_eligible(layout, n, batch)) w = std::max(w, tdg::ppt_workspace_bytes<T>(n, batch));
   return w;
 }
 
@@ -101,13 +100,13 @@ int gtsv_impl(int layout, const T* a, const T* b, const T* c, T* d, unsigned* pi
   }
   if (!work || work_bytes < gtsv_ws_bytes<T>(n, batch)) return TRIDIAG_ERR_WORKSPACE;
   GtsvWs<T> w = carve_gtsv<T>(work, n, batch);
-  if (!pivots && sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch)) {
+  if (!pivots && sizeof(T) == 8 && tdg::ppt_eligible(layout, n, batch)) {
     // many FP64 systems longer than one CTA holds, up to the clusters'
     // 27648 rows: partitions of a few hundred rows, a thread each, instead of
     // clusters of CTAs or the chunked solve (1.5-2.3x faster, measured on
     // GB300; the systems that miss its acceptance test take the clusters)
     bool used = false;
-    cudaError_t e = tdg::launch_ppt<T>(a, b, c, d, d, info, n, batch, work, work_bytes, s, &used);
+    cudaError_t e = tdg::launch_ppt<T>(layout, a, b, c, d, d, info, n, batch, work, work_bytes, s, &used);
     if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
     if (used) return TRIDIAG_SUCCESS;
   }
@@ -334,8 +333,8 @@ int solve_out_impl(int algo, int layout, const T* a, const T* b, const T* c, con
     case TRIDIAG_ALGO_GTSV: {
       bool used = false;
       cudaError_t e = cudaSuccess;
-      if (sizeof(T) == 8 && layout == TRIDIAG_LAYOUT_CONTIGUOUS && tdg::ppt_eligible(n, batch))
-        e = tdg::launch_ppt<T>(a, b, c, d, x, nullptr, n, batch, work, work_bytes, s, &used);
+      if (sizeof(T) == 8 && tdg::ppt_eligible(layout, n, batch))
+        e = tdg::launch_ppt<T>(layout, a, b, c, d, x, nullptr, n, batch, work, work_bytes, s, &used);
       if (e != cudaSuccess) return TRIDIAG_ERR_CUDA;
       if (used) return TRIDIAG_SUCCESS;
       e = n >= PGE_MIN_N ? tdg::launch_pge<T>(layout, a, b, c, d, x, nullptr, n, batch, s, &used) : cudaSuccess;

@@ -35,11 +35,11 @@ cudaError_t launch_thomas_seq(int layout, T* a, T* b, T* c, T* d, int n, int bat
 template <typename T>
 cudaError_t launch_gtsv_seq(int layout, const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv,
                             int* info, int n, int batch, cudaStream_t s);
-// The sequential solve (contiguous) of the systems with mask[j] != 0 only;
+// The sequential solve (contiguous or interleaved) of the systems with mask[j] != 0 only;
 // info[j] = 0 for the others.
 template <typename T>
-cudaError_t launch_gtsv_seq_masked(const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv, int* info,
-                                   int n, int batch, const int* mask, cudaStream_t s);
+cudaError_t launch_gtsv_seq_masked(int layout, const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv,
+                                   int* info, int n, int batch, const int* mask, cudaStream_t s);
 template <typename T>
 cudaError_t launch_gtsv_adjoint(int layout, const T* a, const T* b, const T* c, const T* x, const unsigned* piv,
                                 const T* g, T* ga, T* gb, T* gc, T* gd, T* wz, T* wm, int n, int batch,
@@ -261,11 +261,11 @@ cudaError_t launch_pge_list(const T* a, const T* b, const T* c, const T* d, T* x
 // partition) for contiguous batches of many systems (x may alias d); systems
 // that miss its acceptance test are solved again by launch_pge_list.
 // *used = false when (n, batch) is not covered or the workspace is short.
-bool ppt_eligible(int n, int batch);
+bool ppt_eligible(int layout, int n, int batch);
 template <typename T>
 size_t ppt_workspace_bytes(int n, int batch);
 template <typename T>
-cudaError_t launch_ppt(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+cudaError_t launch_ppt(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
                        void* work, size_t work_bytes, cudaStream_t s, bool* used);
 // out[0]: systems it accepted, out[1]: systems it listed (synchronous).
 cudaError_t ppt_counts(unsigned long long* out, bool reset);

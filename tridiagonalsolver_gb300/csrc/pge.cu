@@ -2012,7 +2012,7 @@ cudaError_t launch_pge_long(const T* a, const T* b, const T* c, T* d, int* info,
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // the flagged systems: sequential partial pivoting in place on d (their
   // right-hand side is still there), w1/w2 now free for its factors
-  return launch_gtsv_seq_masked<T>(a, b, c, d, w1, w2, piv, info, n, batch, flag, s);
+  return launch_gtsv_seq_masked<T>(CONTIG, a, b, c, d, w1, w2, piv, info, n, batch, flag, s);
 }
 
 // Ragged long systems in chunks (the passes above, per system of a size

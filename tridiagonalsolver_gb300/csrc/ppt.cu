@@ -1,5 +1,6 @@
 // Partitioned solve with partial pivoting inside partitions, one thread per
-// (system, partition), for contiguous batches (layout 0); x may alias d.
+// (system, partition), for contiguous (layout 0) and batch-interleaved
+// (layout 2) batches; x may alias d.
 //
 // The one-CTA-per-system partitioned solve (pge.cu) cuts each system into
 // 128 partitions of 32 rows: its separators' system costs ~2.4 FP64
@@ -91,12 +92,19 @@ struct Ppt {
   int* info;
   int* list;   // systems for the fallback, count in cnt[0]
   int* cnt;    // [0] fallback count, [1] fallback ticket
+  int* flag;   // [batch] (interleaved) systems for the fallback
   int n, batch, P, L;
+  bool inter;  // layout 2: row i of system j at i batch + j (else j n + i)
 };
 
 template <typename T>
 __device__ __forceinline__ T& relv(const Ppt<T>& g, int k, int p, int j) {
   return g.rel[((size_t)k * g.P + p) * g.batch + j];
+}
+// element (row i, system j) of a, b, c, d, x
+template <typename T>
+__device__ __forceinline__ size_t ix(const Ppt<T>& g, int i, int j) {
+  return g.inter ? (size_t)i * (size_t)g.batch + (size_t)j : (size_t)j * (size_t)g.n + (size_t)i;
 }
 template <typename T>
 __device__ __forceinline__ size_t fat(const Ppt<T>& g, int i, int j) {
@@ -123,7 +131,6 @@ template <typename T, bool INTERIOR>
 __device__ __forceinline__ void ppt_sweep(const Ppt<T>& g, int j, int p) {
   int lo, mi, dir;
   ppt_geom(g.n, g.L, g.P, p, lo, mi, dir);
-  const size_t sj = (size_t)j * g.n;
   auto row = [&](int k) { return dir > 0 ? lo + k : lo + mi - 1 - k; };
   // swept row k as (na: toward the eliminated side, nb, cn: toward the
   // rows ahead, ny); the outer coefficient of the first row is the left
@@ -132,13 +139,13 @@ __device__ __forceinline__ void ppt_sweep(const Ppt<T>& g, int j, int p) {
   auto load = [&](int k, int u) {
     if (k < mi) {
       const int i = row(k);
-      const T av = (dir > 0 ? k > 0 || INTERIOR : k + 1 < mi || i > 0) ? __ldg(g.a + sj + i) : T(0);
-      const T cval = (dir > 0 ? k + 1 < mi || i + 1 < g.n : k > 0) ? __ldg(g.c + sj + i) : T(0);
-      const T dv = __ldg(g.din + sj + i);
-      if (g.dcopy) g.dcopy[sj + i] = dv;
+      const T av = (dir > 0 ? k > 0 || INTERIOR : k + 1 < mi || i > 0) ? __ldg(g.a + ix(g, i, j)) : T(0);
+      const T cval = (dir > 0 ? k + 1 < mi || i + 1 < g.n : k > 0) ? __ldg(g.c + ix(g, i, j)) : T(0);
+      const T dv = __ldg(g.din + ix(g, i, j));
+      if (g.dcopy) g.dcopy[ix(g, i, j)] = dv;
       qa[u] = dir > 0 ? av : cval;
       qc[u] = dir > 0 ? cval : av;
-      qb[u] = __ldg(g.b + sj + i);
+      qb[u] = __ldg(g.b + ix(g, i, j));
       qy[u] = dv;
     }
   };
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(32 * PPT_SEP_WARPS) ppt_separator_kernel(const
   for (int q = w; q < S; q += PPT_SEP_WARPS) {
     T A = T(0), B = T(1), C = T(0), D = T(0);
     if (live) {
-      const size_t o = (size_t)j * g.n + (size_t)(q + 1) * g.L - 1;
+      const size_t o = ix(g, (q + 1) * g.L - 1, j);
       const T aR = __ldg(g.a + o), cR = __ldg(g.c + o);
       B = __ldg(g.b + o);
       D = __ldg(g.din + o);
@@ -355,7 +362,6 @@ template <typename T, bool INTERIOR>
 __device__ __forceinline__ void ppt_back(const Ppt<T>& g, int j, int p) {
   int lo, mi, dir;
   ppt_geom(g.n, g.L, g.P, p, lo, mi, dir);
-  const size_t sj = (size_t)j * g.n;
   auto row = [&](int k) { return dir > 0 ? lo + k : lo + mi - 1 - k; };
   // separators on the near (left spike) and far side of the sweep
   const T s_near = INTERIOR ? g.sep[(size_t)(p - 1) * g.batch + j] : T(0);
@@ -383,7 +389,7 @@ __device__ __forceinline__ void ppt_back(const Ppt<T>& g, int j, int p) {
   for (int u = 0; u < PPT_UB; ++u) load(mi - 1 - u, u);
   T x1 = fma(-cw, s_far, fma(-qz[0], s_near, qy[0])) * qi[0], x2 = T(0);
   if (mi >= 2) qy[1] = fma(-w_prev, s_far, qy[1]);  // row mi-2's far-spike term
-  g.x[sj + row(mi - 1)] = x1;
+  g.x[ix(g, row(mi - 1), j)] = x1;
   xmax = max(xmax, ppt_mag(x1));
   bad |= !ppt_finite(x1);
   for (int k0 = mi - 1; k0 > 0; k0 -= PPT_UB) {
@@ -410,7 +416,7 @@ __device__ __forceinline__ void ppt_back(const Ppt<T>& g, int j, int p) {
       // z multiplies x two rows on (swap) or the near separator (no swap)
       const T zx = si ? x2 : s_near;
       const T xi = fma(-ui, x1, fma(-zi, zx, yi)) * ii;
-      g.x[sj + row(k)] = xi;
+      g.x[ix(g, row(k), j)] = xi;
       xmax = max(xmax, ppt_mag(xi));
       bad |= !ppt_finite(xi);
       x2 = x1;
@@ -449,7 +455,6 @@ __global__ void __launch_bounds__(32 * PPT_CHECK_WARPS) ppt_check_kernel(const P
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j = blockIdx.x * 32 + lane;
   const bool live = j < g.batch;
-  const size_t sj = (size_t)j * g.n;
   unsigned am = 0, dm = 0, xm = 0;
   for (int p = w; p < g.P && live; p += PPT_CHECK_WARPS) {
     am = max(am, ppt_mag(relv(g, R_AMAX, p, j)));
@@ -472,10 +477,12 @@ __global__ void __launch_bounds__(32 * PPT_CHECK_WARPS) ppt_check_kernel(const P
       PptTol<T>::SEP * fma((double)ppt_from_mag(am, T(0)), (double)ppt_from_mag(xm, T(0)), (double)ppt_from_mag(dm, T(0)));
   bool rb = false;
   for (int q = w; q + 1 < g.P && live && !bad; q += PPT_CHECK_WARPS) {
-    const size_t o = sj + (size_t)(q + 1) * g.L - 1;
+    const int R = (q + 1) * g.L - 1;
+    const size_t o = ix(g, R, j);
     const T s = g.sep[(size_t)q * g.batch + j];
-    const double r = fma(-(double)g.c[o], (double)g.x[o + 1],
-                         fma(-(double)g.b[o], (double)s, fma(-(double)g.a[o], (double)g.x[o - 1], (double)g.din[o])));
+    const double r = fma(-(double)g.c[o], (double)g.x[ix(g, R + 1, j)],
+                         fma(-(double)g.b[o], (double)s,
+                             fma(-(double)g.a[o], (double)g.x[ix(g, R - 1, j)], (double)g.din[o])));
     rb |= !(fabs(r) <= bound) || !ppt_finite(s);
   }
   if (rb) s_bad[lane] = 1;
@@ -487,11 +494,22 @@ __global__ void __launch_bounds__(32 * PPT_CHECK_WARPS) ppt_check_kernel(const P
       if (acc) atomicAdd(&g_ppt_counts[0], (unsigned long long)__popc(acc));
       if (rej) atomicAdd(&g_ppt_counts[1], (unsigned long long)__popc(rej));
     }
-    if (live && bad) g.list[atomicAdd(g.cnt, 1)] = j;
+    if (live && bad) {
+      if (g.inter)
+        g.flag[j] = 1;
+      else
+        g.list[atomicAdd(g.cnt, 1)] = j;
+    }
     if (live && !bad && g.info) g.info[j] = 0;
   }
   for (int q = w; q + 1 < g.P && live && !bad; q += PPT_CHECK_WARPS)
-    g.x[sj + (size_t)(q + 1) * g.L - 1] = g.sep[(size_t)q * g.batch + j];
+    g.x[ix(g, (q + 1) * g.L - 1, j)] = g.sep[(size_t)q * g.batch + j];
+  // (interleaved) a listed system's x restarts from its right-hand side: the
+  // masked sequential solve works in place on x
+  if (g.inter && live && bad) {
+    const T* src = g.dcopy ? g.dcopy : g.din;
+    for (int i = w; i < g.n; i += PPT_CHECK_WARPS) g.x[ix(g, i, j)] = src[ix(g, i, j)];
+  }
 }
 
 inline size_t ppt_align(size_t b) { return (b + 255) / 256 * 256; }
@@ -519,10 +537,15 @@ int ppt_rows(int n, int batch) {
 // at 4096 rows the persistent one-CTA solve is as fast in one launch instead
 // of five) up to the clusters' reach, in batches whose partitions fill the
 // GPU with at most PPT_MAX_P of them.
-bool ppt_eligible(int n, int batch) {
+// Interleaved batches (where the one-CTA solve does not apply and the
+// alternative is a thread per system): from 1024 rows, the same bounds
+// otherwise; their listed systems take the masked sequential solve.
+bool ppt_eligible(int layout, int n, int batch) {
+  if (batch < 1024 || ppt_rows(n, batch) == 0) return false;
   const int one_cta = std::max(pge_variant_max_n<double>(2), pge_variant_max_n<double>(3));
   // (the longest system the listed systems' solve reaches: clusters of 8 CTAs, 27648 FP64 rows)
-  return n > one_cta && n <= pge_variant_max_n<double>(6) && batch >= 1024 && ppt_rows(n, batch) > 0;
+  if (layout == 2) return n >= 1024 && n <= pge_variant_max_n<double>(6);
+  return layout == 0 && n > one_cta && n <= pge_variant_max_n<double>(6);
 }
 
 template <typename T>
@@ -530,14 +553,14 @@ size_t ppt_workspace_bytes(int n, int batch) {
   const size_t e = ppt_align((size_t)n * (size_t)batch * sizeof(T));
   return 5 * e + ppt_align(pivot_words(n, batch) * sizeof(unsigned)) +
          ppt_align((size_t)PPT_REL * PPT_MAX_P * batch * sizeof(T)) +
-         ppt_align((size_t)PPT_MAX_P * batch * sizeof(T)) + ppt_align((size_t)batch * sizeof(int)) + 256;
+         ppt_align((size_t)PPT_MAX_P * batch * sizeof(T)) + 2 * ppt_align((size_t)batch * sizeof(int)) + 256;
 }
 
 template <typename T>
-cudaError_t launch_ppt(const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch, void* work,
-                       size_t work_bytes, cudaStream_t s, bool* used) {
+cudaError_t launch_ppt(int layout, const T* a, const T* b, const T* c, const T* d, T* x, int* info, int n, int batch,
+                       void* work, size_t work_bytes, cudaStream_t s, bool* used) {
   *used = false;
-  if (!ppt_eligible(n, batch) || !work || work_bytes < ppt_workspace_bytes<T>(n, batch)) return cudaSuccess;
+  if (!ppt_eligible(layout, n, batch) || !work || work_bytes < ppt_workspace_bytes<T>(n, batch)) return cudaSuccess;
   const int L = ppt_rows(n, batch);
   Ppt<T> g;
   g.a = a;
@@ -561,13 +584,16 @@ cudaError_t launch_ppt(const T* a, const T* b, const T* c, const T* d, T* x, int
   w += ppt_align((size_t)PPT_MAX_P * batch * sizeof(T));
   g.list = reinterpret_cast<int*>(w);
   w += ppt_align((size_t)batch * sizeof(int));
-  g.cnt = reinterpret_cast<int*>(w);
+  g.flag = reinterpret_cast<int*>(w);
+  w += ppt_align((size_t)batch * sizeof(int));
+  g.cnt = reinterpret_cast<int*>(w);  // (right after flag: one memset clears both)
   g.info = info;
   g.n = n;
   g.batch = batch;
   g.L = L;
   g.P = (n + L - 1) / L;
-  cudaError_t err = cudaMemsetAsync(g.cnt, 0, 2 * sizeof(int), s);
+  g.inter = layout == 2;
+  cudaError_t err = cudaMemsetAsync(g.flag, 0, ppt_align((size_t)batch * sizeof(int)) + 2 * sizeof(int), s);
   if (err != cudaSuccess) return err;
   const dim3 grid((batch + 127) / 128, g.P);
   ppt_forward_kernel<T><<<grid, 128, 0, s>>>(g);
@@ -585,8 +611,13 @@ cudaError_t launch_ppt(const T* a, const T* b, const T* c, const T* d, T* x, int
   ppt_check_kernel<T><<<(batch + 31) / 32, 32 * PPT_CHECK_WARPS, 0, s>>>(g);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  // the listed systems: the one-CTA partitioned solve from the copy of d
-  err = launch_pge_list<T>(a, b, c, g.dcopy ? g.dcopy : d, x, info, n, batch, g.list, g.cnt, g.cnt + 1, s);
+  // the listed systems: the partitioned solve from the (copy of the)
+  // right-hand side; interleaved: the masked sequential solve in place on x
+  // (restored by the check), the factor arrays as its workspace
+  if (g.inter)
+    err = launch_gtsv_seq_masked<T>(2, a, b, c, x, g.fi, g.fu, g.sw, info, n, batch, g.flag, s);
+  else
+    err = launch_pge_list<T>(a, b, c, g.dcopy ? g.dcopy : d, x, info, n, batch, g.list, g.cnt, g.cnt + 1, s);
   if (err == cudaSuccess) *used = true;
   return err;
 }
@@ -602,8 +633,8 @@ cudaError_t ppt_counts(unsigned long long* out, bool reset) {
 
 #define INST(T)                                                                                                \
   template size_t ppt_workspace_bytes<T>(int, int);                                                             \
-  template cudaError_t launch_ppt<T>(const T*, const T*, const T*, const T*, T*, int*, int, int, void*, size_t, \
-                                     cudaStream_t, bool*);
+  template cudaError_t launch_ppt<T>(int, const T*, const T*, const T*, const T*, T*, int*, int, int, void*,      \
+                                     size_t, cudaStream_t, bool*);
 INST(float)
 INST(double)
 #undef INST

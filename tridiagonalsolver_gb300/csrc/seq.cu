@@ -346,8 +346,9 @@ cudaError_t launch_gtsv_seq_l(const T* a, const T* b, const T* c, T* d, T* w1, T
 }
 
 template <typename T>
-cudaError_t launch_gtsv_seq_masked(const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv, int* info,
-                                   int n, int batch, const int* mask, cudaStream_t s) {
+cudaError_t launch_gtsv_seq_masked(int layout, const T* a, const T* b, const T* c, T* d, T* w1, T* w2, unsigned* piv,
+                                   int* info, int n, int batch, const int* mask, cudaStream_t s) {
+  if (layout == INTERLEAVED) return launch_gtsv_seq_l<T, INTERLEAVED>(a, b, c, d, w1, w2, piv, info, n, batch, s, mask);
   return launch_gtsv_seq_l<T, CONTIG>(a, b, c, d, w1, w2, piv, info, n, batch, s, mask);
 }
 
@@ -386,8 +387,8 @@ cudaError_t launch_gtsv_adjoint(int layout, const T* a, const T* b, const T* c, 
 
 #define INST(T)                                                                                                  \
   template cudaError_t launch_thomas_seq<T>(int, T*, T*, T*, T*, int, int, cudaStream_t);                        \
-  template cudaError_t launch_gtsv_seq_masked<T>(const T*, const T*, const T*, T*, T*, T*, unsigned*, int*, int,   \
-                                                 int, const int*, cudaStream_t);                                   \
+  template cudaError_t launch_gtsv_seq_masked<T>(int, const T*, const T*, const T*, T*, T*, T*, unsigned*, int*, \
+                                                 int, int, const int*, cudaStream_t);                              \
   template cudaError_t launch_gtsv_seq<T>(int, const T*, const T*, const T*, T*, T*, T*, unsigned*, int*, int,   \
                                           int, cudaStream_t);                                                    \
   template cudaError_t launch_gtsv_adjoint<T>(int, const T*, const T*, const T*, const T*, const unsigned*,      \

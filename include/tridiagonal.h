@@ -542,9 +542,10 @@ long long tridiag_partition_fallbacks(int reset);
  * Synchronous; reset != 0 clears all four.  Returns a TRIDIAG_* status. */
 int tridiag_partition_path_counts(long long *counts, int reset);
 
-/* tridiag_gtsv_* without a pivot record on many contiguous FP64 systems
- * longer than one CTA's shared memory holds (about 5000 rows) and up to
- * 27648 (batch from 1024, a workspace of tridiag_gtsv_workspace_size()
+/* tridiag_gtsv_* without a pivot record on many FP64 systems -- contiguous
+ * ones longer than one CTA's shared memory holds (about 5000 rows) and up to
+ * 27648, batch-interleaved ones from 1024 rows (batch from 1024, a workspace
+ * of tridiag_gtsv_workspace_size()
  * bytes; also TRIDIAG_ALGO_GTSV of tridiag_solve_out_*) cuts each system
  * into partitions of 64-448 rows, one thread each; counts[0] systems it solved and
  * accepted, counts[1] systems that missed its separator-row test and were

@@ -109,3 +109,25 @@ def test_ragged_refine_ex_checks_need_no_device(lib):
     # the adjoint's gradient outputs are checked first
     assert lib.tridiag_ragged_refine_adjoint_ex_double(p, p, p, p, p, p, None, p, p, p, 1, 1, p, 1 << 20, p,
                                                        None) == _lib.ERR_INVALID_VALUE
+
+
+def test_gtsv_workspace_covers_the_thread_per_partition_solve(lib):
+    """tridiag_gtsv_workspace_size asks for the thread-per-partition solve's
+    factor arrays (five n x batch arrays and the rest) exactly where that
+    solve serves the shape -- FP64 batches of >= 1024 systems, contiguous ones
+    beyond one CTA (up to 27648 rows), interleaved ones from 1024 rows -- and
+    for the other paths' two arrays elsewhere; its counters reject a NULL
+    array before any CUDA call."""
+    from tridiagonalsolver_gb300 import _lib
+
+    al = lambda v: (v + 255) // 256 * 256
+    small = lambda n, b: 2 * al(n * b * 8) + al((n + 31) // 32 * b * 4) + al(b * 4)
+    for layout, n, batch, big in ((0, 4096, 4096, False), (0, 8192, 2048, True), (0, 27648, 1024, True),
+                                  (0, 65536, 1024, False), (0, 8192, 512, False), (2, 4096, 4096, True),
+                                  (2, 1024, 16384, True), (2, 512, 16384, False), (1, 8192, 2048, False)):
+        got = lib.tridiag_gtsv_workspace_size(1, layout, n, batch)
+        assert got >= small(n, batch)
+        assert (got >= 5 * n * batch * 8) == big, (layout, n, batch, got)
+        # FP32 keeps the other paths' workspace
+        assert lib.tridiag_gtsv_workspace_size(0, layout, n, batch) < 5 * n * batch * 4
+    assert lib.tridiag_partition_ppt_counts(None, 0) == _lib.ERR_INVALID_VALUE

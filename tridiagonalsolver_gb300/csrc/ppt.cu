@@ -42,6 +42,7 @@
 // (Tridiagonal_AVX512/tridiagonal_basic.cpp:131-143), and the partitioned
 // GE of WM-pGE (Tridiagonal_CUDA/tridiagonal_wm_pcr.cu:17-884).
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -520,9 +521,24 @@ inline size_t ppt_align(size_t b) { return (b + 255) / 256 * 256; }
 // batch, L = ceil(n / P) rounded up to a multiple of 32, at most PPT_MAX_P.
 constexpr int PPT_MAX_P = 64;
 
+// SM count of the current device, looked up once per device (and once when
+// there is none: workspace-size queries run on machines without a GPU too).
+static int ppt_sms() {
+  static std::atomic<int> cache[65];
+  int dev = 0;
+  const bool have = cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64;
+  std::atomic<int>& slot = cache[have ? dev : 64];
+  int v = slot.load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  v = 152;
+  if (have && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) v = 152;
+  if (v <= 0) v = 152;
+  slot.store(v, std::memory_order_relaxed);
+  return v;
+}
+
 int ppt_rows(int n, int batch) {
-  int dev = 0, sms = 152;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = ppt_sms();
   const long long groups = (batch + 31) / 32;
   long long P = (4LL * 4 * sms + groups / 2) / std::max(1LL, groups);
   P = std::min<long long>(std::max<long long>(P, 3), PPT_MAX_P);
